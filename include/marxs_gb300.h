@@ -1,0 +1,204 @@
+/*
+ * marxs_gb300.h -- C ABI of the GB300 (sm_103a) photon-raytrace backend.
+ *
+ * Plain C: device pointers, sizes and POD descriptors only; no framework
+ * types.  Every entry point is asynchronous on the given CUDA stream
+ * (a cudaStream_t passed as void*; NULL = legacy default stream) and
+ * returns 0 on a successful launch or a CUDA runtime error code.  Errors
+ * found by the kernels themselves (the conditions the reference turns into
+ * exceptions) are OR-ed into a device status word that the caller reads
+ * after synchronising; see MGPU_STATUS_*.
+ *
+ * Reference interfaces (paths inside the MARXS source tree) replaced:
+ *   mgpu_trace              Sequence/BaseContainer.__call__ over a chain of
+ *                           elements, simulator/simulator.py:42-49, each
+ *                           leaf being OpticalElement.__call__ +
+ *                           process_photons, optics/base.py:144-211
+ *   mgpu_facet_grid_build   (no counterpart) nearest-hit candidate lists
+ *                           replacing the O(F) facet loop of
+ *                           Parallel.__call__, simulator.py:42-49, 206-212
+ *   mgpu_plane_intersect    FinitePlane.intersect, math/geometry.py:211-261
+ *   mgpu_cylinder_intersect Cylinder.intersect, math/geometry.py:470-564
+ *   mgpu_parallel_transport parallel_transport, math/polarization.py:151-170
+ */
+#ifndef MARXS_GB300_H
+#define MARXS_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MGPU_ABI_VERSION 1
+#define MGPU_MAX_STAGES 16
+#define MGPU_MAX_OUT 4
+
+/* status bits (device word, OR-ed by kernels) */
+#define MGPU_STATUS_PROB_RANGE   0x1u  /* probability factor outside [0,1]: ValueError, optics/base.py:43-46 */
+#define MGPU_STATUS_ORDER_EMPTY  0x2u  /* no order with cumulative prob > u (EfficiencyFile would raise) */
+#define MGPU_STATUS_BAD_STAGE    0x4u  /* unknown stage kind */
+#define MGPU_STATUS_GRID_RANGE   0x8u  /* a facet's footprint leaves the candidate grid */
+#define MGPU_STATUS_GRID_FULL    0x10u /* candidate list capacity exceeded */
+
+/* precision modes */
+#define MGPU_FP64      0  /* float64 throughout, parity mode */
+#define MGPU_FP32LOCAL 1  /* float32 ray arithmetic in each element's local frame */
+
+/* randomness */
+#define MGPU_RNG_PREDRAWN 0  /* per-photon arrays supplied by the caller */
+#define MGPU_RNG_PHILOX   1  /* Philox4x32-10 keyed by (seed, photon row, stage, draw) */
+
+/* stage kinds */
+#define MGPU_STAGE_LENS     1  /* PerfectLens, optics/mirror.py:53-82 */
+#define MGPU_STAGE_SCATTER  2  /* RadialMirrorScatter, optics/scatter.py:49-77 */
+#define MGPU_STAGE_FLATDET  3  /* FlatDetector, optics/detector.py:72-75 */
+#define MGPU_STAGE_GRATINGS 4  /* Parallel of FlatGrating/CATGrating (or one grating) */
+#define MGPU_STAGE_CYLDET   5  /* CircularDetector on a Cylinder */
+
+/* a float64 photon column: value of photon i at ptr[i * stride] */
+typedef struct {
+    double* ptr;
+    int64_t stride;
+} mgpu_col;
+
+/* a 3-vector column: component c of photon i at ptr[i * stride + c * cstride]
+ * ((N,4) row-major homogeneous arrays: stride 4, cstride 1; SoA planes:
+ * stride 1, cstride = plane pitch) */
+typedef struct {
+    double* ptr;
+    int64_t stride;
+    int64_t cstride;
+} mgpu_vec;
+
+typedef struct {
+    int64_t n;
+    mgpu_vec pos, dir, pol;          /* input state */
+    mgpu_col energy, prob;
+    mgpu_vec pos_out, dir_out, pol_out;  /* output state (may alias inputs) */
+    mgpu_col prob_out;
+} mgpu_photons;
+
+/* one grating facet (float64).  Unit vectors as MARXS derives them from
+ * pos4d (Geometry.__getitem__, math/geometry.py:108-160). */
+typedef struct {
+    double c[3];      /* centre */
+    double ex[3];     /* unit normal e_x */
+    double ey[3];     /* unit e_y */
+    double ez[3];     /* unit e_z */
+    double hy, hz;    /* |v_y|, |v_z| half sizes */
+    double l[3];      /* groove direction e_groove (grating.py:203-207) */
+    double dneg[3];   /* -e_perp_groove (grating.py:239) */
+    double dgrat;     /* grating constant, mm */
+    int32_t id_num;   /* value written to the id column */
+    int32_t selector; /* index into the selector table */
+    int32_t cat;      /* 1: CATGrating sign convention, 0: FlatGrating (-1) */
+    int32_t transmission;
+} mgpu_facet;
+
+/* order selector: OrderSelector (one row) or EfficiencyFile (energy rows) */
+typedef struct {
+    int32_t n_rows;
+    int32_t n_orders;
+    int32_t by_energy;    /* 1: nearest energy row (argmin |E - e|) */
+    int32_t pad;
+    const double* energy; /* n_rows */
+    const double* cdf;    /* n_rows * n_orders, normalised cumulative */
+    const double* total;  /* n_rows, probability factor */
+    const int32_t* orders;/* n_orders */
+} mgpu_selector;
+
+/* uniform candidate grid in a plane (origin o, normal n, in-plane axes a,b) */
+typedef struct {
+    double o[3], n[3], a[3], b[3];
+    double u0, v0, cell;   /* grid origin (u,v) and cell size, mm */
+    int32_t nu, nv;
+    double slope_max;      /* |d.a/d.n|, |d.b/d.n| bound for grid lookup */
+    double margin;         /* extra footprint margin, mm */
+    int32_t* cell_start;   /* nu*nv+1, device */
+    int32_t* cell_items;   /* capacity entries, device */
+    int32_t capacity;
+    int32_t pad;
+} mgpu_grid;
+
+typedef struct {
+    int32_t kind;
+    int32_t id_num;              /* id value for single elements (unused: -9) */
+    int32_t first_writer;        /* bit k: out[k] is new -> write NaN on miss;
+                                    bit 8: id column new -> write -1 on miss */
+    int32_t n_facets;
+    double frame[14];            /* flat: c(3) ex(3) ey(3) ez(3) hy hz */
+    double cyl[32];              /* cylinder: pos4d rows 0-2 (12), inverse rows 0-2 (12),
+                                    zoom_z, R, b1, b2 (angle_between borders) */
+    double p[8];                 /* kind parameters, see below */
+    mgpu_col out[MGPU_MAX_OUT];  /* output columns (NULL ptr = not written) */
+    int32_t* id_out;             /* int32 id column or NULL */
+    int64_t id_stride;
+    const double* draw[2];       /* pre-drawn per-photon values (RNG_PREDRAWN) */
+    int64_t draw_stride;
+    const mgpu_facet* facets;    /* GRATINGS */
+    const mgpu_selector* selectors;
+    int32_t n_selectors;
+    int32_t pad;
+    mgpu_grid grid;              /* GRATINGS: candidate grid (cell_start NULL = brute force) */
+} mgpu_stage;
+/* p[] per kind:
+ *   LENS:    p[0] focal length, p[1] d_center_optical_axis
+ *   SCATTER: p[0] sigma in-plane (rad), p[1] sigma perpendicular (rad)
+ *   FLATDET, CYLDET: p[0] pixsize, p[1] centerpix x, p[2] centerpix y
+ * out[] per kind:
+ *   LENS:     loc0, loc1
+ *   SCATTER:  loc0, loc1, inplanescatter, perpplanescatter
+ *   FLATDET:  loc0 (det_x), loc1 (det_y), detpix_x, detpix_y
+ *   GRATINGS: loc0 (grat_y), loc1 (grat_z), order, blaze   (+ id_out: facet)
+ *   CYLDET:   loc0 (det_phi), loc1 (det_y), detpix_x, detpix_y
+ */
+
+typedef struct {
+    int32_t n_stages;
+    int32_t precision;           /* MGPU_FP64 / MGPU_FP32LOCAL */
+    int32_t rng;                 /* MGPU_RNG_PREDRAWN / MGPU_RNG_PHILOX */
+    int32_t pad;
+    uint64_t seed;
+    uint32_t* status;            /* device status word */
+    unsigned long long* hits;    /* device, n_stages counters (added to) */
+    mgpu_stage stages[MGPU_MAX_STAGES];
+} mgpu_chain;
+
+/* library ABI version (MGPU_ABI_VERSION) */
+int mgpu_abi_version(void);
+
+/* Trace photons through the chain.  Photon state is read from the input
+ * columns and the final state written to the output columns for every
+ * photon; stage columns are written for hits (and defaults for misses
+ * where first_writer says so). */
+int mgpu_trace(const mgpu_chain* chain, const mgpu_photons* photons, void* stream);
+
+/* Build the candidate lists of a grating stage's grid on the device:
+ * grid->cell_start / cell_items are filled from the facet table.
+ * ``counts`` is caller-provided scratch of nu*nv+1 int32. */
+int mgpu_facet_grid_build(const mgpu_facet* facets, int32_t n_facets, mgpu_grid* grid,
+                          int32_t* counts, uint32_t* status, void* stream);
+
+/* FinitePlane.intersect for one element frame (c, ex, ey, ez, hy, hz as in
+ * mgpu_stage.frame).  Outputs: hit (uint8), interpos (vec), local (2 cols). */
+int mgpu_plane_intersect(const double* frame14, int64_t n, mgpu_vec pos, mgpu_vec dir,
+                         uint8_t* hit, mgpu_vec interpos, mgpu_col loc0, mgpu_col loc1,
+                         void* stream);
+
+/* Cylinder.intersect for one element (cyl block as in mgpu_stage.cyl). */
+int mgpu_cylinder_intersect(const double* cyl32, int64_t n, mgpu_vec pos, mgpu_vec dir,
+                            uint8_t* hit, mgpu_vec interpos, mgpu_col loc0, mgpu_col loc1,
+                            void* stream);
+
+/* parallel_transport(dir_old, dir_new, pol) -> pol_out */
+int mgpu_parallel_transport(int64_t n, mgpu_vec dir_old, mgpu_vec dir_new, mgpu_vec pol,
+                            mgpu_vec pol_out, void* stream);
+
+/* number of SMs of the current device (for launch sizing by callers) */
+int mgpu_device_sm_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MARXS_GB300_H */

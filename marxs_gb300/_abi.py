@@ -1,0 +1,150 @@
+"""ctypes mirror of ``include/marxs_gb300.h`` and the library loader.
+
+The structures here must match the C header byte for byte; a CPU test
+compiles the header with the system C compiler and compares every size and
+field offset.  Loading fails loudly when the library has not been built:
+there is no CPU fallback for any of the entry points.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, 'libmarxs_gb300.so')
+
+MGPU_ABI_VERSION = 1
+MAX_STAGES = 16
+MAX_OUT = 4
+
+STATUS_PROB_RANGE = 0x1
+STATUS_ORDER_EMPTY = 0x2
+STATUS_BAD_STAGE = 0x4
+STATUS_GRID_RANGE = 0x8
+STATUS_GRID_FULL = 0x10
+
+FP64 = 0
+FP32LOCAL = 1
+RNG_PREDRAWN = 0
+RNG_PHILOX = 1
+
+STAGE_LENS = 1
+STAGE_SCATTER = 2
+STAGE_FLATDET = 3
+STAGE_GRATINGS = 4
+STAGE_CYLDET = 5
+
+
+class MgpuCol(C.Structure):
+    _fields_ = [('ptr', C.c_void_p), ('stride', C.c_int64)]
+
+
+class MgpuVec(C.Structure):
+    _fields_ = [('ptr', C.c_void_p), ('stride', C.c_int64), ('cstride', C.c_int64)]
+
+
+class MgpuPhotons(C.Structure):
+    _fields_ = [('n', C.c_int64),
+                ('pos', MgpuVec), ('dir', MgpuVec), ('pol', MgpuVec),
+                ('energy', MgpuCol), ('prob', MgpuCol),
+                ('pos_out', MgpuVec), ('dir_out', MgpuVec), ('pol_out', MgpuVec),
+                ('prob_out', MgpuCol)]
+
+
+class MgpuSelector(C.Structure):
+    _fields_ = [('n_rows', C.c_int32), ('n_orders', C.c_int32), ('by_energy', C.c_int32),
+                ('pad', C.c_int32), ('energy', C.c_void_p), ('cdf', C.c_void_p),
+                ('total', C.c_void_p), ('orders', C.c_void_p)]
+
+
+class MgpuGrid(C.Structure):
+    _fields_ = [('o', C.c_double * 3), ('n', C.c_double * 3), ('a', C.c_double * 3),
+                ('b', C.c_double * 3), ('u0', C.c_double), ('v0', C.c_double),
+                ('cell', C.c_double), ('nu', C.c_int32), ('nv', C.c_int32),
+                ('slope_max', C.c_double), ('margin', C.c_double),
+                ('cell_start', C.c_void_p), ('cell_items', C.c_void_p),
+                ('capacity', C.c_int32), ('pad', C.c_int32)]
+
+
+class MgpuStage(C.Structure):
+    _fields_ = [('kind', C.c_int32), ('id_num', C.c_int32), ('first_writer', C.c_int32),
+                ('n_facets', C.c_int32), ('frame', C.c_double * 14), ('cyl', C.c_double * 32),
+                ('p', C.c_double * 8), ('out', MgpuCol * MAX_OUT), ('id_out', C.c_void_p),
+                ('id_stride', C.c_int64), ('draw', C.c_void_p * 2), ('draw_stride', C.c_int64),
+                ('facets', C.c_void_p), ('selectors', C.c_void_p), ('n_selectors', C.c_int32),
+                ('pad', C.c_int32), ('grid', MgpuGrid)]
+
+
+class MgpuChain(C.Structure):
+    _fields_ = [('n_stages', C.c_int32), ('precision', C.c_int32), ('rng', C.c_int32),
+                ('pad', C.c_int32), ('seed', C.c_uint64), ('status', C.c_void_p),
+                ('hits', C.c_void_p), ('stages', MgpuStage * MAX_STAGES)]
+
+
+# facet record as a numpy structured dtype (C layout of mgpu_facet)
+FACET_DTYPE = np.dtype([('c', '<f8', 3), ('ex', '<f8', 3), ('ey', '<f8', 3), ('ez', '<f8', 3),
+                        ('hy', '<f8'), ('hz', '<f8'), ('l', '<f8', 3), ('dneg', '<f8', 3),
+                        ('dgrat', '<f8'), ('id_num', '<i4'), ('selector', '<i4'),
+                        ('cat', '<i4'), ('transmission', '<i4')], align=True)
+
+# name -> (restype, argtypes) of every exported entry point
+SIGNATURES = {
+    'mgpu_abi_version': (C.c_int, []),
+    'mgpu_device_sm_count': (C.c_int, []),
+    'mgpu_trace': (C.c_int, [C.POINTER(MgpuChain), C.POINTER(MgpuPhotons), C.c_void_p]),
+    'mgpu_facet_grid_build': (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(MgpuGrid), C.c_void_p,
+                                        C.c_void_p, C.c_void_p]),
+    'mgpu_plane_intersect': (C.c_int, [C.c_void_p, C.c_int64, MgpuVec, MgpuVec, C.c_void_p,
+                                       MgpuVec, MgpuCol, MgpuCol, C.c_void_p]),
+    'mgpu_cylinder_intersect': (C.c_int, [C.c_void_p, C.c_int64, MgpuVec, MgpuVec, C.c_void_p,
+                                          MgpuVec, MgpuCol, MgpuCol, C.c_void_p]),
+    'mgpu_parallel_transport': (C.c_int, [C.c_int64, MgpuVec, MgpuVec, MgpuVec, MgpuVec,
+                                          C.c_void_p]),
+}
+
+_lib = None
+
+
+class LibraryNotBuilt(RuntimeError):
+    pass
+
+
+def load(path=LIB_PATH):
+    """Load the CUDA library (once) and bind every entry point's signature."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise LibraryNotBuilt('%s is missing: build it with `python -c "import __graft_entry__ as g; '
+                              'g.build()"` (there is no CPU fallback)' % path)
+    lib = C.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if lib.mgpu_abi_version() != MGPU_ABI_VERSION:
+        raise RuntimeError('libmarxs_gb300 ABI version mismatch')
+    _lib = lib
+    return lib
+
+
+def check(code, what):
+    if code != 0:
+        raise RuntimeError('%s failed with CUDA error %d' % (what, code))
+
+
+def col(t, stride=1):
+    """MgpuCol for a device tensor (or None -> absent column)."""
+    if t is None:
+        return MgpuCol(None, 0)
+    return MgpuCol(t.data_ptr(), stride)
+
+
+def vec_aos(t):
+    """MgpuVec over an (N, 4) row-major tensor (homogeneous coordinates)."""
+    return MgpuVec(t.data_ptr(), t.stride(0), t.stride(1))
+
+
+def vec_soa(t):
+    """MgpuVec over a (3, N) tensor of component planes."""
+    return MgpuVec(t.data_ptr(), t.stride(1), t.stride(0))

@@ -1,0 +1,250 @@
+"""Seeded synthetic instruments and photon lists for the benchmark workloads.
+
+All coordinates are in the MARXS frame: optical axis along +x, photons
+travel from large x towards the focus at the origin.
+
+* ``C0`` telescope: annulus aperture r in [300, 500] mm, PerfectLens f=10 m,
+  RadialMirrorScatter (5", 1"), FlatDetector 60x60 mm at the focus,
+  0.024 mm pixels.
+* ``C1`` grating spectrometer: C0 front end, a 20x10 grid of 20x20 mm
+  FlatGrating facets (pitch 22 mm, i.e. 2 mm gaps) centred at x=1500 mm,
+  each tilted by N(0, 0.1 deg) about its in-plane axes (y, z); d=2e-4 mm;
+  an EfficiencyFile-style 64-energy x 13-order table (orders -10..+2,
+  Dirichlet(1) rows); FlatDetector 200x60 mm at the focus.
+* ``C2`` CAT array: lens f=12 m at x=12000, 1000 CATGrating facets of
+  25x25 mm (40 x 25 grid, pitch 26.5 mm) on a Rowland torus R=r=5900 mm,
+  blaze 1.8 deg (rotation about the groove axis), N(0, 30") pose jitter
+  about three axes; energies from a piecewise-linear spectrum on 200 knots
+  in [0.2, 2] keV; CircularDetector (R=5900) on the Rowland circle.
+
+The builders take a namespace of element classes so the same instrument
+can be assembled from this package's classes or from MARXS itself.
+"""
+import math
+from types import SimpleNamespace
+
+import numpy as np
+
+from . import geomath
+
+ARCSEC = math.pi / 180. / 3600.
+
+
+def native_namespace():
+    from . import optics, simulator
+    return SimpleNamespace(
+        PerfectLens=optics.PerfectLens, RadialMirrorScatter=optics.RadialMirrorScatter,
+        FlatDetector=optics.FlatDetector, CircularDetector=optics.CircularDetector,
+        FlatGrating=optics.FlatGrating, CATGrating=optics.CATGrating,
+        OrderSelector=optics.OrderSelector, EfficiencyFile=optics.EfficiencyFile,
+        Cylinder=optics.Cylinder, Parallel=simulator.Parallel, Sequence=simulator.Sequence,
+        angle=lambda rad: rad)
+
+
+# ---------------------------------------------------------------------------
+# photons
+# ---------------------------------------------------------------------------
+def annulus_photons(n, seed, x0, r_in=300., r_out=500., energy=(0.3, 2.0), energies=None):
+    """Photons on an annulus in the plane x=x0, travelling along -x.
+
+    Positions follow the CircleAperture recipe (marxs/optics/aperture.py:138-146):
+    phi ~ U(0, 2 pi), r = sqrt(U(r_in^2/r_out^2, 1)) * r_out.  Polarization
+    angles ~ U[0, pi) are turned into vectors as polarization_vectors does.
+    """
+    rng = np.random.default_rng(seed)
+    n = int(n)
+    phi = rng.uniform(0, 2 * np.pi, n)
+    r = np.sqrt(rng.uniform((r_in / r_out) ** 2, 1., n)) * r_out
+    if energies is None:
+        energies = rng.uniform(energy[0], energy[1], n)
+    polangle = rng.uniform(0, np.pi, n)
+    pos = np.empty((n, 4))
+    pos[:, 0] = x0
+    pos[:, 1] = r * np.cos(phi)
+    pos[:, 2] = r * np.sin(phi)
+    pos[:, 3] = 1.
+    dirs = np.zeros((n, 4))
+    dirs[:, 0] = -1.
+    pol = np.zeros((n, 4))
+    # polarization_vectors for dir = -x: v1 = +y, v2 = r x v1 = -z
+    pol[:, 1] = np.cos(polangle)
+    pol[:, 2] = -np.sin(polangle)
+    return {'pos': pos, 'dir': dirs, 'energy': np.asarray(energies, dtype=float),
+            'polarization': pol, 'probability': np.ones(n)}
+
+
+def piecewise_linear_energies(n, seed, lo=0.2, hi=2.0, n_knots=200):
+    """Inverse-CDF samples of a seeded piecewise-linear spectrum on n_knots."""
+    rng = np.random.default_rng(seed + 1000)
+    knots = np.linspace(lo, hi, n_knots)
+    w = rng.uniform(0.2, 1.0, n_knots)
+    w[rng.integers(0, n_knots, 6)] += rng.uniform(2, 6, 6)     # a few lines
+    h = np.diff(knots)
+    cum = np.concatenate([[0.], np.cumsum(0.5 * (w[1:] + w[:-1]) * h)])
+    target = np.random.default_rng(seed + 2000).uniform(0, 1, int(n)) * cum[-1]
+    j = np.clip(np.searchsorted(cum, target, side='right') - 1, 0, n_knots - 2)
+    # mass inside segment j: h (w0 t + (w1 - w0) t^2 / 2) for t in [0, 1]
+    w0, w1, hj = w[j], w[j + 1], h[j]
+    m = (target - cum[j]) / hj
+    a = 0.5 * (w1 - w0)
+    disc = np.sqrt(np.maximum(w0 * w0 + 4 * a * m, 0.))
+    with np.errstate(invalid='ignore', divide='ignore'):
+        t = np.where(np.abs(a) > 1e-12, (disc - w0) / (2 * a), m / w0)
+    return knots[j] + np.clip(t, 0, 1) * hj
+
+
+def draws_for(elements_with_draws, n, seed):
+    """Per-photon pre-drawn randomness keyed by element object.
+
+    ``elements_with_draws`` lists (element, kind) with kind 'scatter' or
+    'order'.  Scatter angles are sigma * N(0, 1); order draws are U[0, 1).
+    """
+    rng = np.random.default_rng(seed + 77)
+    out = {}
+    for elem, kind in elements_with_draws:
+        if kind == 'scatter':
+            out[elem] = {'inplanescatter': elem.inplanescatter * rng.standard_normal(n),
+                         'perpplanescatter': elem.perpplanescatter * rng.standard_normal(n)}
+        else:
+            out[elem] = {'order_u': rng.uniform(0, 1, n)}
+    return out
+
+
+# ---------------------------------------------------------------------------
+# instruments
+# ---------------------------------------------------------------------------
+def efficiency_table(seed, orders, n_energy=64, lo=0.2, hi=2.0, total=1.0):
+    rng = np.random.default_rng(seed + 500)
+    e = np.linspace(lo, hi, n_energy)
+    p = rng.dirichlet(np.ones(len(orders)), size=n_energy) * total
+    # keep every row total <= 1 after rounding (the element protocol rejects
+    # probabilities above 1, marxs/optics/base.py:43-46)
+    while np.any(np.sum(p, axis=1) > total):
+        over = np.sum(p, axis=1) > total
+        p[over] *= (1 - 2 ** -50)
+    return np.column_stack([e, p])
+
+
+def build_c0(ns):
+    lens = ns.PerfectLens(focallength=10000., position=[10000., 0, 0], zoom=[1, 600, 600])
+    rms = ns.RadialMirrorScatter(inplanescatter=ns.angle(5 * ARCSEC),
+                                 perpplanescatter=ns.angle(1 * ARCSEC),
+                                 position=[10000., 0, 0], zoom=[1, 600, 600])
+    det = ns.FlatDetector(zoom=[1, 30, 30], pixsize=0.024)
+    return SimpleNamespace(elements=[lens, rms, det], lens=lens, scatter=rms, detector=det,
+                           draw_slots=[(rms, 'scatter')], aperture_x=10000.)
+
+
+def c1_facet_poses(seed, ny=20, nz=10, pitch=22., x=1500., tilt_deg=0.1):
+    rng = np.random.default_rng(seed + 300)
+    ys = (np.arange(ny) - (ny - 1) / 2) * pitch
+    zs = (np.arange(nz) - (nz - 1) / 2) * pitch
+    yy, zz = np.meshgrid(ys, zs, indexing='ij')
+    positions = [[x, a, b] for a, b in zip(yy.ravel(), zz.ravel())]
+    tilts = rng.normal(0, np.deg2rad(tilt_deg), size=(len(positions), 2))
+    uncert = [geomath.mat2aff(geomath.euler2mat(0., t[0], t[1], 'sxyz')) for t in tilts]
+    return positions, uncert
+
+
+def build_c1(ns, seed=1, efficiency_file=None):
+    front = build_c0(ns)
+    orders = list(range(-10, 3))
+    table = efficiency_table(seed, orders)
+    eff = ns.EfficiencyFile(table if efficiency_file is None else efficiency_file, orders)
+    positions, uncert = c1_facet_poses(seed)
+    gas = ns.Parallel(elem_class=ns.FlatGrating,
+                      elem_args={'d': 2e-4, 'zoom': [1, 10, 10], 'order_selector': eff},
+                      elem_pos={'position': positions}, id_col='facet')
+    gas.elem_uncertainty = uncert
+    gas.generate_elements()
+    det = ns.FlatDetector(zoom=[1, 100, 30], pixsize=0.024, ignore_pixel_warning=True)
+    return SimpleNamespace(elements=[front.lens, front.scatter, gas, det], lens=front.lens,
+                           scatter=front.scatter, gas=gas, detector=det, selector=eff,
+                           efficiency_table=table,
+                           draw_slots=[(front.scatter, 'scatter'), (gas, 'order')],
+                           aperture_x=10000.)
+
+
+class RowlandTorusGeometry:
+    """Torus with symmetry axis y (marxs/design/rowland.py:61-100), identity pose."""
+
+    def __init__(self, R, r):
+        self.R = R
+        self.r = r
+        self.pos4d = np.eye(4)
+
+    def outer_point(self, y, z):
+        """Point of the outer branch at given (y, z), found along x."""
+        rho = self.R + np.sqrt(self.r ** 2 - y ** 2)
+        return np.array([np.sqrt(rho ** 2 - z ** 2), y, z])
+
+    def normal(self, xyz):
+        """Outward unit normal (rowland.py:281-337) on the outer branch."""
+        x, y, z = xyz
+        s = np.sign(np.sqrt(x ** 2 + z ** 2) - self.R)
+        theta = np.arcsin(s * y / self.r) + (s < 0) * np.pi
+        factor = self.R + self.r * np.cos(theta)
+        phi = np.arctan2(z / factor, x / factor)
+        return np.array([np.cos(theta) * np.cos(phi), np.sin(theta), np.cos(theta) * np.sin(phi)])
+
+
+def c2_facet_poses(seed, ny=40, nz=25, pitch=26.5, R=5900., r=5900., jitter_arcsec=30.):
+    """Facet poses on the torus (ElementsOnTorus placement, rowland.py:560-580)."""
+    torus = RowlandTorusGeometry(R, r)
+    ys = (np.arange(ny) - (ny - 1) / 2) * pitch
+    zs = (np.arange(nz) - (nz - 1) / 2) * pitch
+    poses = []
+    for yv in ys:
+        for zv in zs:
+            p = torus.outer_point(yv, zv)
+            nrm = -torus.normal(p)
+            rot = geomath.ex2vec_fix(nrm, np.array([0., 1., 0.]))
+            poses.append(geomath.compose(p, rot, np.ones(3)))
+    rng = np.random.default_rng(seed + 400)
+    ang = rng.normal(0, jitter_arcsec * ARCSEC, size=(len(poses), 3))
+    uncert = [geomath.compose(np.zeros(3), geomath.euler2mat(a[0], a[1], a[2], 'sxyz'), np.ones(3))
+              for a in ang]
+    return poses, uncert, torus
+
+
+def build_c2(ns, seed=2, efficiency_file=None, n_facets=1000):
+    lens = ns.PerfectLens(focallength=12000., position=[12000., 0, 0], zoom=[1, 600, 600])
+    rms = ns.RadialMirrorScatter(inplanescatter=ns.angle(5 * ARCSEC),
+                                 perpplanescatter=ns.angle(1 * ARCSEC),
+                                 position=[12000., 0, 0], zoom=[1, 600, 600])
+    orders = list(range(-12, 3))
+    table = efficiency_table(seed, orders, total=0.8)
+    eff = ns.EfficiencyFile(table if efficiency_file is None else efficiency_file, orders)
+    poses, uncert, torus = c2_facet_poses(seed)
+    poses, uncert = poses[:n_facets], uncert[:n_facets]
+    blaze = geomath.axangle2mat(np.array([0, 0, 1.]), np.deg2rad(1.8))
+    gas = ns.Parallel(elem_class=ns.CATGrating,
+                      elem_args={'d': 2e-4, 'zoom': [1, 12.5, 12.5], 'orientation': blaze,
+                                 'order_selector': eff},
+                      elem_pos=poses, id_col='facet')
+    gas.elem_uncertainty = uncert
+    gas.generate_elements()
+    cyl = ns.Cylinder.from_rowland(torus, 50., rotation=np.pi,
+                                   kwargs={'phi_lim': [-np.pi / 2, np.pi / 2]})
+    det = ns.CircularDetector(geometry=cyl, pixsize=0.024)
+    return SimpleNamespace(elements=[lens, rms, gas, det], lens=lens, scatter=rms, gas=gas,
+                           detector=det, selector=eff, efficiency_table=table,
+                           draw_slots=[(rms, 'scatter'), (gas, 'order')], aperture_x=12000.)
+
+
+def photons_for(config_name, n, seed):
+    if config_name == 'c2':
+        e = piecewise_linear_energies(n, seed)
+        return annulus_photons(n, seed, 12000., energies=e)
+    return annulus_photons(n, seed, 10000.)
+
+
+def build(config_name, ns=None, seed=None):
+    ns = native_namespace() if ns is None else ns
+    if config_name == 'c0':
+        return build_c0(ns)
+    if config_name == 'c1':
+        return build_c1(ns, seed=1 if seed is None else seed)
+    if config_name == 'c2':
+        return build_c2(ns, seed=2 if seed is None else seed)
+    raise ValueError(config_name)

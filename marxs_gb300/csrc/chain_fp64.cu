@@ -1,0 +1,382 @@
+// Fused element-chain kernel, float64 parity mode.
+//
+// One thread carries one photon through every stage of the chain with its
+// state (pos, dir, polarization, energy, probability) in registers: the
+// photon list is read once and written once per call, which is what makes
+// the chain HBM-bound rather than bound by per-element passes as in MARXS
+// (one full-N numpy pass per element, simulator.py:42-49).
+//
+// Stage semantics follow OpticalElement.process_photons (optics/base.py:
+// 149-211): for hits, element columns are written, probability is
+// multiplied (factor checked to lie in [0, 1]), local coordinates and the id
+// are written and pos <- interpos; misses keep their state, and a column the
+// stage creates receives NaN (or -1 for ids) for them.
+//
+// A grating stage (a Parallel of FlatGrating/CATGrating, simulator.py:
+// 206-441) chooses, per photon, the nearest facet the ray crosses: a
+// uniform grid in the array's mean plane yields candidate facets; photons
+// whose slope exceeds the grid's bound are resolved by the whole warp
+// scanning all facets with a warp min-reduction on (k, facet index).
+#include <cuda_runtime.h>
+#include "mgpu_device.cuh"
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr double kEnergy2Wave = 1.2398419292004202e-06;   // marxs/__init__.py:14
+
+__device__ __forceinline__ PlaneHit plane_intersect_frame(const double* f, d3 pos, d3 dir) {
+    return plane_intersect(arr3(f), arr3(f + 3), arr3(f + 6), arr3(f + 9), f[12], f[13], pos, dir);
+}
+
+__device__ __forceinline__ PlaneHit facet_intersect(const mgpu_facet* fc, d3 pos, d3 dir) {
+    return plane_intersect(ldg3(fc->c), ldg3(fc->ex), ldg3(fc->ey), ldg3(fc->ez),
+                           __ldg(&fc->hy), __ldg(&fc->hz), pos, dir);
+}
+
+// order selection: first order whose cumulative probability exceeds u, on
+// the nearest-energy row for EfficiencyFile (grating.py:88-96) or the only
+// row for OrderSelector (np.random.choice, grating.py:51-57)
+__device__ __forceinline__ int select_order(const mgpu_selector& sel, double e, double u,
+                                            double* prob, uint32_t* status) {
+    int row = 0;
+    if (sel.by_energy) {
+        double best = fabs(sel.energy[0] - e);
+        for (int j = 1; j < sel.n_rows; ++j) {
+            double d = fabs(sel.energy[j] - e);
+            if (d < best) {
+                best = d;
+                row = j;
+            }
+        }
+    }
+    const double* cdf = sel.cdf + (int64_t)row * sel.n_orders;
+    int k = 0;
+    while (k < sel.n_orders && !(cdf[k] > u)) ++k;
+    if (k == sel.n_orders) {
+        atomicOr(status, MGPU_STATUS_ORDER_EMPTY);
+        k = sel.n_orders - 1;
+    }
+    *prob = sel.total[row];
+    return sel.orders[k];
+}
+
+struct Photon {
+    d3 pos, dir, pol;
+    double energy, prob;
+};
+
+__device__ __forceinline__ void write_miss_defaults(const mgpu_stage& st, int64_t i, int nout) {
+    for (int k = 0; k < nout; ++k)
+        if ((st.first_writer >> k) & 1) store_col(st.out[k], i, kNaN);
+    if (st.id_out && ((st.first_writer >> 8) & 1)) st.id_out[i * st.id_stride] = -1;
+}
+
+__device__ __forceinline__ void check_prob(double f, uint32_t* status) {
+    if (f < 0.0 || f > 1.0) atomicOr(status, MGPU_STATUS_PROB_RANGE);
+}
+
+// ------------------------------------------------------------------ stages
+__device__ bool stage_lens(const mgpu_stage& st, Photon& ph, int64_t i) {
+    // PerfectLens.specific_process_photons, optics/mirror.py:53-82
+    PlaneHit h = plane_intersect_frame(st.frame, ph.pos, ph.dir);
+    if (!h.hit) {
+        write_miss_defaults(st, i, 2);
+        return false;
+    }
+    d3 c = arr3(st.frame), ez = arr3(st.frame + 9);
+    d3 popt = c - st.p[1] * ez;
+    d3 focus = popt + st.p[0] * normalize3(ph.dir);
+    d3 nd = normalize3(focus - h.ip);
+    ph.pol = parallel_transport_dev(ph.dir, nd, ph.pol);
+    ph.dir = nd;
+    // default reflectivity: probability *= 1
+    store_col(st.out[0], i, h.ly);
+    store_col(st.out[1], i, h.lz);
+    ph.pos = h.ip;
+    return true;
+}
+
+__device__ bool stage_scatter(const mgpu_stage& st, Photon& ph, int64_t i, int rng,
+                              uint64_t seed, int sidx, uint32_t* status) {
+    // RadialMirrorScatter.specific_process_photons, optics/scatter.py:49-77
+    PlaneHit h = plane_intersect_frame(st.frame, ph.pos, ph.dir);
+    if (!h.hit) {
+        write_miss_defaults(st, i, 4);
+        return false;
+    }
+    double sig_in = st.p[0], sig_perp = st.p[1];
+    double a_in = 0.0, a_perp = 0.0;
+    if (rng == MGPU_RNG_PREDRAWN) {
+        if ((sig_in != 0.0 && st.draw[0] == nullptr) || (sig_perp != 0.0 && st.draw[1] == nullptr)) {
+            atomicOr(status, MGPU_STATUS_BAD_STAGE);
+            return false;
+        }
+        if (sig_in != 0.0) a_in = st.draw[0][i * st.draw_stride];
+        if (sig_perp != 0.0) a_perp = st.draw[1][i * st.draw_stride];
+    } else {
+        double n0, n1;
+        philox_normal2(seed, (uint64_t)i, (uint32_t)sidx, 0u, &n0, &n1);
+        a_in = sig_in * n0;
+        a_perp = sig_perp * n1;
+    }
+    d3 center = arr3(st.frame);
+    d3 radial = ph.pos - center;                 // previous position (scatter.py:56)
+    d3 perpplane = cross3(ph.dir, radial);
+    d3 outdir = ph.dir;
+    if (sig_in != 0.0) outdir = rot_transpose_apply(perpplane, a_in, outdir);
+    if (sig_perp != 0.0) outdir = rot_transpose_apply(radial, a_perp, outdir);
+    ph.pol = parallel_transport_dev(ph.dir, outdir, ph.pol);
+    ph.dir = outdir;
+    store_col(st.out[0], i, h.ly);
+    store_col(st.out[1], i, h.lz);
+    store_col(st.out[2], i, a_in);
+    store_col(st.out[3], i, a_perp);
+    ph.pos = h.ip;
+    return true;
+}
+
+__device__ bool stage_flatdet(const mgpu_stage& st, Photon& ph, int64_t i) {
+    // FlatDetector.specific_process_photons, optics/detector.py:72-75
+    PlaneHit h = plane_intersect_frame(st.frame, ph.pos, ph.dir);
+    if (!h.hit) {
+        write_miss_defaults(st, i, 4);
+        return false;
+    }
+    store_col(st.out[0], i, h.ly);
+    store_col(st.out[1], i, h.lz);
+    store_col(st.out[2], i, h.ly / st.p[0] + st.p[1]);
+    store_col(st.out[3], i, h.lz / st.p[0] + st.p[2]);
+    if (st.id_out) st.id_out[i * st.id_stride] = st.id_num;
+    ph.pos = h.ip;
+    return true;
+}
+
+__device__ bool stage_cyldet(const mgpu_stage& st, Photon& ph, int64_t i) {
+    // Cylinder.intersect (math/geometry.py:470-564) + CircularDetector
+    // (optics/detector.py:115-118)
+    CylHit ch = cylinder_intersect_dev(st.cyl, ph.pos, ph.dir);
+    if (!ch.hit) {
+        write_miss_defaults(st, i, 4);
+        return false;
+    }
+    double phi = ch.phi, R = st.cyl[25];
+    d3 gp = ch.ip;
+    double ly = ch.zl;
+    store_col(st.out[0], i, phi);
+    store_col(st.out[1], i, ly);
+    store_col(st.out[2], i, phi * R / st.p[0] + st.p[1]);
+    store_col(st.out[3], i, ly / st.p[0] + st.p[2]);
+    if (st.id_out) st.id_out[i * st.id_stride] = st.id_num;
+    ph.pos = gp;
+    return true;
+}
+
+// candidate search for a grating stage; returns facet index or -1
+__device__ __forceinline__ int nearest_facet_grid(const mgpu_stage& st, const Photon& ph,
+                                                  bool valid, PlaneHit* best_hit,
+                                                  bool* need_brute) {
+    const mgpu_grid& g = st.grid;
+    *need_brute = false;
+    int best = -1;
+    best_hit->k = 0.0;
+    if (!valid) return -1;
+    if (g.cell_start == nullptr) {
+        *need_brute = true;
+        return -1;
+    }
+    d3 rel = ph.pos - arr3(g.o);
+    double dn = dot3(ph.dir, arr3(g.n));
+    double da = dot3(ph.dir, arr3(g.a));
+    double db = dot3(ph.dir, arr3(g.b));
+    if (!(fabs(da) <= g.slope_max * fabs(dn)) || !(fabs(db) <= g.slope_max * fabs(dn)) ||
+        dn == 0.0) {
+        *need_brute = true;
+        return -1;
+    }
+    double t0 = -dot3(rel, arr3(g.n)) / dn;
+    double u = dot3(rel, arr3(g.a)) + t0 * da;
+    double v = dot3(rel, arr3(g.b)) + t0 * db;
+    double fu = floor((u - g.u0) / g.cell);
+    double fv = floor((v - g.v0) / g.cell);
+    if (!(fu >= 0.0 && fu < (double)g.nu && fv >= 0.0 && fv < (double)g.nv)) return -1;
+    int cell = (int)fu * g.nv + (int)fv;
+    int s0 = __ldg(g.cell_start + cell), s1 = min(__ldg(g.cell_start + cell + 1), g.capacity);
+    for (int q = s0; q < s1; ++q) {
+        int f = __ldg(g.cell_items + q);
+        PlaneHit h = facet_intersect(st.facets + f, ph.pos, ph.dir);
+        if (h.hit && (best < 0 || h.k < best_hit->k || (h.k == best_hit->k && f < best))) {
+            best = f;
+            *best_hit = h;
+        }
+    }
+    return best;
+}
+
+__device__ bool stage_gratings(const mgpu_stage& st, Photon& ph, int64_t i, bool valid,
+                               int rng, uint64_t seed, int sidx, uint32_t* status) {
+    PlaneHit h;
+    bool brute;
+    int f = nearest_facet_grid(st, ph, valid, &h, &brute);
+    // photons the grid cannot bound: the warp scans all facets for each of
+    // them, one photon at a time, and min-reduces (k, facet)
+    unsigned bm = __ballot_sync(MGPU_FULL_MASK, brute);
+    const int lane = threadIdx.x & 31;
+    while (bm) {
+        int src = __ffs(bm) - 1;
+        bm &= bm - 1;
+        d3 p{__shfl_sync(MGPU_FULL_MASK, ph.pos.x, src), __shfl_sync(MGPU_FULL_MASK, ph.pos.y, src),
+             __shfl_sync(MGPU_FULL_MASK, ph.pos.z, src)};
+        d3 d{__shfl_sync(MGPU_FULL_MASK, ph.dir.x, src), __shfl_sync(MGPU_FULL_MASK, ph.dir.y, src),
+             __shfl_sync(MGPU_FULL_MASK, ph.dir.z, src)};
+        double bk = 0.0;
+        int bf = -1;
+        for (int q = lane; q < st.n_facets; q += 32) {
+            PlaneHit hq = facet_intersect(st.facets + q, p, d);
+            if (hq.hit && (bf < 0 || hq.k < bk)) {
+                bf = q;
+                bk = hq.k;
+            }
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            double ok = __shfl_xor_sync(MGPU_FULL_MASK, bk, off);
+            int of = __shfl_xor_sync(MGPU_FULL_MASK, bf, off);
+            bool take = (of >= 0) && (bf < 0 || ok < bk || (ok == bk && of < bf));
+            if (take) {
+                bk = ok;
+                bf = of;
+            }
+        }
+        if (lane == src && bf >= 0) {
+            f = bf;
+            h = facet_intersect(st.facets + bf, ph.pos, ph.dir);
+        }
+    }
+    if (!valid) return false;
+    if (f < 0) {
+        write_miss_defaults(st, i, 4);
+        return false;
+    }
+    // FlatGrating.diffract_photons + specific_process_photons (grating.py:233-277)
+    const mgpu_facet* fc = st.facets + f;
+    d3 l = ldg3(fc->l), dn = ldg3(fc->dneg), n = ldg3(fc->ex);
+    d3 p = normalize3(ph.dir);
+    double wave = kEnergy2Wave / ph.energy;
+    d3 pp = normalize3(p - dot3(p, l) * l);
+    double cb = fabs(dot3(pp, n));
+    cb = fmin(fmax(cb, 0.0), 1.0);
+    double blaze = acos(cb);
+    double u;
+    if (rng == MGPU_RNG_PREDRAWN) {
+        if (st.draw[0] == nullptr) {
+            atomicOr(status, MGPU_STATUS_BAD_STAGE);
+            return false;
+        }
+        u = st.draw[0][i * st.draw_stride];
+    } else {
+        double u1;
+        philox_uniform2(seed, (uint64_t)i, (uint32_t)sidx, 0u, &u, &u1);
+    }
+    double selprob;
+    int m = select_order(st.selectors[__ldg(&fc->selector)], ph.energy, u, &selprob, status);
+    check_prob(selprob, status);
+    double pd0 = dot3(p, dn);
+    double sign;
+    if (__ldg(&fc->cat)) {
+        sign = (pd0 > 0.0) ? 1.0 : ((pd0 < 0.0) ? -1.0 : (pd0 == 0.0 ? 1.0 : pd0));
+    } else {
+        sign = -1.0;
+    }
+    double p_d = pd0 + sign * (double)m * wave / __ldg(&fc->dgrat);
+    double p_l = dot3(p, l);
+    double p_n = sqrt(1.0 - p_d * p_d - p_l * p_l);
+    double pn = dot3(p, n);
+    double direction = (pn > 0.0) ? 1.0 : ((pn < 0.0) ? -1.0 : (pn == 0.0 ? 0.0 : pn));
+    if (!__ldg(&fc->transmission)) direction = -direction;
+    d3 nd = p_d * dn + p_l * l + (direction * p_n) * n;
+    ph.pol = parallel_transport_dev(ph.dir, nd, ph.pol);
+    ph.dir = nd;
+    ph.prob = ph.prob * selprob;
+    store_col(st.out[0], i, h.ly);
+    store_col(st.out[1], i, h.lz);
+    store_col(st.out[2], i, (double)m);
+    store_col(st.out[3], i, blaze);
+    if (st.id_out) st.id_out[i * st.id_stride] = __ldg(&fc->id_num);
+    ph.pos = h.ip;
+    return true;
+}
+
+__global__ void __launch_bounds__(kThreads)
+chain_fp64_kernel(const __grid_constant__ mgpu_chain chain, const __grid_constant__ mgpu_photons io) {
+    __shared__ unsigned int s_hits[MGPU_MAX_STAGES];
+    if (threadIdx.x < MGPU_MAX_STAGES) s_hits[threadIdx.x] = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int64_t n = io.n;
+    const int64_t warp_id = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t base = warp_id * 32; base < n; base += n_warps * 32) {
+        const int64_t i = base + lane;
+        const bool valid = i < n;
+        Photon ph;
+        if (valid) {
+            ph.pos = load3(io.pos, i);
+            ph.dir = load3(io.dir, i);
+            ph.pol = load3(io.pol, i);
+            ph.energy = io.energy.ptr[i * io.energy.stride];
+            ph.prob = io.prob.ptr[i * io.prob.stride];
+        } else {
+            ph.pos = ph.dir = ph.pol = d3{0.0, 0.0, 0.0};
+            ph.energy = 1.0;
+            ph.prob = 0.0;
+        }
+        for (int s = 0; s < chain.n_stages; ++s) {
+            const mgpu_stage& st = chain.stages[s];
+            bool hit = false;
+            switch (st.kind) {
+            case MGPU_STAGE_GRATINGS:
+                hit = stage_gratings(st, ph, i, valid, chain.rng, chain.seed, s, chain.status);
+                break;
+            case MGPU_STAGE_LENS:
+                if (valid) hit = stage_lens(st, ph, i);
+                break;
+            case MGPU_STAGE_SCATTER:
+                if (valid) hit = stage_scatter(st, ph, i, chain.rng, chain.seed, s, chain.status);
+                break;
+            case MGPU_STAGE_FLATDET:
+                if (valid) hit = stage_flatdet(st, ph, i);
+                break;
+            case MGPU_STAGE_CYLDET:
+                if (valid) hit = stage_cyldet(st, ph, i);
+                break;
+            default:
+                if (valid) atomicOr(chain.status, MGPU_STATUS_BAD_STAGE);
+            }
+            unsigned m = __ballot_sync(MGPU_FULL_MASK, hit);
+            if (lane == 0 && m) atomicAdd(&s_hits[s], (unsigned)__popc(m));
+        }
+        if (valid) {
+            store3(io.pos_out, i, ph.pos);
+            store3(io.dir_out, i, ph.dir);
+            store3(io.pol_out, i, ph.pol);
+            io.prob_out.ptr[i * io.prob_out.stride] = ph.prob;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < chain.n_stages && s_hits[threadIdx.x])
+        atomicAdd(chain.hits + threadIdx.x, (unsigned long long)s_hits[threadIdx.x]);
+}
+
+}  // namespace
+
+cudaError_t mgpu_launch_chain_fp64(const mgpu_chain& chain, const mgpu_photons& io,
+                                   cudaStream_t stream, int sm_count) {
+    if (io.n <= 0) return cudaSuccess;
+    int64_t warps = (io.n + 31) / 32;
+    int64_t blocks = (warps * 32 + kThreads - 1) / kThreads;
+    int64_t cap = (int64_t)sm_count * 8;
+    if (blocks > cap) blocks = cap;
+    chain_fp64_kernel<<<(unsigned)blocks, kThreads, 0, stream>>>(chain, io);
+    return cudaGetLastError();
+}

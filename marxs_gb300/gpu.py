@@ -1,0 +1,434 @@
+"""``GpuSequence``: the drop-in GPU backend for a MARXS element chain.
+
+``GpuSequence(elements=[...])(photons)`` behaves like
+``marxs.simulator.Sequence(elements=[...])(photons)`` (simulator.py:42-49)
+for the supported element classes: the photon table is modified in place
+and returned, with the reference's output columns, dtypes and NaN / -1
+defaults; a stage that hits no photon adds no columns (optics/base.py:
+176-177).  All per-photon arithmetic runs in the CUDA library; PyTorch only
+allocates device memory and provides the stream.
+
+Randomness: ``rng='predrawn'`` takes per-photon arrays in ``draws``
+(``{element: {'inplanescatter': a, 'perpplanescatter': b}}`` for a
+RadialMirrorScatter, ``{element_or_parallel: {'order_u': u}}`` for a grating
+stage); ``rng='philox'`` draws in-kernel from Philox4x32-10 keyed by
+(seed, photon row, stage index).
+
+``precision='fp64'`` is the parity mode; ``'fp32local'`` runs the ray
+arithmetic in float32 in each element's local frame.
+"""
+import ctypes as C
+
+import numpy as np
+import torch
+
+from . import _abi
+from .lowering import lower_elements, classnames
+
+_PRECISIONS = {'fp64': _abi.FP64, 'fp32local': _abi.FP32LOCAL}
+_RNGS = {'predrawn': _abi.RNG_PREDRAWN, 'philox': _abi.RNG_PHILOX}
+
+
+def _device(device):
+    if device is None:
+        device = torch.device('cuda', torch.cuda.current_device())
+    device = torch.device(device)
+    if device.type != 'cuda':
+        raise ValueError('GpuSequence runs on a CUDA device only')
+    return device
+
+
+def _stream_handle(stream=None):
+    s = torch.cuda.current_stream() if stream is None else stream
+    return C.c_void_p(s.cuda_stream)
+
+
+class DevicePhotons:
+    """Device-resident photon state in structure-of-arrays form.
+
+    ``pos``, ``dir``, ``pol`` are ``(3, N)`` float64 planes; ``energy`` and
+    ``prob`` are ``(N,)`` float64.
+    """
+
+    def __init__(self, n, device=None, empty=False):
+        device = _device(device)
+        self.n = int(n)
+        mk = torch.empty
+        self.pos = mk((3, self.n), dtype=torch.float64, device=device)
+        self.dir = mk((3, self.n), dtype=torch.float64, device=device)
+        self.pol = mk((3, self.n), dtype=torch.float64, device=device)
+        self.energy = mk((self.n,), dtype=torch.float64, device=device)
+        self.prob = mk((self.n,), dtype=torch.float64, device=device)
+
+    @classmethod
+    def from_columns(cls, photons, device=None):
+        """From (N,4) homogeneous ``pos``/``dir``/``polarization`` + 1-d columns."""
+        n = len(photons['energy'])
+        out = cls(n, device)
+        for name, key in (('pos', 'pos'), ('dir', 'dir'), ('pol', 'polarization')):
+            a = np.asarray(photons[key], dtype=np.float64)[:, :3].T
+            getattr(out, name).copy_(torch.from_numpy(np.ascontiguousarray(a)))
+        out.energy.copy_(torch.from_numpy(np.ascontiguousarray(photons['energy'], dtype=np.float64)))
+        out.prob.copy_(torch.from_numpy(np.ascontiguousarray(photons['probability'],
+                                                             dtype=np.float64)))
+        return out
+
+    def abi(self):
+        return (_abi.vec_soa(self.pos), _abi.vec_soa(self.dir), _abi.vec_soa(self.pol),
+                _abi.col(self.energy), _abi.col(self.prob))
+
+    def nbytes(self):
+        return 11 * 8 * self.n
+
+
+class _Instrument:
+    """Device copy of the lowered chain: facet tables, selectors, grids."""
+
+    def __init__(self, stages, device, stream):
+        self.stages = stages
+        self.device = device
+        self.keep = []            # device tensors referenced by raw pointers
+        self.stage_facets = {}
+        self.stage_selectors = {}
+        self.stage_grid = {}
+        lib = _abi.load()
+        status = torch.zeros(1, dtype=torch.int32, device=device)
+        for si, st in enumerate(stages):
+            if st.kind != _abi.STAGE_GRATINGS:
+                continue
+            fac = torch.from_numpy(st.facets.view(np.uint8).copy()).to(device)
+            self.keep.append(fac)
+            self.stage_facets[si] = fac
+            sel_structs = (_abi.MgpuSelector * len(st.selectors))()
+            for k, s in enumerate(st.selectors):
+                e = torch.from_numpy(np.ascontiguousarray(s.energy)).to(device)
+                cdf = torch.from_numpy(np.ascontiguousarray(s.cdf)).to(device)
+                tot = torch.from_numpy(np.ascontiguousarray(s.total)).to(device)
+                ords = torch.from_numpy(np.ascontiguousarray(s.orders, dtype=np.int32)).to(device)
+                self.keep += [e, cdf, tot, ords]
+                sel_structs[k] = _abi.MgpuSelector(s.cdf.shape[0], s.cdf.shape[1],
+                                                   1 if s.by_energy else 0, 0, e.data_ptr(),
+                                                   cdf.data_ptr(), tot.data_ptr(), ords.data_ptr())
+            raw = np.frombuffer(bytes(sel_structs), dtype=np.uint8).copy()
+            sel_dev = torch.from_numpy(raw).to(device)
+            self.keep.append(sel_dev)
+            self.stage_selectors[si] = sel_dev
+            if st.grid is not None:
+                g = st.grid
+                ncell = g['nu'] * g['nv']
+                start = torch.zeros(ncell + 1, dtype=torch.int32, device=device)
+                items = torch.zeros(g['capacity'], dtype=torch.int32, device=device)
+                counts = torch.zeros(ncell + 1, dtype=torch.int32, device=device)
+                self.keep += [start, items]
+                grid = _abi.MgpuGrid()
+                for key in ('o', 'n', 'a', 'b'):
+                    getattr(grid, key)[:] = [float(x) for x in g[key]]
+                grid.u0, grid.v0, grid.cell = g['u0'], g['v0'], g['cell']
+                grid.nu, grid.nv = g['nu'], g['nv']
+                grid.slope_max, grid.margin = g['slope_max'], g['margin']
+                grid.cell_start, grid.cell_items = start.data_ptr(), items.data_ptr()
+                grid.capacity = g['capacity']
+                _abi.check(lib.mgpu_facet_grid_build(fac.data_ptr(), len(st.facets), C.byref(grid),
+                                                     counts.data_ptr(), status.data_ptr(), stream),
+                           'mgpu_facet_grid_build')
+                self.stage_grid[si] = grid
+                self.keep.append(counts)
+        if self.stage_grid:
+            torch.cuda.current_stream().synchronize()
+            code = int(status.item())
+            if code & (_abi.STATUS_GRID_RANGE | _abi.STATUS_GRID_FULL):
+                raise RuntimeError('facet candidate grid build failed (status 0x%x)' % code)
+
+    def fill_stage(self, si, s):
+        st = self.stages[si]
+        s.kind = st.kind
+        s.id_num = st.id_num
+        s.frame[:] = [float(x) for x in st.frame]
+        s.cyl[:] = [float(x) for x in st.cyl]
+        s.p[:] = [float(x) for x in st.p]
+        if st.kind == _abi.STAGE_GRATINGS:
+            s.n_facets = len(st.facets)
+            s.facets = self.stage_facets[si].data_ptr()
+            s.selectors = self.stage_selectors[si].data_ptr()
+            s.n_selectors = len(st.selectors)
+            if si in self.stage_grid:
+                s.grid = self.stage_grid[si]
+
+
+class ColumnPlan:
+    """Which device buffer each stage writes, and who creates each column.
+
+    Mirrors add_output_cols (marxs/base/base.py:249-286): a float column
+    starts as NaN, an id column as -1, unless the table already has it.
+    """
+
+    def __init__(self, stages, existing=()):
+        self.columns = {}      # name -> 'f8' | 'i4'
+        self.first_writer = {} # name -> stage index
+        self.order = []        # reference column creation order, per stage
+        for si, st in enumerate(stages):
+            for name in st.out_names:
+                if name is None:
+                    continue
+                if name not in self.columns:
+                    self.columns[name] = 'f8'
+                    if name not in existing:
+                        self.first_writer[name] = si
+            if st.id_col is not None:
+                if st.id_col not in self.columns:
+                    self.columns[st.id_col] = 'i4'
+                    if st.id_col not in existing:
+                        self.first_writer[st.id_col] = si
+            self.order.append([c for c in st.new_col_order if c is not None])
+
+
+class GpuSequence:
+    """GPU backend for ``Sequence(elements=[...])`` on supported elements."""
+
+    def __init__(self, elements, precision='fp64', rng='predrawn', seed=0, device=None):
+        if precision not in _PRECISIONS:
+            raise ValueError('precision must be one of %s' % list(_PRECISIONS))
+        if rng not in _RNGS:
+            raise ValueError('rng must be one of %s' % list(_RNGS))
+        for e in elements:
+            if not callable(e):
+                from .simulator import SimulationSetupError
+                raise SimulationSetupError('{0} is not callable.'.format(str(e)))
+        self.elements = list(elements)
+        self.precision = precision
+        self.rng = rng
+        self.seed = int(seed)
+        self.device = _device(device)
+        self._inst = None
+        self._key = None
+        self.last_hits = None
+        self.last_status = 0
+
+    # ------------------------------------------------------------ lowering
+    def _raw_key(self):
+        parts = []
+
+        def walk(e):
+            parts.append(id(e))
+            g = getattr(e, 'geometry', None)
+            if g is not None and hasattr(g, 'pos4d'):
+                parts.append(np.asarray(g.pos4d, dtype=float).tobytes())
+            for attr in ('order_selector', 'focallength', 'inplanescatter', 'perpplanescatter',
+                         'pixsize', '_d', 'd_center_optax', 'transmission', 'id_num'):
+                if hasattr(e, attr):
+                    v = getattr(e, attr)
+                    parts.append(id(v) if attr == 'order_selector' else repr(v))
+            for sub in getattr(e, 'elements', []) or []:
+                walk(sub)
+        for e in self.elements:
+            walk(e)
+        return hash(tuple(parts))
+
+    def lower(self, stream=None):
+        key = self._raw_key()
+        if self._inst is None or key != self._key:
+            stages = lower_elements(self.elements)
+            self._inst = _Instrument(stages, self.device, _stream_handle(stream))
+            self._key = key
+        return self._inst
+
+    @property
+    def stages(self):
+        return self.lower().stages
+
+    # ------------------------------------------------------------ launch
+    def _chain(self, inst, plan, bufs, draws_dev, n, status, hits):
+        chain = _abi.MgpuChain()
+        chain.n_stages = len(inst.stages)
+        chain.precision = _PRECISIONS[self.precision]
+        chain.rng = _RNGS[self.rng]
+        chain.seed = self.seed
+        chain.status = status.data_ptr()
+        chain.hits = hits.data_ptr()
+        for si, st in enumerate(inst.stages):
+            s = chain.stages[si]
+            inst.fill_stage(si, s)
+            fw = 0
+            for k, name in enumerate(st.out_names):
+                if name is None:
+                    continue
+                s.out[k] = _abi.col(bufs[name])
+                if plan.first_writer.get(name) == si:
+                    fw |= 1 << k
+            if st.id_col is not None:
+                s.id_out = bufs[st.id_col].data_ptr()
+                s.id_stride = 1
+                if plan.first_writer.get(st.id_col) == si:
+                    fw |= 1 << 8
+            s.first_writer = fw
+            if self.rng == 'predrawn' and st.draw_names:
+                d = draws_dev.get(si)
+                needed = [k for k, name in enumerate(st.draw_names)
+                          if st.kind != _abi.STAGE_SCATTER or st.p[k] != 0.0]
+                if d is None or any(d[k] is None for k in needed):
+                    raise ValueError('rng="predrawn" needs draws %s for %s' % (
+                        [st.draw_names[k] for k in needed], type(st.element).__name__))
+                for k, t in enumerate(d):
+                    if t is not None:
+                        if t.numel() != n:
+                            raise ValueError('draw arrays must hold one value per photon')
+                        s.draw[k] = t.data_ptr()
+                s.draw_stride = 1
+        return chain
+
+    def _draws_to_device(self, inst, draws, n):
+        out = {}
+        if self.rng != 'predrawn':
+            return out
+        draws = draws or {}
+        for si, st in enumerate(inst.stages):
+            if not st.draw_names:
+                continue
+            d = draws.get(st.element)
+            if d is None:
+                continue
+            ts = []
+            for name in st.draw_names:
+                a = d.get(name)
+                if a is None:
+                    ts.append(None)
+                    continue
+                if isinstance(a, torch.Tensor):
+                    t = a.to(self.device, dtype=torch.float64).contiguous()
+                else:
+                    a = np.ascontiguousarray(a, dtype=np.float64)
+                    if a.shape != (n,):
+                        raise ValueError('draw %r must have shape (%d,)' % (name, n))
+                    t = torch.from_numpy(a).to(self.device)
+                ts.append(t)
+            out[si] = ts
+        return out
+
+    def _raise_status(self, code):
+        self.last_status = code
+        if code & _abi.STATUS_PROB_RANGE:
+            raise ValueError('Found probability outside of the 0..1 arange.')
+        if code & _abi.STATUS_ORDER_EMPTY:
+            raise ValueError('order selection: no order has cumulative probability above the draw')
+        if code:
+            raise RuntimeError('GPU raytrace reported status 0x%x' % code)
+
+    # ------------------------------------------------------------ device path
+    def allocate_columns(self, n, existing=()):
+        """Device buffers for every output column of the chain."""
+        inst = self.lower()
+        plan = ColumnPlan(inst.stages, existing)
+        bufs = {}
+        for name, kind in plan.columns.items():
+            dt = torch.float64 if kind == 'f8' else torch.int32
+            bufs[name] = torch.empty(n, dtype=dt, device=self.device)
+        return plan, bufs
+
+    def trace_device(self, inp, out, plan, bufs, draws=None, stream=None, status=None, hits=None):
+        """Trace device-resident photons (asynchronous on ``stream``).
+
+        ``inp``/``out`` are DevicePhotons (may be the same object); ``plan``
+        and ``bufs`` come from ``allocate_columns``.  Returns the device
+        status word and hit counters (read them after synchronising).
+        """
+        inst = self.lower(stream)
+        n = inp.n
+        if status is None:
+            status = torch.zeros(1, dtype=torch.int32, device=self.device)
+        if hits is None:
+            hits = torch.zeros(_abi.MAX_STAGES, dtype=torch.int64, device=self.device)
+        draws_dev = draws if isinstance(draws, dict) and all(isinstance(k, int) for k in draws) \
+            else self._draws_to_device(inst, draws, n)
+        chain = self._chain(inst, plan, bufs, draws_dev, n, status, hits)
+        ph = _abi.MgpuPhotons()
+        ph.n = n
+        ph.pos, ph.dir, ph.pol, ph.energy, ph.prob = inp.abi()
+        ph.pos_out, ph.dir_out, ph.pol_out, _, ph.prob_out = out.abi()
+        lib = _abi.load()
+        _abi.check(lib.mgpu_trace(C.byref(chain), C.byref(ph), _stream_handle(stream)),
+                   'mgpu_trace')
+        return status, hits
+
+    # ------------------------------------------------------------ table path
+    def __call__(self, photons, draws=None):
+        """Trace a photon table (astropy Table, PhotonTable or dict) in place."""
+        if isinstance(photons, dict):
+            from .table import PhotonTable
+            photons = PhotonTable(photons)
+        n = len(photons)
+        inst = self.lower()
+        dev = self.device
+        colnames = list(photons.colnames)
+        pos = np.asarray(photons['pos'], dtype=np.float64)
+        dirs = np.asarray(photons['dir'], dtype=np.float64)
+        pol = np.asarray(photons['polarization'], dtype=np.float64)
+        if pos.shape != (n, 4) or dirs.shape != (n, 4) or pol.shape != (n, 4):
+            raise ValueError('pos, dir and polarization must be (N, 4) homogeneous columns')
+        if n and (not np.all(dirs[:, 3] == 0) or not np.all(pol[:, 3] == 0)):
+            raise ValueError('dir and polarization must be direction vectors (w = 0).')
+        if n and not np.all(pos[:, 3] == 1):
+            raise ValueError('pos must hold points with w = 1.')
+        if n == 0:
+            return photons
+        plan = ColumnPlan(inst.stages, existing=set(colnames))
+        t_pos = torch.from_numpy(np.ascontiguousarray(pos)).to(dev, non_blocking=True)
+        t_dir = torch.from_numpy(np.ascontiguousarray(dirs)).to(dev, non_blocking=True)
+        t_pol = torch.from_numpy(np.ascontiguousarray(pol)).to(dev, non_blocking=True)
+        t_en = torch.from_numpy(np.ascontiguousarray(photons['energy'], dtype=np.float64)).to(dev)
+        t_pr = torch.from_numpy(np.array(photons['probability'], dtype=np.float64)).to(dev)
+        bufs = {}
+        for name, kind in plan.columns.items():
+            if name in colnames:
+                a = np.asarray(photons[name])
+                a = a.astype(np.float64 if kind == 'f8' else np.int32)
+                bufs[name] = torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+            else:
+                dt = torch.float64 if kind == 'f8' else torch.int32
+                bufs[name] = torch.empty(n, dtype=dt, device=dev)
+        status = torch.zeros(1, dtype=torch.int32, device=dev)
+        hits = torch.zeros(_abi.MAX_STAGES, dtype=torch.int64, device=dev)
+        draws_dev = self._draws_to_device(inst, draws, n)
+        chain = self._chain(inst, plan, bufs, draws_dev, n, status, hits)
+        ph = _abi.MgpuPhotons()
+        ph.n = n
+        ph.pos = ph.pos_out = _abi.vec_aos(t_pos)
+        ph.dir = ph.dir_out = _abi.vec_aos(t_dir)
+        ph.pol = ph.pol_out = _abi.vec_aos(t_pol)
+        ph.energy = _abi.col(t_en)
+        ph.prob = ph.prob_out = _abi.col(t_pr)
+        lib = _abi.load()
+        _abi.check(lib.mgpu_trace(C.byref(chain), C.byref(ph), _stream_handle()), 'mgpu_trace')
+        code = int(status.item())           # synchronises
+        hit_counts = hits.cpu().numpy()[:len(inst.stages)]
+        self.last_hits = hit_counts
+        self._raise_status(code)
+        # state columns, in place
+        _write_back(photons, 'pos', t_pos.cpu().numpy())
+        _write_back(photons, 'dir', t_dir.cpu().numpy())
+        _write_back(photons, 'polarization', t_pol.cpu().numpy())
+        _write_back(photons, 'probability', t_pr.cpu().numpy())
+        # stage columns: existing ones updated, new ones created in the
+        # reference's order for stages that hit at least one photon
+        host = {name: b.cpu().numpy() for name, b in bufs.items()}
+        original = set(colnames)
+        for name in plan.columns:
+            if name in original:
+                _write_back(photons, name, host[name])
+        for si, names in enumerate(plan.order):
+            if hit_counts[si] == 0:
+                continue
+            for name in names:
+                if name in colnames:
+                    continue
+                val = host[name]
+                photons[name] = val.astype(np.int64) if plan.columns[name] == 'i4' else val
+                colnames.append(name)
+        return photons
+
+
+def _write_back(photons, name, value):
+    arr = np.asarray(photons[name])
+    if arr.shape == value.shape and arr.flags.writeable and arr.dtype.kind == value.dtype.kind:
+        arr[...] = value
+    else:
+        photons[name] = value.astype(arr.dtype) if arr.shape == value.shape else value

@@ -1,0 +1,325 @@
+"""Lower a MARXS element tree to the GPU chain description (host, numpy).
+
+Works on this package's element classes and on genuine MARXS objects
+alike: elements are recognised by class name (anywhere in the MRO) and
+read through the attributes MARXS itself uses (``geometry.pos4d``,
+``order_selector``, ``_d``, ``focallength`` ...).  Frame vectors are derived
+from ``pos4d`` with the same numpy expressions as Geometry.__getitem__
+(marxs/math/geometry.py:108-160) so the kernels see identical inputs.
+
+Unsupported elements raise ``NotImplementedError``: there is no CPU path.
+"""
+import math
+from dataclasses import dataclass, field
+from typing import Any, List, Optional
+
+import numpy as np
+
+from . import _abi
+
+
+def classnames(obj):
+    return {c.__name__ for c in type(obj).__mro__}
+
+
+def _vec(pos4d, key):
+    if key == 'center':
+        return pos4d[:, 3]
+    val = pos4d[:, {'x': 0, 'y': 1, 'z': 2}[key[-1]]]
+    if key[:2] == 'e_':
+        return val / np.linalg.norm(val)
+    return val
+
+
+def plane_frame(pos4d):
+    """c, e_x, e_y, e_z, |v_y|, |v_z| as used by FinitePlane.intersect."""
+    pos4d = np.asarray(pos4d, dtype=float)
+    f = np.empty(14)
+    f[0:3] = _vec(pos4d, 'center')[:3]
+    f[3:6] = _vec(pos4d, 'e_x')[:3]
+    f[6:9] = _vec(pos4d, 'e_y')[:3]
+    f[9:12] = _vec(pos4d, 'e_z')[:3]
+    f[12] = np.linalg.norm(_vec(pos4d, 'v_y'))
+    f[13] = np.linalg.norm(_vec(pos4d, 'v_z'))
+    return f
+
+
+def _zoom(pos4d):
+    c0, c1, c2 = np.array(pos4d[:3, :3]).T
+    sx = np.sqrt(np.sum(c0 * c0))
+    c0 = c0 / sx
+    c1 = c1 - np.dot(c0, c1) * c0
+    sy = np.sqrt(np.sum(c1 * c1))
+    c1 = c1 / sy
+    c2 = c2 - (np.dot(c0, c2) * c0 + np.dot(c1, c2) * c1)
+    sz = np.sqrt(np.sum(c2 * c2))
+    if np.linalg.det(np.array([c0, c1, c2 / sz]).T) < 0:
+        sx = -sx
+    return np.array([sx, sy, sz])
+
+
+def cylinder_block(geometry):
+    """pos4d rows, inverse rows, zoom_z, R, reduced phi borders (32 doubles)."""
+    pos4d = np.asarray(geometry.pos4d, dtype=float)
+    inv = np.linalg.inv(pos4d)
+    z = _zoom(pos4d)
+    twopi = 2 * np.pi
+    lim = geometry.coos_limits[0]
+    b = np.zeros(32)
+    b[0:12] = pos4d[:3, :].ravel()
+    b[12:24] = inv[:3, :].ravel()
+    b[24] = z[2]
+    b[25] = z[0]
+    b[26] = (twopi + (lim[0] % twopi)) % twopi
+    b[27] = (twopi + (lim[1] % twopi)) % twopi
+    return b
+
+
+@dataclass
+class SelectorSpec:
+    energy: np.ndarray
+    cdf: np.ndarray           # (rows, orders)
+    total: np.ndarray
+    orders: np.ndarray        # int32
+    by_energy: bool
+
+
+def lower_selector(sel):
+    """Tables of an order selector, computed with the reference's numpy ops."""
+    names = classnames(sel)
+    if 'EfficiencyFile' in names:
+        return SelectorSpec(energy=np.asarray(sel.energy, dtype=float),
+                            cdf=np.ascontiguousarray(sel.cumprob, dtype=float),
+                            total=np.asarray(sel.totalprob, dtype=float),
+                            orders=np.asarray(sel.orders).astype(np.int32), by_energy=True)
+    if 'OrderSelector' in names:
+        p_sum = sel.p.sum()
+        p = sel.p / p_sum
+        cdf = p.cumsum()
+        cdf /= cdf[-1]
+        return SelectorSpec(energy=np.zeros(1), cdf=cdf[None, :].copy(),
+                            total=np.array([p_sum], dtype=float),
+                            orders=np.asarray(sel.orderlist).astype(np.int32), by_energy=False)
+    raise NotImplementedError('order selector %s is not supported on the GPU' % type(sel).__name__)
+
+
+@dataclass
+class StageSpec:
+    kind: int
+    element: Any
+    frame: np.ndarray = field(default_factory=lambda: np.zeros(14))
+    cyl: np.ndarray = field(default_factory=lambda: np.zeros(32))
+    p: np.ndarray = field(default_factory=lambda: np.zeros(8))
+    id_num: int = -9
+    out_names: List[Optional[str]] = field(default_factory=lambda: [None] * 4)
+    id_col: Optional[str] = None
+    new_col_order: List[str] = field(default_factory=list)
+    draw_names: List[str] = field(default_factory=list)
+    facets: Optional[np.ndarray] = None
+    selectors: List[SelectorSpec] = field(default_factory=list)
+    grid: Optional[dict] = None
+
+
+def _loc_names(elem):
+    names = getattr(elem, 'loc_coos_name', None)
+    return [None, None] if names is None else list(names)
+
+
+def _grating_facets(gratings, selectors, sel_index):
+    out = np.zeros(len(gratings), dtype=_abi.FACET_DTYPE)
+    for i, g in enumerate(gratings):
+        if callable(g._d):
+            raise NotImplementedError('position-dependent grating constant (callable d) is not '
+                                      'supported on the GPU')
+        if 'blaze_angle_modifier' in type(g).__dict__:
+            raise NotImplementedError('custom blaze_angle_modifier is not supported on the GPU')
+        pos4d = np.asarray(g.geometry.pos4d, dtype=float)
+        fr = plane_frame(pos4d)
+        groove = g.geometry._geometry.get('groove_angle', 0.)
+        # FlatGrating.e_groove_coos on the flat bases (e_y, e_z, e_x)
+        ex4, ey4 = _vec(pos4d, 'e_y'), _vec(pos4d, 'e_z')
+        e_groove = math.sin(-groove) * ex4 + math.cos(-groove) * ey4
+        e_perp = math.cos(-groove) * ex4 - math.sin(-groove) * ey4
+        out['c'][i] = fr[0:3]
+        out['ex'][i] = fr[3:6]
+        out['ey'][i] = fr[6:9]
+        out['ez'][i] = fr[9:12]
+        out['hy'][i] = fr[12]
+        out['hz'][i] = fr[13]
+        out['l'][i] = e_groove[:3]
+        out['dneg'][i] = (-e_perp)[:3]
+        out['dgrat'][i] = float(g._d)
+        out['id_num'][i] = int(g.id_num)
+        key = id(g.order_selector)
+        if key not in sel_index:
+            sel_index[key] = len(selectors)
+            selectors.append(lower_selector(g.order_selector))
+        out['selector'][i] = sel_index[key]
+        out['cat'][i] = 1 if 'CATGrating' in classnames(g) else 0
+        out['transmission'][i] = 1 if g.transmission else 0
+    return out
+
+
+def grid_params(facets, slope_max=0.15, margin=0.05, cells_per_facet=1.0):
+    """Mean plane, extents and cell size of the candidate grid for a facet table.
+
+    The host computes each facet's grown footprint the same way the device
+    builder does; the extents cover all of them (with a 1 mm pad) and the
+    capacity bounds the total number of (cell, facet) entries.
+    """
+    F = len(facets)
+    c = facets['c']
+    nrm = facets['ex'].mean(axis=0)
+    nrm /= np.linalg.norm(nrm)
+    ay = facets['ey'].mean(axis=0)
+    a = ay - np.dot(ay, nrm) * nrm
+    a /= np.linalg.norm(a)
+    b = np.cross(nrm, a)
+    o = c.mean(axis=0)
+    size = 2 * max(facets['hy'].max(), facets['hz'].max())
+    cell = size / cells_per_facet
+    corners = []
+    for sy in (-1, 1):
+        for sz in (-1, 1):
+            corners.append(c + (sy * facets['hy'])[:, None] * facets['ey'] +
+                           (sz * facets['hz'])[:, None] * facets['ez'])
+    corners = np.stack(corners, axis=1) - o           # (F, 4, 3)
+    u = corners @ a
+    v = corners @ b
+    dep = np.abs(corners @ nrm).max(axis=1)
+    grow = dep * slope_max + margin
+    umin, umax = u.min(axis=1) - grow, u.max(axis=1) + grow
+    vmin, vmax = v.min(axis=1) - grow, v.max(axis=1) + grow
+    u0 = umin.min() - 1.0
+    v0 = vmin.min() - 1.0
+    nu = int(np.floor((umax.max() + 1.0 - u0) / cell)) + 1
+    nv = int(np.floor((vmax.max() + 1.0 - v0) / cell)) + 1
+    # host estimate of the entries, with one spare row/column per facet
+    iu0 = np.floor((umin - 1e-6 - u0) / cell)
+    iu1 = np.floor((umax + 1e-6 - u0) / cell)
+    iv0 = np.floor((vmin - 1e-6 - v0) / cell)
+    iv1 = np.floor((vmax + 1e-6 - v0) / cell)
+    capacity = int(np.sum((iu1 - iu0 + 2) * (iv1 - iv0 + 2))) + 16
+    return dict(o=o, n=nrm, a=a, b=b, u0=u0, v0=v0, cell=cell, nu=nu, nv=nv,
+                slope_max=slope_max, margin=margin, capacity=capacity, n_facets=F)
+
+
+def lower_elements(elements):
+    """Flatten a chain into StageSpecs (depth-first through containers)."""
+    stages = []
+    for e in elements:
+        stages.extend(_lower_one(e))
+    if len(stages) > _abi.MAX_STAGES:
+        raise NotImplementedError('chains of more than %d stages' % _abi.MAX_STAGES)
+    return stages
+
+
+def _grating_stage(owner, gratings, id_col):
+    first = gratings[0]
+    for g in gratings:
+        if not ({'FlatGrating', 'CATGrating'} & classnames(g)):
+            raise NotImplementedError('a Parallel mixing %s with gratings' % type(g).__name__)
+    selectors, sel_index = [], {}
+    facets = _grating_facets(gratings, selectors, sel_index)
+    loc = _loc_names(first)
+    order_name = getattr(first, 'order_name', 'order')
+    blaze_name = getattr(first, 'blaze_name', 'blaze')
+    st = StageSpec(kind=_abi.STAGE_GRATINGS, element=owner,
+                   out_names=[loc[0], loc[1], order_name, blaze_name], id_col=id_col,
+                   draw_names=['order_u'], facets=facets, selectors=selectors)
+    st.new_col_order = [order_name, blaze_name] + ([id_col] if id_col else []) + \
+        [n for n in loc if n is not None]
+    if len(gratings) > 1:
+        st.grid = grid_params(facets)
+    return st
+
+
+def _lower_one(e):
+    names = classnames(e)
+    if 'Parallel' in names:
+        id_col = None
+        if e.elements:
+            id_col = getattr(e.elements[0], 'id_col', None)
+        if not e.elements:
+            return []
+        return [_grating_stage(e, list(e.elements), id_col)]
+    if 'FlatGrating' in names:
+        return [_grating_stage(e, [e], getattr(e, 'id_col', None))]
+    if hasattr(e, 'elements') and ({'Sequence', 'BaseContainer'} & names):
+        out = []
+        for sub in e.elements:
+            out.extend(_lower_one(sub))
+        return out
+    if 'PerfectLens' in names:
+        interp = getattr(e, 'reflectivity_interpolator', None)
+        if interp is not None and not (getattr(interp, '__name__', '') == '<lambda>' and
+                                       'marxs' in getattr(interp, '__module__', '')):
+            raise NotImplementedError('PerfectLens reflectivity_interpolator on the GPU')
+        loc = _loc_names(e)
+        st = StageSpec(kind=_abi.STAGE_LENS, element=e, frame=plane_frame(e.geometry.pos4d),
+                       out_names=[loc[0], loc[1], None, None])
+        st.p[0] = float(e.focallength)
+        st.p[1] = float(getattr(e, 'd_center_optax', 0.))
+        st.new_col_order = [n for n in loc if n is not None]
+        return [_with_id(st, e)]
+    if 'RadialMirrorScatter' in names:
+        loc = _loc_names(e)
+        ic = getattr(e, 'inplanescattercol', 'inplanescatter')
+        pc = getattr(e, 'perpplanescattercol', 'perpplanescatter')
+        st = StageSpec(kind=_abi.STAGE_SCATTER, element=e, frame=plane_frame(e.geometry.pos4d),
+                       out_names=[loc[0], loc[1], ic, pc],
+                       draw_names=['inplanescatter', 'perpplanescatter'])
+        st.p[0] = float(e.inplanescatter)
+        st.p[1] = float(e.perpplanescatter)
+        st.new_col_order = [ic, pc] + [n for n in loc if n is not None]
+        return [_with_id(st, e)]
+    if 'FlatDetector' in names:
+        loc = _loc_names(e)
+        dp = list(getattr(e, 'detpix_name', ['detpix_x', 'detpix_y']))
+        st = StageSpec(kind=_abi.STAGE_FLATDET, element=e, frame=plane_frame(e.geometry.pos4d),
+                       out_names=[loc[0], loc[1], dp[0], dp[1]])
+        st.p[0] = float(e.pixsize)
+        st.p[1] = float(e.centerpix[0])
+        st.p[2] = float(e.centerpix[1])
+        st.new_col_order = dp + [n for n in loc if n is not None]
+        return [_with_id(st, e)]
+    if 'CircularDetector' in names:
+        loc = _loc_names(e)
+        dp = list(getattr(e, 'detpix_name', ['detpix_x', 'detpix_y']))
+        st = StageSpec(kind=_abi.STAGE_CYLDET, element=e, cyl=cylinder_block(e.geometry),
+                       out_names=[loc[0], loc[1], dp[0], dp[1]])
+        st.p[0] = float(e.pixsize)
+        st.p[1] = float(e.centerpix[0])
+        st.p[2] = float(e.centerpix[1])
+        st.new_col_order = dp + [n for n in loc if n is not None]
+        return [_with_id(st, e)]
+    raise NotImplementedError('element %s is not supported by the GPU backend' % type(e).__name__)
+
+
+def _with_id(st, e):
+    idc = getattr(e, 'id_col', None)
+    if idc is not None:
+        st.id_col = idc
+        st.id_num = int(getattr(e, 'id_num', -9))
+        # the id column is created right after the element's output columns
+        n_extra = {_abi.STAGE_LENS: 0, _abi.STAGE_SCATTER: 2}.get(st.kind, 2)
+        st.new_col_order.insert(n_extra, idc)
+    return st
+
+
+def fingerprint(stages):
+    """Hash of everything lowered; a change triggers a re-upload."""
+    import hashlib
+    h = hashlib.sha1()
+    for st in stages:
+        h.update(np.asarray([st.kind, st.id_num], dtype=np.int64).tobytes())
+        h.update(st.frame.tobytes())
+        h.update(st.cyl.tobytes())
+        h.update(st.p.tobytes())
+        h.update(repr((st.out_names, st.id_col)).encode())
+        if st.facets is not None:
+            h.update(st.facets.tobytes())
+        for s in st.selectors:
+            for a in (s.energy, s.cdf, s.total, s.orders):
+                h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()

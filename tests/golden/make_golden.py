@@ -1,0 +1,202 @@
+"""Generate golden raytrace vectors by running the MARXS reference itself.
+
+Run from the repository root (needs the reference source tree, see
+``reference_loader.py``)::
+
+    python tests/golden/make_golden.py
+
+For each workload (c0, c1, c2) this builds the instrument from the
+reference's own classes, traces a small seeded photon list through the
+reference's ``Sequence`` with numpy's global RNG seeded, and records every
+random draw the reference makes.  The draws are mapped back to photons
+(element call order, photon row order within each call), giving per-photon
+arrays that the oracle and the GPU kernels consume in pre-drawn mode.
+
+Outputs ``tests/golden/<config>.npz`` with: input columns (``in_*``),
+per-photon draws (``draw_*``), every output column (``out_*``), the facet
+poses the reference generated, and the count of photons that crossed more
+than one facet (excluded from parity).
+"""
+import io
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, HERE)
+sys.path.insert(0, ROOT)
+
+import reference_loader  # noqa: E402
+from marxs_gb300 import configs  # noqa: E402
+
+N_PHOTONS = {'c0': 2000, 'c1': 3000, 'c2': 3000}
+GLOBAL_SEED = 20261203
+
+
+class Recorder:
+    """Wraps numpy's global-RNG functions the reference calls and logs draws
+    against the element call that is running."""
+
+    def __init__(self):
+        self.calls = []          # list of (element, intersect mask, [draw arrays])
+        self.current = None
+        self._orig = {}
+
+    def install(self):
+        rnd = np.random
+        self._orig = {'normal': rnd.normal, 'choice': rnd.choice, 'rand': rnd.rand}
+        orig = self._orig
+        rec = self
+
+        def normal(loc=0.0, scale=1.0, size=None):
+            v = orig['normal'](loc, scale, size)
+            rec.current[2].append(('normal', np.array(v, copy=True)))
+            return v
+
+        def choice(a, size=None, replace=True, p=None):
+            # legacy RandomState.choice with p: one uniform per draw and
+            # cdf.searchsorted(u, side='right'); checked against numpy below
+            p = np.asarray(p, dtype=float)
+            cdf = p.cumsum()
+            cdf /= cdf[-1]
+            u = np.random.random_sample(size)
+            idx = cdf.searchsorted(u, side='right')
+            rec.current[2].append(('uniform', np.array(u, copy=True)))
+            return np.asarray(a)[idx]
+
+        def rand(*args):
+            v = orig['rand'](*args)
+            rec.current[2].append(('uniform', np.atleast_1d(np.array(v, copy=True))))
+            return v
+
+        rnd.normal, rnd.choice, rnd.rand = normal, choice, rand
+
+    def uninstall(self):
+        for k, v in self._orig.items():
+            setattr(np.random, k, v)
+
+    def wrap(self, elem):
+        orig = elem.specific_process_photons
+        rec = self
+
+        def wrapped(photons, intersect, interpos, intercoos):
+            rec.current = (elem, np.array(intersect, copy=True), [])
+            out = orig(photons, intersect, interpos, intercoos)
+            rec.calls.append(rec.current)
+            rec.current = None
+            return out
+        elem.specific_process_photons = wrapped
+
+
+def check_choice_restatement():
+    """The recorded choice() must equal numpy's legacy implementation."""
+    p = np.array([0.1, 0.05, 0.3, 0.2, 0.35])
+    np.random.seed(5)
+    a = np.random.choice(np.arange(5), size=1000, p=p)
+    np.random.seed(5)
+    cdf = p.cumsum()
+    cdf /= cdf[-1]
+    b = cdf.searchsorted(np.random.random_sample(1000), side='right')
+    assert np.array_equal(a, b)
+
+
+def reference_namespace(marxs):
+    import astropy.units as u
+    from types import SimpleNamespace
+    from marxs.optics import (PerfectLens, RadialMirrorScatter, FlatDetector, CircularDetector,
+                              FlatGrating, CATGrating, OrderSelector, EfficiencyFile)
+    from marxs.math.geometry import Cylinder
+    from marxs.simulator import Parallel, Sequence
+
+    def eff(table, orders):
+        if isinstance(table, np.ndarray):
+            buf = io.StringIO()
+            np.savetxt(buf, table, fmt='%.17g')
+            buf.seek(0)
+            return EfficiencyFile(buf, orders)
+        return EfficiencyFile(table, orders)
+
+    return SimpleNamespace(PerfectLens=PerfectLens, RadialMirrorScatter=RadialMirrorScatter,
+                           FlatDetector=FlatDetector, CircularDetector=CircularDetector,
+                           FlatGrating=FlatGrating, CATGrating=CATGrating,
+                           OrderSelector=OrderSelector, EfficiencyFile=eff, Cylinder=Cylinder,
+                           Parallel=Parallel, Sequence=Sequence, angle=lambda r: r * u.rad)
+
+
+def leaves(elements):
+    out = []
+    for e in elements:
+        if hasattr(e, 'elements'):
+            out.extend(leaves(e.elements))
+        else:
+            out.append(e)
+    return out
+
+
+def generate(name):
+    marxs = reference_loader.load()
+    from astropy.table import Table
+    ns = reference_namespace(marxs)
+    inst = configs.build(name, ns)
+    n = N_PHOTONS[name]
+    ph = configs.photons_for(name, n, seed={'c0': 0, 'c1': 1, 'c2': 2}[name])
+    table = Table({k: v.copy() for k, v in ph.items()})
+
+    rec = Recorder()
+    for e in leaves(inst.elements):
+        rec.wrap(e)
+    seq = ns.Sequence(elements=inst.elements)
+    np.random.seed(GLOBAL_SEED + hash(name) % 1000)
+    rec.install()
+    try:
+        out = seq(table)
+    finally:
+        rec.uninstall()
+
+    # map recorded draws to per-photon arrays
+    draw = {'inplanescatter': np.zeros(n), 'perpplanescatter': np.zeros(n),
+            'order_u': np.full(n, np.nan)}
+    seen = np.zeros(n, dtype=int)
+    for elem, mask, logged in rec.calls:
+        rows = np.nonzero(mask)[0]
+        cname = type(elem).__name__
+        if cname == 'RadialMirrorScatter':
+            kinds = [k for k, _ in logged]
+            vals = [v for _, v in logged]
+            j = 0
+            if elem.inplanescatter != 0:
+                assert kinds[j] == 'normal'
+                draw['inplanescatter'][rows] = vals[j]
+                j += 1
+            if elem.perpplanescatter != 0:
+                assert kinds[j] == 'normal'
+                draw['perpplanescatter'][rows] = vals[j]
+        elif cname in ('FlatGrating', 'CATGrating'):
+            u = np.concatenate([v for k, v in logged if k == 'uniform'])
+            assert len(u) == len(rows)
+            draw['order_u'][rows] = u
+            seen[rows] += 1
+        else:
+            assert not logged, cname
+    multi = seen > 1
+    res = {'n': n, 'multi_hit': multi}
+    for k, v in ph.items():
+        res['in_' + k] = v
+    for k, v in draw.items():
+        res['draw_' + k] = v
+    for k in out.colnames:
+        res['out_' + k] = np.asarray(out[k])
+    if hasattr(inst, 'gas'):
+        res['facet_pos4d'] = np.array([e.geometry.pos4d for e in inst.gas.elements])
+    res['colnames'] = np.array(out.colnames)
+    np.savez_compressed(os.path.join(HERE, name + '.npz'), **res)
+    print(name, 'n=%d' % n, 'columns:', out.colnames, 'multi-hit:', int(multi.sum()))
+    return res
+
+
+if __name__ == '__main__':
+    check_choice_restatement()
+    for name in sys.argv[1:] or ['c0', 'c1', 'c2']:
+        generate(name)

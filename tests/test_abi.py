@@ -1,0 +1,91 @@
+"""The C ABI: header layout agrees with the ctypes mirror; the library loads
+and exports every entry point the header declares (no GPU needed)."""
+import ctypes
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from marxs_gb300 import _abi
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, 'include', 'marxs_gb300.h')
+
+STRUCTS = {
+    'mgpu_col': _abi.MgpuCol, 'mgpu_vec': _abi.MgpuVec, 'mgpu_photons': _abi.MgpuPhotons,
+    'mgpu_selector': _abi.MgpuSelector, 'mgpu_grid': _abi.MgpuGrid,
+    'mgpu_stage': _abi.MgpuStage, 'mgpu_chain': _abi.MgpuChain,
+}
+
+
+def _c_layout(tmp_path):
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "%s"' % HEADER,
+             'int main(void) {']
+    for cname, cls in STRUCTS.items():
+        lines.append('printf("%s size %%zu\\n", sizeof(%s));' % (cname, cname))
+        for fname, _ in cls._fields_:
+            lines.append('printf("%s.%s %%zu\\n", offsetof(%s, %s));' % (cname, fname, cname, fname))
+    lines.append('printf("mgpu_facet size %zu\\n", sizeof(mgpu_facet));')
+    for fname in _abi.FACET_DTYPE.names:
+        lines.append('printf("mgpu_facet.%s %%zu\\n", offsetof(mgpu_facet, %s));' % (fname, fname))
+    lines.append('return 0; }')
+    src = tmp_path / 'layout.c'
+    src.write_text('\n'.join(lines))
+    exe = tmp_path / 'layout'
+    subprocess.run(['gcc', '-std=c99', str(src), '-o', str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout
+    return dict((k, int(v)) for k, v in (line.rsplit(' ', 1) for line in out.strip().splitlines()))
+
+
+def test_struct_layout_matches_header(tmp_path):
+    c = _c_layout(tmp_path)
+    for cname, cls in STRUCTS.items():
+        assert c[cname + ' size'] == ctypes.sizeof(cls), cname
+        for fname, _ in cls._fields_:
+            assert c[cname + '.' + fname] == getattr(cls, fname).offset, (cname, fname)
+    assert c['mgpu_facet size'] == _abi.FACET_DTYPE.itemsize
+    for fname in _abi.FACET_DTYPE.names:
+        assert c['mgpu_facet.' + fname] == _abi.FACET_DTYPE.fields[fname][1], fname
+
+
+def test_header_constants_match():
+    text = open(HEADER).read()
+    consts = dict(re.findall(r'#define (MGPU_\w+)\s+(0x[0-9a-fA-F]+|\d+)', text))
+    assert int(consts['MGPU_ABI_VERSION']) == _abi.MGPU_ABI_VERSION
+    assert int(consts['MGPU_MAX_STAGES']) == _abi.MAX_STAGES
+    assert int(consts['MGPU_MAX_OUT']) == _abi.MAX_OUT
+    for name in ('PROB_RANGE', 'ORDER_EMPTY', 'BAD_STAGE', 'GRID_RANGE', 'GRID_FULL'):
+        assert int(consts['MGPU_STATUS_' + name].rstrip('u'), 16) == getattr(_abi, 'STATUS_' + name)
+    for name in ('LENS', 'SCATTER', 'FLATDET', 'GRATINGS', 'CYLDET'):
+        assert int(consts['MGPU_STAGE_' + name]) == getattr(_abi, 'STAGE_' + name)
+
+
+def _declared_functions():
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r'^\w[\w\s\*]*?\b(mgpu_\w+)\s*\(', text, re.M)))
+
+
+def test_library_exports_every_declared_symbol():
+    if not os.path.exists(_abi.LIB_PATH):
+        pytest.skip('library not built')
+    lib = ctypes.CDLL(_abi.LIB_PATH)
+    declared = _declared_functions()
+    assert declared, 'no functions parsed from header'
+    for name in declared:
+        assert hasattr(lib, name), name
+    assert set(declared) == set(_abi.SIGNATURES), 'ctypes signatures out of sync with header'
+
+
+def test_load_binds_signatures_without_gpu():
+    if not os.path.exists(_abi.LIB_PATH):
+        pytest.skip('library not built')
+    lib = _abi.load()
+    assert lib.mgpu_abi_version() == _abi.MGPU_ABI_VERSION
+
+
+def test_facet_dtype_is_packed_like_c():
+    assert _abi.FACET_DTYPE.itemsize % 8 == 0
+    a = np.zeros(3, _abi.FACET_DTYPE)
+    assert a.nbytes == 3 * _abi.FACET_DTYPE.itemsize
