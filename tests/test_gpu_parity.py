@@ -42,19 +42,48 @@ def _run_gpu(name, precision='fp64'):
     return g, out
 
 
+def _column_report(out, ref, ok):
+    """Per-column (passed, worst relative error) against the golden outputs."""
+    report = {}
+    for col, b in ref.items():
+        a = np.asarray(out[col])
+        if a.dtype != b.dtype:
+            report[col] = (False, 'dtype %s vs %s' % (a.dtype, b.dtype))
+            continue
+        if col in ('facet', 'order'):
+            same = np.array_equal(a[ok], b[ok], equal_nan=True)
+            report[col] = (same, int(np.sum(~((a[ok] == b[ok]) | (np.isnan(a[ok].astype(float)) &
+                                                                 np.isnan(b[ok].astype(float)))))))
+            continue
+        fin = ~np.isnan(b[ok])
+        nan_ok = np.array_equal(np.isnan(a[ok]), np.isnan(b[ok]))
+        scale = SCALES[col]
+        err = np.abs(a[ok][fin] - b[ok][fin]) / np.maximum(np.abs(b[ok][fin]), scale)
+        worst = float(err.max()) if err.size else 0.0
+        passed = nan_ok and close_rel(a[ok], b[ok], RTOL, scale)
+        if col == 'blaze':
+            # arccos is ill-conditioned near normal incidence: an ulp in the
+            # cosine moves the angle by up to sqrt(2 * 2.2e-16) ~ 2e-8 rad
+            d = np.abs(a[ok][fin] - b[ok][fin])
+            passed = nan_ok and bool(np.all(d <= RTOL * np.maximum(np.abs(b[ok][fin]), scale)
+                                            + BLAZE_ABS))
+            worst = float(d.max()) if d.size else 0.0
+        report[col] = (passed, worst if nan_ok else 'NaN pattern differs')
+    return report
+
+
+BLAZE_ABS = 5e-8
+
+
 @pytest.mark.parametrize('name', ['c0', 'c1', 'c2'])
 def test_golden_parity_fp64(name):
     g, out = _run_gpu(name)
     ref = golden_outputs(g)
     assert list(out.colnames) == [str(c) for c in g['colnames']]
     ok = ~g['multi_hit']
-    for col, b in ref.items():
-        a = np.asarray(out[col])
-        assert a.dtype == b.dtype, col
-        if col in ('facet', 'order'):
-            assert np.array_equal(a[ok], b[ok], equal_nan=True), col
-        else:
-            assert close_rel(a[ok], b[ok], RTOL, SCALES[col]), col
+    report = _column_report(out, ref, ok)
+    bad = {k: v for k, v in report.items() if not v[0]}
+    assert not bad, 'columns out of tolerance: %s (all: %s)' % (bad, report)
 
 
 @pytest.mark.parametrize('name', ['c1', 'c2'])
