@@ -1,0 +1,350 @@
+#!/usr/bin/env python
+"""Photon-raytrace throughput of the GB300 backend on the CAT-grating workload.
+
+Workload (one "step" = one pass of the element chain over one batch):
+1e8 photons per GPU through a PerfectLens (f = 12 m), RadialMirrorScatter
+(5", 1"), a Parallel of 1000 CATGrating facets on a Rowland torus
+(R = r = 5900 mm, EfficiencyFile-style 64 x 15 order table, nearest-hit grid
+lookup) and a CircularDetector (R = 5900 mm); Philox in-kernel randomness.
+Photons are synthetic (seeded annulus aperture, piecewise-linear spectrum).
+
+Usage: ``python bench.py [--gpus N --steps K --warmup W --impl native|reference]``.
+Prints one JSON line on rank 0.  ``value`` is device-resident throughput
+(inputs already in HBM); ``e2e`` is the same metric through the public
+``GpuSequence(...)(table)`` call with pinned host buffers, host<->device
+copies included.  ``--impl reference`` times the CPU oracle (the reference
+algorithm restated in numpy) on all host cores on a bounded sample.
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = 'photons/s at 1e8 (FP32-local vs FP64); adjoint grads/s vs finite-diff; µm err'
+UNIT = 'photons/s'
+WORKLOAD = 'cat_rowland_1000facets_circular_detector'
+
+# DRAM bytes per photon of the chain kernel, from the ncu capture summarised in
+# profiles/chain_fp64_c2.md (None until a capture exists for the mode)
+NCU_TRAFFIC_BYTES_PER_PHOTON = {'fp64': None, 'fp32local': None}
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument('--gpus', type=int, default=1)
+    p.add_argument('--steps', type=int, default=10)
+    p.add_argument('--warmup', type=int, default=3)
+    p.add_argument('--impl', default='native', choices=['native', 'reference'])
+    p.add_argument('--photons', type=float, default=1e8, help='photons per GPU per step')
+    p.add_argument('--precision', default='auto', choices=['auto', 'fp64', 'fp32local'])
+    p.add_argument('--no-e2e', action='store_true')
+    p.add_argument('--no-cpu', action='store_true')
+    p.add_argument('--e2e-steps', type=int, default=3)
+    return p.parse_args()
+
+
+def peaks():
+    path = os.path.join(ROOT, 'MEASURED_PEAKS.json')
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d['hbm_gbs']), 'measured'
+    except (OSError, KeyError, ValueError):
+        return 6800.0, 'fallback'
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+              'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+              'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join('/tmp', 'mgpu_clocks_%d_%d.csv' % (os.getpid(), index))
+
+    def start(self):
+        try:
+            self.f = open(self.path, 'w')
+            self.proc = subprocess.Popen(['nvidia-smi', '-i', str(self.index),
+                                          '--query-gpu=' + self.FIELDS, '--format=csv,noheader',
+                                          '-lms', '100'], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['nvidia-smi unavailable']}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.f.close()
+        sm, mx, reasons = [], [], set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(',')]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1].split()[0]))
+                    mx.append(float(parts[2].split()[0]))
+                except ValueError:
+                    continue
+                for name, val in zip(names, parts[5:9]):
+                    if val.lower().startswith('active'):
+                        reasons.add(name)
+        os.unlink(self.path)
+        sm.sort()
+        return {'sm_mhz': sm[len(sm) // 2] if sm else None, 'sm_max_mhz': max(mx) if mx else None,
+                'reasons': sorted(reasons), 'samples': len(sm)}
+
+
+# ---------------------------------------------------------------- CPU legs
+def _oracle_chunk(args):
+    n, seed, row0 = args
+    sys.path.insert(0, ROOT)
+    from marxs_gb300 import configs
+    from oracle.raytrace import run_sequence
+    inst = configs.build('c2')
+    ph = configs.photons_for('c2', n, seed=seed)
+    dr = configs.draws_for(inst.draw_slots, n, seed=seed)
+    t = time.perf_counter()
+    run_sequence(inst.elements, ph, dr)
+    return time.perf_counter() - t
+
+
+def cpu_baseline_single(target_s=12.0):
+    """Single-process oracle on a bounded C2 sample (rank 0, N = 1)."""
+    t_small = _oracle_chunk((4000, 101, 0))
+    n = int(min(200000, max(4000, 4000 * target_s / max(t_small, 1e-3))))
+    dt = _oracle_chunk((n, 102, 0))
+    return {'value': n / dt, 'unit': UNIT, 'cores': 1, 'kind': 'port',
+            'sample': '%d photons of the same workload (1000 facets), one process, '
+                      'float64 numpy oracle with pre-drawn randomness' % n}
+
+
+def run_reference(args):
+    """--impl reference: the CPU oracle on all host cores, bounded sample per step."""
+    import multiprocessing as mp
+    rank = int(os.environ.get('RANK', '0'))
+    if rank != 0:
+        return 0
+    cores = len(os.sched_getaffinity(0))
+    per_worker = 30000
+    ctx = mp.get_context('spawn')
+    with ctx.Pool(cores) as pool:
+        pool.map(_oracle_chunk, [(200, 1, 0)] * cores)      # import + set-up
+        times = []
+        for step in range(args.warmup + args.steps):
+            jobs = [(per_worker, 1000 + step * cores + w, w) for w in range(cores)]
+            t = time.perf_counter()
+            pool.map(_oracle_chunk, jobs)
+            dt = time.perf_counter() - t
+            if step >= args.warmup:
+                times.append(dt)
+    step_s = sum(times) / len(times)
+    value = per_worker * cores / step_s
+    line = {'metric': METRIC, 'value': value, 'unit': UNIT, 'impl': 'reference',
+            'n_gpus': args.gpus, 'steps': args.steps, 'warmup': args.warmup,
+            'ms_per_step': step_s * 1e3, 'higher_is_better': True, 'scaling': 'weak',
+            'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic',
+            'config': {'workload': WORKLOAD, 'photons_per_step': per_worker * cores,
+                       'n_facets': 1000},
+            'cpu_baseline': {'value': value, 'unit': UNIT, 'cores': cores, 'kind': 'port',
+                             'sample': '%d photons per step (%d per process) of the same '
+                                       'workload, float64 numpy oracle' % (per_worker * cores,
+                                                                            per_worker)},
+            'e2e': {'value': value, 'unit': UNIT, 'h2d_bytes_per_step': 0,
+                    'd2h_bytes_per_step': 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------- GPU leg
+def algorithmic_bytes(seq):
+    """Bytes per photon: input state read once (pos, dir, pol 3x8 each,
+    energy 8, probability 8 = 88), final state written once (pos, dir, pol,
+    probability = 80), every stage column written once at its dtype."""
+    cols, draws = seq.column_bytes()
+    return 88 + 80 + cols + draws
+
+
+def main():
+    args = parse()
+    if args.impl == 'reference':
+        return run_reference(args)
+    import numpy as np
+    import torch
+    from marxs_gb300 import configs
+    from marxs_gb300.gpu import GpuSequence, DevicePhotons, pinned_photons
+    from marxs_gb300 import _abi
+
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group('nccl', device_id=torch.device('cuda', local))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    n = int(args.photons)
+    inst = configs.build('c2')
+    host = configs.photons_for('c2', n, seed=2 + 7919 * rank)
+    dev_in = DevicePhotons.from_columns(host)
+    dev_out = DevicePhotons(n)
+    row_base = rank * n
+
+    modes = []
+    if args.precision in ('auto', 'fp32local'):
+        modes.append('fp32local')
+    if args.precision in ('auto', 'fp64'):
+        modes.append('fp64')
+
+    results = {}
+    for mode in modes:
+        seq = GpuSequence(elements=inst.elements, precision=mode, rng='philox', seed=12345)
+        plan, bufs = seq.allocate_columns(n)
+        status = torch.zeros(1, dtype=torch.int32, device='cuda')
+        hits = torch.zeros(_abi.MAX_STAGES, dtype=torch.int64, device='cuda')
+        try:
+            seq.trace_device(dev_in, dev_out, plan, bufs, status=status, hits=hits,
+                             row_base=row_base)
+            torch.cuda.synchronize()
+        except RuntimeError as exc:
+            if args.precision == 'auto':
+                results[mode] = {'error': str(exc)}
+                continue
+            raise
+        stream = torch.cuda.current_stream()
+        for _ in range(args.warmup):
+            seq.trace_device(dev_in, dev_out, plan, bufs, status=status, hits=hits,
+                             row_base=row_base)
+        barrier()
+        clocks = ClockSampler(local)
+        clocks.start()
+        time.sleep(0.3)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(args.steps)]
+        barrier()
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            ev[k][0].record(stream)
+            seq.trace_device(dev_in, dev_out, plan, bufs, status=status, hits=hits,
+                             row_base=row_base)
+            ev[k][1].record(stream)
+        barrier()
+        wall = time.perf_counter() - t0
+        ck = clocks.stop()
+        code = int(status.item())
+        if code:
+            raise RuntimeError('kernel status 0x%x' % code)
+        step_ms = [a.elapsed_time(b) for a, b in ev]
+        mean_ms = sum(step_ms) / len(step_ms)
+        tot_ms = wall * 1e3
+        if dist is not None:
+            t = torch.tensor([tot_ms, mean_ms], device='cuda', dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            tot_ms, mean_ms = t.tolist()
+        results[mode] = {'seq': seq, 'plan': plan, 'bufs': bufs, 'mean_ms': mean_ms,
+                         'wall_ms': tot_ms, 'clocks': ck,
+                         'photons_per_s': world * n * args.steps / (tot_ms / 1e3),
+                         'kernel_photons_per_s': n / (mean_ms / 1e3),
+                         'hits': hits.cpu().tolist()}
+
+    ok_modes = [m for m in modes if 'seq' in results.get(m, {})]
+    head = ok_modes[0]
+    r = results[head]
+    seq = r['seq']
+    hbm, hbm_src = peaks()
+    B = algorithmic_bytes(seq)
+    achieved = B * n / (r['mean_ms'] / 1e3) / 1e9
+    traffic = NCU_TRAFFIC_BYTES_PER_PHOTON.get(head)
+    line = {
+        'metric': METRIC, 'value': r['photons_per_s'], 'unit': UNIT, 'n_gpus': world,
+        'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': r['wall_ms'] / args.steps,
+        'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64',
+        'data': 'synthetic (seeded annulus aperture, piecewise-linear spectrum, seeded '
+                'facet jitter)',
+        'config': {'workload': WORKLOAD, 'photons_per_gpu': n, 'n_facets': len(inst.gas.elements),
+                   'precision': head, 'rng': 'philox', 'layout': 'SoA float64 planes',
+                   'l2': 'inputs (%.1f GB) larger than L2 (129 MB)' % (dev_in.nbytes() / 1e9)},
+        'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': hbm, 'unit': 'GB/s',
+                     'frac': achieved / hbm, 'peak_source': hbm_src,
+                     'bytes_per_photon': B,
+                     'traffic': None if traffic is None else traffic * n,
+                     'kernel': 'chain_%s_kernel' % head},
+        'gpu_launches': args.steps,
+        'clocks': r['clocks'],
+    }
+    for m in modes:
+        rr = results.get(m, {})
+        if 'seq' in rr:
+            line['%s_photons_per_s' % m] = rr['photons_per_s']
+            line['%s_ms_per_step' % m] = rr['mean_ms']
+        elif rr:
+            line['%s_error' % m] = rr.get('error')
+    if 'fp32local' in ok_modes and 'fp64' in ok_modes:
+        line['fp32local_over_fp64'] = (results['fp32local']['photons_per_s'] /
+                                       results['fp64']['photons_per_s'])
+
+    # end to end through the public table call, pinned host buffers
+    if not args.no_e2e:
+        e2e_n = n
+        pristine = pinned_photons(e2e_n)
+        for k in pristine.colnames:
+            np.copyto(pristine[k], host[k][:e2e_n])
+        work = pinned_photons(e2e_n)
+        seq_e = GpuSequence(elements=inst.elements, precision=head, rng='philox', seed=12345)
+        times = []
+        h2d = d2h = 0
+        for step in range(1 + args.e2e_steps):
+            for k in pristine.colnames:
+                torch.from_numpy(work[k]).copy_(torch.from_numpy(pristine[k]))
+            for k in list(work.colnames):
+                if k not in pristine.colnames:
+                    work.remove_column(k)
+            barrier()
+            t = time.perf_counter()
+            seq_e(work, row_base=row_base)
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t
+            if step > 0:
+                times.append(dt)
+        h2d = sum(work[k].nbytes for k in pristine.colnames)
+        d2h = sum(work[k].nbytes for k in work.colnames if k not in ('energy',))
+        e2e_s = sum(times) / len(times)
+        if dist is not None:
+            t = torch.tensor([e2e_s], device='cuda', dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_s = t.item()
+        line['e2e'] = {'value': world * e2e_n / e2e_s, 'unit': UNIT, 'h2d_bytes_per_step': h2d,
+                       'd2h_bytes_per_step': d2h, 'ms_per_step': e2e_s * 1e3,
+                       'api': 'GpuSequence(elements)(PhotonTable) with pinned host columns'}
+    if rank == 0 and world == 1 and not args.no_cpu:
+        line['cpu_baseline'] = cpu_baseline_single()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == '__main__':
+    sys.exit(main())

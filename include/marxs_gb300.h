@@ -47,7 +47,7 @@ extern "C" {
 
 /* randomness */
 #define MGPU_RNG_PREDRAWN 0  /* per-photon arrays supplied by the caller */
-#define MGPU_RNG_PHILOX   1  /* Philox4x32-10 keyed by (seed, photon row, stage, draw) */
+#define MGPU_RNG_PHILOX   1  /* Philox4x32-10 keyed by (seed, row_base + row, stage, draw) */
 
 /* stage kinds */
 #define MGPU_STAGE_LENS     1  /* PerfectLens, optics/mirror.py:53-82 */
@@ -125,14 +125,15 @@ typedef struct {
     int32_t kind;
     int32_t id_num;              /* id value for single elements (unused: -9) */
     int32_t first_writer;        /* bit k: out[k] is new -> write NaN on miss;
-                                    bit 8: id column new -> write -1 on miss */
+                                    bit 8: id column new -> write -1 on miss;
+                                    bit 9: id column holds int64 (else int32) */
     int32_t n_facets;
     double frame[14];            /* flat: c(3) ex(3) ey(3) ez(3) hy hz */
     double cyl[32];              /* cylinder: pos4d rows 0-2 (12), inverse rows 0-2 (12),
                                     zoom_z, R, b1, b2 (angle_between borders) */
     double p[8];                 /* kind parameters, see below */
     mgpu_col out[MGPU_MAX_OUT];  /* output columns (NULL ptr = not written) */
-    int32_t* id_out;             /* int32 id column or NULL */
+    void* id_out;                /* id column (int32 or int64, bit 9) or NULL */
     int64_t id_stride;
     const double* draw[2];       /* pre-drawn per-photon values (RNG_PREDRAWN) */
     int64_t draw_stride;
@@ -160,6 +161,7 @@ typedef struct {
     int32_t rng;                 /* MGPU_RNG_PREDRAWN / MGPU_RNG_PHILOX */
     int32_t pad;
     uint64_t seed;
+    uint64_t row_base;           /* global id of photon row 0 (Philox counter) */
     uint32_t* status;            /* device status word */
     unsigned long long* hits;    /* device, n_stages counters (added to) */
     mgpu_stage stages[MGPU_MAX_STAGES];

@@ -77,7 +77,8 @@ class MgpuStage(C.Structure):
 
 class MgpuChain(C.Structure):
     _fields_ = [('n_stages', C.c_int32), ('precision', C.c_int32), ('rng', C.c_int32),
-                ('pad', C.c_int32), ('seed', C.c_uint64), ('status', C.c_void_p),
+                ('pad', C.c_int32), ('seed', C.c_uint64), ('row_base', C.c_uint64),
+                ('status', C.c_void_p),
                 ('hits', C.c_void_p), ('stages', MgpuStage * MAX_STAGES)]
 
 

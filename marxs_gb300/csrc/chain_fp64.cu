@@ -66,10 +66,15 @@ struct Photon {
     double energy, prob;
 };
 
+__device__ __forceinline__ void store_id(const mgpu_stage& st, int64_t i, int64_t v) {
+    if ((st.first_writer >> 9) & 1) ((int64_t*)st.id_out)[i * st.id_stride] = v;
+    else ((int32_t*)st.id_out)[i * st.id_stride] = (int32_t)v;
+}
+
 __device__ __forceinline__ void write_miss_defaults(const mgpu_stage& st, int64_t i, int nout) {
     for (int k = 0; k < nout; ++k)
         if ((st.first_writer >> k) & 1) store_col(st.out[k], i, kNaN);
-    if (st.id_out && ((st.first_writer >> 8) & 1)) st.id_out[i * st.id_stride] = -1;
+    if (st.id_out && ((st.first_writer >> 8) & 1)) store_id(st, i, -1);
 }
 
 __device__ __forceinline__ void check_prob(double f, uint32_t* status) {
@@ -98,7 +103,7 @@ __device__ bool stage_lens(const mgpu_stage& st, Photon& ph, int64_t i) {
 }
 
 __device__ bool stage_scatter(const mgpu_stage& st, Photon& ph, int64_t i, int rng,
-                              uint64_t seed, int sidx, uint32_t* status) {
+                              uint64_t seed, uint64_t row_base, int sidx, uint32_t* status) {
     // RadialMirrorScatter.specific_process_photons, optics/scatter.py:49-77
     PlaneHit h = plane_intersect_frame(st.frame, ph.pos, ph.dir);
     if (!h.hit) {
@@ -116,7 +121,7 @@ __device__ bool stage_scatter(const mgpu_stage& st, Photon& ph, int64_t i, int r
         if (sig_perp != 0.0) a_perp = st.draw[1][i * st.draw_stride];
     } else {
         double n0, n1;
-        philox_normal2(seed, (uint64_t)i, (uint32_t)sidx, 0u, &n0, &n1);
+        philox_normal2(seed, row_base + (uint64_t)i, (uint32_t)sidx, 0u, &n0, &n1);
         a_in = sig_in * n0;
         a_perp = sig_perp * n1;
     }
@@ -147,7 +152,7 @@ __device__ bool stage_flatdet(const mgpu_stage& st, Photon& ph, int64_t i) {
     store_col(st.out[1], i, h.lz);
     store_col(st.out[2], i, h.ly / st.p[0] + st.p[1]);
     store_col(st.out[3], i, h.lz / st.p[0] + st.p[2]);
-    if (st.id_out) st.id_out[i * st.id_stride] = st.id_num;
+    if (st.id_out) store_id(st, i, st.id_num);
     ph.pos = h.ip;
     return true;
 }
@@ -167,7 +172,7 @@ __device__ bool stage_cyldet(const mgpu_stage& st, Photon& ph, int64_t i) {
     store_col(st.out[1], i, ly);
     store_col(st.out[2], i, phi * R / st.p[0] + st.p[1]);
     store_col(st.out[3], i, ly / st.p[0] + st.p[2]);
-    if (st.id_out) st.id_out[i * st.id_stride] = st.id_num;
+    if (st.id_out) store_id(st, i, st.id_num);
     ph.pos = gp;
     return true;
 }
@@ -214,7 +219,8 @@ __device__ __forceinline__ int nearest_facet_grid(const mgpu_stage& st, const Ph
 }
 
 __device__ bool stage_gratings(const mgpu_stage& st, Photon& ph, int64_t i, bool valid,
-                               int rng, uint64_t seed, int sidx, uint32_t* status) {
+                               int rng, uint64_t seed, uint64_t row_base, int sidx,
+                               uint32_t* status) {
     PlaneHit h;
     bool brute;
     int f = nearest_facet_grid(st, ph, valid, &h, &brute);
@@ -276,7 +282,7 @@ __device__ bool stage_gratings(const mgpu_stage& st, Photon& ph, int64_t i, bool
         u = st.draw[0][i * st.draw_stride];
     } else {
         double u1;
-        philox_uniform2(seed, (uint64_t)i, (uint32_t)sidx, 0u, &u, &u1);
+        philox_uniform2(seed, row_base + (uint64_t)i, (uint32_t)sidx, 0u, &u, &u1);
     }
     double selprob;
     int m = select_order(st.selectors[__ldg(&fc->selector)], ph.energy, u, &selprob, status);
@@ -302,7 +308,7 @@ __device__ bool stage_gratings(const mgpu_stage& st, Photon& ph, int64_t i, bool
     store_col(st.out[1], i, h.lz);
     store_col(st.out[2], i, (double)m);
     store_col(st.out[3], i, blaze);
-    if (st.id_out) st.id_out[i * st.id_stride] = __ldg(&fc->id_num);
+    if (st.id_out) store_id(st, i, __ldg(&fc->id_num));
     ph.pos = h.ip;
     return true;
 }
@@ -336,13 +342,15 @@ chain_fp64_kernel(const __grid_constant__ mgpu_chain chain, const __grid_constan
             bool hit = false;
             switch (st.kind) {
             case MGPU_STAGE_GRATINGS:
-                hit = stage_gratings(st, ph, i, valid, chain.rng, chain.seed, s, chain.status);
+                hit = stage_gratings(st, ph, i, valid, chain.rng, chain.seed, chain.row_base, s,
+                                     chain.status);
                 break;
             case MGPU_STAGE_LENS:
                 if (valid) hit = stage_lens(st, ph, i);
                 break;
             case MGPU_STAGE_SCATTER:
-                if (valid) hit = stage_scatter(st, ph, i, chain.rng, chain.seed, s, chain.status);
+                if (valid) hit = stage_scatter(st, ph, i, chain.rng, chain.seed, chain.row_base, s,
+                                             chain.status);
                 break;
             case MGPU_STAGE_FLATDET:
                 if (valid) hit = stage_flatdet(st, ph, i);

@@ -237,8 +237,9 @@ class GpuSequence:
         return self.lower().stages
 
     # ------------------------------------------------------------ launch
-    def _chain(self, inst, plan, bufs, draws_dev, n, status, hits):
+    def _chain(self, inst, plan, bufs, draws_dev, n, status, hits, row_base=0):
         chain = _abi.MgpuChain()
+        chain.row_base = int(row_base)
         chain.n_stages = len(inst.stages)
         chain.precision = _PRECISIONS[self.precision]
         chain.rng = _RNGS[self.rng]
@@ -256,10 +257,13 @@ class GpuSequence:
                 if plan.first_writer.get(name) == si:
                     fw |= 1 << k
             if st.id_col is not None:
-                s.id_out = bufs[st.id_col].data_ptr()
+                idb = bufs[st.id_col]
+                s.id_out = idb.data_ptr()
                 s.id_stride = 1
                 if plan.first_writer.get(st.id_col) == si:
                     fw |= 1 << 8
+                if idb.dtype == torch.int64:
+                    fw |= 1 << 9
             s.first_writer = fw
             if self.rng == 'predrawn' and st.draw_names:
                 d = draws_dev.get(si)
@@ -314,17 +318,28 @@ class GpuSequence:
             raise RuntimeError('GPU raytrace reported status 0x%x' % code)
 
     # ------------------------------------------------------------ device path
-    def allocate_columns(self, n, existing=()):
-        """Device buffers for every output column of the chain."""
+    def allocate_columns(self, n, existing=(), id_dtype=torch.int32):
+        """Device buffers for every output column of the chain (ids int32 by
+        default; int64 matches the reference's column dtype)."""
         inst = self.lower()
         plan = ColumnPlan(inst.stages, existing)
         bufs = {}
         for name, kind in plan.columns.items():
-            dt = torch.float64 if kind == 'f8' else torch.int32
+            dt = torch.float64 if kind == 'f8' else id_dtype
             bufs[name] = torch.empty(n, dtype=dt, device=self.device)
         return plan, bufs
 
-    def trace_device(self, inp, out, plan, bufs, draws=None, stream=None, status=None, hits=None):
+    def column_bytes(self):
+        """Bytes per photon of every stage column the chain writes (f8 = 8,
+        id = 4), and of the draws it reads in pre-drawn mode."""
+        inst = self.lower()
+        plan = ColumnPlan(inst.stages)
+        cols = sum(8 if k == 'f8' else 4 for k in plan.columns.values())
+        draws = sum(8 * len(st.draw_names) for st in inst.stages) if self.rng == 'predrawn' else 0
+        return cols, draws
+
+    def trace_device(self, inp, out, plan, bufs, draws=None, stream=None, status=None, hits=None,
+                     row_base=0):
         """Trace device-resident photons (asynchronous on ``stream``).
 
         ``inp``/``out`` are DevicePhotons (may be the same object); ``plan``
@@ -339,7 +354,7 @@ class GpuSequence:
             hits = torch.zeros(_abi.MAX_STAGES, dtype=torch.int64, device=self.device)
         draws_dev = draws if isinstance(draws, dict) and all(isinstance(k, int) for k in draws) \
             else self._draws_to_device(inst, draws, n)
-        chain = self._chain(inst, plan, bufs, draws_dev, n, status, hits)
+        chain = self._chain(inst, plan, bufs, draws_dev, n, status, hits, row_base)
         ph = _abi.MgpuPhotons()
         ph.n = n
         ph.pos, ph.dir, ph.pol, ph.energy, ph.prob = inp.abi()
@@ -350,80 +365,124 @@ class GpuSequence:
         return status, hits
 
     # ------------------------------------------------------------ table path
-    def __call__(self, photons, draws=None):
-        """Trace a photon table (astropy Table, PhotonTable or dict) in place."""
+    def __call__(self, photons, draws=None, row_base=0):
+        """Trace a photon table (astropy Table, PhotonTable or dict) in place.
+
+        Host columns are copied to the device, traced, and copied back:
+        state columns into the table's own arrays, new columns appended in
+        the order MARXS creates them.  Host arrays in pinned memory (see
+        ``pinned_photons``) make both copies asynchronous DMA.
+        """
         if isinstance(photons, dict):
             from .table import PhotonTable
             photons = PhotonTable(photons)
         n = len(photons)
         inst = self.lower()
         dev = self.device
+        stream = torch.cuda.current_stream(dev)
         colnames = list(photons.colnames)
-        pos = np.asarray(photons['pos'], dtype=np.float64)
-        dirs = np.asarray(photons['dir'], dtype=np.float64)
-        pol = np.asarray(photons['polarization'], dtype=np.float64)
-        if pos.shape != (n, 4) or dirs.shape != (n, 4) or pol.shape != (n, 4):
-            raise ValueError('pos, dir and polarization must be (N, 4) homogeneous columns')
-        if n and (not np.all(dirs[:, 3] == 0) or not np.all(pol[:, 3] == 0)):
+        host_state = {}
+        for key in ('pos', 'dir', 'polarization'):
+            a = np.asarray(photons[key])
+            if a.shape != (n, 4):
+                raise ValueError('pos, dir and polarization must be (N, 4) homogeneous columns')
+            host_state[key] = a
+        for key in ('energy', 'probability'):
+            host_state[key] = np.asarray(photons[key])
+        if n and (not np.all(host_state['dir'][:, 3] == 0) or
+                  not np.all(host_state['polarization'][:, 3] == 0)):
             raise ValueError('dir and polarization must be direction vectors (w = 0).')
-        if n and not np.all(pos[:, 3] == 1):
+        if n and not np.all(host_state['pos'][:, 3] == 1):
             raise ValueError('pos must hold points with w = 1.')
         if n == 0:
             return photons
         plan = ColumnPlan(inst.stages, existing=set(colnames))
-        t_pos = torch.from_numpy(np.ascontiguousarray(pos)).to(dev, non_blocking=True)
-        t_dir = torch.from_numpy(np.ascontiguousarray(dirs)).to(dev, non_blocking=True)
-        t_pol = torch.from_numpy(np.ascontiguousarray(pol)).to(dev, non_blocking=True)
-        t_en = torch.from_numpy(np.ascontiguousarray(photons['energy'], dtype=np.float64)).to(dev)
-        t_pr = torch.from_numpy(np.array(photons['probability'], dtype=np.float64)).to(dev)
+        dev_state = {k: _h2d(v, dev) for k, v in host_state.items()}
         bufs = {}
         for name, kind in plan.columns.items():
             if name in colnames:
-                a = np.asarray(photons[name])
-                a = a.astype(np.float64 if kind == 'f8' else np.int32)
-                bufs[name] = torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+                a = np.asarray(photons[name]).astype(np.float64 if kind == 'f8' else np.int64)
+                bufs[name] = _h2d(a, dev)
             else:
-                dt = torch.float64 if kind == 'f8' else torch.int32
+                dt = torch.float64 if kind == 'f8' else torch.int64
                 bufs[name] = torch.empty(n, dtype=dt, device=dev)
         status = torch.zeros(1, dtype=torch.int32, device=dev)
         hits = torch.zeros(_abi.MAX_STAGES, dtype=torch.int64, device=dev)
         draws_dev = self._draws_to_device(inst, draws, n)
-        chain = self._chain(inst, plan, bufs, draws_dev, n, status, hits)
+        chain = self._chain(inst, plan, bufs, draws_dev, n, status, hits, row_base)
         ph = _abi.MgpuPhotons()
         ph.n = n
-        ph.pos = ph.pos_out = _abi.vec_aos(t_pos)
-        ph.dir = ph.dir_out = _abi.vec_aos(t_dir)
-        ph.pol = ph.pol_out = _abi.vec_aos(t_pol)
-        ph.energy = _abi.col(t_en)
-        ph.prob = ph.prob_out = _abi.col(t_pr)
+        ph.pos = ph.pos_out = _abi.vec_aos(dev_state['pos'])
+        ph.dir = ph.dir_out = _abi.vec_aos(dev_state['dir'])
+        ph.pol = ph.pol_out = _abi.vec_aos(dev_state['polarization'])
+        ph.energy = _abi.col(dev_state['energy'])
+        ph.prob = ph.prob_out = _abi.col(dev_state['probability'])
         lib = _abi.load()
-        _abi.check(lib.mgpu_trace(C.byref(chain), C.byref(ph), _stream_handle()), 'mgpu_trace')
-        code = int(status.item())           # synchronises
+        _abi.check(lib.mgpu_trace(C.byref(chain), C.byref(ph), _stream_handle(stream)),
+                   'mgpu_trace')
+        # errors are raised before the table is touched, as the reference does
+        code = int(status.item())
         hit_counts = hits.cpu().numpy()[:len(inst.stages)]
         self.last_hits = hit_counts
         self._raise_status(code)
-        # state columns, in place
-        _write_back(photons, 'pos', t_pos.cpu().numpy())
-        _write_back(photons, 'dir', t_dir.cpu().numpy())
-        _write_back(photons, 'polarization', t_pol.cpu().numpy())
-        _write_back(photons, 'probability', t_pr.cpu().numpy())
-        # stage columns: existing ones updated, new ones created in the
-        # reference's order for stages that hit at least one photon
-        host = {name: b.cpu().numpy() for name, b in bufs.items()}
-        original = set(colnames)
+        pending = []
+        for key in ('pos', 'dir', 'polarization', 'probability'):
+            pending.append(_d2h_into(photons, key, dev_state[key]))
+        new_host = {}
         for name in plan.columns:
-            if name in original:
-                _write_back(photons, name, host[name])
+            if name in colnames:
+                pending.append(_d2h_into(photons, name, bufs[name]))
+            else:
+                h = torch.empty(bufs[name].shape, dtype=bufs[name].dtype, pin_memory=True)
+                h.copy_(bufs[name], non_blocking=True)
+                new_host[name] = h
+        stream.synchronize()
+        for fin in pending:
+            if fin is not None:
+                fin()
         for si, names in enumerate(plan.order):
             if hit_counts[si] == 0:
                 continue
             for name in names:
                 if name in colnames:
                     continue
-                val = host[name]
-                photons[name] = val.astype(np.int64) if plan.columns[name] == 'i4' else val
+                photons[name] = new_host[name].numpy()
                 colnames.append(name)
         return photons
+
+
+def pinned_photons(n):
+    """A PhotonTable whose state columns live in pinned host memory."""
+    from .table import PhotonTable
+    t = PhotonTable()
+    for key, shape in (('pos', (n, 4)), ('dir', (n, 4)), ('energy', (n,)),
+                       ('polarization', (n, 4)), ('probability', (n,))):
+        t.columns[key] = torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+    return t
+
+
+def _h2d(a, dev):
+    a = np.asarray(a)
+    if a.dtype != np.float64 and a.dtype.kind == 'f':
+        a = a.astype(np.float64)
+    t = torch.from_numpy(np.ascontiguousarray(a))
+    return t.to(dev, non_blocking=t.is_pinned())
+
+
+def _d2h_into(photons, name, dev_t):
+    """Copy a device column back into the table's own array when possible;
+    returns a finaliser for the cases that need a host-side replacement."""
+    arr = np.asarray(photons[name])
+    if (arr.shape == tuple(dev_t.shape) and arr.flags.writeable and arr.flags.c_contiguous
+            and arr.dtype == np.dtype(str(dev_t.dtype).replace('torch.', ''))):
+        torch.from_numpy(arr).copy_(dev_t, non_blocking=True)
+        return None
+    h = torch.empty(dev_t.shape, dtype=dev_t.dtype, pin_memory=True)
+    h.copy_(dev_t, non_blocking=True)
+
+    def fin():
+        _write_back(photons, name, h.numpy())
+    return fin
 
 
 def _write_back(photons, name, value):
