@@ -180,6 +180,24 @@ def algorithmic_bytes(seq):
     return 88 + 80 + cols + draws
 
 
+def precision_error(a, b, torch):
+    """Detector-position error of FP32-local against float64, same photons and
+    draws, over photons whose facet and order agree (micron)."""
+    fa, fb = a['bufs']['facet'], b['bufs']['facet']
+    oa, ob = a['bufs']['order'], b['bufs']['order']
+    agree = (fa == fb) & ((oa == ob) | (torch.isnan(oa) & torch.isnan(ob)))
+    pa, pb = a['out'].pos, b['out'].pos
+    m = agree & torch.isfinite(pb).all(0) & torch.isfinite(b['bufs']['det_phi'])
+    d = ((pa - pb) ** 2).sum(0).sqrt()[m] * 1e3
+    dphi = ((a['bufs']['det_phi'] - b['bufs']['det_phi']).abs() * 5900.0)[m] * 1e3
+    dy = (a['bufs']['det_y'] - b['bufs']['det_y']).abs()[m] * 1e3
+    out = {'photons_compared': int(m.sum()), 'facet_or_order_mismatch': int((~agree).sum()),
+           'pos_rms_um': float((d ** 2).mean().sqrt()), 'pos_max_um': float(d.max()),
+           'det_phi_R_rms_um': float((dphi ** 2).mean().sqrt()), 'det_phi_R_max_um': float(dphi.max()),
+           'det_y_rms_um': float((dy ** 2).mean().sqrt()), 'det_y_max_um': float(dy.max())}
+    return out
+
+
 def main():
     args = parse()
     if args.impl == 'reference':
@@ -208,7 +226,6 @@ def main():
     inst = configs.build('c2')
     host = configs.photons_for('c2', n, seed=2 + 7919 * rank)
     dev_in = DevicePhotons.from_columns(host)
-    dev_out = DevicePhotons(n)
     row_base = rank * n
 
     modes = []
@@ -220,6 +237,7 @@ def main():
     results = {}
     for mode in modes:
         seq = GpuSequence(elements=inst.elements, precision=mode, rng='philox', seed=12345)
+        dev_out = DevicePhotons(n)
         plan, bufs = seq.allocate_columns(n)
         status = torch.zeros(1, dtype=torch.int32, device='cuda')
         hits = torch.zeros(_abi.MAX_STAGES, dtype=torch.int64, device='cuda')
@@ -262,7 +280,7 @@ def main():
             t = torch.tensor([tot_ms, mean_ms], device='cuda', dtype=torch.float64)
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
             tot_ms, mean_ms = t.tolist()
-        results[mode] = {'seq': seq, 'plan': plan, 'bufs': bufs, 'mean_ms': mean_ms,
+        results[mode] = {'seq': seq, 'plan': plan, 'bufs': bufs, 'out': dev_out, 'mean_ms': mean_ms,
                          'wall_ms': tot_ms, 'clocks': ck,
                          'photons_per_s': world * n * args.steps / (tot_ms / 1e3),
                          'kernel_photons_per_s': n / (mean_ms / 1e3),
@@ -303,6 +321,7 @@ def main():
     if 'fp32local' in ok_modes and 'fp64' in ok_modes:
         line['fp32local_over_fp64'] = (results['fp32local']['photons_per_s'] /
                                        results['fp64']['photons_per_s'])
+        line['um_error'] = precision_error(results['fp32local'], results['fp64'], torch)
 
     # end to end through the public table call, pinned host buffers
     if not args.no_e2e:

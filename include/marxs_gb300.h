@@ -101,12 +101,61 @@ typedef struct {
     int32_t n_rows;
     int32_t n_orders;
     int32_t by_energy;    /* 1: nearest energy row (argmin |E - e|) */
-    int32_t pad;
+    int32_t sorted;       /* 1: energy strictly increasing (binary search allowed) */
     const double* energy; /* n_rows */
     const double* cdf;    /* n_rows * n_orders, normalised cumulative */
     const double* total;  /* n_rows, probability factor */
     const int32_t* orders;/* n_orders */
+    const uint64_t* thresholds; /* n_rows * n_orders: ceil(cdf * 2^53); for a draw
+                                   u = U * 2^-53, cdf > u  <=>  U < threshold */
 } mgpu_selector;
+
+/* FP32-local constants of a flat element (PerfectLens, RadialMirrorScatter,
+ * FlatDetector): centre as float-float, frame and parameters in float32 */
+typedef struct {
+    float c_hi[3], c_lo[3];
+    float ex[3], ey[3], ez[3];
+    float hy, hz;
+    float p[6];            /* kind parameters as in mgpu_stage.p */
+} mgpu_flat32;
+
+/* FP32-local facet record */
+typedef struct {
+    float c_hi[3], c_lo[3];
+    float ex[3], ey[3], ez[3];
+    float hy, hz;
+    float l[3], dneg[3];
+    float wd_hi, wd_lo;    /* energy2wave / d as float-float (keV) */
+    int32_t id_num;
+    int32_t selector;
+    int32_t flags;         /* bit 0: CAT sign convention, bit 1: transmission */
+    int32_t pad;
+} mgpu_facet32;
+
+/* FP32-local constants of a grating stage's candidate grid */
+typedef struct {
+    float o_hi[3], o_lo[3];
+    float n[3], a[3], b[3];
+    float u0, v0, inv_cell, slope_max;
+    int32_t nu, nv;
+} mgpu_grid32;
+
+/* FP32-local constants of a circular cylinder detector.  e1, e2, a are the
+ * unit local axes; angles are resolved against a table of reference angles
+ * k / 1024 rad, k = k0 .. k0 + nk - 1, holding cos and sin as float-float. */
+typedef struct {
+    float c_hi[3], c_lo[3];
+    float e1_hi[3], e1_lo[3];
+    float e2_hi[3], e2_lo[3];
+    float a_hi[3], a_lo[3];
+    float R_hi, R_lo;      /* radius (x zoom) */
+    float Rz;              /* half length (z zoom) */
+    float b1, b2;          /* reduced phi_lim borders */
+    float rpix_hi, rpix_lo;/* R / pixsize */
+    float inv_pix;
+    float cp0, cp1;        /* centerpix */
+    int32_t k0, nk;
+} mgpu_cyl32;
 
 /* uniform candidate grid in a plane (origin o, normal n, in-plane axes a,b) */
 typedef struct {
@@ -142,6 +191,10 @@ typedef struct {
     int32_t n_selectors;
     int32_t pad;
     mgpu_grid grid;              /* GRATINGS: candidate grid (cell_start NULL = brute force) */
+    const void* aux;             /* FP32-local constants: mgpu_flat32 (flat kinds),
+                                    mgpu_grid32 (GRATINGS), mgpu_cyl32 (CYLDET) */
+    const mgpu_facet32* facets32;/* GRATINGS, FP32-local */
+    const float* table;          /* CYLDET, FP32-local: nk x (cos hi, cos lo, sin hi, sin lo) */
 } mgpu_stage;
 /* p[] per kind:
  *   LENS:    p[0] focal length, p[1] d_center_optical_axis

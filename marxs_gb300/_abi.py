@@ -53,8 +53,30 @@ class MgpuPhotons(C.Structure):
 
 class MgpuSelector(C.Structure):
     _fields_ = [('n_rows', C.c_int32), ('n_orders', C.c_int32), ('by_energy', C.c_int32),
-                ('pad', C.c_int32), ('energy', C.c_void_p), ('cdf', C.c_void_p),
-                ('total', C.c_void_p), ('orders', C.c_void_p)]
+                ('sorted', C.c_int32), ('energy', C.c_void_p), ('cdf', C.c_void_p),
+                ('total', C.c_void_p), ('orders', C.c_void_p), ('thresholds', C.c_void_p)]
+
+
+class MgpuFlat32(C.Structure):
+    _fields_ = [('c_hi', C.c_float * 3), ('c_lo', C.c_float * 3), ('ex', C.c_float * 3),
+                ('ey', C.c_float * 3), ('ez', C.c_float * 3), ('hy', C.c_float),
+                ('hz', C.c_float), ('p', C.c_float * 6)]
+
+
+class MgpuGrid32(C.Structure):
+    _fields_ = [('o_hi', C.c_float * 3), ('o_lo', C.c_float * 3), ('n', C.c_float * 3),
+                ('a', C.c_float * 3), ('b', C.c_float * 3), ('u0', C.c_float),
+                ('v0', C.c_float), ('inv_cell', C.c_float), ('slope_max', C.c_float),
+                ('nu', C.c_int32), ('nv', C.c_int32)]
+
+
+class MgpuCyl32(C.Structure):
+    _fields_ = [('c_hi', C.c_float * 3), ('c_lo', C.c_float * 3), ('e1_hi', C.c_float * 3),
+                ('e1_lo', C.c_float * 3), ('e2_hi', C.c_float * 3), ('e2_lo', C.c_float * 3),
+                ('a_hi', C.c_float * 3), ('a_lo', C.c_float * 3), ('R_hi', C.c_float),
+                ('R_lo', C.c_float), ('Rz', C.c_float), ('b1', C.c_float), ('b2', C.c_float),
+                ('rpix_hi', C.c_float), ('rpix_lo', C.c_float), ('inv_pix', C.c_float),
+                ('cp0', C.c_float), ('cp1', C.c_float), ('k0', C.c_int32), ('nk', C.c_int32)]
 
 
 class MgpuGrid(C.Structure):
@@ -72,7 +94,8 @@ class MgpuStage(C.Structure):
                 ('p', C.c_double * 8), ('out', MgpuCol * MAX_OUT), ('id_out', C.c_void_p),
                 ('id_stride', C.c_int64), ('draw', C.c_void_p * 2), ('draw_stride', C.c_int64),
                 ('facets', C.c_void_p), ('selectors', C.c_void_p), ('n_selectors', C.c_int32),
-                ('pad', C.c_int32), ('grid', MgpuGrid)]
+                ('pad', C.c_int32), ('grid', MgpuGrid), ('aux', C.c_void_p),
+                ('facets32', C.c_void_p), ('table', C.c_void_p)]
 
 
 class MgpuChain(C.Structure):
@@ -87,6 +110,12 @@ FACET_DTYPE = np.dtype([('c', '<f8', 3), ('ex', '<f8', 3), ('ey', '<f8', 3), ('e
                         ('hy', '<f8'), ('hz', '<f8'), ('l', '<f8', 3), ('dneg', '<f8', 3),
                         ('dgrat', '<f8'), ('id_num', '<i4'), ('selector', '<i4'),
                         ('cat', '<i4'), ('transmission', '<i4')], align=True)
+
+FACET32_DTYPE = np.dtype([('c_hi', '<f4', 3), ('c_lo', '<f4', 3), ('ex', '<f4', 3),
+                          ('ey', '<f4', 3), ('ez', '<f4', 3), ('hy', '<f4'), ('hz', '<f4'),
+                          ('l', '<f4', 3), ('dneg', '<f4', 3), ('wd_hi', '<f4'), ('wd_lo', '<f4'),
+                          ('id_num', '<i4'), ('selector', '<i4'), ('flags', '<i4'),
+                          ('pad', '<i4')], align=True)
 
 # name -> (restype, argtypes) of every exported entry point
 SIGNATURES = {

@@ -1,10 +1,579 @@
-// Fused element-chain kernel, FP32-local precision mode (placeholder until
-// the mixed-precision kernel lands: the launch reports "not supported").
+// Fused element-chain kernel, FP32-local precision mode.
+//
+// Same stage semantics as the float64 kernel (chain_fp64.cu, which follows
+// OpticalElement.process_photons, optics/base.py:149-211), with the
+// arithmetic split by what each quantity needs:
+//   * photon positions are float-float (hi + lo) in the global frame, so a
+//     ray is re-centred on each element exactly (pos - centre) and the
+//     element's own arithmetic runs in float32 on small local numbers;
+//   * every ray/plane parameter k is refined once against the plane so the
+//     stored position lies on the element (the float32 solve alone leaves it
+//     ~1e-7 k off along the ray);
+//   * directions, polarization, probability and local coordinates are
+//     float32; the grating term m * lambda / d is formed in float-float;
+//   * the cylinder hit is refined by one float-float Newton step and its
+//     angle resolved as (reference angle k/1024 from a float-float table) +
+//     (small float32 residual), so det_phi keeps ~1e-11 rad;
+//   * order selection is exact: a 53-bit draw U against integer thresholds
+//     ceil(cdf * 2^53), and the nearest energy row decided in float64.
+// float64 inputs/outputs are converted on the integer pipe (mgpu_ff.cuh);
+// the FP64 pipe only sees a handful of adds per photon for the final
+// float64 detector coordinates.
 #include <cuda_runtime.h>
-#include "mgpu_device.cuh"
+#include "mgpu_ff.cuh"
+
+namespace {
+
+constexpr int kThreads = 256;
+
+struct PhotonL {
+    ff3 pos;
+    f3 dir, pol;
+    ff energy;
+    double energy_d;
+    float prob;
+};
+
+__device__ __forceinline__ ff3 ldff3(const float* hi, const float* lo) {
+    return ff3{ff{hi[0], lo[0]}, ff{hi[1], lo[1]}, ff{hi[2], lo[2]}};
+}
+
+__device__ __forceinline__ void storef(const mgpu_col& c, int64_t i, float v) {
+    if (c.ptr) c.ptr[i * c.stride] = f2d_bits(v);
+}
+__device__ __forceinline__ void stored(const mgpu_col& c, int64_t i, double v) {
+    if (c.ptr) c.ptr[i * c.stride] = v;
+}
+
+__device__ __forceinline__ void store_id(const mgpu_stage& st, int64_t i, int64_t v) {
+    if ((st.first_writer >> 9) & 1) ((int64_t*)st.id_out)[i * st.id_stride] = v;
+    else ((int32_t*)st.id_out)[i * st.id_stride] = (int32_t)v;
+}
+
+__device__ __forceinline__ void write_miss_defaults(const mgpu_stage& st, int64_t i, int nout) {
+    for (int k = 0; k < nout; ++k)
+        if ((st.first_writer >> k) & 1) stored(st.out[k], i, kNaN);
+    if (st.id_out && ((st.first_writer >> 8) & 1)) store_id(st, i, -1);
+}
+
+// ------------------------------------------------------------ flat planes
+struct HitL {
+    bool hit;
+    float k;
+    ff3 ip;
+    float ly, lz;
+};
+
+// FinitePlane.intersect in the element frame: float32 solve, one
+// refinement against the plane, local coordinates from the exact offset
+__device__ __forceinline__ HitL plane_hit_l(ff3 c, f3 n, f3 ey, f3 ez, float hy, float hz,
+                                            const ff3& pos, f3 dir) {
+    HitL h;
+    f3 rel = ff3_f(ff3_sub(pos, c));
+    float kd = dotf(dir, n);
+    float k = -dotf(rel, n) / kd;
+    ff3 ip = ff3_axpy(pos, k, dir);
+    f3 v = ff3_f(ff3_sub(ip, c));
+    float dk = -dotf(v, n) / kd;
+    if (kd != 0.0f && isfinite(dk)) {
+        k += dk;
+        ip = ff3_axpy(ip, dk, dir);
+        v = v + dk * dir;
+    }
+    h.k = k;
+    h.ip = ip;
+    h.ly = dotf(v, ey);
+    h.lz = dotf(v, ez);
+    h.hit = (kd != 0.0f) && (k >= 0.0f) && (fabsf(h.ly) <= hy) && (fabsf(h.lz) <= hz);
+    return h;
+}
+
+__device__ __forceinline__ HitL flat_hit(const mgpu_flat32* F, const ff3& pos, f3 dir) {
+    return plane_hit_l(ldff3(F->c_hi, F->c_lo), ldf3(F->ex), ldf3(F->ey), ldf3(F->ez), F->hy, F->hz,
+                       pos, dir);
+}
+
+__device__ __forceinline__ HitL facet_hit(const mgpu_facet32* fc, const ff3& pos, f3 dir) {
+    return plane_hit_l(ldff3(fc->c_hi, fc->c_lo), ldf3(fc->ex), ldf3(fc->ey), ldf3(fc->ez),
+                       fc->hy, fc->hz, pos, dir);
+}
+
+// parallel_transport (polarization.py:90-170) in float32
+__device__ __forceinline__ f3 transport_f(f3 d_old, f3 d_new, f3 pol) {
+    f3 a = normf(d_old), b = normf(d_new);
+    f3 s = crossf(a, b);
+    float sn = sqrtf(dotf(s, s));
+    if (sn <= 1e-8f) return pol;
+    s = (1.0f / sn) * s;
+    f3 pin = crossf(a, s), pout = crossf(b, s);
+    float ks = dotf(s, pol), kp = dotf(pin, pol), kd = dotf(a, pol);
+    return f3{s.x * ks + pout.x * kp + b.x * kd, s.y * ks + pout.y * kp + b.y * kd,
+              s.z * ks + pout.z * kp + b.z * kd};
+}
+
+// R^T v for R = axangle2mat(axis, angle): v - sin(a) (k x v) + (1 - cos a) k x (k x v),
+// with 1 - cos a = 2 sin^2(a/2) so small angles keep full relative precision
+__device__ __forceinline__ f3 rot_transpose_f(f3 axis, float a, f3 v) {
+    f3 k = normf(axis);
+    float s = sinf(a);
+    float h = sinf(0.5f * a);
+    float C = 2.0f * h * h;
+    f3 kv = crossf(k, v);
+    f3 kkv = crossf(k, kv);
+    return f3{v.x - s * kv.x + C * kkv.x, v.y - s * kv.y + C * kkv.y, v.z - s * kv.z + C * kkv.z};
+}
+
+// 53-bit uniform as an integer and as float, from the Philox stream the
+// float64 kernel uses (same counters, so both modes draw the same u)
+__device__ __forceinline__ void philox_u53(uint64_t seed, uint64_t row, uint32_t stage,
+                                           uint64_t* U0, uint64_t* U1) {
+    u4 c{(uint32_t)row, (uint32_t)(row >> 32), stage, 0u};
+    u4 r = philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+    *U0 = (((uint64_t)r.x << 21) ^ (uint64_t)(r.y >> 11)) & ((1ull << 53) - 1);
+    *U1 = (((uint64_t)r.z << 21) ^ (uint64_t)(r.w >> 11)) & ((1ull << 53) - 1);
+}
+
+__device__ __forceinline__ float u53_to_f(uint64_t U) {
+    return (float)(uint32_t)(U >> 29) * (1.0f / 16777216.0f);
+}
+
+// ------------------------------------------------------------------ stages
+__device__ bool stage_lens_l(const mgpu_stage& st, PhotonL& ph, int64_t i) {
+    // PerfectLens.specific_process_photons, optics/mirror.py:53-82
+    const mgpu_flat32* F = (const mgpu_flat32*)st.aux;
+    HitL h = flat_hit(F, ph.pos, ph.dir);
+    if (!h.hit) {
+        write_miss_defaults(st, i, 2);
+        return false;
+    }
+    f3 cm = ff3_f(ff3_sub(ldff3(F->c_hi, F->c_lo), h.ip));     // centre - interpos
+    f3 v = cm - F->p[1] * ldf3(F->ez) + F->p[0] * normf(ph.dir);
+    f3 nd = normf(v);
+    ph.pol = transport_f(ph.dir, nd, ph.pol);
+    ph.dir = nd;
+    storef(st.out[0], i, h.ly);
+    storef(st.out[1], i, h.lz);
+    ph.pos = h.ip;
+    return true;
+}
+
+__device__ bool stage_scatter_l(const mgpu_stage& st, PhotonL& ph, int64_t i, int rng,
+                                uint64_t seed, uint64_t row_base, int sidx, uint32_t* status) {
+    // RadialMirrorScatter.specific_process_photons, optics/scatter.py:49-77
+    const mgpu_flat32* F = (const mgpu_flat32*)st.aux;
+    HitL h = flat_hit(F, ph.pos, ph.dir);
+    if (!h.hit) {
+        write_miss_defaults(st, i, 4);
+        return false;
+    }
+    float sig_in = F->p[0], sig_perp = F->p[1];
+    float a_in = 0.0f, a_perp = 0.0f;
+    double a_in_d = 0.0, a_perp_d = 0.0;
+    bool have_d = false;
+    if (rng == MGPU_RNG_PREDRAWN) {
+        if ((sig_in != 0.0f && st.draw[0] == nullptr) || (sig_perp != 0.0f && st.draw[1] == nullptr)) {
+            atomicOr(status, MGPU_STATUS_BAD_STAGE);
+            return false;
+        }
+        if (sig_in != 0.0f) a_in_d = st.draw[0][i * st.draw_stride];
+        if (sig_perp != 0.0f) a_perp_d = st.draw[1][i * st.draw_stride];
+        a_in = d2f_bits(a_in_d);
+        a_perp = d2f_bits(a_perp_d);
+        have_d = true;
+    } else {
+        uint64_t U0, U1;
+        philox_u53(seed, row_base + (uint64_t)i, (uint32_t)sidx, &U0, &U1);
+        float u0 = u53_to_f(U0), u1 = u53_to_f(U1);
+        float r = sqrtf(-2.0f * __logf(1.0f - u0 + 1e-30f));
+        float sn, cs;
+        sincospif(2.0f * u1, &sn, &cs);
+        a_in = sig_in * (r * cs);
+        a_perp = sig_perp * (r * sn);
+    }
+    f3 radial = ff3_f(ff3_sub(ph.pos, ldff3(F->c_hi, F->c_lo)));   // previous position
+    f3 perpplane = crossf(ph.dir, radial);
+    f3 outdir = ph.dir;
+    if (sig_in != 0.0f) outdir = rot_transpose_f(perpplane, a_in, outdir);
+    if (sig_perp != 0.0f) outdir = rot_transpose_f(radial, a_perp, outdir);
+    ph.pol = transport_f(ph.dir, outdir, ph.pol);
+    ph.dir = outdir;
+    storef(st.out[0], i, h.ly);
+    storef(st.out[1], i, h.lz);
+    if (have_d) {
+        stored(st.out[2], i, a_in_d);
+        stored(st.out[3], i, a_perp_d);
+    } else {
+        storef(st.out[2], i, a_in);
+        storef(st.out[3], i, a_perp);
+    }
+    ph.pos = h.ip;
+    return true;
+}
+
+__device__ bool stage_flatdet_l(const mgpu_stage& st, PhotonL& ph, int64_t i) {
+    // FlatDetector.specific_process_photons, optics/detector.py:72-75
+    const mgpu_flat32* F = (const mgpu_flat32*)st.aux;
+    HitL h = flat_hit(F, ph.pos, ph.dir);
+    if (!h.hit) {
+        write_miss_defaults(st, i, 4);
+        return false;
+    }
+    storef(st.out[0], i, h.ly);
+    storef(st.out[1], i, h.lz);
+    storef(st.out[2], i, h.ly * F->p[3] + F->p[1]);
+    storef(st.out[3], i, h.lz * F->p[3] + F->p[2]);
+    if (st.id_out) store_id(st, i, st.id_num);
+    ph.pos = h.ip;
+    return true;
+}
+
+__device__ __forceinline__ bool angle_between_f(float angle, float b1, float b2) {
+    const float twopi = 6.283185307179586f;
+    float a = fmodf(angle, twopi);
+    if (a < 0.0f) a += twopi;
+    if (b1 < b2) return (b1 <= a) && (a <= b2);
+    return (b1 <= a) || (a <= b2);
+}
+
+__device__ bool stage_cyldet_l(const mgpu_stage& st, PhotonL& ph, int64_t i) {
+    // Cylinder.intersect (math/geometry.py:470-564) + CircularDetector
+    // (optics/detector.py:115-118) for a circular tube
+    const mgpu_cyl32* K = (const mgpu_cyl32*)st.aux;
+    ff3 e1 = ldff3(K->e1_hi, K->e1_lo), e2 = ldff3(K->e2_hi, K->e2_lo), ax = ldff3(K->a_hi, K->a_lo);
+    f3 e1f = ldf3(K->e1_hi), e2f = ldf3(K->e2_hi), af = ldf3(K->a_hi);
+    ff R{K->R_hi, K->R_lo};
+    ff3 q = ff3_sub(ph.pos, ldff3(K->c_hi, K->c_lo));
+    ff q1 = ff_dot(q, e1), q2 = ff_dot(q, e2);
+    float q3 = ff_f(ff_dot(q, ax));
+    f3 d = ph.dir;
+    float d1 = dotf(d, e1f), d2 = dotf(d, e2f), d3 = dotf(d, af);
+    float a = d1 * d1 + d2 * d2;
+    float b = ff_f(q1) * d1 + ff_f(q2) * d2;                       // half of the linear term
+    float c = ff_f(ff_sub(ff_add(ff_mul(q1, q1), ff_mul(q2, q2)), ff_mul(R, R)));
+    float disc = b * b - a * c;
+    bool hit = false;
+    float t = 0.0f;
+    if (disc >= 0.0f && a > 0.0f) {
+        float sq = sqrtf(disc);
+        float qq = -(b + copysignf(sq, b));
+        float tA = qq / a, tB = c / qq;
+        float a1 = (b < 0.0f) ? tA : tB;     // (-b + sq) / a
+        float a2 = (b < 0.0f) ? tB : tA;     // (-b - sq) / a
+        float q1f = ff_f(q1), q2f = ff_f(q2);
+        float z1 = q3 + a1 * d3, z2 = q3 + a2 * d3;
+        bool h1 = (a1 >= 0.0f) && (fabsf(z1) <= K->Rz) &&
+                  angle_between_f(atan2f(q2f + a1 * d2, q1f + a1 * d1), K->b1, K->b2);
+        bool h2 = (a2 >= 0.0f) && (fabsf(z2) <= K->Rz) &&
+                  angle_between_f(atan2f(q2f + a2 * d2, q1f + a2 * d1), K->b1, K->b2);
+        if (h1 && h2) {
+            if (a2 < a1) h1 = false;
+            else h2 = false;
+        }
+        if (h1) {
+            hit = true;
+            t = a1;
+        } else if (h2) {
+            hit = true;
+            t = a2;
+        }
+    }
+    if (!hit) {
+        write_miss_defaults(st, i, 4);
+        return false;
+    }
+    // one float-float Newton step on |H_perp|^2 = R^2
+    ff3 H = ff3_axpy(q, t, d);
+    ff h1 = ff_dot(H, e1), h2 = ff_dot(H, e2);
+    ff g = ff_sub(ff_add(ff_mul(h1, h1), ff_mul(h2, h2)), ff_mul(R, R));
+    float dg = 2.0f * (ff_f(h1) * d1 + ff_f(h2) * d2);
+    float dt = -ff_f(g) / dg;
+    if (isfinite(dt)) {
+        H = ff3_axpy(H, dt, d);
+        h1 = ff_dot(H, e1);
+        h2 = ff_dot(H, e2);
+    }
+    float h3 = ff_f(ff_dot(H, ax));
+    // angle: reference k/1024 from the table, then the small residual
+    float phi_a = atan2f(h2.hi, h1.hi);
+    int kk = __float2int_rn(phi_a * 1024.0f);
+    int idx = min(max(kk - K->k0, 0), K->nk - 1);
+    kk = idx + K->k0;
+    const float* tb = st.table + 4 * idx;
+    ff cr{__ldg(tb), __ldg(tb + 1)}, sr{__ldg(tb + 2), __ldg(tb + 3)};
+    ff cp = ff_add(ff_mul(h1, cr), ff_mul(h2, sr));
+    ff sp = ff_sub(ff_mul(h2, cr), ff_mul(h1, sr));
+    float psi = atan2f(ff_f(sp), ff_f(cp));
+    ff phi = fast_two_sum((float)kk * (1.0f / 1024.0f), psi);
+    stored(st.out[0], i, ff2d(phi));
+    storef(st.out[1], i, h3);
+    ff px = ff_add_f(ff_mul(phi, ff{K->rpix_hi, K->rpix_lo}), K->cp0);
+    stored(st.out[2], i, ff2d(px));
+    storef(st.out[3], i, h3 * K->inv_pix + K->cp1);
+    if (st.id_out) store_id(st, i, st.id_num);
+    ph.pos = ff3{ff_add(H.x, ff{K->c_hi[0], K->c_lo[0]}), ff_add(H.y, ff{K->c_hi[1], K->c_lo[1]}),
+                 ff_add(H.z, ff{K->c_hi[2], K->c_lo[2]})};
+    return true;
+}
+
+// exact order selection (see the header comment)
+__device__ __forceinline__ int select_order_l(const mgpu_selector& sel, double e, uint64_t U,
+                                              float* prob, uint32_t* status) {
+    int row = 0;
+    if (sel.by_energy) {
+        const int n = sel.n_rows;
+        if (sel.sorted) {
+            // largest j with E_j <= e (positive doubles order as integers)
+            long long key = __double_as_longlong(e);
+            int lo = 0, hi = n - 1;
+            if (!(key >= __double_as_longlong(sel.energy[0]))) {
+                row = 0;
+            } else {
+                while (lo < hi) {
+                    int mid = (lo + hi + 1) >> 1;
+                    if (__double_as_longlong(sel.energy[mid]) <= key) lo = mid;
+                    else hi = mid - 1;
+                }
+                row = lo;
+                if (row + 1 < n) {
+                    double d0 = fabs(sel.energy[row] - e), d1 = fabs(sel.energy[row + 1] - e);
+                    if (d1 < d0) row = row + 1;
+                }
+            }
+        } else {
+            double best = fabs(sel.energy[0] - e);
+            for (int j = 1; j < n; ++j) {
+                double dd = fabs(sel.energy[j] - e);
+                if (dd < best) {
+                    best = dd;
+                    row = j;
+                }
+            }
+        }
+    }
+    const uint64_t* th = sel.thresholds + (int64_t)row * sel.n_orders;
+    int k = 0;
+    while (k < sel.n_orders && !(U < th[k])) ++k;
+    if (k == sel.n_orders) {
+        atomicOr(status, MGPU_STATUS_ORDER_EMPTY);
+        k = sel.n_orders - 1;
+    }
+    double tot = sel.total[row];
+    *prob = d2f_bits(tot);
+    if (tot < 0.0 || tot > 1.0) atomicOr(status, MGPU_STATUS_PROB_RANGE);
+    return sel.orders[k];
+}
+
+__device__ __forceinline__ int nearest_facet_grid_l(const mgpu_stage& st, const PhotonL& ph,
+                                                    bool valid, HitL* best_hit, bool* need_brute) {
+    const mgpu_grid32* G = (const mgpu_grid32*)st.aux;
+    *need_brute = false;
+    int best = -1;
+    best_hit->k = 0.0f;
+    if (!valid) return -1;
+    if (G == nullptr || st.grid.cell_start == nullptr) {
+        *need_brute = true;
+        return -1;
+    }
+    f3 rel = ff3_f(ff3_sub(ph.pos, ldff3(G->o_hi, G->o_lo)));
+    f3 n = ldf3(G->n), a = ldf3(G->a), b = ldf3(G->b);
+    float dn = dotf(ph.dir, n), da = dotf(ph.dir, a), db = dotf(ph.dir, b);
+    if (!(fabsf(da) <= G->slope_max * fabsf(dn)) || !(fabsf(db) <= G->slope_max * fabsf(dn)) ||
+        dn == 0.0f) {
+        *need_brute = true;
+        return -1;
+    }
+    float t0 = -dotf(rel, n) / dn;
+    float u = dotf(rel, a) + t0 * da;
+    float v = dotf(rel, b) + t0 * db;
+    float fu = floorf((u - G->u0) * G->inv_cell);
+    float fv = floorf((v - G->v0) * G->inv_cell);
+    if (!(fu >= 0.0f && fu < (float)G->nu && fv >= 0.0f && fv < (float)G->nv)) return -1;
+    int cell = (int)fu * G->nv + (int)fv;
+    const mgpu_grid& g = st.grid;
+    int s0 = __ldg(g.cell_start + cell), s1 = min(__ldg(g.cell_start + cell + 1), g.capacity);
+    for (int q = s0; q < s1; ++q) {
+        int f = __ldg(g.cell_items + q);
+        HitL h = facet_hit(st.facets32 + f, ph.pos, ph.dir);
+        if (h.hit && (best < 0 || h.k < best_hit->k || (h.k == best_hit->k && f < best))) {
+            best = f;
+            *best_hit = h;
+        }
+    }
+    return best;
+}
+
+__device__ bool stage_gratings_l(const mgpu_stage& st, PhotonL& ph, int64_t i, bool valid,
+                                 int rng, uint64_t seed, uint64_t row_base, int sidx,
+                                 uint32_t* status) {
+    HitL h;
+    bool brute;
+    int f = nearest_facet_grid_l(st, ph, valid, &h, &brute);
+    unsigned bm = __ballot_sync(MGPU_FULL_MASK, brute);
+    const int lane = threadIdx.x & 31;
+    while (bm) {
+        int src = __ffs(bm) - 1;
+        bm &= bm - 1;
+        ff3 p;
+        p.x = ff{__shfl_sync(MGPU_FULL_MASK, ph.pos.x.hi, src), __shfl_sync(MGPU_FULL_MASK, ph.pos.x.lo, src)};
+        p.y = ff{__shfl_sync(MGPU_FULL_MASK, ph.pos.y.hi, src), __shfl_sync(MGPU_FULL_MASK, ph.pos.y.lo, src)};
+        p.z = ff{__shfl_sync(MGPU_FULL_MASK, ph.pos.z.hi, src), __shfl_sync(MGPU_FULL_MASK, ph.pos.z.lo, src)};
+        f3 d{__shfl_sync(MGPU_FULL_MASK, ph.dir.x, src), __shfl_sync(MGPU_FULL_MASK, ph.dir.y, src),
+             __shfl_sync(MGPU_FULL_MASK, ph.dir.z, src)};
+        float bk = 0.0f;
+        int bf = -1;
+        for (int q = lane; q < st.n_facets; q += 32) {
+            HitL hq = facet_hit(st.facets32 + q, p, d);
+            if (hq.hit && (bf < 0 || hq.k < bk)) {
+                bf = q;
+                bk = hq.k;
+            }
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            float ok = __shfl_xor_sync(MGPU_FULL_MASK, bk, off);
+            int of = __shfl_xor_sync(MGPU_FULL_MASK, bf, off);
+            bool take = (of >= 0) && (bf < 0 || ok < bk || (ok == bk && of < bf));
+            if (take) {
+                bk = ok;
+                bf = of;
+            }
+        }
+        if (lane == src && bf >= 0) {
+            f = bf;
+            h = facet_hit(st.facets32 + bf, ph.pos, ph.dir);
+        }
+    }
+    if (!valid) return false;
+    if (f < 0) {
+        write_miss_defaults(st, i, 4);
+        return false;
+    }
+    // FlatGrating.diffract_photons (grating.py:233-266) in the facet frame
+    const mgpu_facet32* fc = st.facets32 + f;
+    f3 l = ldf3(fc->l), dn = ldf3(fc->dneg), n = ldf3(fc->ex);
+    f3 p = normf(ph.dir);
+    float p_l = dotf(p, l), p_d = dotf(p, dn), p_n = dotf(p, n);
+    float blaze = atan2f(fabsf(p_d), fabsf(p_n));      // = arccos|p_perp . n|
+    uint64_t U;
+    if (rng == MGPU_RNG_PREDRAWN) {
+        if (st.draw[0] == nullptr) {
+            atomicOr(status, MGPU_STATUS_BAD_STAGE);
+            return false;
+        }
+        double u = st.draw[0][i * st.draw_stride];
+        U = (uint64_t)(u * 9007199254740992.0);
+    } else {
+        uint64_t U1;
+        philox_u53(seed, row_base + (uint64_t)i, (uint32_t)sidx, &U, &U1);
+    }
+    float selprob;
+    const int flags = fc->flags;
+    int m = select_order_l(st.selectors[fc->selector], ph.energy_d, U, &selprob, status);
+    float sign;
+    if (flags & 1) sign = (p_d > 0.0f) ? 1.0f : ((p_d < 0.0f) ? -1.0f : 1.0f);
+    else sign = -1.0f;
+    // sign * m * lambda / d in float-float
+    ff term = ff_div(ff{fc->wd_hi, fc->wd_lo}, ph.energy);
+    term = ff_mul_f(term, sign * (float)m);
+    float pd2 = ff_f(ff_add_f(term, p_d));
+    float p_n2 = sqrtf(1.0f - pd2 * pd2 - p_l * p_l);
+    float direction = (p_n > 0.0f) ? 1.0f : ((p_n < 0.0f) ? -1.0f : 0.0f);
+    if (!(flags & 2)) direction = -direction;
+    f3 nd = pd2 * dn + p_l * l + (direction * p_n2) * n;
+    ph.pol = transport_f(ph.dir, nd, ph.pol);
+    ph.dir = nd;
+    ph.prob *= selprob;
+    storef(st.out[0], i, h.ly);
+    storef(st.out[1], i, h.lz);
+    stored(st.out[2], i, f2d_bits((float)m));
+    storef(st.out[3], i, blaze);
+    if (st.id_out) store_id(st, i, fc->id_num);
+    ph.pos = h.ip;
+    return true;
+}
+
+__global__ void __launch_bounds__(kThreads)
+chain_fp32local_kernel(const __grid_constant__ mgpu_chain chain, const __grid_constant__ mgpu_photons io) {
+    __shared__ unsigned int s_hits[MGPU_MAX_STAGES];
+    if (threadIdx.x < MGPU_MAX_STAGES) s_hits[threadIdx.x] = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int64_t n = io.n;
+    const int64_t warp_id = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t base = warp_id * 32; base < n; base += n_warps * 32) {
+        const int64_t i = base + lane;
+        const bool valid = i < n;
+        PhotonL ph;
+        if (valid) {
+            d3 p = load3(io.pos, i), d = load3(io.dir, i), q = load3(io.pol, i);
+            ph.pos = ff3{d2ff_bits(p.x), d2ff_bits(p.y), d2ff_bits(p.z)};
+            ph.dir = f3{d2f_bits(d.x), d2f_bits(d.y), d2f_bits(d.z)};
+            ph.pol = f3{d2f_bits(q.x), d2f_bits(q.y), d2f_bits(q.z)};
+            ph.energy_d = io.energy.ptr[i * io.energy.stride];
+            ph.energy = d2ff_bits(ph.energy_d);
+            ph.prob = d2f_bits(io.prob.ptr[i * io.prob.stride]);
+        } else {
+            ph.pos = ff3{ff{0.f, 0.f}, ff{0.f, 0.f}, ff{0.f, 0.f}};
+            ph.dir = ph.pol = f3{0.f, 0.f, 0.f};
+            ph.energy = ff{1.f, 0.f};
+            ph.energy_d = 1.0;
+            ph.prob = 0.f;
+        }
+        for (int s = 0; s < chain.n_stages; ++s) {
+            const mgpu_stage& st = chain.stages[s];
+            bool hit = false;
+            switch (st.kind) {
+            case MGPU_STAGE_GRATINGS:
+                hit = stage_gratings_l(st, ph, i, valid, chain.rng, chain.seed, chain.row_base, s,
+                                       chain.status);
+                break;
+            case MGPU_STAGE_LENS:
+                if (valid) hit = stage_lens_l(st, ph, i);
+                break;
+            case MGPU_STAGE_SCATTER:
+                if (valid) hit = stage_scatter_l(st, ph, i, chain.rng, chain.seed, chain.row_base, s,
+                                                 chain.status);
+                break;
+            case MGPU_STAGE_FLATDET:
+                if (valid) hit = stage_flatdet_l(st, ph, i);
+                break;
+            case MGPU_STAGE_CYLDET:
+                if (valid) hit = stage_cyldet_l(st, ph, i);
+                break;
+            default:
+                if (valid) atomicOr(chain.status, MGPU_STATUS_BAD_STAGE);
+            }
+            unsigned m = __ballot_sync(MGPU_FULL_MASK, hit);
+            if (lane == 0 && m) atomicAdd(&s_hits[s], (unsigned)__popc(m));
+        }
+        if (valid) {
+            store3(io.pos_out, i, d3{ff2d(ph.pos.x), ff2d(ph.pos.y), ff2d(ph.pos.z)});
+            store3(io.dir_out, i, d3{f2d_bits(ph.dir.x), f2d_bits(ph.dir.y), f2d_bits(ph.dir.z)});
+            store3(io.pol_out, i, d3{f2d_bits(ph.pol.x), f2d_bits(ph.pol.y), f2d_bits(ph.pol.z)});
+            io.prob_out.ptr[i * io.prob_out.stride] = f2d_bits(ph.prob);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < chain.n_stages && s_hits[threadIdx.x])
+        atomicAdd(chain.hits + threadIdx.x, (unsigned long long)s_hits[threadIdx.x]);
+}
+
+}  // namespace
 
 cudaError_t mgpu_launch_chain_fp32local(const mgpu_chain& chain, const mgpu_photons& io,
                                         cudaStream_t stream, int sm_count) {
-    (void)chain; (void)io; (void)stream; (void)sm_count;
-    return cudaErrorNotSupported;
+    if (io.n <= 0) return cudaSuccess;
+    for (int s = 0; s < chain.n_stages; ++s) {
+        const mgpu_stage& st = chain.stages[s];
+        if (st.aux == nullptr) return cudaErrorInvalidValue;
+        if (st.kind == MGPU_STAGE_GRATINGS && st.facets32 == nullptr) return cudaErrorInvalidValue;
+        if (st.kind == MGPU_STAGE_CYLDET && st.table == nullptr) return cudaErrorInvalidValue;
+    }
+    int64_t warps = (io.n + 31) / 32;
+    int64_t blocks = (warps * 32 + kThreads - 1) / kThreads;
+    int64_t cap = (int64_t)sm_count * 8;
+    if (blocks > cap) blocks = cap;
+    chain_fp32local_kernel<<<(unsigned)blocks, kThreads, 0, stream>>>(chain, io);
+    return cudaGetLastError();
 }

@@ -1,0 +1,169 @@
+// Float32 / float-float helpers for the FP32-local kernel (sm_103a).
+//
+// On GB300 every float64 operation -- including float64<->float32
+// conversion -- issues on the FP64 pipe (about 2 per clock per SM, against
+// ~128 FP32 FMAs).  The FP32-local kernel therefore
+//   * converts float64 inputs/outputs with integer bit manipulation (INT
+//     pipe) instead of F2F instructions,
+//   * carries positions as float-float pairs (hi + lo, ~48-bit mantissa)
+//     built from error-free transformations (Dekker/Knuth TwoSum, FMA-based
+//     TwoProd), so that re-centring a ray on an element far from the origin
+//     loses nothing,
+//   * keeps directions, polarization and per-element local arithmetic in
+//     float32.
+#pragma once
+#include <stdint.h>
+#include "mgpu_device.cuh"
+
+struct ff {
+    float hi, lo;
+};
+struct f3 {
+    float x, y, z;
+};
+struct ff3 {
+    ff x, y, z;
+};
+
+__device__ __forceinline__ f3 operator+(f3 a, f3 b) { return f3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ f3 operator-(f3 a, f3 b) { return f3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ f3 operator*(float s, f3 a) { return f3{s * a.x, s * a.y, s * a.z}; }
+__device__ __forceinline__ float dotf(f3 a, f3 b) { return fmaf(a.x, b.x, fmaf(a.y, b.y, a.z * b.z)); }
+__device__ __forceinline__ f3 crossf(f3 a, f3 b) {
+    return f3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+__device__ __forceinline__ f3 normf(f3 v) {
+    float r = rsqrtf(dotf(v, v));
+    return f3{v.x * r, v.y * r, v.z * r};
+}
+__device__ __forceinline__ f3 ldf3(const float* p) { return f3{p[0], p[1], p[2]}; }
+
+// ---------------------------------------------------------------- float-float
+__device__ __forceinline__ ff two_sum(float a, float b) {
+    float s = a + b;
+    float bb = s - a;
+    float e = (a - (s - bb)) + (b - bb);
+    return ff{s, e};
+}
+__device__ __forceinline__ ff fast_two_sum(float a, float b) {   // |a| >= |b|
+    float s = a + b;
+    return ff{s, b - (s - a)};
+}
+__device__ __forceinline__ ff two_prod(float a, float b) {
+    float p = a * b;
+    return ff{p, fmaf(a, b, -p)};
+}
+__device__ __forceinline__ ff ff_add(ff a, ff b) {
+    ff s = two_sum(a.hi, b.hi);
+    ff t = two_sum(a.lo, b.lo);
+    s.lo += t.hi;
+    s = fast_two_sum(s.hi, s.lo);
+    s.lo += t.lo;
+    return fast_two_sum(s.hi, s.lo);
+}
+__device__ __forceinline__ ff ff_neg(ff a) { return ff{-a.hi, -a.lo}; }
+__device__ __forceinline__ ff ff_sub(ff a, ff b) { return ff_add(a, ff_neg(b)); }
+__device__ __forceinline__ ff ff_add_f(ff a, float b) {
+    ff s = two_sum(a.hi, b);
+    s.lo += a.lo;
+    return fast_two_sum(s.hi, s.lo);
+}
+__device__ __forceinline__ ff ff_mul_f(ff a, float b) {
+    ff p = two_prod(a.hi, b);
+    p.lo = fmaf(a.lo, b, p.lo);
+    return fast_two_sum(p.hi, p.lo);
+}
+__device__ __forceinline__ ff ff_mul(ff a, ff b) {
+    ff p = two_prod(a.hi, b.hi);
+    p.lo = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, p.lo));
+    return fast_two_sum(p.hi, p.lo);
+}
+__device__ __forceinline__ ff ff_div(ff a, ff b) {
+    float q1 = __fdividef(a.hi, b.hi);
+    ff r = ff_sub(a, ff_mul_f(b, q1));
+    float q2 = __fdividef(r.hi, b.hi);
+    return fast_two_sum(q1, q2);
+}
+__device__ __forceinline__ float ff_f(ff a) { return a.hi + a.lo; }
+
+__device__ __forceinline__ ff3 ff3_add_f3(ff3 a, f3 b) {
+    return ff3{ff_add_f(a.x, b.x), ff_add_f(a.y, b.y), ff_add_f(a.z, b.z)};
+}
+__device__ __forceinline__ ff3 ff3_sub(ff3 a, ff3 b) {
+    return ff3{ff_sub(a.x, b.x), ff_sub(a.y, b.y), ff_sub(a.z, b.z)};
+}
+__device__ __forceinline__ f3 ff3_f(ff3 a) { return f3{ff_f(a.x), ff_f(a.y), ff_f(a.z)}; }
+// a + k * d with the products formed exactly
+__device__ __forceinline__ ff3 ff3_axpy(ff3 a, float k, f3 d) {
+    return ff3{ff_add(a.x, two_prod(k, d.x)), ff_add(a.y, two_prod(k, d.y)),
+               ff_add(a.z, two_prod(k, d.z))};
+}
+__device__ __forceinline__ ff ff_dot_f(ff3 a, f3 b) {
+    ff s = ff_mul_f(a.x, b.x);
+    s = ff_add(s, ff_mul_f(a.y, b.y));
+    return ff_add(s, ff_mul_f(a.z, b.z));
+}
+__device__ __forceinline__ ff ff_dot(ff3 a, ff3 b) {
+    ff s = ff_mul(a.x, b.x);
+    s = ff_add(s, ff_mul(a.y, b.y));
+    return ff_add(s, ff_mul(a.z, b.z));
+}
+
+// ---------------------------------------------------------- bit conversions
+// float64 -> float32, round to nearest even, on the integer pipe.
+// Magnitudes below 2^-126 flush to signed zero; beyond float range -> inf;
+// NaN stays NaN.
+__device__ __forceinline__ float d2f_bits(double d) {
+    uint32_t hi = (uint32_t)__double2hiint(d), lo = (uint32_t)__double2loint(d);
+    uint32_t sign = hi & 0x80000000u;
+    uint32_t e = (hi >> 20) & 0x7ffu;
+    uint32_t m = __funnelshift_l(lo, hi, 3);            // (hi << 3) | (lo >> 29)
+    uint32_t r = (m - 0x70000000u) & 0x7fffffffu;        // rebias 1023 -> 127
+    uint32_t rem = lo & 0x1fffffffu;
+    r += (rem > 0x10000000u) | ((rem == 0x10000000u) & (r & 1u));
+    uint32_t bits;
+    if (e >= 897u && e <= 1150u) bits = r;
+    else if (e < 897u) bits = 0u;
+    else if (e == 0x7ffu && (((hi & 0xfffffu) | lo) != 0u)) bits = 0x7fc00000u;
+    else bits = 0x7f800000u;
+    return __uint_as_float(bits | sign);
+}
+
+// float32 -> float64, exact, on the integer pipe (denormal floats -> 0)
+__device__ __forceinline__ double f2d_bits(float f) {
+    uint32_t b = __float_as_uint(f);
+    uint32_t sign = b & 0x80000000u, mag = b & 0x7fffffffu;
+    uint32_t hi, lo;
+    if (mag >= 0x00800000u && mag < 0x7f800000u) {
+        hi = (mag >> 3) + 0x38000000u;
+        lo = b << 29;
+    } else if (mag >= 0x7f800000u) {
+        hi = 0x7ff00000u | (mag >> 3);
+        lo = b << 29;
+    } else {
+        hi = 0u;
+        lo = 0u;
+    }
+    return __hiloint2double((int)(hi | sign), (int)lo);
+}
+
+// float64 -> float-float: hi = round(d), lo = (d - hi) rounded, on the
+// integer pipe plus one I2F and one FMUL.  Exact to ~2^-48 relative.
+__device__ __forceinline__ ff d2ff_bits(double d) {
+    float hi = d2f_bits(d);
+    uint32_t dhi = (uint32_t)__double2hiint(d), dlo = (uint32_t)__double2loint(d);
+    uint32_t e = (dhi >> 20) & 0x7ffu;
+    if (e < 897u + 29u || e > 1150u) return ff{hi, 0.0f};
+    // residual = (low 29 mantissa bits - 2^29 if rounded up) * 2^(e - 1075)
+    int32_t rem = (int32_t)(dlo & 0x1fffffffu);
+    uint32_t mag_d = ((dhi & 0x7fffffffu) << 3) | (dlo >> 29);
+    uint32_t mag_f = __float_as_uint(hi) & 0x7fffffffu;
+    if (mag_f != ((mag_d - 0x70000000u) & 0x7fffffffu)) rem -= 0x20000000;   // rounded up
+    float scale = __uint_as_float((e - 1075u + 127u) << 23);
+    float lo = __int2float_rn(rem) * scale;
+    if (dhi & 0x80000000u) lo = -lo;
+    return ff{hi, lo};
+}
+
+// float-float -> float64: one FP64 add of two exact conversions
+__device__ __forceinline__ double ff2d(ff a) { return f2d_bits(a.hi) + f2d_bits(a.lo); }

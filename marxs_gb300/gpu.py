@@ -85,15 +85,41 @@ class _Instrument:
     """Device copy of the lowered chain: facet tables, selectors, grids."""
 
     def __init__(self, stages, device, stream):
+        from . import lowering as L
         self.stages = stages
         self.device = device
         self.keep = []            # device tensors referenced by raw pointers
         self.stage_facets = {}
         self.stage_selectors = {}
         self.stage_grid = {}
+        self.stage_aux = {}       # FP32-local constant blocks
+        self.stage_facets32 = {}
+        self.stage_table = {}
+        self.fp32_error = None
         lib = _abi.load()
         status = torch.zeros(1, dtype=torch.int32, device=device)
+
+        def dev_bytes(raw):
+            t = torch.from_numpy(np.frombuffer(raw, dtype=np.uint8).copy()).to(device)
+            self.keep.append(t)
+            return t
+
         for si, st in enumerate(stages):
+            try:
+                if st.kind in (_abi.STAGE_LENS, _abi.STAGE_SCATTER, _abi.STAGE_FLATDET):
+                    self.stage_aux[si] = dev_bytes(L.flat32_block(st))
+                elif st.kind == _abi.STAGE_CYLDET:
+                    blk, table = L.cyl32_block(st)
+                    self.stage_aux[si] = dev_bytes(blk)
+                    self.stage_table[si] = dev_bytes(table.tobytes())
+                elif st.kind == _abi.STAGE_GRATINGS:
+                    self.stage_facets32[si] = dev_bytes(L.facets32_table(st.facets).tobytes())
+                    if st.grid is not None:
+                        self.stage_aux[si] = dev_bytes(L.grid32_block(st.grid))
+                    else:
+                        self.stage_aux[si] = dev_bytes(bytes(_abi.MgpuGrid32()))
+            except NotImplementedError as exc:
+                self.fp32_error = str(exc)
             if st.kind != _abi.STAGE_GRATINGS:
                 continue
             fac = torch.from_numpy(st.facets.view(np.uint8).copy()).to(device)
@@ -105,10 +131,13 @@ class _Instrument:
                 cdf = torch.from_numpy(np.ascontiguousarray(s.cdf)).to(device)
                 tot = torch.from_numpy(np.ascontiguousarray(s.total)).to(device)
                 ords = torch.from_numpy(np.ascontiguousarray(s.orders, dtype=np.int32)).to(device)
-                self.keep += [e, cdf, tot, ords]
+                thr = torch.from_numpy(L.selector_thresholds(s).view(np.int64)).to(device)
+                self.keep += [e, cdf, tot, ords, thr]
                 sel_structs[k] = _abi.MgpuSelector(s.cdf.shape[0], s.cdf.shape[1],
-                                                   1 if s.by_energy else 0, 0, e.data_ptr(),
-                                                   cdf.data_ptr(), tot.data_ptr(), ords.data_ptr())
+                                                   1 if s.by_energy else 0,
+                                                   1 if L.selector_sorted(s) else 0, e.data_ptr(),
+                                                   cdf.data_ptr(), tot.data_ptr(), ords.data_ptr(),
+                                                   thr.data_ptr())
             raw = np.frombuffer(bytes(sel_structs), dtype=np.uint8).copy()
             sel_dev = torch.from_numpy(raw).to(device)
             self.keep.append(sel_dev)
@@ -153,6 +182,12 @@ class _Instrument:
             s.n_selectors = len(st.selectors)
             if si in self.stage_grid:
                 s.grid = self.stage_grid[si]
+        if si in self.stage_aux:
+            s.aux = self.stage_aux[si].data_ptr()
+        if si in self.stage_facets32:
+            s.facets32 = self.stage_facets32[si].data_ptr()
+        if si in self.stage_table:
+            s.table = self.stage_table[si].data_ptr()
 
 
 class ColumnPlan:
@@ -238,6 +273,8 @@ class GpuSequence:
 
     # ------------------------------------------------------------ launch
     def _chain(self, inst, plan, bufs, draws_dev, n, status, hits, row_base=0):
+        if self.precision == 'fp32local' and inst.fp32_error:
+            raise NotImplementedError(inst.fp32_error)
         chain = _abi.MgpuChain()
         chain.row_base = int(row_base)
         chain.n_stages = len(inst.stages)

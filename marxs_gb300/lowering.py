@@ -323,3 +323,111 @@ def fingerprint(stages):
             for a in (s.energy, s.cdf, s.total, s.orders):
                 h.update(np.ascontiguousarray(a).tobytes())
     return h.hexdigest()
+
+
+# ---------------------------------------------------------------------------
+# FP32-local constant blocks
+# ---------------------------------------------------------------------------
+def split_ff(x):
+    """float64 -> (hi, lo) float32 pair with hi + lo ~ x to ~2^-48."""
+    x = np.asarray(x, dtype=np.float64)
+    hi = x.astype(np.float32)
+    lo = (x - hi.astype(np.float64)).astype(np.float32)
+    return hi, lo
+
+
+def flat32_block(st):
+    b = _abi.MgpuFlat32()
+    hi, lo = split_ff(st.frame[0:3])
+    b.c_hi[:] = [float(v) for v in hi]
+    b.c_lo[:] = [float(v) for v in lo]
+    b.ex[:] = [float(v) for v in np.float32(st.frame[3:6])]
+    b.ey[:] = [float(v) for v in np.float32(st.frame[6:9])]
+    b.ez[:] = [float(v) for v in np.float32(st.frame[9:12])]
+    b.hy = float(np.float32(st.frame[12]))
+    b.hz = float(np.float32(st.frame[13]))
+    p = [float(v) for v in st.p[:6]]
+    if st.kind == _abi.STAGE_FLATDET:
+        p[3] = 1.0 / st.p[0]
+    b.p[:] = p
+    return bytes(b)
+
+
+def facets32_table(facets):
+    out = np.zeros(len(facets), dtype=_abi.FACET32_DTYPE)
+    hi, lo = split_ff(facets['c'])
+    out['c_hi'], out['c_lo'] = hi, lo
+    for k in ('ex', 'ey', 'ez', 'l', 'dneg'):
+        out[k] = facets[k].astype(np.float32)
+    out['hy'] = facets['hy'].astype(np.float32)
+    out['hz'] = facets['hz'].astype(np.float32)
+    wd = 1.2398419292004202e-06 / facets['dgrat']
+    out['wd_hi'], out['wd_lo'] = split_ff(wd)
+    out['id_num'] = facets['id_num']
+    out['selector'] = facets['selector']
+    out['flags'] = facets['cat'] | (facets['transmission'] << 1)
+    return out
+
+
+def grid32_block(g):
+    b = _abi.MgpuGrid32()
+    hi, lo = split_ff(g['o'])
+    b.o_hi[:] = [float(v) for v in hi]
+    b.o_lo[:] = [float(v) for v in lo]
+    for key in ('n', 'a', 'b'):
+        getattr(b, key)[:] = [float(v) for v in np.float32(g[key])]
+    # the float32 lookup grows every footprint by 0.05 mm on the host side
+    b.u0 = float(g['u0'])
+    b.v0 = float(g['v0'])
+    b.inv_cell = float(1.0 / g['cell'])
+    b.slope_max = float(g['slope_max'])
+    b.nu, b.nv = g['nu'], g['nv']
+    return bytes(b)
+
+
+PHI_TABLE_STEP = 1024
+
+
+def cyl32_block(st):
+    """Cylinder constants and the cos/sin table of reference angles k/1024."""
+    from .geomath import decompose44
+    e = st.element
+    pos4d = np.asarray(e.geometry.pos4d, dtype=float)
+    T, R, Z, S = decompose44(pos4d)
+    if not np.isclose(Z[0], Z[1], rtol=1e-12, atol=0) or not np.allclose(S, 0, atol=1e-12):
+        raise NotImplementedError('fp32local supports circular, unsheared cylinders only')
+    b = _abi.MgpuCyl32()
+    for name, vec in (('c', T), ('e1', R[:, 0]), ('e2', R[:, 1]), ('a', R[:, 2])):
+        hi, lo = split_ff(vec)
+        getattr(b, name + '_hi')[:] = [float(v) for v in hi]
+        getattr(b, name + '_lo')[:] = [float(v) for v in lo]
+    rhi, rlo = split_ff(Z[0])
+    b.R_hi, b.R_lo = float(rhi), float(rlo)
+    b.Rz = float(Z[2])
+    b.b1 = float(st.cyl[26])
+    b.b2 = float(st.cyl[27])
+    ph, pl = split_ff(Z[0] / st.p[0])
+    b.rpix_hi, b.rpix_lo = float(ph), float(pl)
+    b.inv_pix = float(1.0 / st.p[0])
+    b.cp0 = float(st.p[1])
+    b.cp1 = float(st.p[2])
+    kmax = int(np.ceil((np.pi + 0.01) * PHI_TABLE_STEP))
+    k = np.arange(-kmax, kmax + 1)
+    ang = k / PHI_TABLE_STEP
+    ch, cl = split_ff(np.cos(ang))
+    sh, sl = split_ff(np.sin(ang))
+    table = np.stack([ch, cl, sh, sl], axis=1).astype(np.float32)
+    b.k0 = int(k[0])
+    b.nk = int(len(k))
+    return bytes(b), table
+
+
+def selector_thresholds(sel):
+    """ceil(cdf * 2^53) per entry: for u = U * 2^-53, cdf > u  <=>  U < threshold."""
+    scaled = np.ascontiguousarray(sel.cdf, dtype=np.float64) * 2.0 ** 53   # exact
+    return np.ceil(scaled).astype(np.uint64)
+
+
+def selector_sorted(sel):
+    e = np.asarray(sel.energy, dtype=np.float64)
+    return bool(sel.by_energy and len(e) > 0 and np.all(e > 0) and np.all(np.diff(e) > 0))

@@ -17,6 +17,7 @@ STRUCTS = {
     'mgpu_col': _abi.MgpuCol, 'mgpu_vec': _abi.MgpuVec, 'mgpu_photons': _abi.MgpuPhotons,
     'mgpu_selector': _abi.MgpuSelector, 'mgpu_grid': _abi.MgpuGrid,
     'mgpu_stage': _abi.MgpuStage, 'mgpu_chain': _abi.MgpuChain,
+    'mgpu_flat32': _abi.MgpuFlat32, 'mgpu_grid32': _abi.MgpuGrid32, 'mgpu_cyl32': _abi.MgpuCyl32,
 }
 
 
@@ -30,6 +31,9 @@ def _c_layout(tmp_path):
     lines.append('printf("mgpu_facet size %zu\\n", sizeof(mgpu_facet));')
     for fname in _abi.FACET_DTYPE.names:
         lines.append('printf("mgpu_facet.%s %%zu\\n", offsetof(mgpu_facet, %s));' % (fname, fname))
+    lines.append('printf("mgpu_facet32 size %zu\\n", sizeof(mgpu_facet32));')
+    for fname in _abi.FACET32_DTYPE.names:
+        lines.append('printf("mgpu_facet32.%s %%zu\\n", offsetof(mgpu_facet32, %s));' % (fname, fname))
     lines.append('return 0; }')
     src = tmp_path / 'layout.c'
     src.write_text('\n'.join(lines))
@@ -48,6 +52,9 @@ def test_struct_layout_matches_header(tmp_path):
     assert c['mgpu_facet size'] == _abi.FACET_DTYPE.itemsize
     for fname in _abi.FACET_DTYPE.names:
         assert c['mgpu_facet.' + fname] == _abi.FACET_DTYPE.fields[fname][1], fname
+    assert c['mgpu_facet32 size'] == _abi.FACET32_DTYPE.itemsize
+    for fname in _abi.FACET32_DTYPE.names:
+        assert c['mgpu_facet32.' + fname] == _abi.FACET32_DTYPE.fields[fname][1], fname
 
 
 def test_header_constants_match():

@@ -1,0 +1,100 @@
+"""FP32-local precision mode against the float64 path and the golden vectors.
+
+The FP32-local kernel re-centres every ray on the element it meets (positions
+are float-float), does the element arithmetic in float32 and keeps float64
+only for the final detector coordinates.  Both modes draw the same Philox
+numbers, so per photon they must pick the same facet and order (except for
+rays within ~1e-5 mm of a facet edge) and land within a fraction of a
+micron of each other.
+
+Tolerances, stated as the acceptance bar of the precision mode:
+* detector-position error over photons whose facet and order agree:
+  RMS <= 0.5 um, max <= 5 um (global x, y, z and (det_phi * R, det_y));
+* facet/order disagreement in at most 1e-4 of the photons;
+* against the reference's golden vectors (pre-drawn draws): the same bars,
+  directions within 1e-6, polarization within 1e-5 (float32 transport of
+  nearly parallel directions).
+"""
+import numpy as np
+import pytest
+
+from conftest import load_golden, golden_inputs, golden_outputs
+
+pytestmark = pytest.mark.gpu
+
+UM = 1e-3   # mm
+
+
+def _trace(inst, host, precision, rng='philox', draws=None):
+    from marxs_gb300 import PhotonTable
+    from marxs_gb300.gpu import GpuSequence
+    seq = GpuSequence(elements=inst.elements, precision=precision, rng=rng, seed=424242)
+    return seq(PhotonTable({k: np.array(v, copy=True) for k, v in host.items()}), draws=draws)
+
+
+def _agree(a, b):
+    fa, fb = np.asarray(a['facet']), np.asarray(b['facet'])
+    oa, ob = np.asarray(a['order']), np.asarray(b['order'])
+    return (fa == fb) & ((oa == ob) | (np.isnan(oa) & np.isnan(ob)))
+
+
+def _pos_err(a, b, mask):
+    pa, pb = np.asarray(a['pos'])[mask, :3], np.asarray(b['pos'])[mask, :3]
+    fin = np.all(np.isfinite(pb), axis=1)
+    d = np.linalg.norm(pa[fin] - pb[fin], axis=1)
+    return d
+
+
+@pytest.mark.parametrize('n', [400000])
+def test_fp32local_vs_fp64_cat_array(n):
+    from marxs_gb300 import configs
+    inst = configs.build('c2')
+    host = configs.photons_for('c2', n, seed=21)
+    a = _trace(inst, host, 'fp32local')
+    b = _trace(inst, host, 'fp64')
+    agree = _agree(a, b)
+    assert (~agree).sum() <= max(1, 1e-4 * n), (~agree).sum()
+    d = _pos_err(a, b, agree)
+    rms, mx = np.sqrt(np.mean(d ** 2)), d.max()
+    R = 5900.0
+    hit = agree & np.isfinite(np.asarray(b['det_phi']))
+    dphi = np.abs(np.asarray(a['det_phi'])[hit] - np.asarray(b['det_phi'])[hit]) * R
+    dy = np.abs(np.asarray(a['det_y'])[hit] - np.asarray(b['det_y'])[hit])
+    report = dict(mismatch=int((~agree).sum()), rms_um=rms / UM, max_um=mx / UM,
+                  phi_rms_um=np.sqrt(np.mean(dphi ** 2)) / UM, phi_max_um=dphi.max() / UM,
+                  dety_max_um=dy.max() / UM)
+    print('fp32local vs fp64:', report)
+    assert rms <= 0.5 * UM and mx <= 5 * UM, report
+    assert np.sqrt(np.mean(dphi ** 2)) <= 0.5 * UM and dphi.max() <= 5 * UM, report
+    assert dy.max() <= 5 * UM, report
+
+
+@pytest.mark.parametrize('name', ['c0', 'c1', 'c2'])
+def test_fp32local_golden(name):
+    from marxs_gb300 import configs
+    g = load_golden(name)
+    inst = configs.build(name)
+    draws = {}
+    for elem, kind in inst.draw_slots:
+        if kind == 'scatter':
+            draws[elem] = {'inplanescatter': g['draw_inplanescatter'],
+                           'perpplanescatter': g['draw_perpplanescatter']}
+        else:
+            draws[elem] = {'order_u': g['draw_order_u']}
+    out = _trace(inst, golden_inputs(g), 'fp32local', rng='predrawn', draws=draws)
+    ref = golden_outputs(g)
+    assert list(out.colnames) == [str(c) for c in g['colnames']]
+    agree = np.ones(g['n'], dtype=bool)
+    if 'facet' in ref:
+        agree = _agree(out, ref)
+        assert (~agree).sum() <= 1, (~agree).sum()
+    d = _pos_err(out, ref, agree)
+    assert np.sqrt(np.mean(d ** 2)) <= 0.5 * UM and d.max() <= 5 * UM, (d.max(), name)
+    for col, tol in (('dir', 1e-6), ('polarization', 1e-5)):
+        x, y = np.asarray(out[col])[agree], ref[col][agree]
+        assert np.nanmax(np.abs(x - y)) <= tol, (col, np.nanmax(np.abs(x - y)))
+    for col in ref:
+        if col in ('pos', 'dir', 'polarization', 'facet', 'order', 'energy'):
+            continue
+        x, y = np.asarray(out[col], dtype=float)[agree], ref[col].astype(float)[agree]
+        assert np.array_equal(np.isnan(x), np.isnan(y)), col
