@@ -110,59 +110,12 @@ __device__ __forceinline__ ff ff_dot(ff3 a, ff3 b) {
 }
 
 // ---------------------------------------------------------- bit conversions
-// float64 -> float32, round to nearest even, on the integer pipe.
-// Magnitudes below 2^-126 flush to signed zero; beyond float range -> inf;
-// NaN stays NaN.
-__device__ __forceinline__ float d2f_bits(double d) {
-    uint32_t hi = (uint32_t)__double2hiint(d), lo = (uint32_t)__double2loint(d);
-    uint32_t sign = hi & 0x80000000u;
-    uint32_t e = (hi >> 20) & 0x7ffu;
-    uint32_t m = __funnelshift_l(lo, hi, 3);            // (hi << 3) | (lo >> 29)
-    uint32_t r = (m - 0x70000000u) & 0x7fffffffu;        // rebias 1023 -> 127
-    uint32_t rem = lo & 0x1fffffffu;
-    r += (rem > 0x10000000u) | ((rem == 0x10000000u) & (r & 1u));
-    uint32_t bits;
-    if (e >= 897u && e <= 1150u) bits = r;
-    else if (e < 897u) bits = 0u;
-    else if (e == 0x7ffu && (((hi & 0xfffffu) | lo) != 0u)) bits = 0x7fc00000u;
-    else bits = 0x7f800000u;
-    return __uint_as_float(bits | sign);
-}
+#include "mgpu_bits.cuh"
 
-// float32 -> float64, exact, on the integer pipe (denormal floats -> 0)
-__device__ __forceinline__ double f2d_bits(float f) {
-    uint32_t b = __float_as_uint(f);
-    uint32_t sign = b & 0x80000000u, mag = b & 0x7fffffffu;
-    uint32_t hi, lo;
-    if (mag >= 0x00800000u && mag < 0x7f800000u) {
-        hi = (mag >> 3) + 0x38000000u;
-        lo = b << 29;
-    } else if (mag >= 0x7f800000u) {
-        hi = 0x7ff00000u | (mag >> 3);
-        lo = b << 29;
-    } else {
-        hi = 0u;
-        lo = 0u;
-    }
-    return __hiloint2double((int)(hi | sign), (int)lo);
-}
-
-// float64 -> float-float: hi = round(d), lo = (d - hi) rounded, on the
-// integer pipe plus one I2F and one FMUL.  Exact to ~2^-48 relative.
 __device__ __forceinline__ ff d2ff_bits(double d) {
-    float hi = d2f_bits(d);
-    uint32_t dhi = (uint32_t)__double2hiint(d), dlo = (uint32_t)__double2loint(d);
-    uint32_t e = (dhi >> 20) & 0x7ffu;
-    if (e < 897u + 29u || e > 1150u) return ff{hi, 0.0f};
-    // residual = (low 29 mantissa bits - 2^29 if rounded up) * 2^(e - 1075)
-    int32_t rem = (int32_t)(dlo & 0x1fffffffu);
-    uint32_t mag_d = ((dhi & 0x7fffffffu) << 3) | (dlo >> 29);
-    uint32_t mag_f = __float_as_uint(hi) & 0x7fffffffu;
-    if (mag_f != ((mag_d - 0x70000000u) & 0x7fffffffu)) rem -= 0x20000000;   // rounded up
-    float scale = __uint_as_float((e - 1075u + 127u) << 23);
-    float lo = __int2float_rn(rem) * scale;
-    if (dhi & 0x80000000u) lo = -lo;
-    return ff{hi, lo};
+    ff r;
+    d2ff_bits_pair(d, &r.hi, &r.lo);
+    return r;
 }
 
 // float-float -> float64: one FP64 add of two exact conversions
