@@ -186,12 +186,15 @@ def precision_error(a, b, torch):
     fa, fb = a['bufs']['facet'], b['bufs']['facet']
     oa, ob = a['bufs']['order'], b['bufs']['order']
     agree = (fa == fb) & ((oa == ob) | (torch.isnan(oa) & torch.isnan(ob)))
+    # a CAT sign decision sign(p . d) taken within float32 noise of zero
+    # (blaze < 1e-6 rad) is a discrete flip like a facet-edge flip
+    agree &= ~((b['bufs']['blaze'] < 1e-6) & (ob != 0))
     pa, pb = a['out'].pos, b['out'].pos
     m = agree & torch.isfinite(pb).all(0) & torch.isfinite(b['bufs']['det_phi'])
     d = ((pa - pb) ** 2).sum(0).sqrt()[m] * 1e3
     dphi = ((a['bufs']['det_phi'] - b['bufs']['det_phi']).abs() * 5900.0)[m] * 1e3
     dy = (a['bufs']['det_y'] - b['bufs']['det_y']).abs()[m] * 1e3
-    out = {'photons_compared': int(m.sum()), 'facet_or_order_mismatch': int((~agree).sum()),
+    out = {'photons_compared': int(m.sum()), 'decision_mismatch': int((~agree).sum()),
            'pos_rms_um': float((d ** 2).mean().sqrt()), 'pos_max_um': float(d.max()),
            'det_phi_R_rms_um': float((dphi ** 2).mean().sqrt()), 'det_phi_R_max_um': float(dphi.max()),
            'det_y_rms_um': float((dy ** 2).mean().sqrt()), 'det_y_max_um': float(dy.max())}

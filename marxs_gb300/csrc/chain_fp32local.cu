@@ -111,16 +111,35 @@ __device__ __forceinline__ f3 transport_f(f3 d_old, f3 d_new, f3 pol) {
               s.z * ks + pout.z * kp + b.z * kd};
 }
 
-// R^T v for R = axangle2mat(axis, angle): v - sin(a) (k x v) + (1 - cos a) k x (k x v),
-// with 1 - cos a = 2 sin^2(a/2) so small angles keep full relative precision
-__device__ __forceinline__ f3 rot_transpose_f(f3 axis, float a, f3 v) {
+// parallel transport for d_new = d_old + delta where the change delta is
+// known directly: the axis d_old x delta keeps full relative precision even
+// when the two directions are nearly parallel (a float32 cross product of the
+// two unit vectors would be dominated by rounding there).
+__device__ __forceinline__ f3 transport_delta_f(f3 d_old, f3 delta, f3 pol) {
+    f3 dn = d_old + delta;
+    f3 sx = crossf(d_old, delta);
+    float n0 = dotf(d_old, d_old), n1 = dotf(dn, dn);
+    float ss = dotf(sx, sx);
+    if (!(ss > 1e-16f * n0 * n1)) return pol;       // |a x b| <= 1e-8: identity
+    f3 s = rsqrtf(ss) * sx;
+    f3 a = rsqrtf(n0) * d_old, b = rsqrtf(n1) * dn;
+    f3 pin = crossf(a, s), pout = crossf(b, s);
+    float ks = dotf(s, pol), kp = dotf(pin, pol), kd = dotf(a, pol);
+    return f3{s.x * ks + pout.x * kp + b.x * kd, s.y * ks + pout.y * kp + b.y * kd,
+              s.z * ks + pout.z * kp + b.z * kd};
+}
+
+// change of v under R^T v for R = axangle2mat(axis, angle):
+// -sin(a) (k x v) + (1 - cos a) k x (k x v), with 1 - cos a = 2 sin^2(a/2)
+// so small angles keep full relative precision
+__device__ __forceinline__ f3 rot_transpose_delta_f(f3 axis, float a, f3 v) {
     f3 k = normf(axis);
     float s = sinf(a);
     float h = sinf(0.5f * a);
     float C = 2.0f * h * h;
     f3 kv = crossf(k, v);
     f3 kkv = crossf(k, kv);
-    return f3{v.x - s * kv.x + C * kkv.x, v.y - s * kv.y + C * kkv.y, v.z - s * kv.z + C * kkv.z};
+    return f3{-s * kv.x + C * kkv.x, -s * kv.y + C * kkv.y, -s * kv.z + C * kkv.z};
 }
 
 // 53-bit uniform as an integer and as float, from the Philox stream the
@@ -183,8 +202,11 @@ __device__ bool stage_scatter_l(const mgpu_stage& st, PhotonL& ph, int64_t i, in
     } else {
         uint64_t U0, U1;
         philox_u53(seed, row_base + (uint64_t)i, (uint32_t)sidx, &U0, &U1);
-        float u0 = u53_to_f(U0), u1 = u53_to_f(U1);
-        float r = sqrtf(-2.0f * __logf(1.0f - u0 + 1e-30f));
+        // 1 - u0 formed exactly from the 53-bit integer keeps the normal's
+        // tail identical to the float64 path's draw
+        float one_minus_u0 = (float)((1ull << 53) - U0) * 1.1102230246251565e-16f;
+        float u1 = u53_to_f(U1);
+        float r = sqrtf(-2.0f * __logf(one_minus_u0));
         float sn, cs;
         sincospif(2.0f * u1, &sn, &cs);
         a_in = sig_in * (r * cs);
@@ -192,11 +214,11 @@ __device__ bool stage_scatter_l(const mgpu_stage& st, PhotonL& ph, int64_t i, in
     }
     f3 radial = ff3_f(ff3_sub(ph.pos, ldff3(F->c_hi, F->c_lo)));   // previous position
     f3 perpplane = crossf(ph.dir, radial);
-    f3 outdir = ph.dir;
-    if (sig_in != 0.0f) outdir = rot_transpose_f(perpplane, a_in, outdir);
-    if (sig_perp != 0.0f) outdir = rot_transpose_f(radial, a_perp, outdir);
-    ph.pol = transport_f(ph.dir, outdir, ph.pol);
-    ph.dir = outdir;
+    f3 delta{0.0f, 0.0f, 0.0f};
+    if (sig_in != 0.0f) delta = rot_transpose_delta_f(perpplane, a_in, ph.dir);
+    if (sig_perp != 0.0f) delta = delta + rot_transpose_delta_f(radial, a_perp, ph.dir + delta);
+    ph.pol = transport_delta_f(ph.dir, delta, ph.pol);
+    ph.dir = ph.dir + delta;
     storef(st.out[0], i, h.ly);
     storef(st.out[1], i, h.lz);
     if (have_d) {
@@ -391,14 +413,35 @@ __device__ __forceinline__ int nearest_facet_grid_l(const mgpu_stage& st, const 
     int cell = (int)fu * G->nv + (int)fv;
     const mgpu_grid& g = st.grid;
     int s0 = __ldg(g.cell_start + cell), s1 = min(__ldg(g.cell_start + cell + 1), g.capacity);
+    float best_k = 0.0f;
     for (int q = s0; q < s1; ++q) {
         int f = __ldg(g.cell_items + q);
-        HitL h = facet_hit(st.facets32 + f, ph.pos, ph.dir);
-        if (h.hit && (best < 0 || h.k < best_hit->k || (h.k == best_hit->k && f < best))) {
+        const mgpu_facet32* fc = st.facets32 + f;
+        // plain float32 test first; the exact float-float test only when the
+        // ray passes within the float32 error band of an edge
+        f3 r{(ph.pos.x.hi - fc->c_hi[0]) + (ph.pos.x.lo - fc->c_lo[0]),
+             (ph.pos.y.hi - fc->c_hi[1]) + (ph.pos.y.lo - fc->c_lo[1]),
+             (ph.pos.z.hi - fc->c_hi[2]) + (ph.pos.z.lo - fc->c_lo[2])};
+        f3 nx = ldf3(fc->ex);
+        float kd = dotf(ph.dir, nx);
+        float k = -dotf(r, nx) / kd;
+        f3 v = r + k * ph.dir;
+        float ly = dotf(v, ldf3(fc->ey)), lz = dotf(v, ldf3(fc->ez));
+        float tol = 1e-6f * (fabsf(r.x) + fabsf(r.y) + fabsf(r.z) + fabsf(k)) + 1e-5f;
+        float my = fabsf(ly) - fc->hy, mz = fabsf(lz) - fc->hz;
+        if (!(kd != 0.0f) || !(k >= -tol) || !(my <= tol) || !(mz <= tol)) continue;
+        bool hit = true;
+        if (!(k > tol) || !(my < -tol) || !(mz < -tol)) {
+            HitL h = facet_hit(fc, ph.pos, ph.dir);
+            hit = h.hit;
+            k = h.k;
+        }
+        if (hit && (best < 0 || k < best_k || (k == best_k && f < best))) {
             best = f;
-            *best_hit = h;
+            best_k = k;
         }
     }
+    if (best >= 0) *best_hit = facet_hit(st.facets32 + best, ph.pos, ph.dir);
     return best;
 }
 
@@ -475,13 +518,19 @@ __device__ bool stage_gratings_l(const mgpu_stage& st, PhotonL& ph, int64_t i, b
     // sign * m * lambda / d in float-float
     ff term = ff_div(ff{fc->wd_hi, fc->wd_lo}, ph.energy);
     term = ff_mul_f(term, sign * (float)m);
+    float tf = ff_f(term);
     float pd2 = ff_f(ff_add_f(term, p_d));
     float p_n2 = sqrtf(1.0f - pd2 * pd2 - p_l * p_l);
-    float direction = (p_n > 0.0f) ? 1.0f : ((p_n < 0.0f) ? -1.0f : 0.0f);
-    if (!(flags & 2)) direction = -direction;
-    f3 nd = pd2 * dn + p_l * l + (direction * p_n2) * n;
-    ph.pol = transport_f(ph.dir, nd, ph.pol);
-    ph.dir = nd;
+    float sgn_n = (p_n > 0.0f) ? 1.0f : ((p_n < 0.0f) ? -1.0f : 0.0f);
+    // change of the unit direction: tf along d, and along n the difference
+    // p_n2 - |p_n| = -tf (2 p_d + tf) / (p_n2 + |p_n|) (no cancellation);
+    // a reflection grating flips the normal component instead
+    float dn_comp;
+    if (flags & 2) dn_comp = sgn_n * (-tf * (2.0f * p_d + tf)) / (p_n2 + fabsf(p_n));
+    else dn_comp = -sgn_n * p_n2 - p_n;
+    f3 delta = tf * dn + dn_comp * n;
+    ph.pol = transport_delta_f(p, delta, ph.pol);
+    ph.dir = p + delta;
     ph.prob *= selprob;
     storef(st.out[0], i, h.ly);
     storef(st.out[1], i, h.lz);

@@ -160,7 +160,7 @@ def _grating_facets(gratings, selectors, sel_index):
     return out
 
 
-def grid_params(facets, slope_max=0.15, margin=0.05, cells_per_facet=1.0):
+def grid_params(facets, slope_max=0.1, margin=0.05, cells_per_facet=2.0):
     """Mean plane, extents and cell size of the candidate grid for a facet table.
 
     The host computes each facet's grown footprint the same way the device
