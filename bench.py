@@ -186,9 +186,9 @@ def precision_error(a, b, torch):
     fa, fb = a['bufs']['facet'], b['bufs']['facet']
     oa, ob = a['bufs']['order'], b['bufs']['order']
     agree = (fa == fb) & ((oa == ob) | (torch.isnan(oa) & torch.isnan(ob)))
-    # a CAT sign decision sign(p . d) taken within float32 noise of zero
-    # (blaze < 1e-6 rad) is a discrete flip like a facet-edge flip
-    agree &= ~((b['bufs']['blaze'] < 1e-6) & (ob != 0))
+    # a CAT sign decision sign(p . d) taken within a few float32 roundings of
+    # zero (blaze < 2e-7 rad) is a discrete flip like a facet-edge flip
+    agree &= ~((b['bufs']['blaze'] < 2e-7) & (ob != 0))
     pa, pb = a['out'].pos, b['out'].pos
     m = agree & torch.isfinite(pb).all(0) & torch.isfinite(b['bufs']['det_phi'])
     d = ((pa - pb) ** 2).sum(0).sqrt()[m] * 1e3

@@ -20,6 +20,7 @@
 // the FP64 pipe only sees a handful of adds per photon for the final
 // float64 detector coordinates.
 #include <cuda_runtime.h>
+#include <utility>
 #include "mgpu_ff.cuh"
 
 namespace {
@@ -132,10 +133,20 @@ __device__ __forceinline__ f3 transport_delta_f(f3 d_old, f3 delta, f3 pol) {
 // change of v under R^T v for R = axangle2mat(axis, angle):
 // -sin(a) (k x v) + (1 - cos a) k x (k x v), with 1 - cos a = 2 sin^2(a/2)
 // so small angles keep full relative precision
+// sin for the small scatter angles (|a| < 1e-2: odd polynomial, error below
+// a^7/5040 relative), the library sine otherwise
+__device__ __forceinline__ float sin_small(float a) {
+    if (fabsf(a) < 1e-2f) {
+        float a2 = a * a;
+        return a * (1.0f - a2 * (1.0f / 6.0f) * (1.0f - a2 * (1.0f / 20.0f)));
+    }
+    return sinf(a);
+}
+
 __device__ __forceinline__ f3 rot_transpose_delta_f(f3 axis, float a, f3 v) {
     f3 k = normf(axis);
-    float s = sinf(a);
-    float h = sinf(0.5f * a);
+    float s = sin_small(a);
+    float h = sin_small(0.5f * a);
     float C = 2.0f * h * h;
     f3 kv = crossf(k, v);
     f3 kkv = crossf(k, kv);
@@ -541,6 +552,73 @@ __device__ bool stage_gratings_l(const mgpu_stage& st, PhotonL& ph, int64_t i, b
     return true;
 }
 
+// one stage, kind known at compile time (KIND > 0) or read from the
+// descriptor (KIND == 0, generic chains)
+template <int KIND>
+__device__ __forceinline__ bool run_stage_l(const mgpu_stage& st, PhotonL& ph, int64_t i,
+                                            bool valid, const mgpu_chain& chain, int s) {
+    const int kind = KIND ? KIND : st.kind;
+    switch (kind) {
+    case MGPU_STAGE_GRATINGS:
+        return stage_gratings_l(st, ph, i, valid, chain.rng, chain.seed, chain.row_base, s,
+                                chain.status);
+    case MGPU_STAGE_LENS:
+        return valid && stage_lens_l(st, ph, i);
+    case MGPU_STAGE_SCATTER:
+        return valid && stage_scatter_l(st, ph, i, chain.rng, chain.seed, chain.row_base, s,
+                                        chain.status);
+    case MGPU_STAGE_FLATDET:
+        return valid && stage_flatdet_l(st, ph, i);
+    case MGPU_STAGE_CYLDET:
+        return valid && stage_cyldet_l(st, ph, i);
+    default:
+        if (valid) atomicOr(chain.status, MGPU_STATUS_BAD_STAGE);
+        return false;
+    }
+}
+
+__device__ __forceinline__ void count_hits(bool hit, unsigned* s_hits, int s, int lane) {
+    unsigned m = __ballot_sync(MGPU_FULL_MASK, hit);
+    if (lane == 0 && m) atomicAdd(&s_hits[s], (unsigned)__popc(m));
+}
+
+// generic chain: stage loop over the descriptors
+struct GenericChain {
+    __device__ static void run(const mgpu_chain& chain, PhotonL& ph, int64_t i, bool valid,
+                               unsigned* s_hits, int lane) {
+        for (int s = 0; s < chain.n_stages; ++s)
+            count_hits(run_stage_l<0>(chain.stages[s], ph, i, valid, chain, s), s_hits, s, lane);
+    }
+};
+
+// fixed chain: stage kinds and descriptor offsets known at compile time, so
+// the per-stage constants are read straight from the parameter bank
+template <int... K>
+struct FixedChain {
+    template <int KIND, int S>
+    __device__ static void step(const mgpu_chain& chain, PhotonL& ph, int64_t i, bool valid,
+                                unsigned* s_hits, int lane) {
+        count_hits(run_stage_l<KIND>(chain.stages[S], ph, i, valid, chain, S), s_hits, S, lane);
+    }
+    template <int... S>
+    __device__ static void run_seq(const mgpu_chain& chain, PhotonL& ph, int64_t i, bool valid,
+                                   unsigned* s_hits, int lane, std::integer_sequence<int, S...>) {
+        (step<K, S>(chain, ph, i, valid, s_hits, lane), ...);
+    }
+    __device__ static void run(const mgpu_chain& chain, PhotonL& ph, int64_t i, bool valid,
+                               unsigned* s_hits, int lane) {
+        run_seq(chain, ph, i, valid, s_hits, lane, std::make_integer_sequence<int, sizeof...(K)>{});
+    }
+    static bool matches(const mgpu_chain& chain) {
+        const int kinds[] = {K...};
+        if (chain.n_stages != (int)sizeof...(K)) return false;
+        for (int s = 0; s < chain.n_stages; ++s)
+            if (chain.stages[s].kind != kinds[s]) return false;
+        return true;
+    }
+};
+
+template <class Chain>
 __global__ void __launch_bounds__(kThreads)
 chain_fp32local_kernel(const __grid_constant__ mgpu_chain chain, const __grid_constant__ mgpu_photons io) {
     __shared__ unsigned int s_hits[MGPU_MAX_STAGES];
@@ -569,33 +647,7 @@ chain_fp32local_kernel(const __grid_constant__ mgpu_chain chain, const __grid_co
             ph.energy_d = 1.0;
             ph.prob = 0.f;
         }
-        for (int s = 0; s < chain.n_stages; ++s) {
-            const mgpu_stage& st = chain.stages[s];
-            bool hit = false;
-            switch (st.kind) {
-            case MGPU_STAGE_GRATINGS:
-                hit = stage_gratings_l(st, ph, i, valid, chain.rng, chain.seed, chain.row_base, s,
-                                       chain.status);
-                break;
-            case MGPU_STAGE_LENS:
-                if (valid) hit = stage_lens_l(st, ph, i);
-                break;
-            case MGPU_STAGE_SCATTER:
-                if (valid) hit = stage_scatter_l(st, ph, i, chain.rng, chain.seed, chain.row_base, s,
-                                                 chain.status);
-                break;
-            case MGPU_STAGE_FLATDET:
-                if (valid) hit = stage_flatdet_l(st, ph, i);
-                break;
-            case MGPU_STAGE_CYLDET:
-                if (valid) hit = stage_cyldet_l(st, ph, i);
-                break;
-            default:
-                if (valid) atomicOr(chain.status, MGPU_STATUS_BAD_STAGE);
-            }
-            unsigned m = __ballot_sync(MGPU_FULL_MASK, hit);
-            if (lane == 0 && m) atomicAdd(&s_hits[s], (unsigned)__popc(m));
-        }
+        Chain::run(chain, ph, i, valid, s_hits, lane);
         if (valid) {
             store3(io.pos_out, i, d3{ff2d(ph.pos.x), ff2d(ph.pos.y), ff2d(ph.pos.z)});
             store3(io.dir_out, i, d3{f2d_bits(ph.dir.x), f2d_bits(ph.dir.y), f2d_bits(ph.dir.z)});
@@ -607,6 +659,12 @@ chain_fp32local_kernel(const __grid_constant__ mgpu_chain chain, const __grid_co
     if (threadIdx.x < chain.n_stages && s_hits[threadIdx.x])
         atomicAdd(chain.hits + threadIdx.x, (unsigned long long)s_hits[threadIdx.x]);
 }
+
+// the chains of the standard instruments: lens, scatter, gratings, cylinder
+// or flat detector; lens, scatter, flat detector
+using ChainCat = FixedChain<MGPU_STAGE_LENS, MGPU_STAGE_SCATTER, MGPU_STAGE_GRATINGS, MGPU_STAGE_CYLDET>;
+using ChainSpec = FixedChain<MGPU_STAGE_LENS, MGPU_STAGE_SCATTER, MGPU_STAGE_GRATINGS, MGPU_STAGE_FLATDET>;
+using ChainTel = FixedChain<MGPU_STAGE_LENS, MGPU_STAGE_SCATTER, MGPU_STAGE_FLATDET>;
 
 }  // namespace
 
@@ -623,6 +681,13 @@ cudaError_t mgpu_launch_chain_fp32local(const mgpu_chain& chain, const mgpu_phot
     int64_t blocks = (warps * 32 + kThreads - 1) / kThreads;
     int64_t cap = (int64_t)sm_count * 8;
     if (blocks > cap) blocks = cap;
-    chain_fp32local_kernel<<<(unsigned)blocks, kThreads, 0, stream>>>(chain, io);
+    if (ChainCat::matches(chain))
+        chain_fp32local_kernel<ChainCat><<<(unsigned)blocks, kThreads, 0, stream>>>(chain, io);
+    else if (ChainSpec::matches(chain))
+        chain_fp32local_kernel<ChainSpec><<<(unsigned)blocks, kThreads, 0, stream>>>(chain, io);
+    else if (ChainTel::matches(chain))
+        chain_fp32local_kernel<ChainTel><<<(unsigned)blocks, kThreads, 0, stream>>>(chain, io);
+    else
+        chain_fp32local_kernel<GenericChain><<<(unsigned)blocks, kThreads, 0, stream>>>(chain, io);
     return cudaGetLastError();
 }

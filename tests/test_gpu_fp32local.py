@@ -11,7 +11,7 @@ Tolerances, stated as the acceptance bar of the precision mode:
 * detector-position error over photons whose facet and order agree:
   RMS <= 0.5 um, max <= 5 um (global x, y, z and (det_phi * R, det_y));
 * facet/order disagreement (plus CAT sign decisions taken within float32
-  noise of zero, blaze < 1e-6 rad) in at most 1e-4 of the photons;
+  noise of zero, blaze < 2e-7 rad) in at most 1e-4 of the photons;
 * against the reference's golden vectors (pre-drawn draws): the same bars,
   directions within 1e-6, polarization within 1e-5 (float32 transport of
   nearly parallel directions).
@@ -24,6 +24,8 @@ from conftest import load_golden, golden_inputs, golden_outputs
 pytestmark = pytest.mark.gpu
 
 UM = 1e-3   # mm
+# |p . d| below this is within a few float32 roundings of zero (6e-8 each)
+SIGN_BAND = 2e-7
 
 
 def _trace(inst, host, precision, rng='philox', draws=None):
@@ -36,14 +38,14 @@ def _trace(inst, host, precision, rng='philox', draws=None):
 def _agree(a, b):
     """Photons whose discrete decisions agree: same facet, same order, and a
     CAT sign decision sign(p . d) that is not within float32 noise of zero
-    (blaze angle >= 1e-6 rad of the float64 result, or order 0)."""
+    (blaze angle of the float64 result >= SIGN_BAND, or order 0)."""
     fa, fb = np.asarray(a['facet']), np.asarray(b['facet'])
     oa, ob = np.asarray(a['order']), np.asarray(b['order'])
     same = (fa == fb) & ((oa == ob) | (np.isnan(oa) & np.isnan(ob)))
-    if 'blaze' in b.colnames:
+    if 'blaze' in b:
         bl = np.asarray(b['blaze'])
         with np.errstate(invalid='ignore'):
-            same &= ~((bl < 1e-6) & (ob != 0))
+            same &= ~((bl < SIGN_BAND) & (ob != 0))
     return same
 
 
