@@ -235,6 +235,25 @@ int mgpu_trace(const mgpu_chain* chain, const mgpu_photons* photons, void* strea
 int mgpu_facet_grid_build(const mgpu_facet* facets, int32_t n_facets, mgpu_grid* grid,
                           int32_t* counts, uint32_t* status, void* stream);
 
+/* Allocation-free variant of mgpu_facet_grid_build; it has no counterpart in
+ * the reference.  For callers that cannot allocate device memory when they
+ * rebuild the grid (a host whose own pool owns the device memory, or a loop
+ * where cudaMalloc/cudaFree would synchronise the device): the per-cell
+ * scratch lives in a fixed device array of MGPU_NOALLOC_MAX_CELLS + 1 int32
+ * (256 KiB, held on every GPU that loads the library until the process
+ * exits), and the entry point calls no allocator.  The caller still passes
+ * the facets, the grid with its cell_start / cell_items outputs, and the
+ * status word.  Grids with nu * nv > MGPU_NOALLOC_MAX_CELLS are rejected with
+ * MGPU_ERR_NOALLOC_LIMIT before anything is launched.  The first call on a
+ * device looks up the array's device address with that device current; make
+ * that first call before any stream capture.  All calls share the array:
+ * each call clears it before use, and calls that overlap on the GPU (other
+ * streams, other host threads) race on it. */
+#define MGPU_NOALLOC_MAX_CELLS 65536
+#define MGPU_ERR_NOALLOC_LIMIT (-2)
+int mgpu_facet_grid_build_noalloc(const mgpu_facet* facets, int32_t n_facets, mgpu_grid* grid,
+                                  uint32_t* status, void* stream);
+
 /* FinitePlane.intersect for one element frame (c, ex, ey, ez, hy, hz as in
  * mgpu_stage.frame).  Outputs: hit (uint8), interpos (vec), local (2 cols). */
 int mgpu_plane_intersect(const double* frame14, int64_t n, mgpu_vec pos, mgpu_vec dir,

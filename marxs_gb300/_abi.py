@@ -23,6 +23,9 @@ STATUS_BAD_STAGE = 0x4
 STATUS_GRID_RANGE = 0x8
 STATUS_GRID_FULL = 0x10
 
+NOALLOC_MAX_CELLS = 65536
+ERR_NOALLOC_LIMIT = -2
+
 FP64 = 0
 FP32LOCAL = 1
 RNG_PREDRAWN = 0
@@ -124,6 +127,8 @@ SIGNATURES = {
     'mgpu_trace': (C.c_int, [C.POINTER(MgpuChain), C.POINTER(MgpuPhotons), C.c_void_p]),
     'mgpu_facet_grid_build': (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(MgpuGrid), C.c_void_p,
                                         C.c_void_p, C.c_void_p]),
+    'mgpu_facet_grid_build_noalloc': (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(MgpuGrid),
+                                                C.c_void_p, C.c_void_p]),
     'mgpu_plane_intersect': (C.c_int, [C.c_void_p, C.c_int64, MgpuVec, MgpuVec, C.c_void_p,
                                        MgpuVec, MgpuCol, MgpuCol, C.c_void_p]),
     'mgpu_cylinder_intersect': (C.c_int, [C.c_void_p, C.c_int64, MgpuVec, MgpuVec, C.c_void_p,

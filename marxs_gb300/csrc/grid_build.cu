@@ -10,6 +10,7 @@
 // in every cell its footprint box, grown by max|delta| * slope_max + margin,
 // overlaps gives each cell a superset of the facets a ray through that cell
 // can hit.  Lists are built as counts -> exclusive scan -> fill (CSR).
+#include <atomic>
 #include <cuda_runtime.h>
 #include "mgpu_device.cuh"
 
@@ -134,4 +135,48 @@ cudaError_t mgpu_launch_grid_build(const mgpu_facet* facets, int n_facets, const
     grid_sort_kernel<<<(n_cells + T - 1) / T, T, 0, stream>>>(g.cell_start, n_cells, g.capacity,
                                                                g.cell_items);
     return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free grid build.
+//
+// Some callers cannot allocate device memory when they (re)build the facet
+// candidate grid: a host application that has handed (nearly) all device
+// memory to its own pool, or a loop that must not call cudaMalloc/cudaFree
+// because those synchronise the device and stall its other streams.  This
+// variant keeps the build's scratch -- one counter per grid cell -- in the
+// fixed array below instead of caller-provided memory.  The array holds
+// MGPU_NOALLOC_MAX_CELLS + 1 int32 (256 KiB) on every GPU that loads the
+// library, for the life of the process.
+// ---------------------------------------------------------------------------
+static __device__ __align__(256) int32_t g_noalloc_counts[MGPU_NOALLOC_MAX_CELLS + 1];
+
+namespace {
+constexpr int kNoallocMaxDevices = 64;
+std::atomic<void*> g_noalloc_addr[kNoallocMaxDevices];
+}  // namespace
+
+extern "C" int mgpu_facet_grid_build_noalloc(const mgpu_facet* facets, int32_t n_facets,
+                                             mgpu_grid* grid, uint32_t* status, void* stream) {
+    if (grid == nullptr || status == nullptr) return (int)cudaErrorInvalidValue;
+    if (grid->nu <= 0 || grid->nv <= 0 || grid->cell_start == nullptr || grid->cell_items == nullptr)
+        return (int)cudaErrorInvalidValue;
+    if ((long long)grid->nu * (long long)grid->nv > MGPU_NOALLOC_MAX_CELLS)
+        return MGPU_ERR_NOALLOC_LIMIT;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return (int)e;
+    if (dev < 0 || dev >= kNoallocMaxDevices) return (int)cudaErrorInvalidDevice;
+    // the host-side name of the array is not a device address: look the
+    // address up once per device, with that device current (first call)
+    void* scratch = g_noalloc_addr[dev].load(std::memory_order_acquire);
+    if (scratch == nullptr) {
+        e = cudaGetSymbolAddress(&scratch, g_noalloc_counts);
+        if (e != cudaSuccess) return (int)e;
+        g_noalloc_addr[dev].store(scratch, std::memory_order_release);
+    }
+    // mgpu_launch_grid_build clears the counters before use, so a call never
+    // sees the previous call's contents
+    return (int)mgpu_launch_grid_build(facets, n_facets, *grid, (int*)scratch, status,
+                                       (cudaStream_t)stream);
 }

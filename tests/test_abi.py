@@ -67,6 +67,9 @@ def test_header_constants_match():
         assert int(consts['MGPU_STATUS_' + name].rstrip('u'), 16) == getattr(_abi, 'STATUS_' + name)
     for name in ('LENS', 'SCATTER', 'FLATDET', 'GRATINGS', 'CYLDET'):
         assert int(consts['MGPU_STAGE_' + name]) == getattr(_abi, 'STAGE_' + name)
+    assert int(consts['MGPU_NOALLOC_MAX_CELLS']) == _abi.NOALLOC_MAX_CELLS
+    assert re.search(r'#define MGPU_ERR_NOALLOC_LIMIT \((-?\d+)\)', text).group(1) == \
+        str(_abi.ERR_NOALLOC_LIMIT)
 
 
 def _declared_functions():
