@@ -119,7 +119,9 @@ __device__ __forceinline__ PlaneHit plane_intersect(d3 c, d3 ex, d3 ey, d3 ez, d
     double kn = dot3(c - pos, ex);
     double kd = dot3(dir, ex);
     r.k = kn / kd;
-    r.ip = pos + r.k * dir;
+    // pos + k * dir with the product rounded on its own, as numpy evaluates it
+    r.ip = d3{__dadd_rn(pos.x, __dmul_rn(r.k, dir.x)), __dadd_rn(pos.y, __dmul_rn(r.k, dir.y)),
+              __dadd_rn(pos.z, __dmul_rn(r.k, dir.z))};
     d3 v = r.ip - c;
     r.ly = dot3(v, ey);
     r.lz = dot3(v, ez);
@@ -183,7 +185,8 @@ __device__ __forceinline__ CylHit cylinder_intersect_dev(const double* cyl, d3 p
         return out;
     }
     out.hit = true;
-    d3 lp = xyz + t * r;
+    d3 lp{__dadd_rn(xyz.x, __dmul_rn(t, r.x)), __dadd_rn(xyz.y, __dmul_rn(t, r.y)),
+          __dadd_rn(xyz.z, __dmul_rn(t, r.z))};
     out.ip = d3{M[0] * lp.x + M[1] * lp.y + M[2] * lp.z + M[3],
                 M[4] * lp.x + M[5] * lp.y + M[6] * lp.z + M[7],
                 M[8] * lp.x + M[9] * lp.y + M[10] * lp.z + M[11]};

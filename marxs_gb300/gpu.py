@@ -528,3 +528,78 @@ def _write_back(photons, name, value):
         arr[...] = value
     else:
         photons[name] = value.astype(arr.dtype) if arr.shape == value.shape else value
+
+
+# ---------------------------------------------------------------------------
+# Geometry entry points on the GPU (same call shapes as the MARXS methods)
+# ---------------------------------------------------------------------------
+def _vec_in(a, dev):
+    t = torch.from_numpy(np.ascontiguousarray(np.asarray(a, dtype=np.float64))).to(dev)
+    if t.dim() == 1:
+        t = t[None, :]
+    return t
+
+
+def plane_intersect(geometry, dir, pos, device=None):
+    """FinitePlane.intersect (marxs/math/geometry.py:211-261) on the GPU.
+
+    ``geometry`` is anything with ``pos4d``; ``dir``/``pos`` are (N, 4).
+    Returns (intersect bool (N,), interpos (N, 4), interpos_local (N, 2)).
+    """
+    from .lowering import plane_frame
+    dev = _device(device)
+    lib = _abi.load()
+    d, p = _vec_in(dir, dev), _vec_in(pos, dev)
+    n = d.shape[0]
+    frame = (C.c_double * 14)(*[float(x) for x in plane_frame(geometry.pos4d)])
+    hit = torch.empty(n, dtype=torch.uint8, device=dev)
+    ip = torch.empty((n, 4), dtype=torch.float64, device=dev)
+    ip[:, 3] = p[:, 3]
+    loc = torch.empty((2, n), dtype=torch.float64, device=dev)
+    _abi.check(lib.mgpu_plane_intersect(frame, n, _abi.vec_aos(p), _abi.vec_aos(d), hit.data_ptr(),
+                                        _abi.vec_aos(ip), _abi.col(loc[0]), _abi.col(loc[1]),
+                                        _stream_handle()), 'mgpu_plane_intersect')
+    return hit.bool().cpu().numpy(), ip.cpu().numpy(), loc.T.contiguous().cpu().numpy()
+
+
+def cylinder_intersect(geometry, dir, pos, device=None):
+    """Cylinder.intersect (marxs/math/geometry.py:470-564) on the GPU."""
+    from .lowering import cylinder_block
+    dirs = np.asarray(dir, dtype=np.float64)
+    if not np.all(dirs[..., 3] == 0):
+        raise ValueError('First input must be direction vectors.')
+    dev = _device(device)
+    lib = _abi.load()
+    d, p = _vec_in(dirs, dev), _vec_in(pos, dev)
+    n = d.shape[0]
+    cyl = (C.c_double * 32)(*[float(x) for x in cylinder_block(geometry)])
+    hit = torch.empty(n, dtype=torch.uint8, device=dev)
+    ip = torch.empty((n, 4), dtype=torch.float64, device=dev)
+    loc = torch.empty((2, n), dtype=torch.float64, device=dev)
+    _abi.check(lib.mgpu_cylinder_intersect(cyl, n, _abi.vec_aos(p), _abi.vec_aos(d),
+                                           hit.data_ptr(), _abi.vec_aos(ip), _abi.col(loc[0]),
+                                           _abi.col(loc[1]), _stream_handle()),
+               'mgpu_cylinder_intersect')
+    hit_np = hit.bool().cpu().numpy()
+    ipn = ip.cpu().numpy()
+    ipn[:, 3] = np.where(hit_np, 1.0, np.nan)
+    return hit_np, ipn, loc.T.contiguous().cpu().numpy()
+
+
+def parallel_transport(dir_old, dir_new, pol_old, device=None):
+    """parallel_transport (marxs/math/polarization.py:151-170) on the GPU;
+    (n, 4) or (n, 3) inputs, returns (n, 4) with w = 0."""
+    dev = _device(device)
+    lib = _abi.load()
+
+    def as4(a):
+        a = np.asarray(a, dtype=np.float64)
+        if a.shape[-1] == 3:
+            a = np.concatenate([a, np.zeros(a.shape[:-1] + (1,))], axis=-1)
+        return _vec_in(a, dev)
+    d0, d1, pol = as4(dir_old), as4(dir_new), as4(pol_old)
+    out = torch.zeros_like(pol)
+    _abi.check(lib.mgpu_parallel_transport(d0.shape[0], _abi.vec_aos(d0), _abi.vec_aos(d1),
+                                           _abi.vec_aos(pol), _abi.vec_aos(out), _stream_handle()),
+               'mgpu_parallel_transport')
+    return out.cpu().numpy()
