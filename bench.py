@@ -30,9 +30,11 @@ METRIC = 'photons/s at 1e8 (FP32-local vs FP64); adjoint grads/s vs finite-diff;
 UNIT = 'photons/s'
 WORKLOAD = 'cat_rowland_1000facets_circular_detector'
 
-# DRAM bytes per photon of the chain kernel, from the ncu capture summarised in
-# profiles/chain_fp64_c2.md (None until a capture exists for the mode)
-NCU_TRAFFIC_BYTES_PER_PHOTON = {'fp64': None, 'fp32local': None}
+# DRAM bytes (read + write) per photon of the chain kernel, from the ncu
+# captures of a 4e6-photon launch (profiles/chain_fp64_c2.md,
+# profiles/chain_fp32local_c2.md), scaled to the launch by photon count
+NCU_TRAFFIC_BYTES_PER_PHOTON = {'fp64': (353.9e6 + 727.0e6) / 4e6,
+                                'fp32local': (353.1e6 + 727.6e6) / 4e6}
 
 
 def parse():
