@@ -45,15 +45,17 @@ def _subset_vs_oracle(inst, host, draws, out, n_sub=2000, seed=0):
             assert close_rel(a[ok], b[ok], 1e-9, 1e-6 if 'scatter' in col else 1.0), col
 
 
-def _invariants(out, host):
+def _invariants(out, host, tol):
+    """tol: 1e-9 for float64, 1e-5 for FP32-local (float32 storage of the
+    direction and polarization, same bar as the golden polarization test)."""
     prob = np.asarray(out['probability'])
-    assert np.all(prob <= np.asarray(host['probability']) + 1e-12)
+    assert np.all(prob <= np.asarray(host['probability']) * (1 + tol))
     pol = np.asarray(out['polarization'])[:, :3]
     d = np.asarray(out['dir'])[:, :3]
     fin = np.all(np.isfinite(d), axis=1)
     dn = d[fin] / np.linalg.norm(d[fin], axis=1)[:, None]
-    assert np.max(np.abs(np.einsum('ij,ij->i', pol[fin], dn))) < 1e-6
-    assert np.max(np.abs(np.linalg.norm(pol[fin], axis=1) - 1)) < 1e-6
+    assert np.max(np.abs(np.einsum('ij,ij->i', pol[fin], dn))) < tol
+    assert np.max(np.abs(np.linalg.norm(pol[fin], axis=1) - 1)) < tol
     if 'facet' in out.colnames:
         assert np.array_equal(np.asarray(out['facet']) == -1, np.isnan(np.asarray(out['order'])))
 
@@ -66,7 +68,7 @@ def test_spectrometer_1e7_fp64():
     draws = configs.draws_for(inst.draw_slots, n, seed=101)
     out = _trace(inst, host, 'fp64', draws)
     _subset_vs_oracle(inst, host, draws, out)
-    _invariants(out, host)
+    _invariants(out, host, 1e-9)
     again = _trace(inst, host, 'fp64', draws)
     for col in out.colnames:
         assert np.array_equal(np.asarray(out[col]), np.asarray(again[col]), equal_nan=True), col
@@ -80,11 +82,11 @@ def test_cat_array_1e8():
     draws = configs.draws_for(inst.draw_slots, n, seed=202)
     out = _trace(inst, host, 'fp64', draws)
     _subset_vs_oracle(inst, host, draws, out, n_sub=1500, seed=1)
-    _invariants(out, host)
+    _invariants(out, host, 1e-9)
     del out
     # FP32-local, Philox, in two shards vs whole
     whole = _trace(inst, host, 'fp32local', rng='philox')
-    _invariants(whole, host)
+    _invariants(whole, host, 1e-5)
     h = n // 2
     half = {k: v[h:] for k, v in host.items()}
     second = _trace(inst, half, 'fp32local', rng='philox', row_base=h)
