@@ -212,6 +212,7 @@ def main():
     from marxs_gb300 import configs
     from marxs_gb300.gpu import GpuSequence, DevicePhotons, pinned_photons
     from marxs_gb300 import _abi
+    from marxs_gb300.sharding import weak_shard, max_over_ranks
 
     world = int(os.environ.get('WORLD_SIZE', '1'))
     rank = int(os.environ.get('RANK', '0'))
@@ -231,7 +232,7 @@ def main():
     inst = configs.build('c2')
     host = configs.photons_for('c2', n, seed=2 + 7919 * rank)
     dev_in = DevicePhotons.from_columns(host)
-    row_base = rank * n
+    row_base = weak_shard(rank, n)[0]      # Philox streams keyed by global photon id
 
     modes = []
     if args.precision in ('auto', 'fp32local'):
@@ -281,10 +282,7 @@ def main():
         step_ms = [a.elapsed_time(b) for a, b in ev]
         mean_ms = sum(step_ms) / len(step_ms)
         tot_ms = wall * 1e3
-        if dist is not None:
-            t = torch.tensor([tot_ms, mean_ms], device='cuda', dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            tot_ms, mean_ms = t.tolist()
+        tot_ms, mean_ms = max_over_ranks([tot_ms, mean_ms], dist, device='cuda')
         results[mode] = {'seq': seq, 'plan': plan, 'bufs': bufs, 'out': dev_out, 'mean_ms': mean_ms,
                          'wall_ms': tot_ms, 'clocks': ck,
                          'photons_per_s': world * n * args.steps / (tot_ms / 1e3),
@@ -354,10 +352,7 @@ def main():
         h2d = sum(work[k].nbytes for k in pristine.colnames)
         d2h = sum(work[k].nbytes for k in work.colnames if k not in ('energy',))
         e2e_s = sum(times) / len(times)
-        if dist is not None:
-            t = torch.tensor([e2e_s], device='cuda', dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e2e_s = t.item()
+        e2e_s = max_over_ranks([e2e_s], dist, device='cuda')[0]
         line['e2e'] = {'value': world * e2e_n / e2e_s, 'unit': UNIT, 'h2d_bytes_per_step': h2d,
                        'd2h_bytes_per_step': d2h, 'ms_per_step': e2e_s * 1e3,
                        'api': 'GpuSequence(elements)(PhotonTable) with pinned host columns'}

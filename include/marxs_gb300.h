@@ -40,6 +40,10 @@ extern "C" {
 #define MGPU_STATUS_BAD_STAGE    0x4u  /* unknown stage kind */
 #define MGPU_STATUS_GRID_RANGE   0x8u  /* a facet's footprint leaves the candidate grid */
 #define MGPU_STATUS_GRID_FULL    0x10u /* candidate list capacity exceeded */
+#define MGPU_STATUS_BAD_W        0x20u /* input pos w != 1 or dir/pol w != 0 (checked on request) */
+
+/* mgpu_chain.flags */
+#define MGPU_FLAG_CHECK_W        0x1u  /* read the homogeneous w of pos/dir/pol and check it */
 
 /* precision modes */
 #define MGPU_FP64      0  /* float64 throughout, parity mode */
@@ -212,7 +216,7 @@ typedef struct {
     int32_t n_stages;
     int32_t precision;           /* MGPU_FP64 / MGPU_FP32LOCAL */
     int32_t rng;                 /* MGPU_RNG_PREDRAWN / MGPU_RNG_PHILOX */
-    int32_t pad;
+    uint32_t flags;              /* MGPU_FLAG_* */
     uint64_t seed;
     uint64_t row_base;           /* global id of photon row 0 (Philox counter) */
     uint32_t* status;            /* device status word */

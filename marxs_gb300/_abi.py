@@ -22,6 +22,8 @@ STATUS_ORDER_EMPTY = 0x2
 STATUS_BAD_STAGE = 0x4
 STATUS_GRID_RANGE = 0x8
 STATUS_GRID_FULL = 0x10
+STATUS_BAD_W = 0x20
+FLAG_CHECK_W = 0x1
 
 NOALLOC_MAX_CELLS = 65536
 ERR_NOALLOC_LIMIT = -2
@@ -103,7 +105,7 @@ class MgpuStage(C.Structure):
 
 class MgpuChain(C.Structure):
     _fields_ = [('n_stages', C.c_int32), ('precision', C.c_int32), ('rng', C.c_int32),
-                ('pad', C.c_int32), ('seed', C.c_uint64), ('row_base', C.c_uint64),
+                ('flags', C.c_uint32), ('seed', C.c_uint64), ('row_base', C.c_uint64),
                 ('status', C.c_void_p),
                 ('hits', C.c_void_p), ('stages', MgpuStage * MAX_STAGES)]
 

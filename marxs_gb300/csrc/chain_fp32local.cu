@@ -647,6 +647,12 @@ chain_fp32local_kernel(const __grid_constant__ mgpu_chain chain, const __grid_co
             ph.energy_d = 1.0;
             ph.prob = 0.f;
         }
+        if (valid && (chain.flags & MGPU_FLAG_CHECK_W)) {
+            if (io.pos.ptr[i * io.pos.stride + 3 * io.pos.cstride] != 1.0 ||
+                io.dir.ptr[i * io.dir.stride + 3 * io.dir.cstride] != 0.0 ||
+                io.pol.ptr[i * io.pol.stride + 3 * io.pol.cstride] != 0.0)
+                atomicOr(chain.status, MGPU_STATUS_BAD_W);
+        }
         Chain::run(chain, ph, i, valid, s_hits, lane);
         if (valid) {
             store3(io.pos_out, i, d3{ff2d(ph.pos.x), ff2d(ph.pos.y), ff2d(ph.pos.z)});

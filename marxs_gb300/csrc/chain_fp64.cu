@@ -337,6 +337,12 @@ chain_fp64_kernel(const __grid_constant__ mgpu_chain chain, const __grid_constan
             ph.energy = 1.0;
             ph.prob = 0.0;
         }
+        if (valid && (chain.flags & MGPU_FLAG_CHECK_W)) {
+            if (io.pos.ptr[i * io.pos.stride + 3 * io.pos.cstride] != 1.0 ||
+                io.dir.ptr[i * io.dir.stride + 3 * io.dir.cstride] != 0.0 ||
+                io.pol.ptr[i * io.pol.stride + 3 * io.pol.cstride] != 0.0)
+                atomicOr(chain.status, MGPU_STATUS_BAD_W);
+        }
         for (int s = 0; s < chain.n_stages; ++s) {
             const mgpu_stage& st = chain.stages[s];
             bool hit = false;

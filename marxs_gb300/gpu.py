@@ -349,6 +349,9 @@ class GpuSequence:
         self.last_status = code
         if code & _abi.STATUS_PROB_RANGE:
             raise ValueError('Found probability outside of the 0..1 arange.')
+        if code & _abi.STATUS_BAD_W:
+            raise ValueError('pos must hold points (w = 1); dir and polarization must be '
+                             'direction vectors (w = 0).')
         if code & _abi.STATUS_ORDER_EMPTY:
             raise ValueError('order selection: no order has cumulative probability above the draw')
         if code:
@@ -402,39 +405,43 @@ class GpuSequence:
         return status, hits
 
     # ------------------------------------------------------------ table path
-    def __call__(self, photons, draws=None, row_base=0):
+    def __call__(self, photons, draws=None, row_base=0, chunk=16_000_000):
         """Trace a photon table (astropy Table, PhotonTable or dict) in place.
 
-        Host columns are copied to the device, traced, and copied back:
-        state columns into the table's own arrays, new columns appended in
-        the order MARXS creates them.  Host arrays in pinned memory (see
-        ``pinned_photons``) make both copies asynchronous DMA.
+        The photons are processed in chunks alternating over two streams:
+        each chunk's host-to-device copy, kernel and device-to-host copy are
+        queued on its stream, so transfers in both directions overlap with
+        compute.  State columns are copied back into the table's own arrays,
+        new columns are attached in the order MARXS creates them.  Host
+        arrays in pinned memory (``pinned_photons``) make the copies true DMA.
+        On an error (raised after the whole call) the table content is
+        unspecified, as in MARXS where earlier elements have already written
+        their columns when a later one raises.
         """
+        import time as _time
+        tm = {}
+        t0 = _time.perf_counter()
         if isinstance(photons, dict):
             from .table import PhotonTable
             photons = PhotonTable(photons)
         n = len(photons)
         inst = self.lower()
+        tm['lower'] = _time.perf_counter() - t0
         dev = self.device
-        stream = torch.cuda.current_stream(dev)
         colnames = list(photons.colnames)
-        host_state = {}
+        host = {}
         for key in ('pos', 'dir', 'polarization'):
             a = np.asarray(photons[key])
             if a.shape != (n, 4):
                 raise ValueError('pos, dir and polarization must be (N, 4) homogeneous columns')
-            host_state[key] = a
+            host[key] = np.ascontiguousarray(a, dtype=np.float64)
         for key in ('energy', 'probability'):
-            host_state[key] = np.asarray(photons[key])
-        if n and (not np.all(host_state['dir'][:, 3] == 0) or
-                  not np.all(host_state['polarization'][:, 3] == 0)):
-            raise ValueError('dir and polarization must be direction vectors (w = 0).')
-        if n and not np.all(host_state['pos'][:, 3] == 1):
-            raise ValueError('pos must hold points with w = 1.')
+            host[key] = np.ascontiguousarray(np.asarray(photons[key]), dtype=np.float64)
         if n == 0:
             return photons
         plan = ColumnPlan(inst.stages, existing=set(colnames))
-        dev_state = {k: _h2d(v, dev) for k, v in host_state.items()}
+        main = torch.cuda.current_stream(dev)
+        dstate = {k: torch.empty(v.shape, dtype=torch.float64, device=dev) for k, v in host.items()}
         bufs = {}
         for name, kind in plan.columns.items():
             if name in colnames:
@@ -446,35 +453,58 @@ class GpuSequence:
         status = torch.zeros(1, dtype=torch.int32, device=dev)
         hits = torch.zeros(_abi.MAX_STAGES, dtype=torch.int64, device=dev)
         draws_dev = self._draws_to_device(inst, draws, n)
-        chain = self._chain(inst, plan, bufs, draws_dev, n, status, hits, row_base)
-        ph = _abi.MgpuPhotons()
-        ph.n = n
-        ph.pos = ph.pos_out = _abi.vec_aos(dev_state['pos'])
-        ph.dir = ph.dir_out = _abi.vec_aos(dev_state['dir'])
-        ph.pol = ph.pol_out = _abi.vec_aos(dev_state['polarization'])
-        ph.energy = _abi.col(dev_state['energy'])
-        ph.prob = ph.prob_out = _abi.col(dev_state['probability'])
+        # where results go on the host
+        targets, fins = {}, []
+        for key in ('pos', 'dir', 'polarization', 'probability'):
+            targets[key], fin = _host_target(photons, key, dstate[key])
+            fins.append(fin)
+        for name in plan.columns:
+            if name in colnames:
+                targets[name], fin = _host_target(photons, name, bufs[name])
+                fins.append(fin)
+            else:
+                targets[name] = torch.empty(bufs[name].shape, dtype=bufs[name].dtype,
+                                            pin_memory=True)
+        tm['setup'] = _time.perf_counter() - t0
         lib = _abi.load()
-        _abi.check(lib.mgpu_trace(C.byref(chain), C.byref(ph), _stream_handle(stream)),
-                   'mgpu_trace')
-        # errors are raised before the table is touched, as the reference does
+        streams = self._side_streams(dev)
+        for st_ in streams:
+            st_.wait_stream(main)
+        for c, a in enumerate(range(0, n, int(chunk))):
+            b = min(n, a + int(chunk))
+            side = streams[c % len(streams)]
+            with torch.cuda.stream(side):
+                for k, v in host.items():
+                    dstate[k][a:b].copy_(torch.from_numpy(v[a:b]), non_blocking=True)
+                sub_bufs = {name: t[a:b] for name, t in bufs.items()}
+                sub_draws = {si: [None if t is None else t[a:b] for t in ts]
+                             for si, ts in draws_dev.items()}
+                chain = self._chain(inst, plan, sub_bufs, sub_draws, b - a, status, hits,
+                                    row_base + a)
+                chain.flags = _abi.FLAG_CHECK_W
+                ph = _abi.MgpuPhotons()
+                ph.n = b - a
+                ph.pos = ph.pos_out = _abi.vec_aos(dstate['pos'][a:b])
+                ph.dir = ph.dir_out = _abi.vec_aos(dstate['dir'][a:b])
+                ph.pol = ph.pol_out = _abi.vec_aos(dstate['polarization'][a:b])
+                ph.energy = _abi.col(dstate['energy'][a:b])
+                ph.prob = ph.prob_out = _abi.col(dstate['probability'][a:b])
+                _abi.check(lib.mgpu_trace(C.byref(chain), C.byref(ph), _stream_handle(side)),
+                           'mgpu_trace')
+                for key in ('pos', 'dir', 'polarization', 'probability'):
+                    targets[key][a:b].copy_(dstate[key][a:b], non_blocking=True)
+                for name in plan.columns:
+                    targets[name][a:b].copy_(bufs[name][a:b], non_blocking=True)
+        for st_ in streams:
+            main.wait_stream(st_)
+        tm['issued'] = _time.perf_counter() - t0
+        main.synchronize()
+        tm['done'] = _time.perf_counter() - t0
         code = int(status.item())
         hit_counts = hits.cpu().numpy()[:len(inst.stages)]
         self.last_hits = hit_counts
         self._raise_status(code)
-        pending = []
-        for key in ('pos', 'dir', 'polarization', 'probability'):
-            pending.append(_d2h_into(photons, key, dev_state[key]))
-        new_host = {}
-        for name in plan.columns:
-            if name in colnames:
-                pending.append(_d2h_into(photons, name, bufs[name]))
-            else:
-                h = torch.empty(bufs[name].shape, dtype=bufs[name].dtype, pin_memory=True)
-                h.copy_(bufs[name], non_blocking=True)
-                new_host[name] = h
-        stream.synchronize()
-        for fin in pending:
+        for fin in fins:
             if fin is not None:
                 fin()
         for si, names in enumerate(plan.order):
@@ -483,9 +513,44 @@ class GpuSequence:
             for name in names:
                 if name in colnames:
                     continue
-                photons[name] = new_host[name].numpy()
+                _attach_column(photons, name, targets[name].numpy())
                 colnames.append(name)
+        tm['total'] = _time.perf_counter() - t0
+        self.last_timing = tm
         return photons
+
+    def _side_streams(self, dev):
+        if getattr(self, '_streams', None) is None:
+            self._streams = [torch.cuda.Stream(dev), torch.cuda.Stream(dev)]
+        return self._streams
+
+
+def _host_target(photons, name, dev_t):
+    """Host tensor that receives a device column: the table's own array when
+    its dtype and layout allow, else a pinned staging buffer plus a
+    finaliser that writes it back."""
+    arr = np.asarray(photons[name])
+    want = np.dtype(str(dev_t.dtype).replace('torch.', ''))
+    if (arr.shape == tuple(dev_t.shape) and arr.flags.writeable and arr.flags.c_contiguous
+            and arr.dtype == want):
+        return torch.from_numpy(arr), None
+    h = torch.empty(dev_t.shape, dtype=dev_t.dtype, pin_memory=True)
+
+    def fin():
+        _write_back(photons, name, h.numpy())
+    return h, fin
+
+
+def _attach_column(photons, name, arr):
+    """Add a freshly made column without copying it again."""
+    from .table import PhotonTable
+    if isinstance(photons, PhotonTable):
+        photons.columns[name] = arr
+        return
+    try:
+        photons.add_column(arr, name=name, copy=False)
+    except TypeError:
+        photons[name] = arr
 
 
 def pinned_photons(n):
@@ -504,22 +569,6 @@ def _h2d(a, dev):
         a = a.astype(np.float64)
     t = torch.from_numpy(np.ascontiguousarray(a))
     return t.to(dev, non_blocking=t.is_pinned())
-
-
-def _d2h_into(photons, name, dev_t):
-    """Copy a device column back into the table's own array when possible;
-    returns a finaliser for the cases that need a host-side replacement."""
-    arr = np.asarray(photons[name])
-    if (arr.shape == tuple(dev_t.shape) and arr.flags.writeable and arr.flags.c_contiguous
-            and arr.dtype == np.dtype(str(dev_t.dtype).replace('torch.', ''))):
-        torch.from_numpy(arr).copy_(dev_t, non_blocking=True)
-        return None
-    h = torch.empty(dev_t.shape, dtype=dev_t.dtype, pin_memory=True)
-    h.copy_(dev_t, non_blocking=True)
-
-    def fin():
-        _write_back(photons, name, h.numpy())
-    return fin
 
 
 def _write_back(photons, name, value):
