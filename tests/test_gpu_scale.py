@@ -46,8 +46,11 @@ def _subset_vs_oracle(inst, host, draws, out, n_sub=2000, seed=0):
 
 
 def _invariants(out, host, tol):
-    """tol: 1e-9 for float64, 1e-5 for FP32-local (float32 storage of the
-    direction and polarization, same bar as the golden polarization test)."""
+    """tol: 2e-8 for float64 -- the reference keeps the polarization unchanged
+    when |d1 x d2| <= 1e-8 (np.isclose in paralleltransport_matrix,
+    polarization.py:135-148), so a direction turned by less than that leaves
+    |pol . dir| up to 1e-8 -- and 1e-5 for FP32-local (float32 storage, same
+    bar as the golden polarization test)."""
     prob = np.asarray(out['probability'])
     assert np.all(prob <= np.asarray(host['probability']) * (1 + tol))
     pol = np.asarray(out['polarization'])[:, :3]
@@ -68,7 +71,7 @@ def test_spectrometer_1e7_fp64():
     draws = configs.draws_for(inst.draw_slots, n, seed=101)
     out = _trace(inst, host, 'fp64', draws)
     _subset_vs_oracle(inst, host, draws, out)
-    _invariants(out, host, 1e-9)
+    _invariants(out, host, 2e-8)
     again = _trace(inst, host, 'fp64', draws)
     for col in out.colnames:
         assert np.array_equal(np.asarray(out[col]), np.asarray(again[col]), equal_nan=True), col
@@ -82,7 +85,7 @@ def test_cat_array_1e8():
     draws = configs.draws_for(inst.draw_slots, n, seed=202)
     out = _trace(inst, host, 'fp64', draws)
     _subset_vs_oracle(inst, host, draws, out, n_sub=1500, seed=1)
-    _invariants(out, host, 1e-9)
+    _invariants(out, host, 2e-8)
     del out
     # FP32-local, Philox, in two shards vs whole
     whole = _trace(inst, host, 'fp32local', rng='philox')
