@@ -73,13 +73,17 @@ __device__ __forceinline__ HitL plane_hit_l(ff3 c, f3 n, f3 ey, f3 ez, float hy,
     f3 rel = ff3_f(ff3_sub(pos, c));
     float kd = dotf(dir, n);
     float k = -dotf(rel, n) / kd;
-    ff3 ip = ff3_axpy(pos, k, dir);
-    f3 v = ff3_f(ff3_sub(ip, c));
-    float dk = -dotf(v, n) / kd;
-    if (kd != 0.0f && isfinite(dk)) {
-        k += dk;
-        ip = ff3_axpy(ip, dk, dir);
-        v = v + dk * dir;
+    ff3 ip = pos;
+    f3 v = rel;
+    if (k != 0.0f) {            // rays that start on the plane (k == 0) need no update
+        ip = ff3_axpy(pos, k, dir);
+        v = ff3_f(ff3_sub(ip, c));
+        float dk = -dotf(v, n) / kd;
+        if (kd != 0.0f && dk != 0.0f && isfinite(dk)) {
+            k += dk;
+            ip = ff3_axpy(ip, dk, dir);
+            v = v + dk * dir;
+        }
     }
     h.k = k;
     h.ip = ip;
@@ -314,16 +318,17 @@ __device__ bool stage_cyldet_l(const mgpu_stage& st, PhotonL& ph, int64_t i) {
         write_miss_defaults(st, i, 4);
         return false;
     }
-    // one float-float Newton step on |H_perp|^2 = R^2
+    // one float-float Newton step on |H_perp|^2 = R^2; the correction dt is
+    // ~1e-3 mm, so the projections are updated by dt * d_i in float32
     ff3 H = ff3_axpy(q, t, d);
     ff h1 = ff_dot(H, e1), h2 = ff_dot(H, e2);
     ff g = ff_sub(ff_add(ff_mul(h1, h1), ff_mul(h2, h2)), ff_mul(R, R));
     float dg = 2.0f * (ff_f(h1) * d1 + ff_f(h2) * d2);
     float dt = -ff_f(g) / dg;
-    if (isfinite(dt)) {
-        H = ff3_axpy(H, dt, d);
-        h1 = ff_dot(H, e1);
-        h2 = ff_dot(H, e2);
+    if (isfinite(dt) && dt != 0.0f) {
+        H = ff3_add_f3(H, dt * d);
+        h1 = ff_add_f(h1, dt * d1);
+        h2 = ff_add_f(h2, dt * d2);
     }
     float h3 = ff_f(ff_dot(H, ax));
     // angle: reference k/1024 from the table, then the small residual
@@ -456,23 +461,21 @@ __device__ __forceinline__ int nearest_facet_grid_l(const mgpu_stage& st, const 
     return best;
 }
 
-__device__ bool stage_gratings_l(const mgpu_stage& st, PhotonL& ph, int64_t i, bool valid,
-                                 int rng, uint64_t seed, uint64_t row_base, int sidx,
-                                 uint32_t* status) {
-    HitL h;
-    bool brute;
-    int f = nearest_facet_grid_l(st, ph, valid, &h, &brute);
-    unsigned bm = __ballot_sync(MGPU_FULL_MASK, brute);
+// photons the grid cannot bound (slope beyond the grid's limit): the whole
+// warp scans all facets for each of them, one photon at a time, with a warp
+// min-reduction on (k, facet).  Rare, so kept out of the hot code.
+__device__ __noinline__ int brute_force_nearest(const mgpu_stage& st, ff3 pos, f3 dir, unsigned bm) {
     const int lane = threadIdx.x & 31;
+    int mine = -1;
     while (bm) {
         int src = __ffs(bm) - 1;
         bm &= bm - 1;
         ff3 p;
-        p.x = ff{__shfl_sync(MGPU_FULL_MASK, ph.pos.x.hi, src), __shfl_sync(MGPU_FULL_MASK, ph.pos.x.lo, src)};
-        p.y = ff{__shfl_sync(MGPU_FULL_MASK, ph.pos.y.hi, src), __shfl_sync(MGPU_FULL_MASK, ph.pos.y.lo, src)};
-        p.z = ff{__shfl_sync(MGPU_FULL_MASK, ph.pos.z.hi, src), __shfl_sync(MGPU_FULL_MASK, ph.pos.z.lo, src)};
-        f3 d{__shfl_sync(MGPU_FULL_MASK, ph.dir.x, src), __shfl_sync(MGPU_FULL_MASK, ph.dir.y, src),
-             __shfl_sync(MGPU_FULL_MASK, ph.dir.z, src)};
+        p.x = ff{__shfl_sync(MGPU_FULL_MASK, pos.x.hi, src), __shfl_sync(MGPU_FULL_MASK, pos.x.lo, src)};
+        p.y = ff{__shfl_sync(MGPU_FULL_MASK, pos.y.hi, src), __shfl_sync(MGPU_FULL_MASK, pos.y.lo, src)};
+        p.z = ff{__shfl_sync(MGPU_FULL_MASK, pos.z.hi, src), __shfl_sync(MGPU_FULL_MASK, pos.z.lo, src)};
+        f3 d{__shfl_sync(MGPU_FULL_MASK, dir.x, src), __shfl_sync(MGPU_FULL_MASK, dir.y, src),
+             __shfl_sync(MGPU_FULL_MASK, dir.z, src)};
         float bk = 0.0f;
         int bf = -1;
         for (int q = lane; q < st.n_facets; q += 32) {
@@ -492,7 +495,21 @@ __device__ bool stage_gratings_l(const mgpu_stage& st, PhotonL& ph, int64_t i, b
                 bf = of;
             }
         }
-        if (lane == src && bf >= 0) {
+        if (lane == src) mine = bf;
+    }
+    return mine;
+}
+
+__device__ bool stage_gratings_l(const mgpu_stage& st, PhotonL& ph, int64_t i, bool valid,
+                                 int rng, uint64_t seed, uint64_t row_base, int sidx,
+                                 uint32_t* status) {
+    HitL h;
+    bool brute;
+    int f = nearest_facet_grid_l(st, ph, valid, &h, &brute);
+    unsigned bm = __ballot_sync(MGPU_FULL_MASK, brute);
+    if (bm) {
+        int bf = brute_force_nearest(st, ph.pos, ph.dir, bm);
+        if (brute && bf >= 0) {
             f = bf;
             h = facet_hit(st.facets32 + bf, ph.pos, ph.dir);
         }
@@ -619,7 +636,7 @@ struct FixedChain {
 };
 
 template <class Chain>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 3)
 chain_fp32local_kernel(const __grid_constant__ mgpu_chain chain, const __grid_constant__ mgpu_photons io) {
     __shared__ unsigned int s_hits[MGPU_MAX_STAGES];
     if (threadIdx.x < MGPU_MAX_STAGES) s_hits[threadIdx.x] = 0;
