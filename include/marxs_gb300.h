@@ -20,6 +20,8 @@
  *   mgpu_plane_intersect    FinitePlane.intersect, math/geometry.py:211-261
  *   mgpu_cylinder_intersect Cylinder.intersect, math/geometry.py:470-564
  *   mgpu_parallel_transport parallel_transport, math/polarization.py:151-170
+ *   mgpu_pose_adjoint       (no counterpart) reverse mode of the element
+ *                           chain above with discrete choices frozen
  */
 #ifndef MARXS_GB300_H
 #define MARXS_GB300_H
@@ -275,6 +277,81 @@ int mgpu_parallel_transport(int64_t n, mgpu_vec dir_old, mgpu_vec dir_new, mgpu_
 
 /* number of SMs of the current device (for launch sizing by callers) */
 int mgpu_device_sm_count(void);
+
+/* ---- pose adjoint: detector moments of frozen photons and their gradient ----
+ *
+ * No single reference interface: it differentiates the forward of
+ * PerfectLens (optics/mirror.py:53-82) -> RadialMirrorScatter
+ * (optics/scatter.py:49-77) -> one FlatGrating/CATGrating facet of a Parallel
+ * array (optics/grating.py:233-277) -> FlatDetector (math/geometry.py:211-261)
+ * or CircularDetector (math/geometry.py:470-564) with every photon's discrete
+ * choices frozen (hits, facet, order, scatter angles, order sign, normal side,
+ * cylinder root).  Parameters theta (device, 7 + 6 F doubles):
+ *   theta[0]            focal length of the lens (absolute, mm)
+ *   theta[1 + 6j + 0..2] translation of facet j's centre (mm)
+ *   theta[1 + 6j + 3..5] rotation of facet j about its centre,
+ *                        R = Rz(a2) Ry(a1) Rx(a0) (static x, y, z Euler angles,
+ *                        as elem_uncertainty uses, design/uncertainties.py:36-38)
+ *   theta[1 + 6F + 0..5] the same six for the detector.
+ * A perturbed element has pos4d = [R M | c + t] for base pos4d = [M | c].
+ * Photons are split into groups (an order, an energy ...); per group g the
+ * kernel sums, over its photons with weight w and detector coordinates (x, y)
+ * taken relative to the group centre ref[2g], ref[2g+1]:
+ *   moments[5g + 0..4] = sum w, sum w x, sum w y, sum w x^2, sum w y^2.
+ * FLAT: (x, y) = det_x, det_y (mm).  CYL: x = det_phi * R (mm), y = det_y (mm).
+ * BACKWARD takes seeds[4g + 0..3] = dL/d(sum w x), dL/d(sum w x^2),
+ * dL/d(sum w y), dL/d(sum w y^2) and adds dL/dtheta to grad, so any loss of
+ * the moments (spot width, centroid offset, resolving power) differentiates
+ * through one launch.  Backward recomputes the forward from the photon input
+ * and keeps each stage's output (position, direction) as its checkpoint;
+ * each stage's internals are recomputed inside its reverse step.
+ * Calls that share one problem must not overlap (rot is their scratch). */
+#define MGPU_ADJ_FREEZE   0   /* write sign / nsign / root from the forward at theta */
+#define MGPU_ADJ_FORWARD  1   /* add moments; x_out / y_out if non-NULL */
+#define MGPU_ADJ_BACKWARD 2   /* add dL/dtheta to grad */
+#define MGPU_ADJ_DET_FLAT 0
+#define MGPU_ADJ_DET_CYL  1
+#define MGPU_ADJ_NMOM     5
+#define MGPU_ADJ_NSEED    4
+#define MGPU_ADJ_MAX_GROUPS 64
+#define MGPU_ADJ_MAX_FACETS 4096
+#define MGPU_ADJ_FACET_CAT          0x1u
+#define MGPU_ADJ_FACET_TRANSMISSION 0x2u
+#define MGPU_STATUS_ADJ_RANGE 0x40u  /* facet or group index out of range, or no cylinder root */
+
+typedef struct {
+    int64_t n;                  /* photons */
+    int32_t n_facets;
+    int32_t n_groups;
+    int32_t det_kind;           /* MGPU_ADJ_DET_* */
+    int32_t reserved;
+    const double* pos;          /* 3 x n (SoA), position before the lens */
+    const double* dir;          /* 3 x n, direction before the lens */
+    const double* alpha;        /* in-plane scatter angle (rad; 0 = no rotation) */
+    const double* beta;         /* perpendicular scatter angle (rad) */
+    const double* energy;       /* keV */
+    const double* weight;       /* photon weight in the moments */
+    const int32_t* facet;       /* index into facets */
+    const int32_t* order;       /* diffraction order */
+    const int32_t* group;       /* moment group; < 0 = photon not counted */
+    int8_t* sign;               /* frozen order sign (written by FREEZE) */
+    int8_t* nsign;              /* frozen normal side (written by FREEZE) */
+    int8_t* root;               /* CYL: frozen root +1 / -1 (written by FREEZE) */
+    double lens[10];            /* centre (3), unit normal e_x (3), unit e_z (3), d_center_optical_axis */
+    double scatter[6];          /* centre (3), unit normal e_x (3) */
+    const double* facets;       /* F x 13: centre, unit normal, groove e_l, -e_perp, grating constant */
+    const uint8_t* facet_flags; /* MGPU_ADJ_FACET_* */
+    double det[32];             /* FLAT: centre, unit e_x, e_y, e_z.  CYL: centre (3), M (9, row
+                                 * major), inverse of M (9), radius, zoom_z, phi_lim lo, hi */
+    const double* ref;          /* device, n_groups x 2 moment centres */
+    double* x_out;              /* optional, FORWARD: per-photon x */
+    double* y_out;              /* optional, FORWARD: per-photon y */
+    double* rot;                /* device scratch, 36 (F + 1) doubles */
+    uint32_t* status;           /* device status word */
+} mgpu_adjoint_problem;
+
+int mgpu_pose_adjoint(const mgpu_adjoint_problem* prob, const double* theta, int32_t mode,
+                      const double* seeds, double* moments, double* grad, void* stream);
 
 #ifdef __cplusplus
 }

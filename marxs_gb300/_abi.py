@@ -27,6 +27,15 @@ FLAG_CHECK_W = 0x1
 
 NOALLOC_MAX_CELLS = 65536
 ERR_NOALLOC_LIMIT = -2
+STATUS_ADJ_RANGE = 0x40
+ADJ_FREEZE, ADJ_FORWARD, ADJ_BACKWARD = 0, 1, 2
+ADJ_DET_FLAT, ADJ_DET_CYL = 0, 1
+ADJ_NMOM = 5
+ADJ_NSEED = 4
+ADJ_MAX_GROUPS = 64
+ADJ_MAX_FACETS = 4096
+ADJ_FACET_CAT = 0x1
+ADJ_FACET_TRANSMISSION = 0x2
 
 FP64 = 0
 FP32LOCAL = 1
@@ -123,6 +132,19 @@ FACET32_DTYPE = np.dtype([('c_hi', '<f4', 3), ('c_lo', '<f4', 3), ('ex', '<f4', 
                           ('pad', '<i4')], align=True)
 
 # name -> (restype, argtypes) of every exported entry point
+class MgpuAdjointProblem(C.Structure):
+    _fields_ = [('n', C.c_int64), ('n_facets', C.c_int32), ('n_groups', C.c_int32),
+                ('det_kind', C.c_int32), ('reserved', C.c_int32),
+                ('pos', C.c_void_p), ('dir', C.c_void_p), ('alpha', C.c_void_p),
+                ('beta', C.c_void_p), ('energy', C.c_void_p), ('weight', C.c_void_p),
+                ('facet', C.c_void_p), ('order', C.c_void_p), ('group', C.c_void_p),
+                ('sign', C.c_void_p), ('nsign', C.c_void_p), ('root', C.c_void_p),
+                ('lens', C.c_double * 10), ('scatter', C.c_double * 6),
+                ('facets', C.c_void_p), ('facet_flags', C.c_void_p),
+                ('det', C.c_double * 32), ('ref', C.c_void_p), ('x_out', C.c_void_p),
+                ('y_out', C.c_void_p), ('rot', C.c_void_p), ('status', C.c_void_p)]
+
+
 SIGNATURES = {
     'mgpu_abi_version': (C.c_int, []),
     'mgpu_device_sm_count': (C.c_int, []),
@@ -137,6 +159,8 @@ SIGNATURES = {
                                           MgpuVec, MgpuCol, MgpuCol, C.c_void_p]),
     'mgpu_parallel_transport': (C.c_int, [C.c_int64, MgpuVec, MgpuVec, MgpuVec, MgpuVec,
                                           C.c_void_p]),
+    'mgpu_pose_adjoint': (C.c_int, [C.POINTER(MgpuAdjointProblem), C.c_void_p, C.c_int32,
+                                    C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
 }
 
 _lib = None
