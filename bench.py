@@ -48,6 +48,11 @@ def parse():
     p.add_argument('--no-e2e', action='store_true')
     p.add_argument('--no-cpu', action='store_true')
     p.add_argument('--e2e-steps', type=int, default=3)
+    p.add_argument('--no-adjoint', action='store_true')
+    p.add_argument('--adjoint-photons', type=float, default=1e6)
+    p.add_argument('--no-design', action='store_true')
+    p.add_argument('--design-photons', type=float, default=1e7)
+    p.add_argument('--design-steps', type=int, default=50)
     return p.parse_args()
 
 
@@ -203,6 +208,177 @@ def precision_error(a, b, torch):
     return out
 
 
+def adjoint_bench(args, torch):
+    """Pose gradients on the 200-facet spectrometer: hand-written adjoint vs
+    central finite differences (h = 1e-4 mm / 1e-6 rad) over all 1,207
+    parameters.  Loss: RMS cross-dispersion width of the order -5 spot +
+    squared offset of its dispersion centroid from the nominal position
+    (rounded to 1 mm).  Orders and scatter angles come from one FP32-local
+    Philox trace of the photons and are then held fixed."""
+    import numpy as np
+    from marxs_gb300 import configs
+    from marxs_gb300.adjoint import PoseModel, spot_loss
+    from marxs_gb300.gpu import DevicePhotons, GpuSequence
+    n = int(args.adjoint_photons)
+    inst = configs.build('c1')
+    host = configs.photons_for('c1', n, seed=3)
+    model = PoseModel(inst.elements)
+    fr, _ = model.trace(host, orders=[-5], precision='fp32local', rng='philox', seed=3)
+    loss = spot_loss(float(torch.round(fr.ref[0, 0])), group=0)
+    theta = model.theta0('cuda')
+    stream = torch.cuda.current_stream()
+    for _ in range(5):
+        fr.loss_and_grad(theta, loss)
+    K = 20
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    torch.cuda.synchronize()
+    ev[0].record(stream)
+    for _ in range(K):
+        L, g = fr.loss_and_grad(theta, loss)
+    ev[1].record(stream)
+    torch.cuda.synchronize()
+    grad_ms = ev[0].elapsed_time(ev[1]) / K
+    fr.finite_differences(theta, loss, params=np.arange(16))        # warm
+    torch.cuda.synchronize()
+    ev[0].record(stream)
+    fd = fr.finite_differences(theta, loss)
+    ev[1].record(stream)
+    torch.cuda.synchronize()
+    fd_ms = ev[0].elapsed_time(ev[1])
+    g_np, fd_np = g.cpu().numpy(), fd.cpu().numpy()
+    blk = 0.0
+    for idx in model.param_slices().values():
+        sc = np.max(np.abs(fd_np[idx]))
+        if sc > 0:
+            blk = max(blk, float(np.max(np.abs(g_np[idx] - fd_np[idx])) / sc))
+    # one forward pass of the plain FP64 raytrace over the same photons, with
+    # the orders and scatter angles fixed (pre-drawn): the forward a
+    # raytrace-based finite difference repeats 2 x 1,207 times
+    draws = configs.draws_for(inst.draw_slots, n, seed=3)
+    seq = GpuSequence(inst.elements, precision='fp64', rng='predrawn')
+    dev_in = DevicePhotons.from_columns(host)
+    dev_out = DevicePhotons(n)
+    plan, bufs = seq.allocate_columns(n)
+    draws_dev = seq._draws_to_device(seq.lower(), draws, n)
+    for _ in range(3):
+        seq.trace_device(dev_in, dev_out, plan, bufs, draws=draws_dev)
+    torch.cuda.synchronize()
+    ev[0].record(stream)
+    for _ in range(5):
+        seq.trace_device(dev_in, dev_out, plan, bufs, draws=draws_dev)
+    ev[1].record(stream)
+    torch.cuda.synchronize()
+    trace_ms = ev[0].elapsed_time(ev[1]) / 5
+    fd_trace_ms = 2 * model.n_params * trace_ms
+    return {
+        'workload': 'spectrometer_200facets_flat_detector: order -5 spot loss, '
+                    '%d parameters' % model.n_params,
+        'photons_traced': n, 'photons_in_loss': fr.n, 'params': model.n_params,
+        'dtype': 'f64', 'grad_ms': grad_ms, 'grads_per_s': 1e3 / grad_ms,
+        'fd_ms': fd_ms, 'fd_launches': 2 * model.n_params,
+        'speedup_vs_fd': fd_ms / grad_ms,
+        'fd_raytrace_ms': fd_trace_ms, 'raytrace_fp64_ms_per_pass': trace_ms,
+        'speedup_vs_fd_raytrace': fd_trace_ms / grad_ms,
+        'rel_err_vs_fd': float(np.linalg.norm(g_np - fd_np) / np.linalg.norm(fd_np)),
+        'blockwise_rel_err_vs_fd': blk, 'loss': float(L),
+        'fd_note': 'fd_ms: central differences on the frozen float64 forward kernel '
+                   '(2 x params launches); fd_raytrace_ms: 2 x params x one measured FP64 '
+                   'raytrace pass of all traced photons with pre-drawn randomness'}
+
+
+def design_bench(args, torch):
+    """Adam on the 1000 CAT facet tilts and the detector pose (3,006
+    parameters), maximising the mean resolving power of orders -8..-3 at
+    0.5 keV; every step re-traces the photons (FP32-local, fresh Philox
+    draws), freezes the trace and takes the gradient through the adjoint."""
+    import numpy as np
+    from marxs_gb300 import configs
+    from marxs_gb300.adjoint import PoseModel, design_loop, moment_stats, resolving_power
+    from marxs_gb300.gpu import DevicePhotons, GpuSequence
+    orders = [-8, -7, -6, -5, -4, -3]
+    n = int(args.design_photons)
+    inst = configs.build('c2')
+    host = configs.annulus_photons(n, 5, inst.aperture_x, energies=np.full(n, 0.5))
+    photons = DevicePhotons.from_columns(host)
+    del host
+    model = PoseModel(inst.elements)
+    torch.cuda.reset_peak_memory_stats()
+    base = torch.cuda.memory_allocated()
+    res = design_loop(model, photons, orders, steps=args.design_steps, seed=1000)
+    hist = res['history']
+    step_s = [h['seconds'] for h in hist[1:]] or [hist[0]['seconds']]
+
+    def evaluate(theta, seed=4242):
+        try:
+            model.apply(theta)
+            fr, _ = model.trace(photons, orders + [0], precision='fp32local', rng='philox',
+                                seed=seed, theta=theta)
+        finally:
+            model.restore()
+        cnt = torch.bincount(fr.group.long(), minlength=len(orders) + 1).cpu().numpy()
+        groups = [g for g in range(len(orders)) if cnt[g] >= 20]
+        return fr, float(resolving_power(len(orders), groups)(moment_stats(fr.moments(theta),
+                                                                           fr.ref))), groups
+
+    th0 = model.theta0('cuda')
+    _, r0, _ = evaluate(th0)
+    fr, r1, groups = evaluate(res['theta'])
+    # finite differences of the same loss on the frozen float64 forward: time a
+    # subset of the optimised parameters and scale to all of them
+    sl = model.param_slices()
+    opt_idx = np.concatenate([sl['facet_rotation'], sl['detector_translation'],
+                              sl['detector_rotation']])
+    loss = resolving_power(len(orders), groups)
+    sub = opt_idx[:: max(1, len(opt_idx) // 64)]
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    stream = torch.cuda.current_stream()
+    fr.finite_differences(res['theta'], loss, params=sub[:4])
+    torch.cuda.synchronize()
+    ev[0].record(stream)
+    fr.finite_differences(res['theta'], loss, params=sub)
+    ev[1].record(stream)
+    torch.cuda.synchronize()
+    fd_s = ev[0].elapsed_time(ev[1]) / 1e3 * len(opt_idx) / len(sub)
+    for _ in range(2):
+        fr.loss_and_grad(res['theta'], loss)
+    torch.cuda.synchronize()
+    ev[0].record(stream)
+    for _ in range(5):
+        fr.loss_and_grad(res['theta'], loss)
+    ev[1].record(stream)
+    torch.cuda.synchronize()
+    grad_s = ev[0].elapsed_time(ev[1]) / 1e3 / 5
+    seq = GpuSequence(inst.elements, precision='fp64', rng='philox', seed=1)
+    out = DevicePhotons(n)
+    plan, bufs = seq.allocate_columns(n)
+    for _ in range(2):
+        seq.trace_device(photons, out, plan, bufs)
+    torch.cuda.synchronize()
+    ev[0].record(stream)
+    for _ in range(3):
+        seq.trace_device(photons, out, plan, bufs)
+    ev[1].record(stream)
+    torch.cuda.synchronize()
+    trace_s = ev[0].elapsed_time(ev[1]) / 1e3 / 3
+    return {
+        'workload': 'cat_rowland_1000facets_circular_detector at 0.5 keV: mean resolving '
+                    'power of orders -8..-3, Adam over facet tilts + detector pose',
+        'photons_per_step': n, 'steps': len(hist), 'params_optimised': int(len(opt_idx)),
+        'seconds_per_step': float(np.mean(step_s)),
+        'resolving_power_nominal': r0, 'resolving_power_final': r1,
+        'resolving_power_history': [round(h['resolving_power'], 3) for h in hist],
+        'photons_in_loss': fr.n, 'gradient_s': grad_s,
+        'fd_frozen_s_per_gradient': fd_s, 'fd_frozen_sample_params': int(len(sub)),
+        'fd_raytrace_fp64_s_per_gradient': 2 * len(opt_idx) * trace_s,
+        'raytrace_fp64_s_per_pass': trace_s,
+        'speedup_vs_fd_frozen': fd_s / grad_s,
+        'speedup_vs_fd_raytrace': 2 * len(opt_idx) * trace_s / grad_s,
+        'peak_device_bytes_above_inputs': int(max(h['peak_bytes'] for h in hist) - base),
+        'note': 'seconds_per_step includes the re-trace, lowering of the moved facets, '
+                'freeze, forward and backward; gradient_s is forward + backward of the '
+                'adjoint alone; fd_frozen scales a timed subset of the parameters'}
+
+
 def main():
     args = parse()
     if args.impl == 'reference':
@@ -356,6 +532,14 @@ def main():
         line['e2e'] = {'value': world * e2e_n / e2e_s, 'unit': UNIT, 'h2d_bytes_per_step': h2d,
                        'd2h_bytes_per_step': d2h, 'ms_per_step': e2e_s * 1e3,
                        'api': 'GpuSequence(elements)(PhotonTable) with pinned host columns'}
+    if rank == 0 and world == 1 and not args.no_adjoint:
+        for k in ('seq', 'plan', 'bufs', 'out'):
+            for rr in results.values():
+                rr.pop(k, None)
+        torch.cuda.empty_cache()
+        line['adjoint'] = adjoint_bench(args, torch)
+    if rank == 0 and world == 1 and not args.no_design:
+        line['design'] = design_bench(args, torch)
     if rank == 0 and world == 1 and not args.no_cpu:
         line['cpu_baseline'] = cpu_baseline_single()
     if rank == 0:

@@ -477,3 +477,70 @@ def resolving_power(zero_group, groups):
         d = (s['mean_x'][..., groups] - s['mean_x'][..., zero_group:zero_group + 1]).abs()
         return (d / (FWHM_PER_SIGMA * torch.sqrt(s['var_x'][..., groups]))).mean(-1)
     return rp
+
+
+def design_loop(model, photons, orders, zero_order=0, steps=50, lr=0.2, rot_scale=1e-4,
+                trans_scale=0.5, optimise=('facet_rotation', 'detector_translation',
+                                           'detector_rotation'),
+                precision='fp32local', seed=0, min_photons=20, theta_init=None, callback=None):
+    """Adam on the poses of the chain, maximising the mean resolving power of
+    ``orders`` (distance from the ``zero_order`` centroid over FWHM).
+
+    Every step re-poses the elements at the current parameters, traces
+    ``photons`` (host columns or DevicePhotons) with fresh Philox draws, freezes
+    the trace and takes the gradient through the adjoint.  Parameters are
+    optimised in units of ``rot_scale`` (rad) and ``trans_scale`` (mm),
+    starting from ``theta_init`` (default: nominal).  The elements are left
+    at the nominal poses on return; the result holds the final theta and
+    per-step history.
+    """
+    import time
+    dev = photons.pos.device if hasattr(photons, 'pos') else torch.device('cuda')
+    theta0 = model.theta0(dev)
+    sl = model.param_slices()
+    idx = torch.from_numpy(np.concatenate([sl[k] for k in optimise])).to(dev)
+    scale = torch.full((len(idx),), trans_scale, dtype=torch.float64, device=dev)
+    rot_keys = {'facet_rotation', 'detector_rotation'}
+    off = 0
+    for k in optimise:
+        if k in rot_keys:
+            scale[off:off + len(sl[k])] = rot_scale
+        off += len(sl[k])
+    base = theta0.clone()
+    if theta_init is not None:
+        base = torch.as_tensor(theta_init, dtype=torch.float64, device=dev).clone()
+    u = ((base - theta0)[idx] / scale).clone().requires_grad_(True)
+    base[idx] = theta0[idx]
+    opt = torch.optim.Adam([u], lr=lr)
+    all_orders = list(orders) + [zero_order]
+    history = []
+    try:
+        for step in range(steps):
+            t0 = time.perf_counter()
+            theta = base.clone()
+            theta[idx] += scale * u.detach()
+            model.apply(theta)
+            fr, _ = model.trace(photons, all_orders, precision=precision, rng='philox',
+                                seed=seed + step, theta=theta, device=dev)
+            counts = torch.bincount(fr.group.long(), minlength=len(all_orders)).cpu().numpy()
+            groups = [g for g in range(len(orders)) if counts[g] >= min_photons]
+            rp = resolving_power(len(orders), groups)
+            th = theta.detach().requires_grad_(True)
+            R = rp(moment_stats(PoseMoments.apply(th, fr), fr.ref))
+            (gt,) = torch.autograd.grad(-R, th)
+            opt.zero_grad()
+            u.grad = gt[idx] * scale
+            opt.step()
+            torch.cuda.synchronize(dev)
+            rec = {'step': step, 'resolving_power': float(R.detach()), 'photons_in_loss': fr.n,
+                   'seconds': time.perf_counter() - t0,
+                   'peak_bytes': torch.cuda.max_memory_allocated(dev)}
+            history.append(rec)
+            if callback is not None:
+                callback(rec)
+            del fr
+    finally:
+        model.restore()
+    theta = base.clone()
+    theta[idx] += scale * u.detach()
+    return {'theta': theta, 'history': history}

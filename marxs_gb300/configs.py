@@ -12,7 +12,9 @@ travel from large x towards the focus at the origin.
   an EfficiencyFile-style 64-energy x 13-order table (orders -10..+2,
   Dirichlet(1) rows); FlatDetector 200x60 mm at the focus.
 * ``C2`` CAT array: lens f=12 m at x=12000, 1000 CATGrating facets of
-  25x25 mm (40 x 25 grid, pitch 26.5 mm) on a Rowland torus R=r=5900 mm,
+  25x25 mm (25 along the dispersion direction y x 40 along z, pitch
+  26.5 mm, so that |y| <= 318 mm keeps every photon on the blaze side:
+  relative incidence y / 11800 < 1.8 deg) on a Rowland torus R=r=5900 mm,
   blaze 1.8 deg (rotation about the groove axis), N(0, 30") pose jitter
   about three axes; energies from a piecewise-linear spectrum on 200 knots
   in [0.2, 2] keV; CircularDetector (R=5900) on the Rowland circle.
@@ -188,7 +190,7 @@ class RowlandTorusGeometry:
         return np.array([np.cos(theta) * np.cos(phi), np.sin(theta), np.cos(theta) * np.sin(phi)])
 
 
-def c2_facet_poses(seed, ny=40, nz=25, pitch=26.5, R=5900., r=5900., jitter_arcsec=30.):
+def c2_facet_poses(seed, ny=25, nz=40, pitch=26.5, R=5900., r=5900., jitter_arcsec=30.):
     """Facet poses on the torus (ElementsOnTorus placement, rowland.py:560-580)."""
     torus = RowlandTorusGeometry(R, r)
     ys = (np.arange(ny) - (ny - 1) / 2) * pitch

@@ -148,6 +148,17 @@ def test_perturbed_coordinates_equal_a_raytrace_of_moved_elements(name, request)
         (bufs['order'][rows] == bufs0['order'][rows])
     loc = 'det_x' if 'det_x' in bufs else 'det_phi'
     same &= torch.isfinite(bufs[loc][rows])
+    # photons may also switch CAT order sign (p . d changes sign near normal
+    # incidence) or cylinder root: choices the frozen forward holds fixed
+    from marxs_gb300 import _abi
+    flags = model.facet_flags
+    moved = AT.freeze(theta.cpu(), case['prob'],
+                      torch.from_numpy((flags & _abi.ADJ_FACET_CAT) > 0),
+                      torch.from_numpy((flags & _abi.ADJ_FACET_TRANSMISSION) > 0),
+                      phi_lim=(model.det_block[23], model.det_block[24]))
+    for k in ('sign', 'nsign', 'root'):
+        if k in moved:
+            same &= (moved[k] == case['prob'][k]).to(same.device)
     assert same.float().mean().item() > 0.9
     x, y = fr.xy(theta)
     if loc == 'det_x':
@@ -207,7 +218,8 @@ def test_autograd_function_backpropagates_into_theta(c1):
     L = c1['loss'](moment_stats(PoseMoments.apply(theta, fr), fr.ref))
     L.backward()
     _, g = fr.loss_and_grad(theta.detach(), c1['loss'])
-    assert torch.allclose(theta.grad, g, rtol=1e-12, atol=0)
+    # same kernels; only the order of the atomic sums differs
+    assert torch.allclose(theta.grad, g, rtol=1e-10, atol=1e-12 * float(g.abs().max()))
 
 
 def test_moments_are_deterministic_up_to_summation_order(c1):
