@@ -39,6 +39,7 @@ def native_namespace():
         FlatDetector=optics.FlatDetector, CircularDetector=optics.CircularDetector,
         FlatGrating=optics.FlatGrating, CATGrating=optics.CATGrating,
         OrderSelector=optics.OrderSelector, EfficiencyFile=optics.EfficiencyFile,
+        InterpolateEfficiencyTable=optics.InterpolateEfficiencyTable.from_grid,
         Cylinder=optics.Cylinder, Parallel=simulator.Parallel, Sequence=simulator.Sequence,
         angle=lambda rad: rad)
 
@@ -209,14 +210,50 @@ def c2_facet_poses(seed, ny=25, nz=40, pitch=26.5, R=5900., r=5900., jitter_arcs
     return poses, uncert, torus
 
 
-def build_c2(ns, seed=2, efficiency_file=None, n_facets=1000):
-    lens = ns.PerfectLens(focallength=12000., position=[12000., 0, 0], zoom=[1, 600, 600])
+def cat_efficiency_grid(seed, orders, total=0.8):
+    """Synthetic CAT order efficiencies on a (wavelength nm, blaze deg) grid:
+    27 wavelengths in [0.5, 7] nm x 17 blaze angles in [0, 4] deg, Dirichlet(1)
+    split of ``total`` over the orders at every node; (n_orders, 27, 17)."""
+    rng = np.random.default_rng(seed + 900)
+    wave = np.linspace(0.5, 7.0, 27)
+    blaze = np.linspace(0.0, 4.0, 17)
+    p = rng.dirichlet(np.ones(len(orders)), size=(len(wave), len(blaze))) * total
+    while np.any(np.sum(p, axis=-1) > total):
+        over = np.sum(p, axis=-1) > total
+        p[over] *= (1 - 2 ** -50)
+    return wave, blaze, np.moveaxis(p, -1, 0)
+
+
+def lens_reflectivity(seed):
+    """Synthetic mirror reflectivity R(energy keV, grazing angle rad) as a
+    degree-1 RectBivariateSpline (the form of PerfectLens's
+    reflectivity_interpolator, optics/mirror.py:45-48, 73-79): 30 energies in
+    [0.1, 3] keV x 21 angles in [0, 0.02] rad."""
+    from scipy.interpolate import RectBivariateSpline
+    rng = np.random.default_rng(seed + 950)
+    e = np.linspace(0.1, 3.0, 30)
+    a = np.linspace(0.0, 0.02, 21)
+    ee, aa = np.meshgrid(e, a, indexing='ij')
+    R = 0.95 - 0.08 * ee - 12.0 * aa + 0.02 * rng.standard_normal(ee.shape)
+    return RectBivariateSpline(e, a, np.clip(R, 0.0, 1.0), kx=1, ky=1)
+
+
+def build_c2(ns, seed=2, efficiency_file=None, n_facets=1000, interpolated=False):
+    """The CAT array; ``interpolated`` gives the lens a reflectivity
+    interpolator and the facets an InterpolateEfficiencyTable selector."""
+    lens_kw = {'reflectivity_interpolator': lens_reflectivity(seed)} if interpolated else {}
+    lens = ns.PerfectLens(focallength=12000., position=[12000., 0, 0], zoom=[1, 600, 600],
+                          **lens_kw)
     rms = ns.RadialMirrorScatter(inplanescatter=ns.angle(5 * ARCSEC),
                                  perpplanescatter=ns.angle(1 * ARCSEC),
                                  position=[12000., 0, 0], zoom=[1, 600, 600])
     orders = list(range(-12, 3))
-    table = efficiency_table(seed, orders, total=0.8)
-    eff = ns.EfficiencyFile(table if efficiency_file is None else efficiency_file, orders)
+    if interpolated:
+        table = cat_efficiency_grid(seed, orders)
+        eff = ns.InterpolateEfficiencyTable(table[0], table[1], table[2], orders)
+    else:
+        table = efficiency_table(seed, orders, total=0.8)
+        eff = ns.EfficiencyFile(table if efficiency_file is None else efficiency_file, orders)
     poses, uncert, torus = c2_facet_poses(seed)
     poses, uncert = poses[:n_facets], uncert[:n_facets]
     blaze = geomath.axangle2mat(np.array([0, 0, 1.]), np.deg2rad(1.8))
@@ -235,7 +272,7 @@ def build_c2(ns, seed=2, efficiency_file=None, n_facets=1000):
 
 
 def photons_for(config_name, n, seed):
-    if config_name == 'c2':
+    if config_name in ('c2', 'c5'):
         e = piecewise_linear_energies(n, seed)
         return annulus_photons(n, seed, 12000., energies=e)
     return annulus_photons(n, seed, 10000.)
@@ -249,4 +286,6 @@ def build(config_name, ns=None, seed=None):
         return build_c1(ns, seed=1 if seed is None else seed)
     if config_name == 'c2':
         return build_c2(ns, seed=2 if seed is None else seed)
+    if config_name == 'c5':
+        return build_c2(ns, seed=5 if seed is None else seed, interpolated=True)
     raise ValueError(config_name)

@@ -15,6 +15,8 @@ kernels.  Constructor keywords follow the reference:
 """
 import warnings
 
+import math
+
 import numpy as np
 
 from .geomath import parse_position_keywords, decompose44, compose, axangle2mat
@@ -135,6 +137,46 @@ class EfficiencyFile:
         self.prob = dat[:, 1:]
         self.totalprob = np.sum(self.prob, axis=1)
         self.cumprob = np.cumsum(self.prob, axis=1) / self.totalprob[:, None]
+
+
+class InterpolateEfficiencyTable:
+    """Order probabilities interpolated in (wavelength, blaze angle)
+    (missions/mitsnl/catgrating.py:63-144): one RectBivariateSpline of degree
+    ``k`` per order on a regular grid.
+
+    ``tab`` is table-like: first column wavelength (nm), second blaze angle
+    (deg), rows flattened wavelength-major as tablerows_to_2d reads them
+    (utils.py:59-100), then one column per order named by the order number.
+    ``from_grid`` builds the same from arrays.
+    """
+
+    def __init__(self, tab, k=1):
+        from scipy.interpolate import RectBivariateSpline
+        names = list(tab.colnames)
+        x = np.asarray(tab[names[0]], dtype=float)
+        y = np.asarray(tab[names[1]], dtype=float)
+        n_x, n_y = len(set(x)), len(set(y))
+        if len(x) != n_x * n_y:
+            raise ValueError('Data is not on regular grid.')
+        wave = x[::n_y]
+        theta = y[:n_y] * (math.pi / 180.)
+        self.orders = np.array([int(n) for n in names[2:]])
+        self.interpolators = [
+            RectBivariateSpline(wave, theta, np.asarray(tab[nm], dtype=float).reshape(n_x, n_y),
+                                kx=k, ky=k) for nm in names[2:]]
+
+    @classmethod
+    def from_grid(cls, wave_nm, blaze_deg, probs, orders, k=1):
+        """probs: (n_orders, n_wave, n_blaze)."""
+        ww, bb = np.meshgrid(np.asarray(wave_nm, float), np.asarray(blaze_deg, float),
+                             indexing='ij')
+        tab = {'wave': ww.ravel(), 'blaze': bb.ravel()}
+        for i, o in enumerate(orders):
+            tab[str(int(o))] = np.asarray(probs[i], dtype=float).ravel()
+
+        class _Tab(dict):
+            colnames = property(lambda self: list(self.keys()))
+        return cls(_Tab(tab), k=k)
 
 
 class SimulationSequenceElement:

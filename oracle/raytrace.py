@@ -236,15 +236,59 @@ def cylinder_intersect(pos4d, phi_lim, dir, pos):
 # --------------------------------------------------------------------------
 # order selection: marxs/optics/grating.py
 # --------------------------------------------------------------------------
-def order_select(selector, energy, u):
-    """OrderSelector (grating.py:51-57) / EfficiencyFile (grating.py:88-96).
+HC_KEV_NM = 1.2398419843320026   # h c in keV nm (CODATA 2018, as astropy's spectral())
+
+
+def bisp_k1(tx, ty, c, x, y):
+    """scipy RectBivariateSpline(kx=1, ky=1).ev(x, y): FITPACK fpbisp for
+    degree 1 (arguments clamped to [t[1], t[n-2]]; interval l = last knot
+    <= arg, at most n-3; de Boor weights f = 1/(t[l+1]-t[l]),
+    h0 = f (t[l+1]-arg), h1 = f (arg-t[l]); value = sum over the 2x2
+    coefficients of (c * hx) * hy in x-major order)."""
+    x = np.asarray(x, dtype=float)
+    y = np.asarray(y, dtype=float)
+    tx, ty, c = np.asarray(tx), np.asarray(ty), np.asarray(c)
+
+    def weights(t, a):
+        n = len(t)
+        arg = np.minimum(np.maximum(a, t[1]), t[n - 2])
+        l = np.minimum(1 + np.searchsorted(t[2:n - 1], arg, side='right'), n - 3)
+        f = 1.0 / (t[l + 1] - t[l])
+        return l, f * (t[l + 1] - arg), f * (arg - t[l])
+
+    lx, hx0, hx1 = weights(tx, x)
+    ly, hy0, hy1 = weights(ty, y)
+    nky1 = len(ty) - 2
+    base = (lx - 1) * nky1 + (ly - 1)
+    sp = np.zeros(len(x))
+    for dx, hx in ((0, hx0), (1, hx1)):
+        for dy, hy in ((0, hy0), (1, hy1)):
+            sp = sp + c[base + dx * nky1 + dy] * hx * hy
+    return sp
+
+
+def order_select(selector, energy, u, blaze=None):
+    """OrderSelector (grating.py:51-57) / EfficiencyFile (grating.py:88-96) /
+    InterpolateEfficiencyTable (missions/mitsnl/catgrating.py:101-144).
 
     ``u`` holds one uniform per photon.  OrderSelector draws through
     ``np.random.choice(p=...)``, i.e. ``searchsorted(cdf/cdf[-1], u, 'right')``;
     EfficiencyFile takes the nearest energy row and the first order whose
-    cumulative probability exceeds ``u``.
+    cumulative probability exceeds ``u``; InterpolateEfficiencyTable
+    evaluates one spline per order at (wavelength in nm, blaze angle), sums
+    them (row by row), normalises the running sum and takes
+    ``argmax(cumprob > u)`` -- order index 0 when no entry exceeds ``u``.
     """
     names = _classnames(selector)
+    if hasattr(selector, 'interpolators'):
+        wave = HC_KEV_NM / np.asarray(energy, dtype=float)
+        interpprobs = np.empty((len(selector.orders), len(energy)))
+        for i, ip in enumerate(selector.interpolators):
+            interpprobs[i, :] = ip.ev(wave, blaze)
+        totalprob = np.sum(interpprobs, axis=0)
+        cumprob = np.cumsum(interpprobs, axis=0) / totalprob
+        ind = np.argmax(cumprob > u, axis=0)
+        return np.asarray(selector.orders)[ind], totalprob
     if 'EfficiencyFile' in names:
         ind = np.array([np.argmin(np.abs(selector.energy - e)) for e in energy], dtype=int)
         orderind = np.empty(len(energy), dtype=int)
@@ -290,7 +334,8 @@ def flat_grating_process(g, photons, intersect, intercoos, u):
     p_perp_to_grooves = norm_vector(p - np.einsum('ij,ij->i', p, l)[:, None] * l)
     blazeangle = np.arccos(np.clip(np.abs(np.einsum('ij,ij->i', p_perp_to_grooves, n)), 0, 1))
     blazeangle += np.zeros(n_hit)
-    m, prob = order_select(g.order_selector, photons['energy'][intersect], u[intersect])
+    m, prob = order_select(g.order_selector, photons['energy'][intersect], u[intersect],
+                           blazeangle)
     if 'CATGrating' in _classnames(g):
         dotproduct = np.einsum('ij,ij->i', p, d)
         sign = np.sign(dotproduct)

@@ -5,7 +5,7 @@ Run from the repository root (needs the reference source tree, see
 
     python tests/golden/make_golden.py
 
-For each workload (c0, c1, c2) this builds the instrument from the
+For each workload (c0, c1, c2, c5) this builds the instrument from the
 reference's own classes, traces a small seeded photon list through the
 reference's ``Sequence`` with numpy's global RNG seeded, and records every
 random draw the reference makes.  The draws are mapped back to photons
@@ -20,6 +20,7 @@ than one facet (excluded from parity).
 import io
 import os
 import sys
+import zlib
 
 import numpy as np
 
@@ -31,7 +32,7 @@ sys.path.insert(0, ROOT)
 import reference_loader  # noqa: E402
 from marxs_gb300 import configs  # noqa: E402
 
-N_PHOTONS = {'c0': 2000, 'c1': 3000, 'c2': 3000}
+N_PHOTONS = {'c0': 2000, 'c1': 3000, 'c2': 3000, 'c5': 3000}
 GLOBAL_SEED = 20261203
 
 
@@ -110,6 +111,17 @@ def reference_namespace(marxs):
     from marxs.math.geometry import Cylinder
     from marxs.simulator import Parallel, Sequence
 
+    def interpolated(wave_nm, blaze_deg, probs, orders):
+        # the reference class reads a flattened (wavelength, blaze) table
+        from astropy.table import Column, Table
+        from marxs.missions.mitsnl.catgrating import InterpolateEfficiencyTable
+        ww, bb = np.meshgrid(wave_nm, blaze_deg, indexing='ij')
+        cols = [Column(ww.ravel(), name='wave', unit=u.nm),
+                Column(bb.ravel(), name='blaze', unit=u.deg)]
+        cols += [Column(np.asarray(probs[i]).ravel(), name=str(int(o)))
+                 for i, o in enumerate(orders)]
+        return InterpolateEfficiencyTable(Table(cols), k=1)
+
     def eff(table, orders):
         if isinstance(table, np.ndarray):
             buf = io.StringIO()
@@ -121,7 +133,8 @@ def reference_namespace(marxs):
     return SimpleNamespace(PerfectLens=PerfectLens, RadialMirrorScatter=RadialMirrorScatter,
                            FlatDetector=FlatDetector, CircularDetector=CircularDetector,
                            FlatGrating=FlatGrating, CATGrating=CATGrating,
-                           OrderSelector=OrderSelector, EfficiencyFile=eff, Cylinder=Cylinder,
+                           OrderSelector=OrderSelector, EfficiencyFile=eff,
+                           InterpolateEfficiencyTable=interpolated, Cylinder=Cylinder,
                            Parallel=Parallel, Sequence=Sequence, angle=lambda r: r * u.rad)
 
 
@@ -141,14 +154,14 @@ def generate(name):
     ns = reference_namespace(marxs)
     inst = configs.build(name, ns)
     n = N_PHOTONS[name]
-    ph = configs.photons_for(name, n, seed={'c0': 0, 'c1': 1, 'c2': 2}[name])
+    ph = configs.photons_for(name, n, seed={'c0': 0, 'c1': 1, 'c2': 2, 'c5': 5}[name])
     table = Table({k: v.copy() for k, v in ph.items()})
 
     rec = Recorder()
     for e in leaves(inst.elements):
         rec.wrap(e)
     seq = ns.Sequence(elements=inst.elements)
-    np.random.seed(GLOBAL_SEED + hash(name) % 1000)
+    np.random.seed(GLOBAL_SEED + zlib.crc32(name.encode()) % 1000)
     rec.install()
     try:
         out = seq(table)

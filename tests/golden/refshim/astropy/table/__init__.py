@@ -32,8 +32,23 @@ class Column(np.ndarray):
     def data(self):
         return self.view(np.ndarray)
 
+    def to(self, unit, equivalencies=None):
+        from astropy.units import Quantity
+        return Quantity(self.view(np.ndarray), self.unit).to(unit, equivalencies=equivalencies)
+
 
 MaskedColumn = Column
+
+
+class TableColumns(OrderedDict):
+    """Columns by name, by position, or a slice of positions."""
+
+    def __getitem__(self, key):
+        if isinstance(key, (int, np.integer)):
+            return list(self.values())[key]
+        if isinstance(key, slice):
+            return TableColumns(list(self.items())[key])
+        return OrderedDict.__getitem__(self, key)
 
 
 class Row:
@@ -52,7 +67,7 @@ class Row:
 class Table:
     def __init__(self, data=None, names=None, meta=None, masked=None, copy=True,
                  dtype=None, rows=None):
-        self.columns = OrderedDict()
+        self.columns = TableColumns()
         self.meta = OrderedDict(meta or {})
         if data is None:
             return
@@ -67,6 +82,8 @@ class Table:
             for i, col in enumerate(data):
                 name = names[i] if names is not None else getattr(col, 'name', 'col%d' % i)
                 self[name] = col
+                if getattr(col, 'unit', None) is not None:
+                    self.columns[name].unit = col.unit
 
     @property
     def colnames(self):
@@ -127,8 +144,35 @@ class Table:
         return out
 
     @classmethod
-    def read(cls, *args, **kwargs):
-        raise NotImplementedError('Table.read is not provided by the test shim')
+    def read(cls, filename, format=None, **kwargs):
+        """ECSV only: '#' header with '- {name: .., unit: ..}' column
+        entries, a line of column names, whitespace-separated values."""
+        import re
+        import astropy.units as u
+        if format not in (None, 'ascii.ecsv'):
+            raise NotImplementedError('Table.read: only ECSV in the test shim')
+        units, names, rows = {}, None, []
+        with open(filename) as fh:
+            for line in fh:
+                if line.startswith('#'):
+                    m = re.search(r'name:\s*([^,}]+).*?(?:unit:\s*([^,}]+))?[,}]', line)
+                    if m and 'datatype' in line:
+                        units[m.group(1).strip()] = (m.group(2) or '').strip() or None
+                    continue
+                if not line.strip():
+                    continue
+                if names is None:
+                    names = line.split()
+                    continue
+                rows.append([float(v) for v in line.split()])
+        data = np.array(rows, dtype=float).reshape(-1, len(names))
+        out = cls()
+        for j, name in enumerate(names):
+            out[name] = data[:, j]
+            un = units.get(name)
+            if un is not None:
+                out.columns[name].unit = getattr(u, un)
+        return out
 
 
 QTable = Table

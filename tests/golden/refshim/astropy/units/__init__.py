@@ -15,6 +15,9 @@ class UnitConversionError(Exception):
 
 
 class Unit:
+    # ndarray * unit -> Unit.__rmul__ (numpy defers), as astropy units do
+    __array_ufunc__ = None
+
     def __init__(self, name, kind, scale):
         self.name = name
         self.kind = kind
@@ -100,7 +103,7 @@ class Quantity(np.ndarray):
                 # E [keV] * lambda [nm] = hc
                 v = self.value * self.unit.scale
                 out = _HC_KEV_NM / v
-                return Quantity(out / other.scale, other)
+                return Quantity(out * (nm.scale / other.scale), other)
         raise UnitConversionError('%s -> %s' % (self.unit, other))
 
     def decompose(self):

@@ -25,7 +25,7 @@ def _draws(inst, g):
     return draws
 
 
-@pytest.mark.parametrize('name', ['c0', 'c1', 'c2'])
+@pytest.mark.parametrize('name', ['c0', 'c1', 'c2', 'c5'])
 def test_oracle_reproduces_reference_bitwise(name):
     g = load_golden(name)
     inst = configs.build(name)
@@ -39,7 +39,7 @@ def test_oracle_reproduces_reference_bitwise(name):
     assert stats.get('multi_hit', 0) == int(g['multi_hit'].sum())
 
 
-@pytest.mark.parametrize('name', ['c1', 'c2'])
+@pytest.mark.parametrize('name', ['c1', 'c2', 'c5'])
 def test_native_facet_poses_equal_reference(name):
     """Parallel.generate_elements restated on the host gives the same poses."""
     g = load_golden(name)
@@ -54,6 +54,33 @@ def test_golden_workloads_are_nontrivial():
         assert (ref['facet'] >= 0).mean() > lo
         orders = np.unique(ref['order'][np.isfinite(ref['order'])])
         assert len(orders) >= 10
+
+
+def test_interpolated_workload_exercises_both_splines():
+    """c5: the lens reflectivity lowers the probability and the interpolated
+    CAT table spreads photons over many orders."""
+    ref = golden_outputs(load_golden('c5'))
+    inp = golden_inputs(load_golden('c5'))
+    assert np.all(ref['probability'] < inp['probability'])
+    orders = np.unique(ref['order'][np.isfinite(ref['order'])])
+    assert len(orders) >= 10
+
+
+def test_fitpack_degree1_restatement_equals_scipy():
+    """bisp_k1 (FITPACK fpbisp for kx = ky = 1) against scipy's
+    RectBivariateSpline.ev, inside and outside the grid, bit for bit."""
+    from scipy.interpolate import RectBivariateSpline
+    from oracle.raytrace import bisp_k1
+    rng = np.random.default_rng(3)
+    for nx, ny in ((2, 2), (5, 3), (40, 17), (100, 100)):
+        x = np.sort(rng.uniform(-2, 5, nx)) if nx > 2 else np.array([0.0, 1.5])
+        y = np.sort(rng.uniform(0, 0.1, ny))
+        ip = RectBivariateSpline(x, y, rng.random((nx, ny)), kx=1, ky=1)
+        tx, ty = ip.get_knots()
+        px = np.concatenate([rng.uniform(x[0] - 1, x[-1] + 1, 3000), x, [x[0], x[-1]]])
+        py = np.concatenate([rng.uniform(y[0] - 0.05, y[-1] + 0.05, 3000), y[:1].repeat(nx),
+                             [y[0], y[-1]]])
+        assert np.array_equal(bisp_k1(tx, ty, ip.get_coeffs(), px, py), ip.ev(px, py))
 
 
 @pytest.mark.parametrize('name', ['c0', 'c1'])
