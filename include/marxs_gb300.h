@@ -102,7 +102,25 @@ typedef struct {
     int32_t transmission;
 } mgpu_facet;
 
-/* order selector: OrderSelector (one row) or EfficiencyFile (energy rows) */
+/* Degree-1 tensor-product spline, scipy RectBivariateSpline(kx=1, ky=1) as
+ * FITPACK evaluates it (fpbisp): arguments clamped to [tx[1], tx[nx-2]] and
+ * [ty[1], ty[ny-2]]; n_surf surfaces share the knots, surface s has the
+ * (nx-2)(ny-2) coefficients c[s (nx-2)(ny-2) ...], x-major. */
+typedef struct {
+    int32_t nx, ny;       /* knot counts (grid points + 2) */
+    int32_t n_surf;       /* 0 = no spline */
+    int32_t pad;
+    const double* tx;
+    const double* ty;
+    const double* c;
+} mgpu_spline1;
+
+#define MGPU_SEL_CDF    0  /* cumulative rows: OrderSelector, EfficiencyFile */
+#define MGPU_SEL_SPLINE 1  /* one spline per order in (wavelength nm, blaze rad):
+                              InterpolateEfficiencyTable, missions/mitsnl/catgrating.py:63-144 */
+
+/* order selector: OrderSelector (one row), EfficiencyFile (energy rows) or
+ * InterpolateEfficiencyTable (kind SPLINE) */
 typedef struct {
     int32_t n_rows;
     int32_t n_orders;
@@ -114,6 +132,9 @@ typedef struct {
     const int32_t* orders;/* n_orders */
     const uint64_t* thresholds; /* n_rows * n_orders: ceil(cdf * 2^53); for a draw
                                    u = U * 2^-53, cdf > u  <=>  U < threshold */
+    int32_t kind;         /* MGPU_SEL_* */
+    int32_t pad;
+    mgpu_spline1 spline;  /* SPLINE: n_surf = n_orders surfaces */
 } mgpu_selector;
 
 /* FP32-local constants of a flat element (PerfectLens, RadialMirrorScatter,
@@ -201,6 +222,8 @@ typedef struct {
                                     mgpu_grid32 (GRATINGS), mgpu_cyl32 (CYLDET) */
     const mgpu_facet32* facets32;/* GRATINGS, FP32-local */
     const float* table;          /* CYLDET, FP32-local: nk x (cos hi, cos lo, sin hi, sin lo) */
+    mgpu_spline1 spline;         /* LENS: reflectivity_interpolator(energy, angle / 4), squared
+                                    into the probability (optics/mirror.py:73-79); n_surf 0 = 1 */
 } mgpu_stage;
 /* p[] per kind:
  *   LENS:    p[0] focal length, p[1] d_center_optical_axis

@@ -28,6 +28,7 @@ FLAG_CHECK_W = 0x1
 NOALLOC_MAX_CELLS = 65536
 ERR_NOALLOC_LIMIT = -2
 STATUS_ADJ_RANGE = 0x40
+SEL_CDF, SEL_SPLINE = 0, 1
 ADJ_FREEZE, ADJ_FORWARD, ADJ_BACKWARD = 0, 1, 2
 ADJ_DET_FLAT, ADJ_DET_CYL = 0, 1
 ADJ_NMOM = 5
@@ -65,10 +66,16 @@ class MgpuPhotons(C.Structure):
                 ('prob_out', MgpuCol)]
 
 
+class MgpuSpline1(C.Structure):
+    _fields_ = [('nx', C.c_int32), ('ny', C.c_int32), ('n_surf', C.c_int32), ('pad', C.c_int32),
+                ('tx', C.c_void_p), ('ty', C.c_void_p), ('c', C.c_void_p)]
+
+
 class MgpuSelector(C.Structure):
     _fields_ = [('n_rows', C.c_int32), ('n_orders', C.c_int32), ('by_energy', C.c_int32),
                 ('sorted', C.c_int32), ('energy', C.c_void_p), ('cdf', C.c_void_p),
-                ('total', C.c_void_p), ('orders', C.c_void_p), ('thresholds', C.c_void_p)]
+                ('total', C.c_void_p), ('orders', C.c_void_p), ('thresholds', C.c_void_p),
+                ('kind', C.c_int32), ('pad', C.c_int32), ('spline', MgpuSpline1)]
 
 
 class MgpuFlat32(C.Structure):
@@ -109,7 +116,7 @@ class MgpuStage(C.Structure):
                 ('id_stride', C.c_int64), ('draw', C.c_void_p * 2), ('draw_stride', C.c_int64),
                 ('facets', C.c_void_p), ('selectors', C.c_void_p), ('n_selectors', C.c_int32),
                 ('pad', C.c_int32), ('grid', MgpuGrid), ('aux', C.c_void_p),
-                ('facets32', C.c_void_p), ('table', C.c_void_p)]
+                ('facets32', C.c_void_p), ('table', C.c_void_p), ('spline', MgpuSpline1)]
 
 
 class MgpuChain(C.Structure):

@@ -172,7 +172,7 @@ __device__ __forceinline__ float u53_to_f(uint64_t U) {
 }
 
 // ------------------------------------------------------------------ stages
-__device__ bool stage_lens_l(const mgpu_stage& st, PhotonL& ph, int64_t i) {
+__device__ bool stage_lens_l(const mgpu_stage& st, PhotonL& ph, int64_t i, uint32_t* status) {
     // PerfectLens.specific_process_photons, optics/mirror.py:53-82
     const mgpu_flat32* F = (const mgpu_flat32*)st.aux;
     HitL h = flat_hit(F, ph.pos, ph.dir);
@@ -183,6 +183,17 @@ __device__ bool stage_lens_l(const mgpu_stage& st, PhotonL& ph, int64_t i) {
     f3 cm = ff3_f(ff3_sub(ldff3(F->c_hi, F->c_lo), h.ip));     // centre - interpos
     f3 v = cm - F->p[1] * ldf3(F->ez) + F->p[0] * normf(ph.dir);
     f3 nd = normf(v);
+    if (st.spline.n_surf > 0) {
+        // probability *= reflectivity_interpolator(E, angle / 4) ** 2 (mirror.py:73-79);
+        // the angle from atan2(|a x b|, a . b), accurate for small deflections
+        f3 od = normf(ph.dir);
+        f3 cr = crossf(od, nd);
+        float angle = atan2f(sqrtf(dotf(cr, cr)), fabsf(dotf(od, nd)));
+        double r = spline1_at(st.spline, ph.energy_d, 0.25 * (double)angle);
+        r = r * r;
+        if (r < 0.0 || r > 1.0) atomicOr(status, MGPU_STATUS_PROB_RANGE);
+        ph.prob = ph.prob * (float)r;
+    }
     ph.pol = transport_f(ph.dir, nd, ph.pol);
     ph.dir = nd;
     storef(st.out[0], i, h.ly);
@@ -527,20 +538,32 @@ __device__ bool stage_gratings_l(const mgpu_stage& st, PhotonL& ph, int64_t i, b
     float p_l = dotf(p, l), p_d = dotf(p, dn), p_n = dotf(p, n);
     float blaze = atan2f(fabsf(p_d), fabsf(p_n));      // = arccos|p_perp . n|
     uint64_t U;
+    double u_pre = 0.0;
     if (rng == MGPU_RNG_PREDRAWN) {
         if (st.draw[0] == nullptr) {
             atomicOr(status, MGPU_STATUS_BAD_STAGE);
             return false;
         }
-        double u = st.draw[0][i * st.draw_stride];
-        U = (uint64_t)(u * 9007199254740992.0);
+        u_pre = st.draw[0][i * st.draw_stride];
+        U = (uint64_t)(u_pre * 9007199254740992.0);
     } else {
         uint64_t U1;
         philox_u53(seed, row_base + (uint64_t)i, (uint32_t)sidx, &U, &U1);
     }
     float selprob;
     const int flags = fc->flags;
-    int m = select_order_l(st.selectors[fc->selector], ph.energy_d, U, &selprob, status);
+    const mgpu_selector& sel = st.selectors[fc->selector];
+    int m;
+    if (sel.kind == MGPU_SEL_SPLINE) {
+        // float64 evaluation of the interpolated table (float32 blaze angle)
+        double u = (rng == MGPU_RNG_PREDRAWN) ? u_pre : (double)U * (1.0 / 9007199254740992.0);
+        double tot;
+        m = select_order_spline(sel, ph.energy_d, (double)blaze, u, &tot);
+        if (tot < 0.0 || tot > 1.0) atomicOr(status, MGPU_STATUS_PROB_RANGE);
+        selprob = (float)tot;
+    } else {
+        m = select_order_l(sel, ph.energy_d, U, &selprob, status);
+    }
     float sign;
     if (flags & 1) sign = (p_d > 0.0f) ? 1.0f : ((p_d < 0.0f) ? -1.0f : 1.0f);
     else sign = -1.0f;
@@ -581,7 +604,7 @@ __device__ __forceinline__ bool run_stage_l(const mgpu_stage& st, PhotonL& ph, i
         return stage_gratings_l(st, ph, i, valid, chain.rng, chain.seed, chain.row_base, s,
                                 chain.status);
     case MGPU_STAGE_LENS:
-        return valid && stage_lens_l(st, ph, i);
+        return valid && stage_lens_l(st, ph, i, chain.status);
     case MGPU_STAGE_SCATTER:
         return valid && stage_scatter_l(st, ph, i, chain.rng, chain.seed, chain.row_base, s,
                                         chain.status);

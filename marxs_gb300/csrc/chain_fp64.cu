@@ -82,7 +82,7 @@ __device__ __forceinline__ void check_prob(double f, uint32_t* status) {
 }
 
 // ------------------------------------------------------------------ stages
-__device__ bool stage_lens(const mgpu_stage& st, Photon& ph, int64_t i) {
+__device__ bool stage_lens(const mgpu_stage& st, Photon& ph, int64_t i, uint32_t* status) {
     // PerfectLens.specific_process_photons, optics/mirror.py:53-82
     PlaneHit h = plane_intersect_frame(st.frame, ph.pos, ph.dir);
     if (!h.hit) {
@@ -93,9 +93,16 @@ __device__ bool stage_lens(const mgpu_stage& st, Photon& ph, int64_t i) {
     d3 popt = c - st.p[1] * ez;
     d3 focus = popt + st.p[0] * normalize3(ph.dir);
     d3 nd = normalize3(focus - h.ip);
+    if (st.spline.n_surf > 0) {
+        // probability *= reflectivity_interpolator(E, angle / 4) ** 2 (mirror.py:73-79)
+        double angle = acos(fabs(dot3(nd, normalize3(ph.dir))));
+        double r = spline1_at(st.spline, ph.energy, angle / 4.0);
+        r = __dmul_rn(r, r);
+        check_prob(r, status);
+        ph.prob = ph.prob * r;
+    }
     ph.pol = parallel_transport_dev(ph.dir, nd, ph.pol);
     ph.dir = nd;
-    // default reflectivity: probability *= 1
     store_col(st.out[0], i, h.ly);
     store_col(st.out[1], i, h.lz);
     ph.pos = h.ip;
@@ -285,7 +292,10 @@ __device__ bool stage_gratings(const mgpu_stage& st, Photon& ph, int64_t i, bool
         philox_uniform2(seed, row_base + (uint64_t)i, (uint32_t)sidx, 0u, &u, &u1);
     }
     double selprob;
-    int m = select_order(st.selectors[__ldg(&fc->selector)], ph.energy, u, &selprob, status);
+    const mgpu_selector& sel = st.selectors[__ldg(&fc->selector)];
+    int m;
+    if (sel.kind == MGPU_SEL_SPLINE) m = select_order_spline(sel, ph.energy, blaze, u, &selprob);
+    else m = select_order(sel, ph.energy, u, &selprob, status);
     check_prob(selprob, status);
     double pd0 = dot3(p, dn);
     double sign;
@@ -352,7 +362,7 @@ chain_fp64_kernel(const __grid_constant__ mgpu_chain chain, const __grid_constan
                                      chain.status);
                 break;
             case MGPU_STAGE_LENS:
-                if (valid) hit = stage_lens(st, ph, i);
+                if (valid) hit = stage_lens(st, ph, i, chain.status);
                 break;
             case MGPU_STAGE_SCATTER:
                 if (valid) hit = stage_scatter(st, ph, i, chain.rng, chain.seed, chain.row_base, s,

@@ -240,3 +240,84 @@ __device__ __forceinline__ void philox_normal2(uint64_t seed, uint64_t row, uint
     *n0 = r * c;
     *n1 = r * s;
 }
+
+// ---------------------------------------------------------------------------
+// Degree-1 tensor spline as scipy's RectBivariateSpline(kx=1, ky=1).ev
+// evaluates it (FITPACK fpbisp + fpbspl): the argument is clamped to
+// [t[1], t[n-2]] (a NaN stays NaN), the interval l is the first one with
+// arg < t[l+1], capped at n-3, the weights are f (t[l+1] - arg) and
+// f (arg - t[l]) with f = 1 / (t[l+1] - t[l]), and the value is
+// sum over the 2x2 coefficients of (c * hx) * hy, x-major, added to 0 in that
+// order.  Multiplies and adds are issued unfused so the result is the one
+// the float64 reference computes.
+struct Spline1W {
+    int base;
+    double hx0, hx1, hy0, hy1;
+};
+
+__device__ __forceinline__ void spline1_axis(const double* t, int n, double a, int& l, double& h0,
+                                             double& h1) {
+    double arg = a;
+    if (arg < t[1]) arg = t[1];
+    if (arg > t[n - 2]) arg = t[n - 2];
+    // first j in [2, n-2] with t[j] > arg (n-1 when none); l = j - 1, at most n - 3
+    int lo = 2, hi = n - 1;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (t[mid] > arg) hi = mid;
+        else lo = mid + 1;
+    }
+    l = lo - 1;
+    if (l > n - 3) l = n - 3;
+    const double f = 1.0 / (t[l + 1] - t[l]);
+    h0 = __dmul_rn(f, t[l + 1] - arg);
+    h1 = __dmul_rn(f, arg - t[l]);
+}
+
+__device__ __forceinline__ Spline1W spline1_weights(const mgpu_spline1& S, double x, double y) {
+    Spline1W w;
+    int lx, ly;
+    spline1_axis(S.tx, S.nx, x, lx, w.hx0, w.hx1);
+    spline1_axis(S.ty, S.ny, y, ly, w.hy0, w.hy1);
+    w.base = (lx - 1) * (S.ny - 2) + (ly - 1);
+    return w;
+}
+
+__device__ __forceinline__ double spline1_value(const mgpu_spline1& S, int s, const Spline1W& w) {
+    const int nky1 = S.ny - 2;
+    const double* c = S.c + (size_t)s * (size_t)(S.nx - 2) * (size_t)nky1 + w.base;
+    double sp = 0.0;
+    sp = __dadd_rn(sp, __dmul_rn(__dmul_rn(c[0], w.hx0), w.hy0));
+    sp = __dadd_rn(sp, __dmul_rn(__dmul_rn(c[1], w.hx0), w.hy1));
+    sp = __dadd_rn(sp, __dmul_rn(__dmul_rn(c[nky1], w.hx1), w.hy0));
+    sp = __dadd_rn(sp, __dmul_rn(__dmul_rn(c[nky1 + 1], w.hx1), w.hy1));
+    return sp;
+}
+
+// spline surface 0 at (x, y)
+__device__ __forceinline__ double spline1_at(const mgpu_spline1& S, double x, double y) {
+    return spline1_value(S, 0, spline1_weights(S, x, y));
+}
+
+// h c in keV nm, the factor of astropy's spectral() keV -> nm conversion
+#define MGPU_HC_KEV_NM 1.2398419843320026
+
+// InterpolateEfficiencyTable.__call__ (missions/mitsnl/catgrating.py:101-144):
+// each order's spline at (wavelength nm, blaze rad); total = their sum in
+// order; the chosen index is the first whose running sum / total exceeds u
+// (numpy argmax: index 0 when none does); the probability factor is total.
+__device__ __forceinline__ int select_order_spline(const mgpu_selector& sel, double energy,
+                                                   double blaze, double u, double* prob) {
+    const double wave = MGPU_HC_KEV_NM / energy;
+    const Spline1W w = spline1_weights(sel.spline, wave, blaze);
+    double total = 0.0;
+    for (int k = 0; k < sel.n_orders; ++k) total = __dadd_rn(total, spline1_value(sel.spline, k, w));
+    double cum = 0.0;
+    int pick = -1;
+    for (int k = 0; k < sel.n_orders && pick < 0; ++k) {
+        cum = __dadd_rn(cum, spline1_value(sel.spline, k, w));
+        if (cum / total > u) pick = k;
+    }
+    *prob = total;
+    return sel.orders[pick < 0 ? 0 : pick];
+}

@@ -104,7 +104,22 @@ class _Instrument:
             self.keep.append(t)
             return t
 
+        def spline_struct(sp):
+            out = _abi.MgpuSpline1()
+            if sp is None:
+                return out
+            ts = [torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).to(device)
+                  for a in sp]
+            self.keep += ts
+            out.nx, out.ny, out.n_surf = len(sp[0]), len(sp[1]), int(sp[2].shape[0])
+            out.tx, out.ty, out.c = ts[0].data_ptr(), ts[1].data_ptr(), ts[2].data_ptr()
+            return out
+
+        self.stage_spline = {}
+
         for si, st in enumerate(stages):
+            if st.spline is not None:
+                self.stage_spline[si] = spline_struct(st.spline)
             try:
                 if st.kind in (_abi.STAGE_LENS, _abi.STAGE_SCATTER, _abi.STAGE_FLATDET):
                     self.stage_aux[si] = dev_bytes(L.flat32_block(st))
@@ -137,7 +152,8 @@ class _Instrument:
                                                    1 if s.by_energy else 0,
                                                    1 if L.selector_sorted(s) else 0, e.data_ptr(),
                                                    cdf.data_ptr(), tot.data_ptr(), ords.data_ptr(),
-                                                   thr.data_ptr())
+                                                   thr.data_ptr(), s.kind, 0,
+                                                   spline_struct(s.spline))
             raw = np.frombuffer(bytes(sel_structs), dtype=np.uint8).copy()
             sel_dev = torch.from_numpy(raw).to(device)
             self.keep.append(sel_dev)
@@ -188,6 +204,8 @@ class _Instrument:
             s.facets32 = self.stage_facets32[si].data_ptr()
         if si in self.stage_table:
             s.table = self.stage_table[si].data_ptr()
+        if si in self.stage_spline:
+            s.spline = self.stage_spline[si]
 
 
 class ColumnPlan:

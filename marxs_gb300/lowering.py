@@ -82,11 +82,53 @@ class SelectorSpec:
     total: np.ndarray
     orders: np.ndarray        # int32
     by_energy: bool
+    kind: int = 0             # _abi.SEL_CDF / SEL_SPLINE
+    spline: Optional[tuple] = None   # SEL_SPLINE: (tx, ty, c[n_orders, ...])
+
+
+def spline1_arrays(ip, what):
+    """(tx, ty, coefficients) of a degree-1 scipy RectBivariateSpline."""
+    if not (hasattr(ip, 'get_knots') and tuple(getattr(ip, 'degrees', ())) == (1, 1)):
+        raise NotImplementedError('%s: only degree-1 RectBivariateSpline (kx = ky = 1) is '
+                                  'supported on the GPU' % what)
+    tx, ty = ip.get_knots()
+    c = np.asarray(ip.get_coeffs(), dtype=float)
+    if c.size != (len(tx) - 2) * (len(ty) - 2):
+        raise NotImplementedError('%s: unexpected spline coefficient layout' % what)
+    return np.asarray(tx, dtype=float), np.asarray(ty, dtype=float), c
+
+
+def lens_spline(lens):
+    """Reflectivity spline of a PerfectLens, or None for the default
+    (probability unchanged, optics/mirror.py:45-48)."""
+    interp = getattr(lens, 'reflectivity_interpolator', None)
+    if interp is None:
+        return None
+    if getattr(interp, '__name__', '') == '<lambda>' and \
+            'marxs' in getattr(interp, '__module__', ''):
+        return None
+    tx, ty, c = spline1_arrays(interp, 'PerfectLens reflectivity_interpolator')
+    return tx, ty, c[None, :]
 
 
 def lower_selector(sel):
     """Tables of an order selector, computed with the reference's numpy ops."""
     names = classnames(sel)
+    if hasattr(sel, 'interpolators') and hasattr(sel, 'orders'):
+        # InterpolateEfficiencyTable (missions/mitsnl/catgrating.py:63-144)
+        tx = ty = None
+        cs = []
+        for ip in sel.interpolators:
+            kx, ky, c = spline1_arrays(ip, 'InterpolateEfficiencyTable')
+            if tx is None:
+                tx, ty = kx, ky
+            elif not (np.array_equal(tx, kx) and np.array_equal(ty, ky)):
+                raise NotImplementedError('InterpolateEfficiencyTable: orders on different grids')
+            cs.append(c)
+        n = len(cs)
+        return SelectorSpec(energy=np.zeros(1), cdf=np.zeros((1, n)), total=np.zeros(1),
+                            orders=np.asarray(sel.orders).astype(np.int32), by_energy=False,
+                            kind=_abi.SEL_SPLINE, spline=(tx, ty, np.stack(cs)))
     if 'EfficiencyFile' in names:
         return SelectorSpec(energy=np.asarray(sel.energy, dtype=float),
                             cdf=np.ascontiguousarray(sel.cumprob, dtype=float),
@@ -118,6 +160,7 @@ class StageSpec:
     facets: Optional[np.ndarray] = None
     selectors: List[SelectorSpec] = field(default_factory=list)
     grid: Optional[dict] = None
+    spline: Optional[tuple] = None   # LENS reflectivity (tx, ty, c[1, ...])
 
 
 def _loc_names(elem):
@@ -251,13 +294,9 @@ def _lower_one(e):
             out.extend(_lower_one(sub))
         return out
     if 'PerfectLens' in names:
-        interp = getattr(e, 'reflectivity_interpolator', None)
-        if interp is not None and not (getattr(interp, '__name__', '') == '<lambda>' and
-                                       'marxs' in getattr(interp, '__module__', '')):
-            raise NotImplementedError('PerfectLens reflectivity_interpolator on the GPU')
         loc = _loc_names(e)
         st = StageSpec(kind=_abi.STAGE_LENS, element=e, frame=plane_frame(e.geometry.pos4d),
-                       out_names=[loc[0], loc[1], None, None])
+                       out_names=[loc[0], loc[1], None, None], spline=lens_spline(e))
         st.p[0] = float(e.focallength)
         st.p[1] = float(getattr(e, 'd_center_optax', 0.))
         st.new_col_order = [n for n in loc if n is not None]
@@ -319,6 +358,10 @@ def fingerprint(stages):
         h.update(repr((st.out_names, st.id_col)).encode())
         if st.facets is not None:
             h.update(st.facets.tobytes())
+        for sp in [st.spline] + [s.spline for s in st.selectors]:
+            if sp is not None:
+                for a in sp:
+                    h.update(np.ascontiguousarray(a).tobytes())
         for s in st.selectors:
             for a in (s.energy, s.cdf, s.total, s.orders):
                 h.update(np.ascontiguousarray(a).tobytes())

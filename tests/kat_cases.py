@@ -5,7 +5,7 @@ Each case takes a runner and asserts the reference's known answers:
 * polarization transport: marxs/math/tests/test_polarization.py:36-72
 * gratings: marxs/optics/tests/test_grating.py:16-223
 * detector pixels: marxs/optics/tests/test_detector.py:16-36
-* lens: marxs/optics/tests/test_mirror.py:14-59
+* lens: marxs/optics/tests/test_mirror.py:14-80
 * scatter special cases: marxs/optics/tests/test_scatter.py:46-74
 
 A runner provides ``plane_intersect(geometry, dir, pos)``,
@@ -302,6 +302,22 @@ def case_perfect_lens_offset(r):
     p1 = r.trace([lens], test_photons(1))
     p2 = r.trace([lens2], test_photons(1))
     assert np.allclose(p1['dir'], p2['dir'])
+
+
+def case_perfect_lens_reflectivity(r):
+    """test_PerfectLens_refl (test_mirror.py:62-80): a degree-1 spline of
+    exp(-sqrt((x/2)^2 + y^2)) on a 100 x 100 grid, at (1 keV, 0 rad), squared."""
+    from scipy.interpolate import RectBivariateSpline
+    xarr = np.linspace(-3, 3, 100)
+    yarr = np.linspace(-3, 3, 100)
+    xgrid, ygrid = np.meshgrid(xarr, yarr, indexing='ij')
+    zdata = np.exp(-np.sqrt((xgrid / 2) ** 2 + ygrid ** 2))
+    interp = RectBivariateSpline(xarr, yarr, zdata, kx=1, ky=1)
+    lens = PerfectLens(focallength=123.0, reflectivity_interpolator=interp)
+    out = r.trace([lens], test_photons(1))
+    assert np.allclose(out['energy'], 1)
+    assert np.allclose(out['polarization'], [0, 1, 0, 0])
+    assert np.allclose(out['probability'], 0.367205)
 
 
 # ------------------------------------------------------------------ scatter

@@ -18,7 +18,7 @@ STRUCTS = {
     'mgpu_selector': _abi.MgpuSelector, 'mgpu_grid': _abi.MgpuGrid,
     'mgpu_stage': _abi.MgpuStage, 'mgpu_chain': _abi.MgpuChain,
     'mgpu_flat32': _abi.MgpuFlat32, 'mgpu_grid32': _abi.MgpuGrid32, 'mgpu_cyl32': _abi.MgpuCyl32,
-    'mgpu_adjoint_problem': _abi.MgpuAdjointProblem,
+    'mgpu_adjoint_problem': _abi.MgpuAdjointProblem, 'mgpu_spline1': _abi.MgpuSpline1,
 }
 
 
@@ -70,6 +70,8 @@ def test_header_constants_match():
         assert int(consts['MGPU_STAGE_' + name]) == getattr(_abi, 'STAGE_' + name)
     assert int(consts['MGPU_NOALLOC_MAX_CELLS']) == _abi.NOALLOC_MAX_CELLS
     assert int(consts['MGPU_STATUS_ADJ_RANGE'].rstrip('u'), 16) == _abi.STATUS_ADJ_RANGE
+    assert int(consts['MGPU_SEL_CDF']) == _abi.SEL_CDF
+    assert int(consts['MGPU_SEL_SPLINE']) == _abi.SEL_SPLINE
     for name in ('FREEZE', 'FORWARD', 'BACKWARD', 'DET_FLAT', 'DET_CYL', 'NMOM', 'NSEED',
                  'MAX_GROUPS', 'MAX_FACETS'):
         assert int(consts['MGPU_ADJ_' + name]) == getattr(_abi, 'ADJ_' + name), name

@@ -80,7 +80,7 @@ def test_fp32local_vs_fp64_cat_array(n):
     assert dy.max() <= 5 * UM, report
 
 
-@pytest.mark.parametrize('name', ['c0', 'c1', 'c2'])
+@pytest.mark.parametrize('name', ['c0', 'c1', 'c2', 'c5'])
 def test_fp32local_golden(name):
     from marxs_gb300 import configs
     g = load_golden(name)
@@ -104,6 +104,9 @@ def test_fp32local_golden(name):
     for col, tol in (('dir', 1e-6), ('polarization', 1e-5)):
         x, y = np.asarray(out[col])[agree], ref[col][agree]
         assert np.nanmax(np.abs(x - y)) <= tol, (col, np.nanmax(np.abs(x - y)))
+    # float32 probability (products of the element factors)
+    x, y = np.asarray(out['probability'])[agree], ref['probability'][agree]
+    assert np.max(np.abs(x - y) / np.maximum(y, 1e-30)) <= 2e-6
     for col in ref:
         if col in ('pos', 'dir', 'polarization', 'facet', 'order', 'energy'):
             continue

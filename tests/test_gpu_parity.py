@@ -75,7 +75,7 @@ def _column_report(out, ref, ok):
 BLAZE_ABS = 5e-8
 
 
-@pytest.mark.parametrize('name', ['c0', 'c1', 'c2'])
+@pytest.mark.parametrize('name', ['c0', 'c1', 'c2', 'c5'])
 def test_golden_parity_fp64(name):
     g, out = _run_gpu(name)
     ref = golden_outputs(g)
@@ -86,7 +86,7 @@ def test_golden_parity_fp64(name):
     assert not bad, 'columns out of tolerance: %s (all: %s)' % (bad, report)
 
 
-@pytest.mark.parametrize('name', ['c1', 'c2'])
+@pytest.mark.parametrize('name', ['c1', 'c2', 'c5'])
 def test_golden_hits_are_counted(name):
     from marxs_gb300 import configs
     g, out = _run_gpu(name)
