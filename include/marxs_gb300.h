@@ -125,7 +125,8 @@ typedef struct {
     int32_t n_rows;
     int32_t n_orders;
     int32_t by_energy;    /* 1: nearest energy row (argmin |E - e|) */
-    int32_t sorted;       /* 1: energy strictly increasing (binary search allowed) */
+    int32_t sorted;       /* 1: energy strictly increasing and every cdf row
+                             non-decreasing (binary searches allowed) */
     const double* energy; /* n_rows */
     const double* cdf;    /* n_rows * n_orders, normalised cumulative */
     const double* total;  /* n_rows, probability factor */
@@ -222,6 +223,8 @@ typedef struct {
                                     mgpu_grid32 (GRATINGS), mgpu_cyl32 (CYLDET) */
     const mgpu_facet32* facets32;/* GRATINGS, FP32-local */
     const float* table;          /* CYLDET, FP32-local: nk x (cos hi, cos lo, sin hi, sin lo) */
+    const float* cand32;         /* GRATINGS, FP32-local: 16 floats per facet, 16-byte aligned:
+                                    (c_hi, hy), (e_x, hz), (e_y, e_z.x), (e_z.y, e_z.z, 0, 0) */
     mgpu_spline1 spline;         /* LENS: reflectivity_interpolator(energy, angle / 4), squared
                                     into the probability (optics/mirror.py:73-79); n_surf 0 = 1 */
 } mgpu_stage;

@@ -116,7 +116,8 @@ class MgpuStage(C.Structure):
                 ('id_stride', C.c_int64), ('draw', C.c_void_p * 2), ('draw_stride', C.c_int64),
                 ('facets', C.c_void_p), ('selectors', C.c_void_p), ('n_selectors', C.c_int32),
                 ('pad', C.c_int32), ('grid', MgpuGrid), ('aux', C.c_void_p),
-                ('facets32', C.c_void_p), ('table', C.c_void_p), ('spline', MgpuSpline1)]
+                ('facets32', C.c_void_p), ('table', C.c_void_p), ('cand32', C.c_void_p),
+                ('spline', MgpuSpline1)]
 
 
 class MgpuChain(C.Structure):

@@ -80,8 +80,9 @@ __device__ __forceinline__ HitL plane_hit_l(ff3 c, f3 n, f3 ey, f3 ez, float hy,
         v = ff3_f(ff3_sub(ip, c));
         float dk = -dotf(v, n) / kd;
         if (kd != 0.0f && dk != 0.0f && isfinite(dk)) {
+            // |dk| ~ float32 error of k: dk * dir is exact to ~1e-10 mm in float32
             k += dk;
-            ip = ff3_axpy(ip, dk, dir);
+            ip = ff3_add_f3(ip, dk * dir);
             v = v + dk * dir;
         }
     }
@@ -291,13 +292,15 @@ __device__ bool stage_cyldet_l(const mgpu_stage& st, PhotonL& ph, int64_t i) {
     f3 e1f = ldf3(K->e1_hi), e2f = ldf3(K->e2_hi), af = ldf3(K->a_hi);
     ff R{K->R_hi, K->R_lo};
     ff3 q = ff3_sub(ph.pos, ldff3(K->c_hi, K->c_lo));
-    ff q1 = ff_dot(q, e1), q2 = ff_dot(q, e2);
-    float q3 = ff_f(ff_dot(q, ax));
+    // the root is found in float32 (error ~1e-3 mm from the cancellation in
+    // c at |q_perp| ~ R), the float-float Newton step below makes it exact
+    const f3 qf = ff3_f(q);
+    const float q1f = dotf(qf, e1f), q2f = dotf(qf, e2f), q3 = dotf(qf, af);
     f3 d = ph.dir;
     float d1 = dotf(d, e1f), d2 = dotf(d, e2f), d3 = dotf(d, af);
     float a = d1 * d1 + d2 * d2;
-    float b = ff_f(q1) * d1 + ff_f(q2) * d2;                       // half of the linear term
-    float c = ff_f(ff_sub(ff_add(ff_mul(q1, q1), ff_mul(q2, q2)), ff_mul(R, R)));
+    float b = q1f * d1 + q2f * d2;                                  // half of the linear term
+    float c = (q1f - K->R_hi) * (q1f + K->R_hi) + q2f * q2f;
     float disc = b * b - a * c;
     bool hit = false;
     float t = 0.0f;
@@ -307,7 +310,6 @@ __device__ bool stage_cyldet_l(const mgpu_stage& st, PhotonL& ph, int64_t i) {
         float tA = qq / a, tB = c / qq;
         float a1 = (b < 0.0f) ? tA : tB;     // (-b + sq) / a
         float a2 = (b < 0.0f) ? tB : tA;     // (-b - sq) / a
-        float q1f = ff_f(q1), q2f = ff_f(q2);
         float z1 = q3 + a1 * d3, z2 = q3 + a2 * d3;
         bool h1 = (a1 >= 0.0f) && (fabsf(z1) <= K->Rz) &&
                   angle_between_f(atan2f(q2f + a1 * d2, q1f + a1 * d1), K->b1, K->b2);
@@ -373,15 +375,15 @@ __device__ __forceinline__ int select_order_l(const mgpu_selector& sel, double e
         if (sel.sorted) {
             // largest j with E_j <= e (positive doubles order as integers)
             long long key = __double_as_longlong(e);
-            int lo = 0, hi = n - 1;
-            if (!(key >= __double_as_longlong(sel.energy[0]))) {
+            const double e0 = sel.energy[0], e1 = sel.energy[n - 1];
+            if (!(key >= __double_as_longlong(e0))) {
                 row = 0;
             } else {
-                while (lo < hi) {
-                    int mid = (lo + hi + 1) >> 1;
-                    if (__double_as_longlong(sel.energy[mid]) <= key) lo = mid;
-                    else hi = mid - 1;
-                }
+                // guess from a uniform grid, then step to the largest j with E_j <= e
+                float g = __fdividef((float)(e - e0), (float)(e1 - e0)) * (float)(n - 1);
+                int lo = min(max((int)g, 0), n - 1);
+                while (lo + 1 < n && __double_as_longlong(sel.energy[lo + 1]) <= key) ++lo;
+                while (lo > 0 && __double_as_longlong(sel.energy[lo]) > key) --lo;
                 row = lo;
                 if (row + 1 < n) {
                     double d0 = fabs(sel.energy[row] - e), d1 = fabs(sel.energy[row + 1] - e);
@@ -401,7 +403,16 @@ __device__ __forceinline__ int select_order_l(const mgpu_selector& sel, double e
     }
     const uint64_t* th = sel.thresholds + (int64_t)row * sel.n_orders;
     int k = 0;
-    while (k < sel.n_orders && !(U < th[k])) ++k;
+    if (sel.sorted) {
+        int hi = sel.n_orders;
+        while (k < hi) {
+            int mid = (k + hi) >> 1;
+            if (U < th[mid]) hi = mid;
+            else k = mid + 1;
+        }
+    } else {
+        while (k < sel.n_orders && !(U < th[k])) ++k;
+    }
     if (k == sel.n_orders) {
         atomicOr(status, MGPU_STATUS_ORDER_EMPTY);
         k = sel.n_orders - 1;
@@ -443,23 +454,25 @@ __device__ __forceinline__ int nearest_facet_grid_l(const mgpu_stage& st, const 
     float best_k = 0.0f;
     for (int q = s0; q < s1; ++q) {
         int f = __ldg(g.cell_items + q);
-        const mgpu_facet32* fc = st.facets32 + f;
-        // plain float32 test first; the exact float-float test only when the
-        // ray passes within the float32 error band of an edge
-        f3 r{(ph.pos.x.hi - fc->c_hi[0]) + (ph.pos.x.lo - fc->c_lo[0]),
-             (ph.pos.y.hi - fc->c_hi[1]) + (ph.pos.y.lo - fc->c_lo[1]),
-             (ph.pos.z.hi - fc->c_hi[2]) + (ph.pos.z.lo - fc->c_lo[2])};
-        f3 nx = ldf3(fc->ex);
+        // plain float32 test on the packed record first (centre without its
+        // low word, <= 2^-25 |c|); the exact float-float test only when the
+        // ray passes within the error band of an edge
+        const float4* cr = reinterpret_cast<const float4*>(st.cand32) + 4 * f;
+        const float4 A = __ldg(cr), B = __ldg(cr + 1), E = __ldg(cr + 2), D = __ldg(cr + 3);
+        f3 r{(ph.pos.x.hi - A.x) + ph.pos.x.lo, (ph.pos.y.hi - A.y) + ph.pos.y.lo,
+             (ph.pos.z.hi - A.z) + ph.pos.z.lo};
+        f3 nx{B.x, B.y, B.z};
         float kd = dotf(ph.dir, nx);
         float k = -dotf(r, nx) / kd;
         f3 v = r + k * ph.dir;
-        float ly = dotf(v, ldf3(fc->ey)), lz = dotf(v, ldf3(fc->ez));
-        float tol = 1e-6f * (fabsf(r.x) + fabsf(r.y) + fabsf(r.z) + fabsf(k)) + 1e-5f;
-        float my = fabsf(ly) - fc->hy, mz = fabsf(lz) - fc->hz;
+        float ly = dotf(v, f3{E.x, E.y, E.z}), lz = dotf(v, f3{E.w, D.x, D.y});
+        float tol = 1e-6f * (fabsf(ph.pos.x.hi) + fabsf(ph.pos.y.hi) + fabsf(ph.pos.z.hi) +
+                             fabsf(r.x) + fabsf(r.y) + fabsf(r.z) + fabsf(k)) + 1e-5f;
+        float my = fabsf(ly) - A.w, mz = fabsf(lz) - B.w;
         if (!(kd != 0.0f) || !(k >= -tol) || !(my <= tol) || !(mz <= tol)) continue;
         bool hit = true;
         if (!(k > tol) || !(my < -tol) || !(mz < -tol)) {
-            HitL h = facet_hit(fc, ph.pos, ph.dir);
+            HitL h = facet_hit(st.facets32 + f, ph.pos, ph.dir);
             hit = h.hit;
             k = h.k;
         }
@@ -468,7 +481,6 @@ __device__ __forceinline__ int nearest_facet_grid_l(const mgpu_stage& st, const 
             best_k = k;
         }
     }
-    if (best >= 0) *best_hit = facet_hit(st.facets32 + best, ph.pos, ph.dir);
     return best;
 }
 
@@ -521,16 +533,14 @@ __device__ bool stage_gratings_l(const mgpu_stage& st, PhotonL& ph, int64_t i, b
     unsigned bm = __ballot_sync(MGPU_FULL_MASK, brute);
     if (bm) {
         int bf = brute_force_nearest(st, ph.pos, ph.dir, bm);
-        if (brute && bf >= 0) {
-            f = bf;
-            h = facet_hit(st.facets32 + bf, ph.pos, ph.dir);
-        }
+        if (brute) f = bf;
     }
     if (!valid) return false;
     if (f < 0) {
         write_miss_defaults(st, i, 4);
         return false;
     }
+    h = facet_hit(st.facets32 + f, ph.pos, ph.dir);
     // FlatGrating.diffract_photons (grating.py:233-266) in the facet frame
     const mgpu_facet32* fc = st.facets32 + f;
     f3 l = ldf3(fc->l), dn = ldf3(fc->dneg), n = ldf3(fc->ex);
@@ -721,7 +731,9 @@ cudaError_t mgpu_launch_chain_fp32local(const mgpu_chain& chain, const mgpu_phot
     for (int s = 0; s < chain.n_stages; ++s) {
         const mgpu_stage& st = chain.stages[s];
         if (st.aux == nullptr) return cudaErrorInvalidValue;
-        if (st.kind == MGPU_STAGE_GRATINGS && st.facets32 == nullptr) return cudaErrorInvalidValue;
+        if (st.kind == MGPU_STAGE_GRATINGS &&
+            (st.facets32 == nullptr || st.cand32 == nullptr || ((uintptr_t)st.cand32 & 15u) != 0))
+            return cudaErrorInvalidValue;
         if (st.kind == MGPU_STAGE_CYLDET && st.table == nullptr) return cudaErrorInvalidValue;
     }
     int64_t warps = (io.n + 31) / 32;

@@ -94,6 +94,7 @@ class _Instrument:
         self.stage_grid = {}
         self.stage_aux = {}       # FP32-local constant blocks
         self.stage_facets32 = {}
+        self.stage_cand32 = {}
         self.stage_table = {}
         self.fp32_error = None
         lib = _abi.load()
@@ -128,7 +129,9 @@ class _Instrument:
                     self.stage_aux[si] = dev_bytes(blk)
                     self.stage_table[si] = dev_bytes(table.tobytes())
                 elif st.kind == _abi.STAGE_GRATINGS:
-                    self.stage_facets32[si] = dev_bytes(L.facets32_table(st.facets).tobytes())
+                    t32 = L.facets32_table(st.facets)
+                    self.stage_facets32[si] = dev_bytes(t32.tobytes())
+                    self.stage_cand32[si] = dev_bytes(L.facets_cand32(t32).tobytes())
                     if st.grid is not None:
                         self.stage_aux[si] = dev_bytes(L.grid32_block(st.grid))
                     else:
@@ -202,6 +205,7 @@ class _Instrument:
             s.aux = self.stage_aux[si].data_ptr()
         if si in self.stage_facets32:
             s.facets32 = self.stage_facets32[si].data_ptr()
+            s.cand32 = self.stage_cand32[si].data_ptr()
         if si in self.stage_table:
             s.table = self.stage_table[si].data_ptr()
         if si in self.stage_spline:
