@@ -136,6 +136,8 @@ typedef struct {
     int32_t kind;         /* MGPU_SEL_* */
     int32_t pad;
     mgpu_spline1 spline;  /* SPLINE: n_surf = n_orders surfaces */
+    const uint8_t* guide; /* optional, sorted rows only: n_rows x 64, entry b = first order
+                             index k with U < threshold[k] for U = b * 2^47 */
 } mgpu_selector;
 
 /* FP32-local constants of a flat element (PerfectLens, RadialMirrorScatter,

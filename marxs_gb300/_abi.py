@@ -75,7 +75,8 @@ class MgpuSelector(C.Structure):
     _fields_ = [('n_rows', C.c_int32), ('n_orders', C.c_int32), ('by_energy', C.c_int32),
                 ('sorted', C.c_int32), ('energy', C.c_void_p), ('cdf', C.c_void_p),
                 ('total', C.c_void_p), ('orders', C.c_void_p), ('thresholds', C.c_void_p),
-                ('kind', C.c_int32), ('pad', C.c_int32), ('spline', MgpuSpline1)]
+                ('kind', C.c_int32), ('pad', C.c_int32), ('spline', MgpuSpline1),
+                ('guide', C.c_void_p)]
 
 
 class MgpuFlat32(C.Structure):

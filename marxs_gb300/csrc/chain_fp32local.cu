@@ -70,7 +70,10 @@ struct HitL {
 __device__ __forceinline__ HitL plane_hit_l(ff3 c, f3 n, f3 ey, f3 ez, float hy, float hz,
                                             const ff3& pos, f3 dir) {
     HitL h;
-    f3 rel = ff3_f(ff3_sub(pos, c));
+    // first solve from a float32 offset (error ~2^-24 |pos|, removed by the
+    // refinement against the float-float offset below)
+    f3 rel{(pos.x.hi - c.x.hi) + (pos.x.lo - c.x.lo), (pos.y.hi - c.y.hi) + (pos.y.lo - c.y.lo),
+           (pos.z.hi - c.z.hi) + (pos.z.lo - c.z.lo)};
     float kd = dotf(dir, n);
     float k = -dotf(rel, n) / kd;
     ff3 ip = pos;
@@ -403,7 +406,11 @@ __device__ __forceinline__ int select_order_l(const mgpu_selector& sel, double e
     }
     const uint64_t* th = sel.thresholds + (int64_t)row * sel.n_orders;
     int k = 0;
-    if (sel.sorted) {
+    if (sel.guide) {
+        // start at the first order of the draw's 1/64 bin, then step
+        k = __ldg(sel.guide + row * 64 + (int)(U >> 47));
+        while (k < sel.n_orders && !(U < th[k])) ++k;
+    } else if (sel.sorted) {
         int hi = sel.n_orders;
         while (k < hi) {
             int mid = (k + hi) >> 1;
@@ -670,7 +677,9 @@ struct FixedChain {
 };
 
 template <class Chain>
-__global__ void __launch_bounds__(kThreads)
+// 3 blocks of 256 per SM (<= 84 registers): measured 4 % faster than the
+// unconstrained allocation (100 registers, 2 blocks)
+__global__ void __launch_bounds__(kThreads, 3)
 chain_fp32local_kernel(const __grid_constant__ mgpu_chain chain, const __grid_constant__ mgpu_photons io) {
     __shared__ unsigned int s_hits[MGPU_MAX_STAGES];
     if (threadIdx.x < MGPU_MAX_STAGES) s_hits[threadIdx.x] = 0;

@@ -151,12 +151,18 @@ class _Instrument:
                 ords = torch.from_numpy(np.ascontiguousarray(s.orders, dtype=np.int32)).to(device)
                 thr = torch.from_numpy(L.selector_thresholds(s).view(np.int64)).to(device)
                 self.keep += [e, cdf, tot, ords, thr]
+                gd = L.selector_guide(s) if s.kind == _abi.SEL_CDF else None
+                gd_ptr = 0
+                if gd is not None:
+                    gdt = torch.from_numpy(np.ascontiguousarray(gd)).to(device)
+                    self.keep.append(gdt)
+                    gd_ptr = gdt.data_ptr()
                 sel_structs[k] = _abi.MgpuSelector(s.cdf.shape[0], s.cdf.shape[1],
                                                    1 if s.by_energy else 0,
                                                    1 if L.selector_sorted(s) else 0, e.data_ptr(),
                                                    cdf.data_ptr(), tot.data_ptr(), ords.data_ptr(),
                                                    thr.data_ptr(), s.kind, 0,
-                                                   spline_struct(s.spline))
+                                                   spline_struct(s.spline), gd_ptr)
             raw = np.frombuffer(bytes(sel_structs), dtype=np.uint8).copy()
             sel_dev = torch.from_numpy(raw).to(device)
             self.keep.append(sel_dev)

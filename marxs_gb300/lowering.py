@@ -203,13 +203,24 @@ def _grating_facets(gratings, selectors, sel_index):
     return out
 
 
-def grid_params(facets, slope_max=0.1, margin=0.05, cells_per_facet=2.0):
+def grid_params(facets, slope_max=0.1, margin=0.05, cells_per_facet=16.0, max_cells=1 << 20):
     """Mean plane, extents and cell size of the candidate grid for a facet table.
 
     The host computes each facet's grown footprint the same way the device
     builder does; the extents cover all of them (with a 1 mm pad) and the
-    capacity bounds the total number of (cell, facet) entries.
+    capacity bounds the total number of (cell, facet) entries.  Cells are
+    1/cells_per_facet of a facet edge (16: ~1.2 candidates per cell on a
+    tiled array, against ~3.6 with 2), coarsened if the grid would exceed
+    ``max_cells``.
     """
+    g = _grid_params(facets, slope_max, margin, cells_per_facet)
+    while g['nu'] * g['nv'] > max_cells and cells_per_facet > 1.0:
+        cells_per_facet = max(1.0, cells_per_facet * 0.9 * (max_cells / (g['nu'] * g['nv'])) ** 0.5)
+        g = _grid_params(facets, slope_max, margin, cells_per_facet)
+    return g
+
+
+def _grid_params(facets, slope_max, margin, cells_per_facet):
     F = len(facets)
     c = facets['c']
     nrm = facets['ex'].mean(axis=0)
@@ -484,6 +495,21 @@ def selector_thresholds(sel):
     """ceil(cdf * 2^53) per entry: for u = U * 2^-53, cdf > u  <=>  U < threshold."""
     scaled = np.ascontiguousarray(sel.cdf, dtype=np.float64) * 2.0 ** 53   # exact
     return np.ceil(scaled).astype(np.uint64)
+
+
+def selector_guide(sel):
+    """Guide table for the order search of a sorted selector: per row, 64
+    entries, entry b = first order index k with U < threshold[k] for the draw
+    U = b * 2^47 (uint8); None when the rows are not sorted or too long."""
+    if not selector_sorted(sel) or sel.cdf.shape[1] > 255:
+        return None
+    th = selector_thresholds(sel).reshape(sel.cdf.shape)
+    starts = np.arange(64, dtype=np.uint64) << np.uint64(47)
+    guide = np.empty((th.shape[0], 64), dtype=np.uint8)
+    for r in range(th.shape[0]):
+        # number of thresholds <= U = first index with U < threshold
+        guide[r] = np.searchsorted(th[r], starts, side='right')
+    return guide
 
 
 def selector_sorted(sel):

@@ -108,3 +108,24 @@ def test_facet_dtype_is_packed_like_c():
     assert _abi.FACET_DTYPE.itemsize % 8 == 0
     a = np.zeros(3, _abi.FACET_DTYPE)
     assert a.nbytes == 3 * _abi.FACET_DTYPE.itemsize
+
+
+def test_order_guide_table_gives_the_linear_search_result():
+    """The guide table (host side of the FP32-local order search) plus forward
+    steps reproduces the first index with U < threshold for every row."""
+    from marxs_gb300 import configs, lowering
+    inst = configs.build('c2')
+    sel = lowering.lower_selector(inst.selector)
+    th = lowering.selector_thresholds(sel).reshape(sel.cdf.shape)
+    guide = lowering.selector_guide(sel)
+    assert guide is not None and guide.shape == (th.shape[0], 64)
+    rng = np.random.default_rng(0)
+    U = np.concatenate([rng.integers(0, 2 ** 53, 20000, dtype=np.uint64),
+                        th.ravel(), th.ravel() - np.uint64(1), np.arange(64, dtype=np.uint64) << np.uint64(47)])
+    for r in range(0, th.shape[0], 7):
+        ref = np.array([np.argmax(np.append(u < th[r], True)) for u in U[:3000]])
+        k = guide[r][(U[:3000] >> np.uint64(47)).astype(int)].astype(int)
+        for j in range(len(k)):
+            while k[j] < th.shape[1] and not (U[j] < th[r][k[j]]):
+                k[j] += 1
+        assert np.array_equal(k, ref)

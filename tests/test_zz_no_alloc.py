@@ -22,11 +22,15 @@ pytestmark = pytest.mark.gpu
 
 
 def _grating_stage(name):
+    """Facets of the workload and a candidate grid inside the allocation-free
+    entry point's cell limit (2 cells per facet edge)."""
     from marxs_gb300 import configs, _abi
-    from marxs_gb300.lowering import lower_elements
+    from marxs_gb300.lowering import grid_params, lower_elements
     inst = configs.build(name)
     st = [s for s in lower_elements(inst.elements) if s.kind == _abi.STAGE_GRATINGS][0]
-    return st.facets, st.grid
+    g = grid_params(st.facets, cells_per_facet=2.0)
+    assert g['nu'] * g['nv'] <= _abi.NOALLOC_MAX_CELLS
+    return st.facets, g
 
 
 def _build(facets, g, noalloc):
