@@ -34,7 +34,7 @@ WORKLOAD = 'cat_rowland_1000facets_circular_detector'
 # captures of a 4e6-photon launch (profiles/chain_fp64_c2.md,
 # profiles/chain_fp32local_c2.md), scaled to the launch by photon count
 NCU_TRAFFIC_BYTES_PER_PHOTON = {'fp64': (353.9e6 + 727.0e6) / 4e6,
-                                'fp32local': (353.1e6 + 727.6e6) / 4e6}
+                                'fp32local': (355.9e6 + 732.1e6) / 4e6}
 
 
 def parse():
