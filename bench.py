@@ -208,6 +208,46 @@ def precision_error(a, b, torch):
     return out
 
 
+def source_pipeline_bench(args, torch, inst, n, head, row_base, dist):
+    """Photons made on the GPU (point source, RandomArbitraryPdf spectrum on
+    the workload's 200 energy knots, unpolarized, through a CircleAperture
+    annulus r in [300, 500] mm), traced, and the detector event columns
+    (det_phi, det_y, order, facet) copied to pinned host memory: no photon
+    list crosses the host link."""
+    import numpy as np
+    from marxs_gb300 import configs
+    from marxs_gb300.gpu import DevicePhotons, GpuSequence
+    from marxs_gb300.source import CircleAperture, DeviceSource
+    from marxs_gb300.sharding import max_over_ranks
+    knots, dens = configs.spectrum_knots(2)
+    ap = CircleAperture(position=[12000., 0, 0], zoom=[1, 500, 500], r_inner=300.)
+    src = DeviceSource(ap, energy={'energy': knots, 'fluxdensity': dens})
+    seq = GpuSequence(elements=inst.elements, precision=head, rng='philox', seed=12345)
+    ph = DevicePhotons(n)
+    out = DevicePhotons(n)
+    plan, bufs = seq.allocate_columns(n)
+    cols = ['det_phi', 'det_y', 'order', 'facet']
+    host = {k: torch.empty(n, dtype=bufs[k].dtype, pin_memory=True) for k in cols}
+    d2h = sum(host[k].numel() * host[k].element_size() for k in cols)
+    times = []
+    for step in range(1 + args.e2e_steps):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        src.generate(n, seed=7 + step, row_base=row_base, out=ph)
+        seq.trace_device(ph, out, plan, bufs, row_base=row_base)
+        for k in cols:
+            host[k].copy_(bufs[k], non_blocking=True)
+        torch.cuda.synchronize()
+        if step > 0:
+            times.append(time.perf_counter() - t)
+    s = max_over_ranks([sum(times) / len(times)], dist, device='cuda')[0]
+    world = dist.get_world_size() if dist is not None else 1
+    return {'value': world * n / s, 'unit': UNIT, 'ms_per_step': s * 1e3,
+            'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': d2h,
+            'api': 'DeviceSource(CircleAperture, spectrum).generate -> '
+                   'GpuSequence.trace_device -> detector columns to pinned host memory'}
+
+
 def adjoint_bench(args, torch):
     """Pose gradients on the 200-facet spectrometer: hand-written adjoint vs
     central finite differences (h = 1e-4 mm / 1e-6 rad) over all 1,207
@@ -532,6 +572,8 @@ def main():
         line['e2e'] = {'value': world * e2e_n / e2e_s, 'unit': UNIT, 'h2d_bytes_per_step': h2d,
                        'd2h_bytes_per_step': d2h, 'ms_per_step': e2e_s * 1e3,
                        'api': 'GpuSequence(elements)(PhotonTable) with pinned host columns'}
+    if not args.no_e2e:
+        line['source_pipeline'] = source_pipeline_bench(args, torch, inst, n, head, row_base, dist)
     if rank == 0 and world == 1 and not args.no_adjoint:
         for k in ('seq', 'plan', 'bufs', 'out'):
             for rr in results.values():

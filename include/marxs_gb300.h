@@ -306,6 +306,47 @@ int mgpu_parallel_transport(int64_t n, mgpu_vec dir_old, mgpu_vec dir_new, mgpu_
 /* number of SMs of the current device (for launch sizing by callers) */
 int mgpu_device_sm_count(void);
 
+/* ---- photon generation on the device ----
+ *
+ * A point source seen through a CircleAperture, written straight into
+ * device photon columns (replaces, for this source/aperture pair,
+ * Source.generate_photons -> FixedPointing -> CircleAperture):
+ *   energy   constant, or RandomArbitraryPdf (math/random.py:4-95):
+ *            choice = cdf[last] * u0, i = first index with cdf[i] >= choice,
+ *            j = index[i], E = x[j - 1] + width[j] * u1 (x[-1] = last edge)
+ *   angle    constant, or 2 pi * u2 (unpolarized, source/basesources.py:203-204)
+ *   pol      v1 cos(angle) + v2 sin(angle) (polarization_vectors,
+ *            math/polarization.py:12-63, basis of the fixed direction)
+ *   position CircleAperture.generate_local_xy (optics/aperture.py:138-146):
+ *            phi = phi0 + (phi1 - phi0) u3, r = sqrt(ri2 + (1 - ri2) u4),
+ *            pos = centre + r cos(phi) v_y + r sin(phi) v_z
+ *   prob     clip(dir . -e_x, 0, 1) (aperture.py:72-76)
+ * Uniforms: Philox keyed by (seed, row_base + row, 0x5000 + k) or pre-drawn
+ * (draws[k * n + row], k = 0..4). */
+typedef struct {
+    int64_t n;
+    uint64_t seed, row_base;
+    int32_t rng;             /* MGPU_RNG_* */
+    int32_t n_bins;          /* energy pdf bins (0: constant energy) */
+    double energy;           /* keV, when n_bins == 0 */
+    const double* e_x;       /* n_bins upper bin edges */
+    const double* e_width;   /* n_bins bin widths (e_width[0] = 0) */
+    const double* e_cdf;     /* n_bins cumulative sum of the (sorted) pdf * width */
+    const int32_t* e_index;  /* n_bins sort index (identity when unsorted) */
+    int32_t pol_random;      /* 1: angle = 2 pi u2; 0: pol_angle */
+    int32_t pad;
+    double pol_angle;
+    double dir[3];           /* unit direction of travel */
+    double pol_v1[3], pol_v2[3];
+    double center[3], v_y[3], v_z[3];
+    double phi0, phi1, r_inner2;
+    double prob;             /* probability of every photon */
+    const double* draws;     /* RNG_PREDRAWN: 5 x n uniforms */
+} mgpu_source;
+
+int mgpu_generate_photons(const mgpu_source* src, mgpu_vec pos, mgpu_vec dir, mgpu_vec pol,
+                          mgpu_col energy, mgpu_col prob, void* stream);
+
 /* ---- pose adjoint: detector moments of frozen photons and their gradient ----
  *
  * No single reference interface: it differentiates the forward of

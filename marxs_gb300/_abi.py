@@ -141,6 +141,17 @@ FACET32_DTYPE = np.dtype([('c_hi', '<f4', 3), ('c_lo', '<f4', 3), ('ex', '<f4', 
                           ('pad', '<i4')], align=True)
 
 # name -> (restype, argtypes) of every exported entry point
+class MgpuSource(C.Structure):
+    _fields_ = [('n', C.c_int64), ('seed', C.c_uint64), ('row_base', C.c_uint64),
+                ('rng', C.c_int32), ('n_bins', C.c_int32), ('energy', C.c_double),
+                ('e_x', C.c_void_p), ('e_width', C.c_void_p), ('e_cdf', C.c_void_p),
+                ('e_index', C.c_void_p), ('pol_random', C.c_int32), ('pad', C.c_int32),
+                ('pol_angle', C.c_double), ('dir', C.c_double * 3), ('pol_v1', C.c_double * 3),
+                ('pol_v2', C.c_double * 3), ('center', C.c_double * 3), ('v_y', C.c_double * 3),
+                ('v_z', C.c_double * 3), ('phi0', C.c_double), ('phi1', C.c_double),
+                ('r_inner2', C.c_double), ('prob', C.c_double), ('draws', C.c_void_p)]
+
+
 class MgpuAdjointProblem(C.Structure):
     _fields_ = [('n', C.c_int64), ('n_facets', C.c_int32), ('n_groups', C.c_int32),
                 ('det_kind', C.c_int32), ('reserved', C.c_int32),
@@ -168,6 +179,8 @@ SIGNATURES = {
                                           MgpuVec, MgpuCol, MgpuCol, C.c_void_p]),
     'mgpu_parallel_transport': (C.c_int, [C.c_int64, MgpuVec, MgpuVec, MgpuVec, MgpuVec,
                                           C.c_void_p]),
+    'mgpu_generate_photons': (C.c_int, [C.POINTER(MgpuSource), MgpuVec, MgpuVec, MgpuVec, MgpuCol,
+                                        MgpuCol, C.c_void_p]),
     'mgpu_pose_adjoint': (C.c_int, [C.POINTER(MgpuAdjointProblem), C.c_void_p, C.c_int32,
                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
 }

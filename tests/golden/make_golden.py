@@ -209,7 +209,76 @@ def generate(name):
     return res
 
 
+def check_uniform_restatement():
+    """numpy's legacy uniform(low, high) is low + (high - low) * random_sample."""
+    np.random.seed(6)
+    a = np.random.uniform(0.3, 2.7, 1000)
+    np.random.seed(6)
+    b = 0.3 + (2.7 - 0.3) * np.random.random_sample(1000)
+    assert np.array_equal(a, b)
+
+
+def generate_source():
+    """Point-source photons through a CircleAperture, from the reference's
+    own RandomArbitraryPdf, polarization_vectors and CircleAperture; the
+    unpolarized angle draw is the reference's np.random.uniform(0, 2 pi, n)
+    (basesources.py:203-204).  Every uniform is recorded."""
+    reference_loader.load()
+    from astropy.table import Table
+    from marxs.math.random import RandomArbitraryPdf
+    from marxs.math.polarization import polarization_vectors
+    from marxs.optics.aperture import CircleAperture
+    n = 4000
+    rng = np.random.default_rng(31)
+    x = np.linspace(0.2, 2.0, 60)
+    flux = rng.random(60) + 0.05
+    flux[7] = 0.0
+    pdf_in = np.hstack(([0], flux[1:]))       # Source.generate_energies, basesources.py:190-196
+    log = []
+    orig = {'uniform': np.random.uniform, 'rand': np.random.rand}
+
+    def uniform(low=0.0, high=1.0, size=None):
+        u = np.random.random_sample(size)
+        log.append(np.array(u, copy=True))
+        return low + (high - low) * u
+
+    def rand(*args):
+        u = np.random.random_sample(args if args else None)
+        log.append(np.array(u, copy=True))
+        return u
+
+    np.random.seed(GLOBAL_SEED + 7)
+    np.random.uniform, np.random.rand = uniform, rand
+    try:
+        sampler = RandomArbitraryPdf(x, pdf_in)
+        energies = sampler(n)
+        angles = np.random.uniform(0, 2 * np.pi, n)
+        dirs = np.tile([-1., 0., 0., 0.], (n, 1))
+        pol = polarization_vectors(dirs, angles)
+        photons = Table({'dir': dirs, 'energy': energies, 'polarization': pol,
+                         'probability': np.ones(n)})
+        ap = CircleAperture(position=[12000., 0, 0], zoom=[1, 500, 500], r_inner=300.,
+                            phi=[0.1, 5.9])
+        photons = ap(photons)
+    finally:
+        np.random.uniform, np.random.rand = orig['uniform'], orig['rand']
+    assert len(log) == 5 and all(len(v) == n for v in log)
+    res = {'n': n, 'x': x, 'pdf_in': pdf_in, 'ap_pos4d': np.asarray(ap.geometry.pos4d),
+           'r_inner': 300., 'phi': np.array([0.1, 5.9]), 'draws': np.stack(log),
+           'cdf': sampler.cdf, 'sortindex': sampler.sortindex, 'bin_width': sampler.bin_width}
+    for k in ('pos', 'dir', 'energy', 'polarization', 'probability'):
+        res['out_' + k] = np.asarray(photons[k])
+    np.savez_compressed(os.path.join(HERE, 'source.npz'), **res)
+    print('source n=%d' % n)
+    return res
+
+
 if __name__ == '__main__':
     check_choice_restatement()
-    for name in sys.argv[1:] or ['c0', 'c1', 'c2']:
-        generate(name)
+    check_uniform_restatement()
+    names = sys.argv[1:] or ['c0', 'c1', 'c2', 'c5', 'source']
+    for name in names:
+        if name == 'source':
+            generate_source()
+        else:
+            generate(name)

@@ -19,6 +19,7 @@ STRUCTS = {
     'mgpu_stage': _abi.MgpuStage, 'mgpu_chain': _abi.MgpuChain,
     'mgpu_flat32': _abi.MgpuFlat32, 'mgpu_grid32': _abi.MgpuGrid32, 'mgpu_cyl32': _abi.MgpuCyl32,
     'mgpu_adjoint_problem': _abi.MgpuAdjointProblem, 'mgpu_spline1': _abi.MgpuSpline1,
+    'mgpu_source': _abi.MgpuSource,
 }
 
 

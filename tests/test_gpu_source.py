@@ -1,0 +1,109 @@
+"""Photon generation on the GPU (point source through a CircleAperture).
+
+* pre-drawn mode against the golden vectors recorded from the reference's own
+  RandomArbitraryPdf, polarization_vectors and CircleAperture: energy and
+  probability bit-exact (same float64 operations), position and polarization
+  to 1e-12 (library sin/cos/sqrt differ in the last bit);
+* Philox mode follows the reference distributions (KS p > 1e-3 against the
+  restatement fed numpy uniforms): energies, aperture radius and angle,
+  polarization angle;
+* generated photons trace through the CAT array like host-made ones, and
+  the Philox streams are keyed by global photon id.
+"""
+import numpy as np
+import pytest
+import torch
+from scipy import stats
+
+from conftest import load_golden
+
+pytestmark = pytest.mark.gpu
+
+
+def _source(g, **kw):
+    from marxs_gb300.source import CircleAperture, DeviceSource, RandomArbitraryPdf
+    ap = CircleAperture(pos4d=g['ap_pos4d'], r_inner=float(g['r_inner']), phi=list(g['phi']))
+    return DeviceSource(ap, energy=RandomArbitraryPdf(g['x'], g['pdf_in']), **kw)
+
+
+def _host(out):
+    return {'pos': out.pos.T.cpu().numpy(), 'dir': out.dir.T.cpu().numpy(),
+            'polarization': out.pol.T.cpu().numpy(), 'energy': out.energy.cpu().numpy(),
+            'probability': out.prob.cpu().numpy()}
+
+
+def test_predrawn_generation_matches_reference():
+    g = load_golden('source')
+    n = int(g['n'])
+    out = _host(_source(g).generate(n, draws=torch.from_numpy(g['draws']).cuda()))
+    assert np.array_equal(out['energy'], g['out_energy'])
+    assert np.array_equal(out['probability'], g['out_probability'])
+    assert np.array_equal(out['dir'], g['out_dir'][:, :3])
+    for k in ('pos', 'polarization'):
+        ref = g['out_' + k][:, :3]
+        assert np.max(np.abs(out[k] - ref) / np.maximum(np.abs(ref), 1.0)) < 1e-12, k
+
+
+def test_philox_generation_follows_reference_distributions():
+    from oracle import source as S
+    g = load_golden('source')
+    n = 200_000
+    src = _source(g)
+    out = _host(src.generate(n, seed=11))
+    ref = S.generate(src.center, src.v_y, src.v_z, src.e_x, src.phi, src.r_inner_norm,
+                     src.direction, (g['x'], g['bin_width'], g['cdf'], g['sortindex'], True),
+                     None, np.random.default_rng(5).random((5, n)))
+    assert stats.ks_2samp(out['energy'], ref['energy']).pvalue > 1e-3
+    rel = out['pos'] - src.center
+    R = np.linalg.norm(src.v_y)
+    r = np.hypot(rel @ (src.v_y / R), rel @ (src.v_z / R)) / R
+    phi = np.arctan2(rel @ (src.v_z / R), rel @ (src.v_y / R)) % (2 * np.pi)
+    ri2 = src.r_inner_norm ** 2
+    assert stats.kstest((r ** 2 - ri2) / (1 - ri2), 'uniform').pvalue > 1e-3
+    assert stats.kstest((phi - src.phi[0]) / (src.phi[1] - src.phi[0]), 'uniform').pvalue > 1e-3
+    ang = np.arctan2(out['polarization'] @ src.v2, out['polarization'] @ src.v1) % (2 * np.pi)
+    assert stats.kstest(ang / (2 * np.pi), 'uniform').pvalue > 1e-3
+    assert np.max(np.abs(np.linalg.norm(out['polarization'], axis=1) - 1)) < 1e-12
+
+
+def test_streams_are_keyed_by_global_photon_id():
+    g = load_golden('source')
+    src = _source(g)
+    whole = src.generate(10_000, seed=3)
+    half = src.generate(5_000, seed=3, row_base=5_000)
+    for a, b in ((whole.pos[:, 5000:], half.pos), (whole.energy[5000:], half.energy),
+                 (whole.pol[:, 5000:], half.pol)):
+        assert torch.equal(a, b)
+
+
+def test_generated_photons_trace_like_host_photons():
+    """Device photons go through the CAT array; the same photons copied to the
+    host and traced through the table API give the same columns."""
+    from marxs_gb300 import configs, PhotonTable
+    from marxs_gb300.gpu import GpuSequence
+    from marxs_gb300.source import CircleAperture, DeviceSource
+    inst = configs.build('c2')
+    ap = CircleAperture(position=[12000., 0, 0], zoom=[1, 500, 500], r_inner=300.)
+    src = DeviceSource(ap, energy={'energy': np.linspace(0.3, 2.0, 40),
+                                   'fluxdensity': np.ones(40)})
+    n = 100_000
+    dev = src.generate(n, seed=9)
+    seq = GpuSequence(inst.elements, precision='fp32local', rng='philox', seed=4)
+    plan, bufs = seq.allocate_columns(n)
+    from marxs_gb300.gpu import DevicePhotons
+    out = DevicePhotons(n)
+    status, hits = seq.trace_device(dev, out, plan, bufs)
+    torch.cuda.synchronize()
+    assert int(status.item()) == 0
+    assert (bufs['facet'] >= 0).float().mean().item() > 0.3
+    host = _host(dev)
+    table = PhotonTable({'pos': np.c_[host['pos'], np.ones(n)], 'dir': np.c_[host['dir'], np.zeros(n)],
+                         'polarization': np.c_[host['polarization'], np.zeros(n)],
+                         'energy': host['energy'], 'probability': host['probability']})
+    ref = seq(table)
+    assert torch.equal(torch.from_numpy(np.asarray(ref['facet'])).cuda().to(bufs['facet'].dtype),
+                       bufs['facet'])
+    d = np.asarray(ref['det_phi'])
+    a = bufs['det_phi'].cpu().numpy()
+    assert np.array_equal(np.isnan(a), np.isnan(d))
+    assert np.array_equal(a[~np.isnan(a)], d[~np.isnan(d)])
