@@ -40,6 +40,7 @@ def native_namespace():
         FlatGrating=optics.FlatGrating, CATGrating=optics.CATGrating,
         OrderSelector=optics.OrderSelector, EfficiencyFile=optics.EfficiencyFile,
         InterpolateEfficiencyTable=optics.InterpolateEfficiencyTable.from_grid,
+        CATL1L2Stack=optics.CATL1L2Stack,
         Cylinder=optics.Cylinder, Parallel=simulator.Parallel, Sequence=simulator.Sequence,
         angle=lambda rad: rad)
 
@@ -105,8 +106,10 @@ def piecewise_linear_energies(n, seed, lo=0.2, hi=2.0, n_knots=200):
 def draws_for(elements_with_draws, n, seed):
     """Per-photon pre-drawn randomness keyed by element object.
 
-    ``elements_with_draws`` lists (element, kind) with kind 'scatter' or
-    'order'.  Scatter angles are sigma * N(0, 1); order draws are U[0, 1).
+    ``elements_with_draws`` lists (element, kind) with kind 'scatter',
+    'order' or 'catstack'.  Scatter angles are sigma * N(0, 1); order draws
+    are U[0, 1); a CAT stack adds the L1 order and support uniforms, the L2
+    scatter's N(0, 1) and the uniform of its turn about the ray.
     """
     rng = np.random.default_rng(seed + 77)
     out = {}
@@ -114,6 +117,10 @@ def draws_for(elements_with_draws, n, seed):
         if kind == 'scatter':
             out[elem] = {'inplanescatter': elem.inplanescatter * rng.standard_normal(n),
                          'perpplanescatter': elem.perpplanescatter * rng.standard_normal(n)}
+        elif kind == 'catstack':
+            out[elem] = {'order_u': rng.uniform(0, 1, n), 'l1_order_u': rng.uniform(0, 1, n),
+                         'l1_support_u': rng.uniform(0, 1, n),
+                         'l2_normal': rng.standard_normal(n), 'l2_phi_u': rng.uniform(0, 1, n)}
         else:
             out[elem] = {'order_u': rng.uniform(0, 1, n)}
     return out
@@ -244,9 +251,19 @@ def lens_reflectivity(seed):
     return RectBivariateSpline(e, a, np.clip(R, 0.0, 1.0), kx=1, ky=1)
 
 
-def build_c2(ns, seed=2, efficiency_file=None, n_facets=1000, interpolated=False):
+def l1_transmission_table():
+    """Synthetic transmission of a CAT facet's L1 support (energy keV,
+    fraction): smooth, rising from 0.04 at 0.05 keV to 0.96 at 5 keV."""
+    e = np.linspace(0.05, 5.0, 400)
+    return e, 0.96 * np.exp(-(0.12 / e) ** 1.5)
+
+
+def build_c2(ns, seed=2, efficiency_file=None, n_facets=1000, interpolated=False,
+             cat_stack=False):
     """The CAT array; ``interpolated`` gives the lens a reflectivity
-    interpolator and the facets an InterpolateEfficiencyTable selector."""
+    interpolator and the facets an InterpolateEfficiencyTable selector;
+    ``cat_stack`` makes every facet a CATL1L2Stack (grating, quality factor,
+    L1 and L2 supports)."""
     lens_kw = {'reflectivity_interpolator': lens_reflectivity(seed)} if interpolated else {}
     lens = ns.PerfectLens(focallength=12000., position=[12000., 0, 0], zoom=[1, 600, 600],
                           **lens_kw)
@@ -263,10 +280,17 @@ def build_c2(ns, seed=2, efficiency_file=None, n_facets=1000, interpolated=False
     poses, uncert, torus = c2_facet_poses(seed)
     poses, uncert = poses[:n_facets], uncert[:n_facets]
     blaze = geomath.axangle2mat(np.array([0, 0, 1.]), np.deg2rad(1.8))
-    gas = ns.Parallel(elem_class=ns.CATGrating,
-                      elem_args={'d': 2e-4, 'zoom': [1, 12.5, 12.5], 'orientation': blaze,
-                                 'order_selector': eff},
-                      elem_pos=poses, id_col='facet')
+    if cat_stack:
+        gas = ns.Parallel(elem_class=ns.CATL1L2Stack,
+                          elem_args={'d': 2e-4, 'zoom': [1, 12.5, 12.5], 'orientation': blaze,
+                                     'order_selector': eff,
+                                     'l1_transmission': l1_transmission_table()},
+                          elem_pos=poses, id_col='facet')
+    else:
+        gas = ns.Parallel(elem_class=ns.CATGrating,
+                          elem_args={'d': 2e-4, 'zoom': [1, 12.5, 12.5], 'orientation': blaze,
+                                     'order_selector': eff},
+                          elem_pos=poses, id_col='facet')
     gas.elem_uncertainty = uncert
     gas.generate_elements()
     cyl = ns.Cylinder.from_rowland(torus, 50., rotation=np.pi,
@@ -274,11 +298,12 @@ def build_c2(ns, seed=2, efficiency_file=None, n_facets=1000, interpolated=False
     det = ns.CircularDetector(geometry=cyl, pixsize=0.024)
     return SimpleNamespace(elements=[lens, rms, gas, det], lens=lens, scatter=rms, gas=gas,
                            detector=det, selector=eff, efficiency_table=table,
-                           draw_slots=[(rms, 'scatter'), (gas, 'order')], aperture_x=12000.)
+                           draw_slots=[(rms, 'scatter'), (gas, 'catstack' if cat_stack else 'order')],
+                           aperture_x=12000.)
 
 
 def photons_for(config_name, n, seed):
-    if config_name in ('c2', 'c5'):
+    if config_name in ('c2', 'c5', 'c6'):
         e = piecewise_linear_energies(n, seed)
         return annulus_photons(n, seed, 12000., energies=e)
     return annulus_photons(n, seed, 10000.)
@@ -294,4 +319,6 @@ def build(config_name, ns=None, seed=None):
         return build_c2(ns, seed=2 if seed is None else seed)
     if config_name == 'c5':
         return build_c2(ns, seed=5 if seed is None else seed, interpolated=True)
+    if config_name == 'c6':
+        return build_c2(ns, seed=6 if seed is None else seed, interpolated=True, cat_stack=True)
     raise ValueError(config_name)

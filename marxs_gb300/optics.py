@@ -291,6 +291,112 @@ class CATGrating(FlatGrating):
     order_sign_kind = 'cat'    # sign = sign(p . d), 0 -> +1 (grating.py:291-301)
 
 
+class NonParallelCATGrating(CATGrating):
+    """CAT grating whose bar walls tilt linearly across the facet: blaze +=
+    blaze_center + local y * d_blaze_mm (missions/mitsnl/catgrating.py:305-333)."""
+
+    def __init__(self, **kwargs):
+        self.d_blaze_mm = kwargs.pop('d_blaze_mm', 0)
+        self.blaze_center = kwargs.pop('blaze_center', 0)
+        super().__init__(**kwargs)
+
+
+class QualityFactor(FlatOpticalElement):
+    """probability *= exp(-(2 pi sigma / d)^2) ** (order^2) (catgrating.py:147-162);
+    ``qualityfactor`` = {'d': ..., 'sigma': ...} in one length unit."""
+
+    def __init__(self, qualityfactor=None, **kwargs):
+        q = qualityfactor or {'d': 200., 'sigma': 1.75}
+        self.factor = np.exp(- (2 * np.pi * q['sigma'] / q['d']) ** 2)
+        super().__init__(**kwargs)
+
+
+class L1(CATGrating):
+    """L1 support of a CAT grating (catgrating.py:171-207): a CAT grating of
+    period l1_dims['period'] (mm); a fraction 1 - openfraction of the photons
+    hits the support bars instead, keeps its direction, gets order 0 and the
+    transmission ``transmission`` = (energy keV, fraction) interpolated
+    linearly (scipy interp1d, as the reference builds from its Si table)."""
+    blaze_name = 'blaze_L1'
+    order_name = 'order_L1'
+
+    def __init__(self, l1_dims=None, transmission=None, **kwargs):
+        from scipy.interpolate import interp1d
+        dims = l1_dims or {'bardepth': 0.004, 'period': 0.005, 'barwidth': 0.0009}
+        if not dims['barwidth'] < dims['period']:
+            raise ValueError('Period of grating must be larger than bar width.')
+        if transmission is None:
+            raise ValueError('L1 needs the support transmission table (energy keV, fraction)')
+        self.openfraction = 1 - dims['barwidth'] / dims['period']
+        self.transfunc = interp1d(np.asarray(transmission[0], dtype=float),
+                                  np.asarray(transmission[1], dtype=float))
+        kwargs['d'] = dims['period']
+        super().__init__(**kwargs)
+
+
+class L2Abs(FlatOpticalElement):
+    """L2 absorption and shadowing (catgrating.py:210-245): probability *=
+    (inner/period)^2 - bardepth inner sin(angle) / (period^2 / 2 sqrt 3)."""
+
+    def __init__(self, l2_dims=None, **kwargs):
+        dims = l2_dims or {'bardepth': 0.5, 'period': 0.9622504, 'barwidth': 0.0962250}
+        if not dims['barwidth'] < dims['period']:
+            raise ValueError('Period of grating must be larger than bar width.')
+        self.bardepth = dims['bardepth']
+        self.period = dims['period']
+        self.barwidth = dims['barwidth']
+        super().__init__(**kwargs)
+        self.innerfree = self.period - self.barwidth
+
+
+class L2Diffraction(FlatOpticalElement):
+    """Gaussian scatter by the L2 hexagons (catgrating.py:248-268): sigma =
+    1.22 * 0.4 * arcsin(lambda / inner), a random direction around the ray
+    (RandomGaussianScatter, optics/scatter.py:80-150)."""
+    scattername = 'L2Diffraction'
+
+    def __init__(self, l2_dims=None, **kwargs):
+        dims = l2_dims or {'bardepth': 0.5, 'period': 0.9622504, 'barwidth': 0.0962250}
+        self.innerfree = dims['period'] - dims['barwidth']
+        super().__init__(**kwargs)
+
+
+class FlatStack(FlatOpticalElement):
+    """Several layers acting at one flat element (optics/base.py:218-281):
+    ``elements`` classes, ``keywords`` their keyword dicts; every layer gets
+    the stack's pose."""
+
+    def __init__(self, **kwargs):
+        elements = kwargs.pop('elements')
+        keywords = kwargs.pop('keywords')
+        super().__init__(**kwargs)
+        self.elements = [elem(pos4d=self.pos4d, **k) for elem, k in zip(elements, keywords)]
+
+
+class CATL1L2Stack(FlatStack):
+    """CAT facet with its L1 and L2 supports (catgrating.py:336-377): layers
+    NonParallelCATGrating, QualityFactor, L1 (grooves at pi/2 + groove_angle),
+    L2Abs, L2Diffraction.  ``l1_transmission`` = (energy keV, fraction)."""
+
+    def __init__(self, l1_dims=None, l2_dims=None, l1_order_selector=None, qualityfactor=None,
+                 l1_transmission=None, **kwargs):
+        if l1_order_selector is None:
+            l1_order_selector = OrderSelector(
+                np.array([-4, -3, -2, -1, 0, 1, 2, 3, 4]),
+                p=np.array([0.006, 0.0135, 0.022, 0.028, 0.861, 0.028, 0.022, 0.0135, 0.006]))
+        groove_angle = kwargs.pop('groove_angle', 0.)
+        kwargs['elements'] = [NonParallelCATGrating, QualityFactor, L1, L2Abs, L2Diffraction]
+        kwargs['keywords'] = [{'order_selector': kwargs.pop('order_selector'),
+                               'd': kwargs.pop('d', 0.0002), 'groove_angle': groove_angle},
+                              {'qualityfactor': qualityfactor},
+                              {'l1_dims': l1_dims, 'order_selector': l1_order_selector,
+                               'groove_angle': np.pi / 2. + groove_angle,
+                               'transmission': l1_transmission},
+                              {'l2_dims': l2_dims},
+                              {'l2_dims': l2_dims}]
+        super().__init__(**kwargs)
+
+
 class BaseContainer(SimulationSequenceElement):
     elements = []
 
@@ -306,4 +412,5 @@ class BaseContainer(SimulationSequenceElement):
 
 __all__ = ['GeometryError', 'FinitePlane', 'Cylinder', 'OrderSelector', 'EfficiencyFile',
            'PerfectLens', 'RadialMirrorScatter', 'FlatDetector', 'CircularDetector',
-           'FlatGrating', 'CATGrating']
+           'FlatGrating', 'CATGrating', 'NonParallelCATGrating', 'QualityFactor', 'L1', 'L2Abs',
+           'L2Diffraction', 'FlatStack', 'CATL1L2Stack', 'InterpolateEfficiencyTable']

@@ -333,7 +333,11 @@ def flat_grating_process(g, photons, intersect, intercoos, u):
     wave = ENERGY2WAVE / photons['energy'][intersect]
     p_perp_to_grooves = norm_vector(p - np.einsum('ij,ij->i', p, l)[:, None] * l)
     blazeangle = np.arccos(np.clip(np.abs(np.einsum('ij,ij->i', p_perp_to_grooves, n)), 0, 1))
-    blazeangle += np.zeros(n_hit)
+    if hasattr(g, 'd_blaze_mm'):
+        # NonParallelCATGrating.blaze_angle_modifier, missions/mitsnl/catgrating.py:324-333
+        blazeangle += g.blaze_center + intercoos[intersect, 0] * g.d_blaze_mm
+    else:
+        blazeangle += np.zeros(n_hit)
     m, prob = order_select(g.order_selector, photons['energy'][intersect], u[intersect],
                            blazeangle)
     if 'CATGrating' in _classnames(g):
@@ -458,6 +462,66 @@ def process_photons(elem, photons, intersect, interpos, intercoos, outcols):
     return photons
 
 
+def gaussian_scatter_process(elem, photons, intersect, normals, phi_u):
+    """RandomGaussianScatter.specific_process_photons (optics/scatter.py:109-150)
+    with L2Diffraction.scatter (missions/mitsnl/catgrating.py:263-268):
+    sigma = 1.22 * 0.4 * arcsin(lambda / inner), angle = N(0, 1) * sigma about
+    dir x guess, then a uniform turn about the direction."""
+    pdir = norm_vector(h2e(photons['dir'][intersect]))
+    guessvec = np.zeros_like(pdir)
+    ind = np.abs(pdir[:, 0]) < 0.99999
+    guessvec[ind, 0] = 1
+    guessvec[~ind, 1] = 1
+    perpvec = np.cross(pdir, guessvec)
+    wave = (HC_KEV_NM / (photons['energy'][intersect] * 1.0)) * (1e-6 / 1.0)   # keV -> mm
+    sigma = 1.22 * 0.4 * np.arcsin(wave / elem.innerfree)
+    angle = normals[intersect] * sigma
+    rot = axangle2mat(perpvec, angle)
+    outdir = np.einsum('...ij,...i->...j', rot, pdir)
+    angle2 = phi_u[intersect] * 2 * np.pi
+    rot = axangle2mat(pdir, angle2)
+    outdir = e2h(np.einsum('...ij,...i->...j', rot, outdir), 0)
+    pol = parallel_transport(photons['dir'][intersect, :], outdir,
+                             photons['polarization'][intersect, :])
+    return {'dir': outdir, 'polarization': pol, elem.scattername: angle}
+
+
+def cat_stack_process(stack, photons, intersect, interpos, intercoos, d):
+    """FlatStack.process_photons (optics/base.py:264-281) of a CATL1L2Stack
+    (missions/mitsnl/catgrating.py:336-377): the stack's own id and local
+    columns, then each layer at the same intersection."""
+    process_photons(stack, photons, intersect, interpos, intercoos, {})
+    grat, qf, l1, l2abs, l2diff = stack.elements
+    # membrane (NonParallelCATGrating)
+    out = flat_grating_process(grat, photons, intersect, intercoos, d['order_u'])
+    process_photons(grat, photons, intersect, interpos, intercoos, out)
+    # QualityFactor, catgrating.py:160-161
+    process_photons(qf, photons, intersect, interpos, intercoos,
+                    {'probability': qf.factor ** (photons['order'][intersect] ** 2)})
+    # L1, catgrating.py:196-207: a CAT grating, or the support bars
+    out = flat_grating_process(l1, photons, intersect, intercoos, d['l1_order_u'])
+    sup = d['l1_support_u'][intersect] > l1.openfraction
+    ind = intersect.nonzero()[0][sup]
+    out['dir'][sup] = photons['dir'][ind, :]
+    out['polarization'][sup] = photons['polarization'][ind, :]
+    out[l1.order_name][sup] = 0
+    out['probability'][sup] = l1.transfunc(photons['energy'][ind])
+    process_photons(l1, photons, intersect, interpos, intercoos, out)
+    # L2Abs, catgrating.py:231-245 (en = e_x of the flat element)
+    p3 = norm_vector(photons['dir'][intersect])
+    en = np.tile(_geom_vec(l2abs.geometry.pos4d, 'e_x'), (len(p3), 1))
+    angle = np.arccos(np.abs(np.einsum('ij,ij->i', p3, en)))
+    openfraction = (l2abs.innerfree / l2abs.period) ** 2
+    shadowarea = (l2abs.bardepth * l2abs.innerfree * np.sin(angle))
+    totalarea = l2abs.period ** 2 / 2 * np.sqrt(3)
+    process_photons(l2abs, photons, intersect, interpos, intercoos,
+                    {'probability': openfraction - shadowarea / totalarea})
+    # L2Diffraction
+    out = gaussian_scatter_process(l2diff, photons, intersect, d['l2_normal'], d['l2_phi_u'])
+    process_photons(l2diff, photons, intersect, interpos, intercoos, out)
+    return photons
+
+
 def run_element(elem, photons, draws, stats):
     """One leaf element: OpticalElement.__call__ (optics/base.py:144-147)."""
     names = _classnames(elem)
@@ -470,6 +534,9 @@ def run_element(elem, photons, draws, stats):
     if intersect.sum() == 0:
         return photons, intersect
     d = draws.get(elem, {})
+    if 'CATL1L2Stack' in names:
+        cat_stack_process(elem, photons, intersect, interpos, intercoos, d)
+        return photons, intersect
     if 'FlatGrating' in names:
         u = d['order_u']
         outcols = flat_grating_process(elem, photons, intersect, intercoos, u)

@@ -5,7 +5,7 @@ Run from the repository root (needs the reference source tree, see
 
     python tests/golden/make_golden.py
 
-For each workload (c0, c1, c2, c5) this builds the instrument from the
+For each workload (c0, c1, c2, c5, c6) this builds the instrument from the
 reference's own classes, traces a small seeded photon list through the
 reference's ``Sequence`` with numpy's global RNG seeded, and records every
 random draw the reference makes.  The draws are mapped back to photons
@@ -32,7 +32,7 @@ sys.path.insert(0, ROOT)
 import reference_loader  # noqa: E402
 from marxs_gb300 import configs  # noqa: E402
 
-N_PHOTONS = {'c0': 2000, 'c1': 3000, 'c2': 3000, 'c5': 3000}
+N_PHOTONS = {'c0': 2000, 'c1': 3000, 'c2': 3000, 'c5': 3000, 'c6': 3000}
 GLOBAL_SEED = 20261203
 
 
@@ -72,7 +72,14 @@ class Recorder:
             rec.current[2].append(('uniform', np.atleast_1d(np.array(v, copy=True))))
             return v
 
-        rnd.normal, rnd.choice, rnd.rand = normal, choice, rand
+        def uniform(low=0.0, high=1.0, size=None):
+            # legacy RandomState.uniform = low + (high - low) * random_sample
+            u = np.random.random_sample(size)
+            rec.current[2].append(('uniform', np.atleast_1d(np.array(u, copy=True))))
+            return low + (high - low) * u
+
+        self._orig['uniform'] = rnd.uniform
+        rnd.normal, rnd.choice, rnd.rand, rnd.uniform = normal, choice, rand, uniform
 
     def uninstall(self):
         for k, v in self._orig.items():
@@ -130,7 +137,21 @@ def reference_namespace(marxs):
             return EfficiencyFile(buf, orders)
         return EfficiencyFile(table, orders)
 
+    def cat_stack_class():
+        # the reference stack, with the L1 support transmission given as a
+        # table (the reference reads it from its Si data file)
+        from scipy.interpolate import interp1d
+        from marxs.missions.mitsnl.catgrating import CATL1L2Stack
+
+        class Stack(CATL1L2Stack):
+            def __init__(self, l1_transmission=None, **kwargs):
+                super().__init__(**kwargs)
+                if l1_transmission is not None:
+                    self.elements[2].transfunc = interp1d(*l1_transmission)
+        return Stack
+
     return SimpleNamespace(PerfectLens=PerfectLens, RadialMirrorScatter=RadialMirrorScatter,
+                           CATL1L2Stack=cat_stack_class(),
                            FlatDetector=FlatDetector, CircularDetector=CircularDetector,
                            FlatGrating=FlatGrating, CATGrating=CATGrating,
                            OrderSelector=OrderSelector, EfficiencyFile=eff,
@@ -154,7 +175,7 @@ def generate(name):
     ns = reference_namespace(marxs)
     inst = configs.build(name, ns)
     n = N_PHOTONS[name]
-    ph = configs.photons_for(name, n, seed={'c0': 0, 'c1': 1, 'c2': 2, 'c5': 5}[name])
+    ph = configs.photons_for(name, n, seed={'c0': 0, 'c1': 1, 'c2': 2, 'c5': 5, 'c6': 6}[name])
     table = Table({k: v.copy() for k, v in ph.items()})
 
     rec = Recorder()
@@ -170,7 +191,9 @@ def generate(name):
 
     # map recorded draws to per-photon arrays
     draw = {'inplanescatter': np.zeros(n), 'perpplanescatter': np.zeros(n),
-            'order_u': np.full(n, np.nan)}
+            'order_u': np.full(n, np.nan), 'l1_order_u': np.full(n, np.nan),
+            'l1_support_u': np.full(n, np.nan), 'l2_normal': np.full(n, np.nan),
+            'l2_phi_u': np.full(n, np.nan)}
     seen = np.zeros(n, dtype=int)
     for elem, mask, logged in rec.calls:
         rows = np.nonzero(mask)[0]
@@ -186,11 +209,21 @@ def generate(name):
             if elem.perpplanescatter != 0:
                 assert kinds[j] == 'normal'
                 draw['perpplanescatter'][rows] = vals[j]
-        elif cname in ('FlatGrating', 'CATGrating'):
+        elif cname in ('FlatGrating', 'CATGrating', 'NonParallelCATGrating'):
             u = np.concatenate([v for k, v in logged if k == 'uniform'])
             assert len(u) == len(rows)
             draw['order_u'][rows] = u
             seen[rows] += 1
+        elif cname == 'L1':
+            # order draw (choice), then the support draw (rand)
+            assert [k for k, _ in logged] == ['uniform', 'uniform']
+            draw['l1_order_u'][rows] = logged[0][1]
+            draw['l1_support_u'][rows] = logged[1][1]
+        elif cname == 'L2Diffraction':
+            # scatter angle (normal), then the direction around the ray (uniform)
+            assert [k for k, _ in logged] == ['normal', 'uniform']
+            draw['l2_normal'][rows] = logged[0][1]
+            draw['l2_phi_u'][rows] = logged[1][1]
         else:
             assert not logged, cname
     multi = seen > 1
@@ -198,7 +231,8 @@ def generate(name):
     for k, v in ph.items():
         res['in_' + k] = v
     for k, v in draw.items():
-        res['draw_' + k] = v
+        if k in ('inplanescatter', 'perpplanescatter', 'order_u') or not np.all(np.isnan(v)):
+            res['draw_' + k] = v
     for k in out.colnames:
         res['out_' + k] = np.asarray(out[k])
     if hasattr(inst, 'gas'):
@@ -276,7 +310,7 @@ def generate_source():
 if __name__ == '__main__':
     check_choice_restatement()
     check_uniform_restatement()
-    names = sys.argv[1:] or ['c0', 'c1', 'c2', 'c5', 'source']
+    names = sys.argv[1:] or ['c0', 'c1', 'c2', 'c5', 'c6', 'source']
     for name in names:
         if name == 'source':
             generate_source()

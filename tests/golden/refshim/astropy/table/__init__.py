@@ -155,9 +155,10 @@ class Table:
         with open(filename) as fh:
             for line in fh:
                 if line.startswith('#'):
-                    m = re.search(r'name:\s*([^,}]+).*?(?:unit:\s*([^,}]+))?[,}]', line)
+                    m = re.search(r'name:\s*([^,}]+)', line)
                     if m and 'datatype' in line:
-                        units[m.group(1).strip()] = (m.group(2) or '').strip() or None
+                        un = re.search(r'unit:\s*([^,}]+)', line)
+                        units[m.group(1).strip()] = un.group(1).strip() if un else None
                     continue
                 if not line.strip():
                     continue

@@ -20,12 +20,15 @@ def _draws(inst, g):
         if kind == 'scatter':
             draws[elem] = {'inplanescatter': g['draw_inplanescatter'],
                            'perpplanescatter': g['draw_perpplanescatter']}
+        elif kind == 'catstack':
+            draws[elem] = {k: g['draw_' + k] for k in ('order_u', 'l1_order_u', 'l1_support_u',
+                                                        'l2_normal', 'l2_phi_u')}
         else:
             draws[elem] = {'order_u': g['draw_order_u']}
     return draws
 
 
-@pytest.mark.parametrize('name', ['c0', 'c1', 'c2', 'c5'])
+@pytest.mark.parametrize('name', ['c0', 'c1', 'c2', 'c5', 'c6'])
 def test_oracle_reproduces_reference_bitwise(name):
     g = load_golden(name)
     inst = configs.build(name)
@@ -39,7 +42,7 @@ def test_oracle_reproduces_reference_bitwise(name):
     assert stats.get('multi_hit', 0) == int(g['multi_hit'].sum())
 
 
-@pytest.mark.parametrize('name', ['c1', 'c2', 'c5'])
+@pytest.mark.parametrize('name', ['c1', 'c2', 'c5', 'c6'])
 def test_native_facet_poses_equal_reference(name):
     """Parallel.generate_elements restated on the host gives the same poses."""
     g = load_golden(name)
