@@ -34,7 +34,8 @@ extern "C" {
 
 #define MGPU_ABI_VERSION 1
 #define MGPU_MAX_STAGES 16
-#define MGPU_MAX_OUT 4
+#define MGPU_MAX_OUT 10
+#define MGPU_MAX_DRAWS 6
 
 /* status bits (device word, OR-ed by kernels) */
 #define MGPU_STATUS_PROB_RANGE   0x1u  /* probability factor outside [0,1]: ValueError, optics/base.py:43-46 */
@@ -43,6 +44,7 @@ extern "C" {
 #define MGPU_STATUS_GRID_RANGE   0x8u  /* a facet's footprint leaves the candidate grid */
 #define MGPU_STATUS_GRID_FULL    0x10u /* candidate list capacity exceeded */
 #define MGPU_STATUS_BAD_W        0x20u /* input pos w != 1 or dir/pol w != 0 (checked on request) */
+#define MGPU_STATUS_TABLE_RANGE  0x80u /* value outside an interpolation table (interp1d raises) */
 
 /* mgpu_chain.flags */
 #define MGPU_FLAG_CHECK_W        0x1u  /* read the homogeneous w of pos/dir/pol and check it */
@@ -200,12 +202,42 @@ typedef struct {
     int32_t pad;
 } mgpu_grid;
 
+/* Layers of a CATL1L2Stack facet after its grating membrane
+ * (missions/mitsnl/catgrating.py:147-377), shared by all facets of a stage:
+ *   membrane blaze += blaze_center + local y * d_blaze_mm (NonParallelCATGrating)
+ *   QualityFactor   probability *= qf ** (order^2)
+ *   L1              a CAT grating (grooves l1_vec, period l1_d, selector
+ *                   l1_selector) or, when the support draw > l1_open, the ray
+ *                   unchanged with order 0 and probability interp(E) of the
+ *                   table (l1_trans_e, l1_trans_t) (np.interp / interp1d)
+ *   L2Abs           probability *= l2_open - l2_shadow * sin(angle) / l2_total
+ *   L2Diffraction   Gaussian turn by N(0,1) * 1.22 * 0.4 * asin(lambda / l2_inner)
+ *                   about dir x guess, then a uniform turn about dir
+ * Stage outputs: out[0..3] grat_y, grat_z, order, blaze; out[4..5] y, z;
+ * out[6..8] order_L1, blaze_L1, L2Diffraction.  Draws: draw[0] order,
+ * draw[1] L1 order, draw[2] L1 support, draw[3] L2 N(0,1), draw[4] L2 turn. */
+typedef struct mgpu_catstack {
+    double blaze_center, d_blaze_mm;
+    double qf;
+    double l1_open;
+    double l1_d;                 /* L1 period, mm */
+    const double* l1_vec;        /* n_facets x 6: L1 groove direction, -perp groove direction */
+    int32_t l1_selector;         /* index into the stage's selectors */
+    int32_t l1_n_trans;
+    const double* l1_trans_e;    /* keV, increasing */
+    const double* l1_trans_t;
+    double l2_open;              /* (inner / period)^2 */
+    double l2_shadow;            /* bardepth * inner */
+    double l2_total;             /* period^2 / 2 * sqrt(3) */
+    double l2_inner;             /* period - barwidth, mm */
+} mgpu_catstack;
+
 typedef struct {
     int32_t kind;
     int32_t id_num;              /* id value for single elements (unused: -9) */
-    int32_t first_writer;        /* bit k: out[k] is new -> write NaN on miss;
-                                    bit 8: id column new -> write -1 on miss;
-                                    bit 9: id column holds int64 (else int32) */
+    int32_t first_writer;        /* bit k (k < MGPU_MAX_OUT): out[k] is new -> write NaN
+                                    on miss; bit 16: id column new -> write -1 on miss;
+                                    bit 17: id column holds int64 (else int32) */
     int32_t n_facets;
     double frame[14];            /* flat: c(3) ex(3) ey(3) ez(3) hy hz */
     double cyl[32];              /* cylinder: pos4d rows 0-2 (12), inverse rows 0-2 (12),
@@ -214,7 +246,7 @@ typedef struct {
     mgpu_col out[MGPU_MAX_OUT];  /* output columns (NULL ptr = not written) */
     void* id_out;                /* id column (int32 or int64, bit 9) or NULL */
     int64_t id_stride;
-    const double* draw[2];       /* pre-drawn per-photon values (RNG_PREDRAWN) */
+    const double* draw[MGPU_MAX_DRAWS]; /* pre-drawn per-photon values (RNG_PREDRAWN) */
     int64_t draw_stride;
     const mgpu_facet* facets;    /* GRATINGS */
     const mgpu_selector* selectors;
@@ -229,6 +261,7 @@ typedef struct {
                                     (c_hi, hy), (e_x, hz), (e_y, e_z.x), (e_z.y, e_z.z, 0, 0) */
     mgpu_spline1 spline;         /* LENS: reflectivity_interpolator(energy, angle / 4), squared
                                     into the probability (optics/mirror.py:73-79); n_surf 0 = 1 */
+    const struct mgpu_catstack* stack; /* GRATINGS: facets are CATL1L2Stacks (NULL: plain) */
 } mgpu_stage;
 /* p[] per kind:
  *   LENS:    p[0] focal length, p[1] d_center_optical_axis

@@ -15,7 +15,8 @@ LIB_PATH = os.path.join(HERE, 'libmarxs_gb300.so')
 
 MGPU_ABI_VERSION = 1
 MAX_STAGES = 16
-MAX_OUT = 4
+MAX_OUT = 10
+MAX_DRAWS = 6
 
 STATUS_PROB_RANGE = 0x1
 STATUS_ORDER_EMPTY = 0x2
@@ -23,6 +24,7 @@ STATUS_BAD_STAGE = 0x4
 STATUS_GRID_RANGE = 0x8
 STATUS_GRID_FULL = 0x10
 STATUS_BAD_W = 0x20
+STATUS_TABLE_RANGE = 0x80
 FLAG_CHECK_W = 0x1
 
 NOALLOC_MAX_CELLS = 65536
@@ -110,15 +112,24 @@ class MgpuGrid(C.Structure):
                 ('capacity', C.c_int32), ('pad', C.c_int32)]
 
 
+class MgpuCatStack(C.Structure):
+    _fields_ = [('blaze_center', C.c_double), ('d_blaze_mm', C.c_double), ('qf', C.c_double),
+                ('l1_open', C.c_double), ('l1_d', C.c_double), ('l1_vec', C.c_void_p),
+                ('l1_selector', C.c_int32), ('l1_n_trans', C.c_int32), ('l1_trans_e', C.c_void_p),
+                ('l1_trans_t', C.c_void_p), ('l2_open', C.c_double), ('l2_shadow', C.c_double),
+                ('l2_total', C.c_double), ('l2_inner', C.c_double)]
+
+
 class MgpuStage(C.Structure):
     _fields_ = [('kind', C.c_int32), ('id_num', C.c_int32), ('first_writer', C.c_int32),
                 ('n_facets', C.c_int32), ('frame', C.c_double * 14), ('cyl', C.c_double * 32),
                 ('p', C.c_double * 8), ('out', MgpuCol * MAX_OUT), ('id_out', C.c_void_p),
-                ('id_stride', C.c_int64), ('draw', C.c_void_p * 2), ('draw_stride', C.c_int64),
+                ('id_stride', C.c_int64), ('draw', C.c_void_p * MAX_DRAWS),
+                ('draw_stride', C.c_int64),
                 ('facets', C.c_void_p), ('selectors', C.c_void_p), ('n_selectors', C.c_int32),
                 ('pad', C.c_int32), ('grid', MgpuGrid), ('aux', C.c_void_p),
                 ('facets32', C.c_void_p), ('table', C.c_void_p), ('cand32', C.c_void_p),
-                ('spline', MgpuSpline1)]
+                ('spline', MgpuSpline1), ('stack', C.c_void_p)]
 
 
 class MgpuChain(C.Structure):

@@ -54,14 +54,14 @@ __device__ __forceinline__ void stored(const mgpu_col& c, int64_t i, double v) {
 }
 
 __device__ __forceinline__ void store_id(const mgpu_stage& st, int64_t i, int64_t v) {
-    if ((st.first_writer >> 9) & 1) ((int64_t*)st.id_out)[i * st.id_stride] = v;
+    if ((st.first_writer >> 17) & 1) ((int64_t*)st.id_out)[i * st.id_stride] = v;
     else ((int32_t*)st.id_out)[i * st.id_stride] = (int32_t)v;
 }
 
 __device__ __forceinline__ void write_miss_defaults(const mgpu_stage& st, int64_t i, int nout) {
     for (int k = 0; k < nout; ++k)
         if ((st.first_writer >> k) & 1) stored(st.out[k], i, kNaN);
-    if (st.id_out && ((st.first_writer >> 8) & 1)) store_id(st, i, -1);
+    if (st.id_out && ((st.first_writer >> 16) & 1)) store_id(st, i, -1);
 }
 
 // ------------------------------------------------------------ flat planes

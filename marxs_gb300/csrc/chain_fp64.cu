@@ -67,14 +67,14 @@ struct Photon {
 };
 
 __device__ __forceinline__ void store_id(const mgpu_stage& st, int64_t i, int64_t v) {
-    if ((st.first_writer >> 9) & 1) ((int64_t*)st.id_out)[i * st.id_stride] = v;
+    if ((st.first_writer >> 17) & 1) ((int64_t*)st.id_out)[i * st.id_stride] = v;
     else ((int32_t*)st.id_out)[i * st.id_stride] = (int32_t)v;
 }
 
 __device__ __forceinline__ void write_miss_defaults(const mgpu_stage& st, int64_t i, int nout) {
     for (int k = 0; k < nout; ++k)
         if ((st.first_writer >> k) & 1) store_col(st.out[k], i, kNaN);
-    if (st.id_out && ((st.first_writer >> 8) & 1)) store_id(st, i, -1);
+    if (st.id_out && ((st.first_writer >> 16) & 1)) store_id(st, i, -1);
 }
 
 __device__ __forceinline__ void check_prob(double f, uint32_t* status) {
@@ -225,6 +225,93 @@ __device__ __forceinline__ int nearest_facet_grid(const mgpu_stage& st, const Ph
     return best;
 }
 
+// np.interp / scipy interp1d (linear): largest j <= n - 2 with x[j] <= v,
+// slope (y[j+1] - y[j]) / (x[j+1] - x[j]), slope * (v - x[j]) + y[j]; the
+// last knot maps to y[n-1]; outside the table interp1d raises (status bit)
+__device__ double np_interp(const double* x, const double* y, int n, double v, uint32_t* status) {
+    if (!(v >= x[0] && v <= x[n - 1])) {
+        atomicOr(status, MGPU_STATUS_TABLE_RANGE);
+        return kNaN;
+    }
+    if (v == x[n - 1]) return y[n - 1];
+    int lo = 0, hi = n - 1;
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (x[mid] <= v) lo = mid;
+        else hi = mid;
+    }
+    double slope = (y[lo + 1] - y[lo]) / (x[lo + 1] - x[lo]);
+    return __dadd_rn(__dmul_rn(slope, v - x[lo]), y[lo]);
+}
+
+// CATL1L2Stack layers after the membrane (missions/mitsnl/catgrating.py):
+// QualityFactor (:160-161), L1 (:196-207), L2Abs (:231-245), L2Diffraction
+// (:263-268) through RandomGaussianScatter (optics/scatter.py:109-150).
+// Out of line: only stages of stacked facets call it.
+__device__ __noinline__ void cat_stack_layers(const mgpu_stage& st, const mgpu_catstack& K, int f,
+                                              int m, const PlaneHit& h, double u_l1,
+                                              double u_sup, double z_l2, double u_phi,
+                                              Photon& ph, int64_t i, uint32_t* status) {
+    const mgpu_facet* fc = st.facets + f;
+    const d3 n = ldg3(fc->ex);
+    // QualityFactor: factor ** (order ** 2)
+    const double mm = (double)m;
+    const double q = pow(K.qf, mm * mm);
+    check_prob(q, status);
+    ph.prob = ph.prob * q;
+    // L1: a CAT grating with grooves at pi/2, or the support bars
+    const d3 l1 = ldg3(K.l1_vec + 6 * f), d1 = ldg3(K.l1_vec + 6 * f + 3);
+    const d3 p = normalize3(ph.dir);
+    const double wave = kEnergy2Wave / ph.energy;
+    const d3 pp = normalize3(p - dot3(p, l1) * l1);
+    double cb = fabs(dot3(pp, n));
+    cb = fmin(fmax(cb, 0.0), 1.0);
+    const double blaze1 = acos(cb);
+    double prob1;
+    int m1 = select_order(st.selectors[K.l1_selector], ph.energy, u_l1, &prob1, status);
+    d3 nd = ph.dir, npol = ph.pol;
+    if (u_sup > K.l1_open) {
+        m1 = 0;
+        prob1 = np_interp(K.l1_trans_e, K.l1_trans_t, K.l1_n_trans, ph.energy, status);
+    } else {
+        const double pd0 = dot3(p, d1);
+        const double sign = (pd0 > 0.0) ? 1.0 : ((pd0 < 0.0) ? -1.0 : (pd0 == 0.0 ? 1.0 : pd0));
+        const double p_d = pd0 + sign * (double)m1 * wave / K.l1_d;
+        const double p_l = dot3(p, l1);
+        const double p_n = sqrt(1.0 - p_d * p_d - p_l * p_l);
+        const double pn = dot3(p, n);
+        const double direction = (pn > 0.0) ? 1.0 : ((pn < 0.0) ? -1.0 : (pn == 0.0 ? 0.0 : pn));
+        nd = p_d * d1 + p_l * l1 + (direction * p_n) * n;
+        npol = parallel_transport_dev(ph.dir, nd, ph.pol);
+    }
+    check_prob(prob1, status);
+    ph.dir = nd;
+    ph.pol = npol;
+    ph.prob = ph.prob * prob1;
+    store_col(st.out[6], i, (double)m1);
+    store_col(st.out[7], i, blaze1);
+    // L2Abs: open fraction minus the shadow of the inclined hexagon walls
+    const d3 p3 = normalize3(ph.dir);
+    const double angle = acos(fabs(dot3(p3, n)));
+    const double a2 = K.l2_open - (K.l2_shadow * sin(angle)) / K.l2_total;
+    check_prob(a2, status);
+    ph.prob = ph.prob * a2;
+    // L2Diffraction: N(0,1) * sigma about dir x guess, then a uniform turn
+    const d3 pdir = normalize3(ph.dir);
+    const d3 guess = (fabs(pdir.x) < 0.99999) ? d3{1.0, 0.0, 0.0} : d3{0.0, 1.0, 0.0};
+    const d3 perp = cross3(pdir, guess);
+    const double wave_mm = __dmul_rn(MGPU_HC_KEV_NM / ph.energy, 1e-6);
+    const double sigma = (1.22 * 0.4) * asin(wave_mm / K.l2_inner);
+    const double ang = z_l2 * sigma;
+    d3 o = rot_transpose_apply(perp, ang, pdir);
+    o = rot_transpose_apply(pdir, (u_phi * 2.0) * 3.141592653589793, o);
+    ph.pol = parallel_transport_dev(ph.dir, o, ph.pol);
+    ph.dir = o;
+    store_col(st.out[8], i, ang);
+    store_col(st.out[4], i, h.ly);
+    store_col(st.out[5], i, h.lz);
+}
+
 __device__ bool stage_gratings(const mgpu_stage& st, Photon& ph, int64_t i, bool valid,
                                int rng, uint64_t seed, uint64_t row_base, int sidx,
                                uint32_t* status) {
@@ -268,7 +355,7 @@ __device__ bool stage_gratings(const mgpu_stage& st, Photon& ph, int64_t i, bool
     }
     if (!valid) return false;
     if (f < 0) {
-        write_miss_defaults(st, i, 4);
+        write_miss_defaults(st, i, MGPU_MAX_OUT);
         return false;
     }
     // FlatGrating.diffract_photons + specific_process_photons (grating.py:233-277)
@@ -280,15 +367,20 @@ __device__ bool stage_gratings(const mgpu_stage& st, Photon& ph, int64_t i, bool
     double cb = fabs(dot3(pp, n));
     cb = fmin(fmax(cb, 0.0), 1.0);
     double blaze = acos(cb);
-    double u;
+    if (st.stack) {
+        // NonParallelCATGrating.blaze_angle_modifier (catgrating.py:324-333)
+        blaze = __dadd_rn(blaze, __dadd_rn(st.stack->blaze_center,
+                                           __dmul_rn(h.ly, st.stack->d_blaze_mm)));
+    }
+    double u, u1;
     if (rng == MGPU_RNG_PREDRAWN) {
         if (st.draw[0] == nullptr) {
             atomicOr(status, MGPU_STATUS_BAD_STAGE);
             return false;
         }
         u = st.draw[0][i * st.draw_stride];
+        u1 = st.draw[1] ? st.draw[1][i * st.draw_stride] : 0.0;
     } else {
-        double u1;
         philox_uniform2(seed, row_base + (uint64_t)i, (uint32_t)sidx, 0u, &u, &u1);
     }
     double selprob;
@@ -319,6 +411,23 @@ __device__ bool stage_gratings(const mgpu_stage& st, Photon& ph, int64_t i, bool
     store_col(st.out[2], i, (double)m);
     store_col(st.out[3], i, blaze);
     if (st.id_out) store_id(st, i, __ldg(&fc->id_num));
+    if (st.stack) {
+        double u_sup, u_phi, z, z1;
+        if (rng == MGPU_RNG_PREDRAWN) {
+            if (!st.draw[1] || !st.draw[2] || !st.draw[3] || !st.draw[4]) {
+                atomicOr(status, MGPU_STATUS_BAD_STAGE);
+                return false;
+            }
+            u_sup = st.draw[2][i * st.draw_stride];
+            z = st.draw[3][i * st.draw_stride];
+            u_phi = st.draw[4][i * st.draw_stride];
+        } else {
+            const uint64_t row = row_base + (uint64_t)i;
+            philox_uniform2(seed, row, (uint32_t)sidx, 1u, &u_sup, &u_phi);
+            philox_normal2(seed, row, (uint32_t)sidx, 2u, &z, &z1);
+        }
+        cat_stack_layers(st, *st.stack, f, m, h, u1, u_sup, z, u_phi, ph, i, status);
+    }
     ph.pos = h.ip;
     return true;
 }

@@ -117,10 +117,25 @@ class _Instrument:
             return out
 
         self.stage_spline = {}
+        self.stage_stack = {}
+
+        def f64(a):
+            t = torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).to(device)
+            self.keep.append(t)
+            return t.data_ptr()
 
         for si, st in enumerate(stages):
             if st.spline is not None:
                 self.stage_spline[si] = spline_struct(st.spline)
+            if st.stack is not None:
+                k = st.stack
+                cs = _abi.MgpuCatStack(k['blaze_center'], k['d_blaze_mm'], k['qf'], k['l1_open'],
+                                       k['l1_d'], f64(k['l1_vec']), k['l1_selector'],
+                                       len(k['l1_trans_e']), f64(k['l1_trans_e']),
+                                       f64(k['l1_trans_t']), k['l2_open'], k['l2_shadow'],
+                                       k['l2_total'], k['l2_inner'])
+                self.stage_stack[si] = dev_bytes(bytes(cs))
+                self.fp32_error = ('CATL1L2Stack facets are traced in precision="fp64" only')
             try:
                 if st.kind in (_abi.STAGE_LENS, _abi.STAGE_SCATTER, _abi.STAGE_FLATDET):
                     self.stage_aux[si] = dev_bytes(L.flat32_block(st))
@@ -216,6 +231,8 @@ class _Instrument:
             s.table = self.stage_table[si].data_ptr()
         if si in self.stage_spline:
             s.spline = self.stage_spline[si]
+        if si in self.stage_stack:
+            s.stack = self.stage_stack[si].data_ptr()
 
 
 class ColumnPlan:
@@ -326,9 +343,9 @@ class GpuSequence:
                 s.id_out = idb.data_ptr()
                 s.id_stride = 1
                 if plan.first_writer.get(st.id_col) == si:
-                    fw |= 1 << 8
+                    fw |= 1 << 16
                 if idb.dtype == torch.int64:
-                    fw |= 1 << 9
+                    fw |= 1 << 17
             s.first_writer = fw
             if self.rng == 'predrawn' and st.draw_names:
                 d = draws_dev.get(si)

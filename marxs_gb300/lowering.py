@@ -161,6 +161,7 @@ class StageSpec:
     selectors: List[SelectorSpec] = field(default_factory=list)
     grid: Optional[dict] = None
     spline: Optional[tuple] = None   # LENS reflectivity (tx, ty, c[1, ...])
+    stack: Optional[dict] = None     # GRATINGS of CATL1L2Stack facets: layer constants
 
 
 def _loc_names(elem):
@@ -288,6 +289,79 @@ def _grating_stage(owner, gratings, id_col):
     return st
 
 
+_STACK_LAYERS = ('CATGrating', 'QualityFactor', 'L1', 'L2Abs', 'L2Diffraction')
+
+
+def _is_cat_stack(e):
+    layers = getattr(e, 'elements', None)
+    return ('FlatStack' in classnames(e) and layers is not None and len(layers) == 5 and
+            all(name in classnames(layer) for name, layer in zip(_STACK_LAYERS, layers)))
+
+
+def _value(q):
+    return float(np.asarray(q, dtype=float))
+
+
+def _cat_stack_stage(owner, stacks, id_col):
+    """Facet-array stage for a Parallel of CATL1L2Stack facets
+    (missions/mitsnl/catgrating.py:336-377)."""
+    membranes = [st.elements[0] for st in stacks]
+    st = _grating_stage(owner, membranes, id_col)
+    st.facets['id_num'] = [int(x.id_num) for x in stacks]
+    l1s = [x.elements[2] for x in stacks]
+    # one L1 order table for all facets (their selectors must agree)
+    spec0 = lower_selector(l1s[0].order_selector)
+    for x in l1s[1:]:
+        if x.order_selector is not l1s[0].order_selector:
+            sp = lower_selector(x.order_selector)
+            if not (np.array_equal(sp.cdf, spec0.cdf) and np.array_equal(sp.total, spec0.total)
+                    and np.array_equal(sp.orders, spec0.orders)):
+                raise NotImplementedError('CATL1L2Stack facets with different L1 order selectors')
+    st.selectors.append(spec0)
+    l1tab = _grating_facets(l1s, st.selectors,
+                            {id(x.order_selector): len(st.selectors) - 1 for x in l1s})
+    m0, qf, l1, l2abs, l2diff = stacks[0].elements
+
+    def shared(get, what):
+        v0 = get(stacks[0])
+        for x in stacks[1:]:
+            if not np.array_equal(np.asarray(get(x), dtype=float), np.asarray(v0, dtype=float)):
+                raise NotImplementedError('CATL1L2Stack facets with different %s' % what)
+        return v0
+    shared(lambda x: [_value(getattr(x.elements[0], 'blaze_center', 0.)),
+                      _value(getattr(x.elements[0], 'd_blaze_mm', 0.))], 'blaze modifiers')
+    shared(lambda x: _value(x.elements[1].factor), 'quality factors')
+    shared(lambda x: [_value(x.elements[2].openfraction), _value(x.elements[2]._d)], 'L1 support')
+    shared(lambda x: np.r_[np.asarray(x.elements[2].transfunc.x, dtype=float),
+                           np.asarray(x.elements[2].transfunc.y, dtype=float)], 'L1 transmission')
+    shared(lambda x: [_value(x.elements[3].bardepth), _value(x.elements[3].period),
+                      _value(x.elements[3].innerfree), _value(x.elements[4].innerfree)], 'L2 support')
+    if len(set(l1tab['selector'])) != 1 or not np.all(l1tab['cat'] == 1) or \
+            not np.all(l1tab['transmission'] == 1):
+        raise NotImplementedError('CATL1L2Stack: L1 layers must share one order selector')
+    inner, period = _value(l2abs.innerfree), _value(l2abs.period)
+    st.stack = dict(
+        blaze_center=_value(getattr(m0, 'blaze_center', 0.)),
+        d_blaze_mm=_value(getattr(m0, 'd_blaze_mm', 0.)),
+        qf=_value(qf.factor), l1_open=_value(l1.openfraction), l1_d=float(l1tab['dgrat'][0]),
+        l1_vec=np.ascontiguousarray(np.concatenate([l1tab['l'], l1tab['dneg']], axis=1)),
+        l1_selector=int(l1tab['selector'][0]),
+        l1_trans_e=np.asarray(l1.transfunc.x, dtype=float),
+        l1_trans_t=np.asarray(l1.transfunc.y, dtype=float),
+        l2_open=(inner / period) ** 2, l2_shadow=_value(l2abs.bardepth) * inner,
+        l2_total=period ** 2 / 2 * np.sqrt(3), l2_inner=_value(l2diff.innerfree))
+    loc_stack = _loc_names(stacks[0])
+    loc = _loc_names(m0)
+    st.out_names = [loc[0], loc[1], getattr(m0, 'order_name', 'order'),
+                    getattr(m0, 'blaze_name', 'blaze'), loc_stack[0], loc_stack[1],
+                    getattr(l1, 'order_name', 'order_L1'), getattr(l1, 'blaze_name', 'blaze_L1'),
+                    getattr(l2diff, 'scattername', 'L2Diffraction')]
+    st.new_col_order = [c for c in ([id_col] + loc_stack + st.out_names[2:4] + loc +
+                                    st.out_names[6:9]) if c is not None]
+    st.draw_names = ['order_u', 'l1_order_u', 'l1_support_u', 'l2_normal', 'l2_phi_u']
+    return st
+
+
 def _lower_one(e):
     names = classnames(e)
     if 'Parallel' in names:
@@ -296,6 +370,8 @@ def _lower_one(e):
             id_col = getattr(e.elements[0], 'id_col', None)
         if not e.elements:
             return []
+        if all(_is_cat_stack(x) for x in e.elements):
+            return [_cat_stack_stage(e, list(e.elements), id_col)]
         return [_grating_stage(e, list(e.elements), id_col)]
     if 'FlatGrating' in names:
         return [_grating_stage(e, [e], getattr(e, 'id_col', None))]

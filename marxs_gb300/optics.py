@@ -373,6 +373,12 @@ class FlatStack(FlatOpticalElement):
         self.elements = [elem(pos4d=self.pos4d, **k) for elem, k in zip(elements, keywords)]
 
 
+# L1 diffraction orders of the 2018 Arcus gratings (catgrating.py:44-48)
+L1_ORDER_SELECTOR = OrderSelector(
+    np.array([-4, -3, -2, -1, 0, 1, 2, 3, 4]),
+    p=np.array([0.006, 0.0135, 0.022, 0.028, 0.861, 0.028, 0.022, 0.0135, 0.006]))
+
+
 class CATL1L2Stack(FlatStack):
     """CAT facet with its L1 and L2 supports (catgrating.py:336-377): layers
     NonParallelCATGrating, QualityFactor, L1 (grooves at pi/2 + groove_angle),
@@ -381,9 +387,7 @@ class CATL1L2Stack(FlatStack):
     def __init__(self, l1_dims=None, l2_dims=None, l1_order_selector=None, qualityfactor=None,
                  l1_transmission=None, **kwargs):
         if l1_order_selector is None:
-            l1_order_selector = OrderSelector(
-                np.array([-4, -3, -2, -1, 0, 1, 2, 3, 4]),
-                p=np.array([0.006, 0.0135, 0.022, 0.028, 0.861, 0.028, 0.022, 0.0135, 0.006]))
+            l1_order_selector = L1_ORDER_SELECTOR
         groove_angle = kwargs.pop('groove_angle', 0.)
         kwargs['elements'] = [NonParallelCATGrating, QualityFactor, L1, L2Abs, L2Diffraction]
         kwargs['keywords'] = [{'order_selector': kwargs.pop('order_selector'),

@@ -21,7 +21,8 @@ pytestmark = pytest.mark.gpu
 SCALES = {'pos': 1.0, 'dir': 1.0, 'polarization': 1.0, 'probability': 1.0, 'energy': 1.0,
           'mirror_x': 1.0, 'mirror_y': 1.0, 'y': 1.0, 'z': 1.0, 'inplanescatter': 1e-6,
           'perpplanescatter': 1e-6, 'grat_y': 1.0, 'grat_z': 1.0, 'blaze': 1e-3,
-          'det_x': 1.0, 'det_y': 1.0, 'det_phi': 1e-3, 'detpix_x': 1.0, 'detpix_y': 1.0}
+          'det_x': 1.0, 'det_y': 1.0, 'det_phi': 1e-3, 'detpix_x': 1.0, 'detpix_y': 1.0,
+          'blaze_L1': 1e-3, 'L2Diffraction': 1e-6}
 RTOL = 1e-9
 
 
@@ -35,6 +36,9 @@ def _run_gpu(name, precision='fp64'):
         if kind == 'scatter':
             draws[elem] = {'inplanescatter': g['draw_inplanescatter'],
                            'perpplanescatter': g['draw_perpplanescatter']}
+        elif kind == 'catstack':
+            draws[elem] = {k: g['draw_' + k] for k in ('order_u', 'l1_order_u', 'l1_support_u',
+                                                        'l2_normal', 'l2_phi_u')}
         else:
             draws[elem] = {'order_u': g['draw_order_u']}
     seq = GpuSequence(elements=inst.elements, precision=precision, rng='predrawn')
@@ -75,7 +79,7 @@ def _column_report(out, ref, ok):
 BLAZE_ABS = 5e-8
 
 
-@pytest.mark.parametrize('name', ['c0', 'c1', 'c2', 'c5'])
+@pytest.mark.parametrize('name', ['c0', 'c1', 'c2', 'c5', 'c6'])
 def test_golden_parity_fp64(name):
     g, out = _run_gpu(name)
     ref = golden_outputs(g)
@@ -86,9 +90,24 @@ def test_golden_parity_fp64(name):
     assert not bad, 'columns out of tolerance: %s (all: %s)' % (bad, report)
 
 
-@pytest.mark.parametrize('name', ['c1', 'c2', 'c5'])
+@pytest.mark.parametrize('name', ['c1', 'c2', 'c5', 'c6'])
 def test_golden_hits_are_counted(name):
     from marxs_gb300 import configs
     g, out = _run_gpu(name)
     ref = golden_outputs(g)
     assert (np.asarray(out['facet']) >= 0).sum() == (ref['facet'] >= 0).sum() > 0
+
+
+def test_cat_stack_columns_and_fp32_local_refusal():
+    """CATL1L2Stack facets: the L1 order column is exact (the reference's
+    own L1 draws decide it) and the FP32-local mode says it is not
+    available for stacks."""
+    from marxs_gb300 import configs, PhotonTable
+    from marxs_gb300.gpu import GpuSequence
+    g, out = _run_gpu('c6')
+    ref = golden_outputs(g)
+    assert np.array_equal(np.asarray(out['order_L1']), ref['order_L1'], equal_nan=True)
+    inst = configs.build('c6')
+    with pytest.raises(NotImplementedError, match='fp64'):
+        GpuSequence(inst.elements, precision='fp32local', rng='philox')(
+            PhotonTable(golden_inputs(g)))

@@ -95,3 +95,26 @@ def test_philox_streams_are_keyed_by_global_photon_id():
     for col in ('pos', 'dir', 'order', 'facet', 'det_phi'):
         joined = np.concatenate([np.asarray(a[col]), np.asarray(b[col])])
         assert np.array_equal(joined, np.asarray(whole[col]), equal_nan=True), col
+
+
+def test_cat_stack_distributions():
+    """CATL1L2Stack facets with in-kernel draws: membrane and L1 order
+    histograms (chi-square) and L2 scatter angles (KS) follow the oracle fed
+    numpy draws of the reference distributions."""
+    from marxs_gb300 import configs
+    inst = configs.build('c6')
+    n = 30000
+    host = configs.photons_for('c6', n, seed=13)
+    out = _gpu(inst, host, 'fp64', seed=21)
+    ref = _oracle(inst, host, 44)
+    for col, orders in (('order', np.arange(-12, 3)), ('order_L1', np.arange(-4, 5))):
+        a = np.array([(np.asarray(out[col]) == m).sum() for m in orders])
+        b = np.array([(ref[col] == m).sum() for m in orders])
+        keep = (a + b) > 0
+        chi2, p, _, _ = stats.chi2_contingency(np.vstack([a[keep], b[keep]]))
+        assert p > 1e-3, (col, p, a, b)
+    x = np.asarray(out['L2Diffraction'])
+    y = ref['L2Diffraction']
+    x, y = x[np.isfinite(x)], y[np.isfinite(y)]
+    assert abs(len(x) - len(y)) < 5 * np.sqrt(len(y))
+    assert stats.ks_2samp(x, y).pvalue > 1e-3
