@@ -5,7 +5,7 @@ reference made, and every output column of the reference's own Sequence
 (see tests/golden/make_golden.py).  The float64 GPU chain, fed the same
 draws, must reproduce them:
 
-* ``facet`` and ``order`` bit-exact for every photon;
+* ``facet``, ``order`` (and ``order_L1`` of CAT stacks) bit-exact for every photon;
 * every float column within 1e-9 relative, |a - b| <= 1e-9 * max(|b|, s)
   with s the column's natural scale (1 mm, 1 for unit vectors, 1 pixel,
   1e-3 rad), and NaN exactly where the reference has NaN;
@@ -54,7 +54,7 @@ def _column_report(out, ref, ok):
         if a.dtype != b.dtype:
             report[col] = (False, 'dtype %s vs %s' % (a.dtype, b.dtype))
             continue
-        if col in ('facet', 'order'):
+        if col in ('facet', 'order', 'order_L1'):
             same = np.array_equal(a[ok], b[ok], equal_nan=True)
             report[col] = (same, int(np.sum(~((a[ok] == b[ok]) | (np.isnan(a[ok].astype(float)) &
                                                                  np.isnan(b[ok].astype(float)))))))
