@@ -80,6 +80,22 @@ def euler_sxyz(a):
     return euler2mat(a[0], a[1], a[2], 'sxyz')
 
 
+def euler_sxyz_batch(a):
+    """(F, 3) angles -> (F, 3, 3) matrices Rz(a2) Ry(a1) Rx(a0)."""
+    c, s = np.cos(a), np.sin(a)
+    F = len(a)
+    Rx = np.zeros((F, 3, 3))
+    Ry = np.zeros((F, 3, 3))
+    Rz = np.zeros((F, 3, 3))
+    Rx[:, 0, 0] = 1
+    Rx[:, 1, 1], Rx[:, 1, 2], Rx[:, 2, 1], Rx[:, 2, 2] = c[:, 0], -s[:, 0], s[:, 0], c[:, 0]
+    Ry[:, 1, 1] = 1
+    Ry[:, 0, 0], Ry[:, 0, 2], Ry[:, 2, 0], Ry[:, 2, 2] = c[:, 1], s[:, 1], -s[:, 1], c[:, 1]
+    Rz[:, 2, 2] = 1
+    Rz[:, 0, 0], Rz[:, 0, 1], Rz[:, 1, 0], Rz[:, 1, 1] = c[:, 2], -s[:, 2], s[:, 2], c[:, 2]
+    return Rz @ Ry @ Rx
+
+
 class PoseModel:
     """Nominal poses of the chain and the map from theta to element poses.
 
@@ -101,6 +117,7 @@ class PoseModel:
         self.n_params = 7 + 6 * self.n_facets
         self.focallength = float(self.lens.focallength)
         self.facet_pos4d = [np.array(g.geometry.pos4d, dtype=float) for g in self.gratings]
+        self._base_stack = np.stack(self.facet_pos4d)
         self.det_pos4d = np.array(self.detector.geometry.pos4d, dtype=float)
         self.facet_index = {int(g.id_num): i for i, g in enumerate(self.gratings)}
         self._tables()
@@ -167,12 +184,17 @@ class PoseModel:
 
     # --------------------------------------------------------- poses <- theta
     def apply(self, theta):
-        """Set the element poses (and focal length) for ``theta``."""
+        """Set the element poses (and focal length) for ``theta`` (all facets
+        at once: R = Rz Ry Rx per facet, pos4d = [R M | c + t])."""
         th = np.asarray(theta.detach().cpu() if torch.is_tensor(theta) else theta, dtype=float)
         self.lens.focallength = float(th[0])
-        for j, g in enumerate(self.gratings):
-            g.geometry.pos4d = self._perturbed(self.facet_pos4d[j], th[1 + 6 * j:7 + 6 * j])
         F = self.n_facets
+        p6 = th[1:1 + 6 * F].reshape(F, 6)
+        new = np.array(self._base_stack, copy=True)
+        new[:, :3, :3] = euler_sxyz_batch(p6[:, 3:6]) @ self._base_stack[:, :3, :3]
+        new[:, :3, 3] += p6[:, 0:3]
+        for g, m in zip(self.gratings, new):
+            g.geometry.pos4d = m
         self.detector.geometry.pos4d = self._perturbed(self.det_pos4d, th[1 + 6 * F:7 + 6 * F])
 
     def restore(self):
@@ -544,3 +566,39 @@ def design_loop(model, photons, orders, zero_order=0, steps=50, lr=0.2, rot_scal
     theta = base.clone()
     theta[idx] += scale * u.detach()
     return {'theta': theta, 'history': history}
+
+
+class GraphedGradient:
+    """loss_fn(stats) and dL/dtheta of frozen photons as one CUDA graph.
+
+    The forward launch, the torch loss over the moments, the autograd step
+    and the reverse launch are captured once; each call copies theta into
+    the captured input and replays the graph, so a gradient costs the two
+    kernels and no host-side dispatch.  The frozen photons, their group
+    centres and ``loss_fn`` are fixed at capture time.
+    """
+
+    def __init__(self, frozen, loss_fn, theta=None, warmup=3):
+        self.frozen = frozen
+        dev = frozen.device
+        self.theta = (frozen.model.theta0(dev) if theta is None else
+                      torch.as_tensor(theta, dtype=torch.float64, device=dev)).clone()
+        side = torch.cuda.Stream(device=dev)
+        side.wait_stream(torch.cuda.current_stream(dev))
+        old = frozen.stream
+        frozen.stream = side
+        try:
+            with torch.cuda.stream(side):
+                for _ in range(warmup):
+                    frozen.loss_and_grad(self.theta, loss_fn)
+            torch.cuda.current_stream(dev).wait_stream(side)
+            self.graph = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(self.graph, stream=side):
+                self.loss, self.grad = frozen.loss_and_grad(self.theta, loss_fn)
+        finally:
+            frozen.stream = old
+
+    def __call__(self, theta):
+        self.theta.copy_(torch.as_tensor(theta, dtype=torch.float64, device=self.theta.device))
+        self.graph.replay()
+        return self.loss, self.grad

@@ -169,38 +169,58 @@ def _loc_names(elem):
     return [None, None] if names is None else list(names)
 
 
+def _norms(v):
+    """Euclidean norms of the rows of v (F, 4)."""
+    return np.sqrt(np.einsum('ij,ij->i', v, v))
+
+
 def _grating_facets(gratings, selectors, sel_index):
-    out = np.zeros(len(gratings), dtype=_abi.FACET_DTYPE)
-    for i, g in enumerate(gratings):
+    """Facet table of a list of gratings (vectorised over the facets): the
+    frame of Geometry.__getitem__ (math/geometry.py:108-160) and the groove
+    frame of FlatGrating.e_groove_coos (optics/grating.py:186-207)."""
+    n = len(gratings)
+    out = np.zeros(n, dtype=_abi.FACET_DTYPE)
+    for g in gratings:
         if callable(g._d):
             raise NotImplementedError('position-dependent grating constant (callable d) is not '
                                       'supported on the GPU')
-        if 'blaze_angle_modifier' in type(g).__dict__:
+        if 'blaze_angle_modifier' in type(g).__dict__ and not hasattr(g, 'd_blaze_mm'):
             raise NotImplementedError('custom blaze_angle_modifier is not supported on the GPU')
-        pos4d = np.asarray(g.geometry.pos4d, dtype=float)
-        fr = plane_frame(pos4d)
-        groove = g.geometry._geometry.get('groove_angle', 0.)
-        # FlatGrating.e_groove_coos on the flat bases (e_y, e_z, e_x)
-        ex4, ey4 = _vec(pos4d, 'e_y'), _vec(pos4d, 'e_z')
-        e_groove = math.sin(-groove) * ex4 + math.cos(-groove) * ey4
-        e_perp = math.cos(-groove) * ex4 - math.sin(-groove) * ey4
-        out['c'][i] = fr[0:3]
-        out['ex'][i] = fr[3:6]
-        out['ey'][i] = fr[6:9]
-        out['ez'][i] = fr[9:12]
-        out['hy'][i] = fr[12]
-        out['hz'][i] = fr[13]
-        out['l'][i] = e_groove[:3]
-        out['dneg'][i] = (-e_perp)[:3]
-        out['dgrat'][i] = float(g._d)
-        out['id_num'][i] = int(g.id_num)
+    P = np.stack([np.asarray(g.geometry.pos4d, dtype=float) for g in gratings])   # (F, 4, 4)
+    vx, vy, vz = P[:, :, 0], P[:, :, 1], P[:, :, 2]
+    nx, ny, nz = _norms(vx), _norms(vy), _norms(vz)
+    ex4, ey4, ez4 = vx / nx[:, None], vy / ny[:, None], vz / nz[:, None]
+    out['c'] = P[:, :3, 3]
+    out['ex'] = ex4[:, :3]
+    out['ey'] = ey4[:, :3]
+    out['ez'] = ez4[:, :3]
+    out['hy'] = ny
+    out['hz'] = nz
+    # FlatGrating.e_groove_coos on the flat bases (e_y, e_z, e_x): math.sin /
+    # math.cos of each distinct groove angle, as the reference evaluates them
+    groove = np.array([float(g.geometry._geometry.get('groove_angle', 0.)) for g in gratings])
+    sn = np.empty(n)
+    cs = np.empty(n)
+    for gv in np.unique(groove):
+        k = groove == gv
+        sn[k] = math.sin(-gv)
+        cs[k] = math.cos(-gv)
+    e_groove = sn[:, None] * ey4 + cs[:, None] * ez4
+    e_perp = cs[:, None] * ey4 - sn[:, None] * ez4
+    out['l'] = e_groove[:, :3]
+    out['dneg'] = (-e_perp)[:, :3]
+    out['dgrat'] = [float(g._d) for g in gratings]
+    out['id_num'] = [int(g.id_num) for g in gratings]
+    sel = np.empty(n, dtype=np.int32)
+    for i, g in enumerate(gratings):
         key = id(g.order_selector)
         if key not in sel_index:
             sel_index[key] = len(selectors)
             selectors.append(lower_selector(g.order_selector))
-        out['selector'][i] = sel_index[key]
-        out['cat'][i] = 1 if 'CATGrating' in classnames(g) else 0
-        out['transmission'][i] = 1 if g.transmission else 0
+        sel[i] = sel_index[key]
+    out['selector'] = sel
+    out['cat'] = [1 if 'CATGrating' in classnames(g) else 0 for g in gratings]
+    out['transmission'] = [1 if g.transmission else 0 for g in gratings]
     return out
 
 

@@ -265,3 +265,16 @@ def test_adjoint_is_over_100x_faster_than_finite_differences(c1):
     torch.cuda.synchronize()
     t_fd = time.perf_counter() - t0
     assert t_fd / t_adj >= 100, (t_fd, t_adj)
+
+
+def test_graphed_gradient_equals_direct_gradient(c1):
+    """The CUDA-graph replay gives the gradient of the current theta."""
+    from marxs_gb300.adjoint import GraphedGradient
+    fr, model = c1['fr'], c1['model']
+    gg = GraphedGradient(fr, c1['loss'])
+    for seed in (4, 5):
+        theta = _random_theta(model, seed, scale=0.5)
+        L, g = gg(theta)
+        L0, g0 = fr.loss_and_grad(theta, c1['loss'])
+        assert abs(float(L) - float(L0)) <= 1e-12 * abs(float(L0))
+        assert torch.allclose(g, g0, rtol=1e-10, atol=1e-12 * float(g0.abs().max()))
