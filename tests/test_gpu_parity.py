@@ -65,7 +65,7 @@ def _column_report(out, ref, ok):
         err = np.abs(a[ok][fin] - b[ok][fin]) / np.maximum(np.abs(b[ok][fin]), scale)
         worst = float(err.max()) if err.size else 0.0
         passed = nan_ok and close_rel(a[ok], b[ok], RTOL, scale)
-        if col == 'blaze':
+        if col in ('blaze', 'blaze_L1'):
             # arccos is ill-conditioned near normal incidence: an ulp in the
             # cosine moves the angle by up to sqrt(2 * 2.2e-16) ~ 2e-8 rad
             d = np.abs(a[ok][fin] - b[ok][fin])
