@@ -217,35 +217,29 @@ def source_pipeline_bench(args, torch, inst, n, head, row_base, dist):
     import numpy as np
     from marxs_gb300 import configs
     from marxs_gb300.gpu import DevicePhotons, GpuSequence
-    from marxs_gb300.source import CircleAperture, DeviceSource
+    from marxs_gb300.source import CircleAperture, DeviceSource, simulate_events
     from marxs_gb300.sharding import max_over_ranks
     knots, dens = configs.spectrum_knots(2)
     ap = CircleAperture(position=[12000., 0, 0], zoom=[1, 500, 500], r_inner=300.)
     src = DeviceSource(ap, energy={'energy': knots, 'fluxdensity': dens})
     seq = GpuSequence(elements=inst.elements, precision=head, rng='philox', seed=12345)
-    ph = DevicePhotons(n)
-    out = DevicePhotons(n)
-    plan, bufs = seq.allocate_columns(n)
     cols = ['det_phi', 'det_y', 'order', 'facet']
-    host = {k: torch.empty(n, dtype=bufs[k].dtype, pin_memory=True) for k in cols}
-    d2h = sum(host[k].numel() * host[k].element_size() for k in cols)
+    out = simulate_events(src, seq, n, cols, seed=7, row_base=row_base)
+    d2h = sum(out[k].numel() * out[k].element_size() for k in cols)
     times = []
     for step in range(1 + args.e2e_steps):
         torch.cuda.synchronize()
         t = time.perf_counter()
-        src.generate(n, seed=7 + step, row_base=row_base, out=ph)
-        seq.trace_device(ph, out, plan, bufs, row_base=row_base)
-        for k in cols:
-            host[k].copy_(bufs[k], non_blocking=True)
-        torch.cuda.synchronize()
+        simulate_events(src, seq, n, cols, seed=7 + step, row_base=row_base, out=out)
         if step > 0:
             times.append(time.perf_counter() - t)
     s = max_over_ranks([sum(times) / len(times)], dist, device='cuda')[0]
     world = dist.get_world_size() if dist is not None else 1
     return {'value': world * n / s, 'unit': UNIT, 'ms_per_step': s * 1e3,
             'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': d2h,
-            'api': 'DeviceSource(CircleAperture, spectrum).generate -> '
-                   'GpuSequence.trace_device -> detector columns to pinned host memory'}
+            'api': 'simulate_events(DeviceSource(CircleAperture, spectrum), GpuSequence): '
+                   'generate + trace + event columns to pinned host memory, chunks of 8e6 '
+                   'on two streams'}
 
 
 def adjoint_bench(args, torch):

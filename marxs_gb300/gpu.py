@@ -450,7 +450,7 @@ class GpuSequence:
         return status, hits
 
     # ------------------------------------------------------------ table path
-    def __call__(self, photons, draws=None, row_base=0, chunk=16_000_000):
+    def __call__(self, photons, draws=None, row_base=0, chunk=8_000_000):
         """Trace a photon table (astropy Table, PhotonTable or dict) in place.
 
         The photons are processed in chunks alternating over two streams:

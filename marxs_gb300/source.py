@@ -168,3 +168,69 @@ class DeviceSource:
         _abi.check(lib.mgpu_generate_photons(C.byref(S), pos, dirs, pol, en, pr,
                                              C.c_void_p(s.cuda_stream)), 'mgpu_generate_photons')
         return out
+
+
+def simulate_events(source, seq, n, columns=('det_phi', 'det_y', 'order', 'facet'), seed=0,
+                    row_base=0, chunk=8_000_000, out=None):
+    """Generate ``n`` photons on the GPU, trace them through ``seq`` and
+    return the detector event ``columns`` in pinned host memory.
+
+    The photons are processed in chunks alternating over two streams: while
+    one chunk is generated and traced, the previous chunk's event columns
+    travel to the host, so the host link (the limit for the event list) is
+    busy while the GPU computes.  Photon ``k`` of the list gets global id
+    ``row_base + k`` whatever the chunking, so the result does not depend on
+    ``chunk``.  ``out``: optional dict of pinned host tensors to fill.
+    """
+    from .gpu import DevicePhotons
+    dev = source.device
+    chunk = max(1, min(int(chunk), int(n)))
+    inst = seq.lower()
+    streams = [torch.cuda.Stream(device=dev), torch.cuda.Stream(device=dev)]
+    slots = []
+    for s in streams:
+        with torch.cuda.stream(s):
+            plan, bufs = seq.allocate_columns(chunk)
+            slots.append({'ph': DevicePhotons(chunk, dev), 'plan': plan, 'bufs': bufs,
+                          'status': torch.zeros(1, dtype=torch.int32, device=dev),
+                          'hits': torch.zeros(_abi.MAX_STAGES, dtype=torch.int64, device=dev)})
+    missing = [c for c in columns if c not in slots[0]['bufs']]
+    if missing:
+        raise ValueError('the chain writes no column %s' % missing)
+    if out is None:
+        out = {c: torch.empty(n, dtype=slots[0]['bufs'][c].dtype, pin_memory=True)
+               for c in columns}
+    cur = torch.cuda.current_stream(dev)
+    for s in streams:
+        s.wait_stream(cur)
+    for k, start in enumerate(range(0, n, chunk)):
+        m = min(chunk, n - start)
+        sl = slots[k % 2]
+        s = streams[k % 2]
+        with torch.cuda.stream(s):
+            # this slot's buffers are reused only on stream s, after its last copy
+            ph = sl['ph'] if m == chunk else _view(sl['ph'], m)
+            source.generate(m, seed=seed, row_base=row_base + start, out=ph, stream=s)
+            seq.trace_device(ph, ph, sl['plan'], {c: b[:m] for c, b in sl['bufs'].items()},
+                             stream=s, status=sl['status'], hits=sl['hits'],
+                             row_base=row_base + start)
+            for c in columns:
+                out[c][start:start + m].copy_(sl['bufs'][c][:m], non_blocking=True)
+    for s in streams:
+        cur.wait_stream(s)
+    torch.cuda.synchronize(dev)
+    for sl in slots:
+        code = int(sl['status'].item())
+        if code:
+            seq._raise_status(code)
+    return out
+
+
+def _view(ph, m):
+    """The first m photons of a DevicePhotons (views, no copy)."""
+    from .gpu import DevicePhotons
+    v = DevicePhotons.__new__(DevicePhotons)
+    v.n = m
+    v.pos, v.dir, v.pol = ph.pos[:, :m], ph.dir[:, :m], ph.pol[:, :m]
+    v.energy, v.prob = ph.energy[:m], ph.prob[:m]
+    return v

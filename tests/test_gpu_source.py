@@ -107,3 +107,32 @@ def test_generated_photons_trace_like_host_photons():
     a = bufs['det_phi'].cpu().numpy()
     assert np.array_equal(np.isnan(a), np.isnan(d))
     assert np.array_equal(a[~np.isnan(a)], d[~np.isnan(d)])
+
+
+def test_simulate_events_does_not_depend_on_chunking():
+    """The two-stream chunked pipeline gives the event list of one generate +
+    trace_device over all photons, whatever the chunk size (ragged last
+    chunk included)."""
+    from marxs_gb300 import configs
+    from marxs_gb300.gpu import DevicePhotons, GpuSequence
+    from marxs_gb300.source import CircleAperture, DeviceSource, simulate_events
+    inst = configs.build('c2')
+    ap = CircleAperture(position=[12000., 0, 0], zoom=[1, 500, 500], r_inner=300.)
+    src = DeviceSource(ap, energy={'energy': np.linspace(0.3, 2.0, 40),
+                                   'fluxdensity': np.ones(40)})
+    seq = GpuSequence(inst.elements, precision='fp32local', rng='philox', seed=4)
+    n = 50_000
+    cols = ('det_phi', 'det_y', 'order', 'facet')
+    ph = src.generate(n, seed=21, row_base=100)
+    plan, bufs = seq.allocate_columns(n)
+    status, _ = seq.trace_device(ph, ph, plan, bufs, row_base=100)
+    torch.cuda.synchronize()
+    assert int(status.item()) == 0
+    for chunk in (n, 16_384, 7_001):
+        ev = simulate_events(src, seq, n, cols, seed=21, row_base=100, chunk=chunk)
+        for c in cols:
+            assert ev[c].is_pinned()
+            a, b = ev[c].numpy(), bufs[c].cpu().numpy()
+            assert np.array_equal(a, b, equal_nan=a.dtype.kind == 'f'), (chunk, c)
+    with pytest.raises(ValueError):
+        simulate_events(src, seq, 10, ('no_such_column',))
