@@ -455,6 +455,64 @@ typedef struct {
 int mgpu_pose_adjoint(const mgpu_adjoint_problem* prob, const double* theta, int32_t mode,
                       const double* seeds, double* moments, double* grad, void* stream);
 
+/* ---- per-order statistics of a photon list (analysis reductions) ----
+ *
+ * Replaces, for device-resident event columns, the per-order loops of
+ *   resolvingpower_from_photonlist  analysis/gratings.py:215-270
+ *   effectivearea_from_photonlist   analysis/gratings.py:333-363
+ *   CaptureResAeff.__call__         analysis/gratings.py:470-501
+ * and astropy.stats.sigma_clipped_stats with the defaults those call it with
+ * (cenfunc median, stdfunc std, std_ddof 0, sigma 3, maxiters 5).
+ *
+ * Photons are grouped by the value of their order column: group g holds the
+ * photons whose order equals orders[g] (order_type MGPU_ORDER_NONE: every
+ * photon is in group 0).  Per group the call computes
+ *   n_member  photons in the group that pass the filter (RES_FILTER: finite
+ *             value and probability > 0), the count the reference compares
+ *             with 20;
+ *   the sigma-clipped mean, median and std of the group's finite values;
+ *   aeff_sum  sum of probability over the group's photons (aeff_mask != 0
+ *             when a mask is given), no other filter.
+ * All sums are deterministic (fixed reduction order); the median is exact. */
+#define MGPU_STATS_MAX_GROUPS 64
+#define MGPU_STATS_NRES 8
+/* result columns, n_groups x MGPU_STATS_NRES doubles */
+#define MGPU_STATS_MEAN     0
+#define MGPU_STATS_MEDIAN   1
+#define MGPU_STATS_STD      2
+#define MGPU_STATS_N_CLIP   3  /* values left after clipping */
+#define MGPU_STATS_N_MEMBER 4
+#define MGPU_STATS_AEFF     5
+#define MGPU_STATS_N_FINITE 6  /* finite members: the values that enter the clipping */
+#define MGPU_STATS_ROUNDS   7  /* clipping iterations run */
+#define MGPU_ORDER_NONE 0
+#define MGPU_ORDER_F64  1
+#define MGPU_ORDER_I32  2
+#define MGPU_ORDER_I64  3
+#define MGPU_STATS_RES_FILTER 0x1u  /* members need a finite value and probability > 0 */
+#define MGPU_STATS_AEFF_ONLY  0x2u  /* counts and aeff_sum only: no clipping (statistics NaN) */
+
+typedef struct {
+    int64_t n;                  /* photons */
+    mgpu_col value;             /* the dispersion coordinate (f64) */
+    const void* order;          /* order column (order_type), element i at order[i * order_stride] */
+    int64_t order_stride;
+    int32_t order_type;         /* MGPU_ORDER_* */
+    int32_t n_groups;           /* 1 .. MGPU_STATS_MAX_GROUPS */
+    mgpu_col prob;              /* probability (f64); ptr NULL = 1 for every photon */
+    const uint8_t* aeff_mask;   /* optional: photons counted in aeff_sum (nonzero) */
+    uint32_t flags;             /* MGPU_STATS_* */
+    int32_t maxiters;           /* clipping iterations (>= 1) */
+    double sigma;               /* clip at median -/+ sigma * std */
+    double orders[MGPU_STATS_MAX_GROUPS];
+    void* work;                 /* device workspace, mgpu_order_stats_workspace bytes, 256-B aligned */
+    int64_t work_bytes;
+    double* result;             /* device, n_groups x MGPU_STATS_NRES */
+} mgpu_stats_problem;
+
+int64_t mgpu_order_stats_workspace(int64_t n, int32_t n_groups);
+int mgpu_order_stats(const mgpu_stats_problem* prob, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -176,6 +176,24 @@ class MgpuAdjointProblem(C.Structure):
                 ('y_out', C.c_void_p), ('rot', C.c_void_p), ('status', C.c_void_p)]
 
 
+STATS_MAX_GROUPS = 64
+STATS_NRES = 8
+STATS_MEAN, STATS_MEDIAN, STATS_STD, STATS_N_CLIP = 0, 1, 2, 3
+STATS_N_MEMBER, STATS_AEFF, STATS_N_FINITE, STATS_ROUNDS = 4, 5, 6, 7
+ORDER_NONE, ORDER_F64, ORDER_I32, ORDER_I64 = 0, 1, 2, 3
+STATS_RES_FILTER = 0x1
+STATS_AEFF_ONLY = 0x2
+
+
+class MgpuStatsProblem(C.Structure):
+    _fields_ = [('n', C.c_int64), ('value', MgpuCol), ('order', C.c_void_p),
+                ('order_stride', C.c_int64), ('order_type', C.c_int32), ('n_groups', C.c_int32),
+                ('prob', MgpuCol), ('aeff_mask', C.c_void_p), ('flags', C.c_uint32),
+                ('maxiters', C.c_int32), ('sigma', C.c_double),
+                ('orders', C.c_double * STATS_MAX_GROUPS), ('work', C.c_void_p),
+                ('work_bytes', C.c_int64), ('result', C.c_void_p)]
+
+
 SIGNATURES = {
     'mgpu_abi_version': (C.c_int, []),
     'mgpu_device_sm_count': (C.c_int, []),
@@ -194,6 +212,8 @@ SIGNATURES = {
                                         MgpuCol, C.c_void_p]),
     'mgpu_pose_adjoint': (C.c_int, [C.POINTER(MgpuAdjointProblem), C.c_void_p, C.c_int32,
                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    'mgpu_order_stats_workspace': (C.c_int64, [C.c_int64, C.c_int32]),
+    'mgpu_order_stats': (C.c_int, [C.POINTER(MgpuStatsProblem), C.c_void_p]),
 }
 
 _lib = None

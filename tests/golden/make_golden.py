@@ -307,12 +307,88 @@ def generate_source():
     return res
 
 
+def analysis_photons(seed=41, n=20_000):
+    """A synthetic event list: orders -10..10 (float, NaN = no grating hit),
+    Gaussian dispersion positions with a few far outliers, some non-finite
+    positions, probabilities with zeros, a CCD_ID column with gaps (-1).
+    Orders -10, 9 and 10 get 25, 20 and 21 photons (either side of the
+    reference's > 20 rule)."""
+    rng = np.random.default_rng(seed)
+    orders = np.arange(-10, 11)
+    weights = np.exp(-0.5 * ((orders + 4) / 3.) ** 2) + 0.05
+    order = rng.choice(orders, size=n, p=weights / weights.sum()).astype(float)
+    order[np.isin(order, [-10, 9, 10])] = -1.0
+    order[rng.random(n) < 0.05] = np.nan
+    special = np.zeros(n, dtype=bool)
+    for o, k in ((-10, 25), (9, 20), (10, 21)):
+        idx = rng.choice(np.flatnonzero((order == -1) & ~special), size=k, replace=False)
+        order[idx] = o
+        special[idx] = True
+    det_x = 30. * order + rng.normal(0, 0.02 + 0.002 * np.abs(np.nan_to_num(order)), n)
+    out = (rng.random(n) < 0.01) & ~special
+    det_x[out] += rng.standard_cauchy(out.sum()) * 5.
+    det_x[(rng.random(n) < 0.01) & ~special] = np.nan
+    det_x[np.isnan(order)] = np.nan
+    prob = rng.random(n)
+    prob[rng.random(n) < 0.03] = 0.0
+    ccd = rng.integers(0, 8, n)
+    ccd[rng.random(n) < 0.1] = -1
+    return {'order': order, 'det_x': det_x, 'probability': prob, 'CCD_ID': ccd}
+
+
+def generate_analysis():
+    """The reference's per-order analysis functions (analysis/gratings.py) on a
+    synthetic event list; astropy's sigma_clipped_stats is the oracle's
+    restatement (refshim/astropy/stats)."""
+    reference_loader.load()
+    from astropy.table import Table
+    from marxs.analysis import gratings as G
+    cols = analysis_photons()
+    photons = Table({k: v for k, v in cols.items()})
+    orders = np.arange(-10, 11)
+    res = {k: v for k, v in cols.items()}
+    res['orders'] = orders
+    r, pos, std = G.resolvingpower_from_photonlist(photons, orders, col='det_x')
+    res['rp_res'], res['rp_pos'], res['rp_std'] = r, pos, std
+    r, pos, std = G.resolvingpower_from_photonlist(photons, orders, col='det_x', zeropos=0.5)
+    res['rpz_res'], res['rpz_pos'], res['rpz_std'] = r, pos, std
+    res['aeff'] = G.effectivearea_from_photonlist(photons, orders, len(photons), A_geom=2.)
+    for name, cap in (('cap', G.CaptureResAeff(A_geom=3., orders=orders, dispersion_coord='det_x')),
+                      ('ccd', G.CaptureResAeff_CCDgaps(aeff_filter_col='CCD_ID', A_geom=3.,
+                                                       orders=orders, dispersion_coord='det_x'))):
+        out = cap(photons)
+        for k in ('Aeff0', 'Aeffgrat', 'Aeff', 'Rgrat', 'R'):
+            res['%s_%s' % (name, k)] = np.ma.filled(np.ma.asarray(out[k], dtype=float), np.nan)
+    # too few zeroth-order photons: R of every order is NaN
+    few = {k: v.copy() for k, v in cols.items()}
+    zero = np.flatnonzero(few['order'] == 0)
+    few['order'][zero[19:]] = np.nan
+    out = G.CaptureResAeff(orders=orders, dispersion_coord='det_x')(Table(few))
+    res['few_order'] = few['order']
+    res['few_R'] = np.asarray(out['R'], dtype=float)
+    res['few_Aeff'] = np.asarray(out['Aeff'], dtype=float)
+    rng = np.random.default_rng(43)
+    r = rng.random((2, 4, 5)) * 4000
+    r[rng.random(r.shape) < 0.3] = np.nan
+    a = rng.random((2, 4, 5)) * 50
+    res['avg_r_in'], res['avg_aeff_in'] = r, a
+    for ax, key in ((None, 'none'), (0, '0'), (2, '2')):
+        ra, aa = G.average_R_Aeff(r, a, axis=ax)
+        res['avg_r_' + key] = np.ma.filled(np.ma.asarray(ra, dtype=float), np.nan)
+        res['avg_aeff_' + key] = np.asarray(aa, dtype=float)
+    np.savez_compressed(os.path.join(HERE, 'analysis.npz'), **res)
+    print('analysis n=%d' % len(photons))
+    return res
+
+
 if __name__ == '__main__':
     check_choice_restatement()
     check_uniform_restatement()
-    names = sys.argv[1:] or ['c0', 'c1', 'c2', 'c5', 'c6', 'source']
+    names = sys.argv[1:] or ['c0', 'c1', 'c2', 'c5', 'c6', 'source', 'analysis']
     for name in names:
         if name == 'source':
             generate_source()
+        elif name == 'analysis':
+            generate_analysis()
         else:
             generate(name)

@@ -32,6 +32,10 @@ class Column(np.ndarray):
     def data(self):
         return self.view(np.ndarray)
 
+    @property
+    def value(self):
+        return self.view(np.ndarray)
+
     def to(self, unit, equivalencies=None):
         from astropy.units import Quantity
         return Quantity(self.view(np.ndarray), self.unit).to(unit, equivalencies=equivalencies)
