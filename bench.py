@@ -242,6 +242,41 @@ def source_pipeline_bench(args, torch, inst, n, head, row_base, dist):
                    'on two streams'}
 
 
+def analysis_bench(args, torch, rr, n):
+    """CaptureResAeff (orders -10..10, det_phi) over the event columns the
+    timed trace left on the device: the per-order effective area and
+    sigma-clipped resolving power, one mgpu_order_stats call per step; the
+    oracle on a 1e6-photon host sample of the same columns beside it."""
+    import numpy as np
+    from marxs_gb300.analysis import CaptureResAeff
+    from oracle import analysis as A
+    bufs, out = rr['bufs'], rr['out']
+    cols = {'order': bufs['order'], 'det_phi': bufs['det_phi'], 'probability': out.prob}
+    cap = CaptureResAeff(orders=np.arange(-10, 11), dispersion_coord='det_phi')
+    res = cap(cols)
+    stream = torch.cuda.current_stream()
+    times = []
+    for _ in range(3):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        res = cap(cols)
+        b.record(stream)
+        torch.cuda.synchronize()
+        times.append(a.elapsed_time(b))
+    ms = min(times)
+    m = min(n, 1_000_000)
+    host = {k: v[:m].cpu().numpy() for k, v in cols.items()}
+    t = time.perf_counter()
+    A.capture_res_aeff(host['order'], host['det_phi'], host['probability'], np.arange(-10, 11))
+    cpu_s = time.perf_counter() - t
+    return {'value': n / (ms / 1e3), 'unit': 'photons/s', 'ms_per_call': ms,
+            'orders': 21, 'Rgrat': float(res['Rgrat']),
+            'bytes_read_per_photon': 24,
+            'cpu_baseline': {'value': m / cpu_s, 'unit': 'photons/s', 'cores': 1, 'kind': 'port',
+                             'sample': '%d photons of the same columns, numpy oracle' % m},
+            'api': 'CaptureResAeff(orders=-10..10, dispersion_coord="det_phi")(device columns)'}
+
+
 def adjoint_bench(args, torch):
     """Pose gradients on the 200-facet spectrometer: hand-written adjoint vs
     central finite differences (h = 1e-4 mm / 1e-6 rad) over all 1,207
@@ -582,6 +617,8 @@ def main():
                        'api': 'GpuSequence(elements)(PhotonTable) with pinned host columns'}
     if not args.no_e2e:
         line['source_pipeline'] = source_pipeline_bench(args, torch, inst, n, head, row_base, dist)
+    if rank == 0 and world == 1:
+        line['analysis'] = analysis_bench(args, torch, results[head], n)
     if rank == 0 and world == 1 and not args.no_adjoint:
         for k in ('seq', 'plan', 'bufs', 'out'):
             for rr in results.values():

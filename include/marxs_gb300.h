@@ -513,6 +513,42 @@ typedef struct {
 int64_t mgpu_order_stats_workspace(int64_t n, int32_t n_groups);
 int mgpu_order_stats(const mgpu_stats_problem* prob, void* stream);
 
+/* ---- facet poses of a Parallel on the device (tolerancing) ----
+ *
+ * Replaces Parallel.generate_elements (simulator/simulator.py:384-440) for
+ * the facets of one grating stage after wiggle / moveglobal /
+ * moveindividual (design/tolerancing.py:45-111): element i is posed as
+ *   pos4d_i = outer T(t_i) T(c_i) R(a_i) M_i
+ * where outer = the Parallel's pos4d times its global uncertainty, (c_i, M_i)
+ * the uncertainty-free local pose, t_i the translation and R(a_i) the Euler
+ * sxyz rotation of the element uncertainty.  DRAW takes (t_i, a_i) as
+ * offset + sigma * z with z standard normals from Philox keyed by (seed,
+ * facet index) -- the distribution of generate_facet_uncertainty,
+ * design/uncertainties.py:8-39.  The facet frame (c, e_x, e_y, e_z, hy, hz,
+ * groove l, -e_perp) is rewritten in place; the other facet fields are
+ * kept.  Rebuild the candidate grid with mgpu_facet_grid_build afterwards. */
+#define MGPU_POSE_ZERO  0   /* no element uncertainty */
+#define MGPU_POSE_DRAW  1   /* Gaussian draws */
+#define MGPU_POSE_GIVEN 2   /* given[6 i ...] = dx, dy, dz (mm), rx, ry, rz (rad) */
+
+typedef struct {
+    int32_t n_facets;
+    int32_t mode;               /* MGPU_POSE_* */
+    uint64_t seed;              /* DRAW */
+    double sigma[6];            /* DRAW: Gaussian sigma of dx, dy, dz, rx, ry, rz */
+    double offset[6];           /* DRAW: mean of the same */
+    const double* given;        /* GIVEN: device, n_facets x 6 */
+    double* perturb_out;        /* optional, device, n_facets x 6: the (t, a) used */
+    double outer[16];           /* row-major 4x4: Parallel pos4d times its uncertainty */
+    const double* local;        /* device, n_facets x 12: c (3), M (3x3 row-major) */
+    const double* groove;       /* device, n_facets x 2: sin(-groove angle), cos(-groove angle) */
+    mgpu_facet* facets;         /* device, rewritten in place */
+    mgpu_facet32* facets32;     /* optional, device: FP32-local records rewritten */
+    float* cand32;              /* optional, device, 16-B aligned, n_facets x 16 floats */
+} mgpu_pose_update;
+
+int mgpu_facet_poses(const mgpu_pose_update* update, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -194,6 +194,17 @@ class MgpuStatsProblem(C.Structure):
                 ('work_bytes', C.c_int64), ('result', C.c_void_p)]
 
 
+POSE_ZERO, POSE_DRAW, POSE_GIVEN = 0, 1, 2
+
+
+class MgpuPoseUpdate(C.Structure):
+    _fields_ = [('n_facets', C.c_int32), ('mode', C.c_int32), ('seed', C.c_uint64),
+                ('sigma', C.c_double * 6), ('offset', C.c_double * 6), ('given', C.c_void_p),
+                ('perturb_out', C.c_void_p), ('outer', C.c_double * 16), ('local', C.c_void_p),
+                ('groove', C.c_void_p), ('facets', C.c_void_p), ('facets32', C.c_void_p),
+                ('cand32', C.c_void_p)]
+
+
 SIGNATURES = {
     'mgpu_abi_version': (C.c_int, []),
     'mgpu_device_sm_count': (C.c_int, []),
@@ -214,6 +225,7 @@ SIGNATURES = {
                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     'mgpu_order_stats_workspace': (C.c_int64, [C.c_int64, C.c_int32]),
     'mgpu_order_stats': (C.c_int, [C.POINTER(MgpuStatsProblem), C.c_void_p]),
+    'mgpu_facet_poses': (C.c_int, [C.POINTER(MgpuPoseUpdate), C.c_void_p]),
 }
 
 _lib = None

@@ -381,14 +381,64 @@ def generate_analysis():
     return res
 
 
+from pose_case import build_pose_parallel, pose_case  # noqa: E402
+
+
+def generate_poses():
+    """The reference's wiggle, moveglobal and moveindividual
+    (design/tolerancing.py:45-111) on a Parallel of CAT facets; the normal
+    draws of generate_facet_uncertainty are recorded."""
+    marxs = reference_loader.load()
+    from transforms3d.euler import euler2mat
+    from marxs.simulator import Parallel
+    from marxs.optics import CATGrating, OrderSelector
+    from marxs.design import tolerancing as T
+    from types import SimpleNamespace
+    ns = SimpleNamespace(Parallel=Parallel, CATGrating=CATGrating, OrderSelector=OrderSelector)
+    case = pose_case()
+    gas = build_pose_parallel(ns, case, euler2mat)
+    res = dict(case)
+    res['base_pos4d'] = np.stack([e.geometry.pos4d for e in gas.elements])
+    log = []
+    orig = np.random.normal
+
+    def normal(loc=0.0, scale=1.0, size=None):
+        z = np.random.standard_normal(size)
+        log.append(np.array(z, copy=True))
+        return loc + scale * z
+
+    np.random.seed(GLOBAL_SEED + 11)
+    np.random.normal = normal
+    try:
+        T.wiggle(gas, dx=0.5, dy=0.3, dz=0.2, rx=1e-3, ry=2e-3, rz=5e-4)
+    finally:
+        np.random.normal = orig
+    assert len(log) == 2
+    res['wiggle_sigma'] = np.array([0.5, 0.3, 0.2, 1e-3, 2e-3, 5e-4])
+    res['wiggle_pert'] = np.hstack([0 + res['wiggle_sigma'][:3] * log[0],
+                                    0 + res['wiggle_sigma'][3:] * log[1]])
+    res['wiggle_pos4d'] = np.stack([e.geometry.pos4d for e in gas.elements])
+    res['global_move'] = np.array([1.0, -2.0, 0.5, 1e-3, -1e-3, 2e-3])
+    T.moveglobal(gas, *res['global_move'])
+    res['global_pos4d'] = np.stack([e.geometry.pos4d for e in gas.elements])
+    res['indiv_move'] = np.array([0.1, 0.2, 0.3, 1e-4, 2e-4, 3e-4])
+    T.moveindividual(gas, *res['indiv_move'])
+    res['indiv_pos4d'] = np.stack([e.geometry.pos4d for e in gas.elements])
+    np.savez_compressed(os.path.join(HERE, 'poses.npz'), **res)
+    print('poses n=%d' % len(gas.elements))
+    return res
+
+
 if __name__ == '__main__':
     check_choice_restatement()
     check_uniform_restatement()
-    names = sys.argv[1:] or ['c0', 'c1', 'c2', 'c5', 'c6', 'source', 'analysis']
+    names = sys.argv[1:] or ['c0', 'c1', 'c2', 'c5', 'c6', 'source', 'analysis', 'poses']
     for name in names:
         if name == 'source':
             generate_source()
         elif name == 'analysis':
             generate_analysis()
+        elif name == 'poses':
+            generate_poses()
         else:
             generate(name)

@@ -20,6 +20,7 @@ STRUCTS = {
     'mgpu_flat32': _abi.MgpuFlat32, 'mgpu_grid32': _abi.MgpuGrid32, 'mgpu_cyl32': _abi.MgpuCyl32,
     'mgpu_adjoint_problem': _abi.MgpuAdjointProblem, 'mgpu_spline1': _abi.MgpuSpline1,
     'mgpu_source': _abi.MgpuSource, 'mgpu_stats_problem': _abi.MgpuStatsProblem,
+    'mgpu_pose_update': _abi.MgpuPoseUpdate,
 }
 
 
@@ -83,6 +84,8 @@ def test_header_constants_match():
         assert int(consts['MGPU_STATS_' + name]) == getattr(_abi, 'STATS_' + name), name
     for name in ('RES_FILTER', 'AEFF_ONLY'):
         assert int(consts['MGPU_STATS_' + name].rstrip('u'), 16) == getattr(_abi, 'STATS_' + name)
+    for name in ('ZERO', 'DRAW', 'GIVEN'):
+        assert int(consts['MGPU_POSE_' + name]) == getattr(_abi, 'POSE_' + name), name
     for name in ('NONE', 'F64', 'I32', 'I64'):
         assert int(consts['MGPU_ORDER_' + name]) == getattr(_abi, 'ORDER_' + name), name
     assert re.search(r'#define MGPU_ERR_NOALLOC_LIMIT \((-?\d+)\)', text).group(1) == \
