@@ -53,6 +53,9 @@ def parse():
     p.add_argument('--no-design', action='store_true')
     p.add_argument('--design-photons', type=float, default=1e7)
     p.add_argument('--design-steps', type=int, default=50)
+    p.add_argument('--no-tolerancing', action='store_true')
+    p.add_argument('--tolerancing-photons', type=float, default=1e7)
+    p.add_argument('--tolerancing-sets', type=int, default=10)
     return p.parse_args()
 
 
@@ -275,6 +278,64 @@ def analysis_bench(args, torch, rr, n):
             'cpu_baseline': {'value': m / cpu_s, 'unit': 'photons/s', 'cores': 1, 'kind': 'port',
                              'sample': '%d photons of the same columns, numpy oracle' % m},
             'api': 'CaptureResAeff(orders=-10..10, dispersion_coord="det_phi")(device columns)'}
+
+
+def tolerancing_bench(args, torch):
+    """run_tolerances over facet wiggles of the 1000-facet CAT array
+    (sigma 0.5 mm / 1 arcmin per axis, a new realisation per parameter set),
+    1e7 photons at 0.5 keV generated once on the device, FP32-local trace,
+    CaptureResAeff (orders -8..0, det_phi) per set: device poses against the
+    same loop with the wiggle applied on the host (Parallel.generate_elements,
+    lowering and upload of the facet tables, grid build)."""
+    import numpy as np
+    from marxs_gb300 import configs, geomath
+    from marxs_gb300.analysis import CaptureResAeff
+    from marxs_gb300.gpu import DevicePhotons, GpuSequence
+    from marxs_gb300.source import CircleAperture, DeviceSource
+    from marxs_gb300.tolerancing import DeviceFacetPoses, run_tolerances, wiggle
+    n = int(args.tolerancing_photons)
+    K = int(args.tolerancing_sets)
+    arcmin = np.deg2rad(1. / 60)
+    params = [{'dx': 0.5, 'dy': 0.5, 'dz': 0.5, 'rx': arcmin, 'ry': arcmin, 'rz': arcmin}] * K
+    inst = configs.build('c2')
+    seq = GpuSequence(elements=inst.elements, precision='fp32local', rng='philox', seed=21)
+    poses = DeviceFacetPoses(seq, inst.gas, seed=3)
+    ap = CircleAperture(position=[12000., 0, 0], zoom=[1, 500, 500], r_inner=300.)
+    photons = DeviceSource(ap, energy=0.5).generate(n, seed=9)
+    cap = CaptureResAeff(orders=np.arange(-8, 1), dispersion_coord='det_phi')
+    run_tolerances(photons, seq, wiggle, poses, params[:2], cap)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    res = run_tolerances(photons, seq, wiggle, poses, params, cap)
+    torch.cuda.synchronize()
+    dev_s = (time.perf_counter() - t) / K
+    # host wiggle: new elem_uncertainty, generate_elements, relower, trace, analyse
+    rng = np.random.default_rng(0)
+    F = len(inst.gas.elements)
+    plan, bufs = seq.allocate_columns(n)
+    out = DevicePhotons(n)
+    host_s = []
+    for k in range(3):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        tr = rng.normal(0, 0.5, (F, 3))
+        rot = rng.normal(0, arcmin, (F, 3))
+        inst.gas.elem_uncertainty = [geomath.compose(a, geomath.euler2mat(*b, 'sxyz'), np.ones(3))
+                                     for a, b in zip(tr, rot)]
+        inst.gas.generate_elements()
+        hseq = GpuSequence(elements=inst.elements, precision='fp32local', rng='philox', seed=21)
+        plan, bufs = hseq.allocate_columns(n)
+        hseq.trace_device(photons, out, plan, bufs)
+        cap(dict(bufs, probability=out.prob))
+        torch.cuda.synchronize()
+        host_s.append(time.perf_counter() - t)
+    host = float(np.median(host_s))
+    return {'value': 1.0 / dev_s, 'unit': 'parameter sets/s', 's_per_set': dev_s,
+            'photons_per_set': n, 'sets': K, 'host_pose_s_per_set': host,
+            'speedup_vs_host_poses': host / dev_s,
+            'Rgrat_first_last': [float(res[0]['Rgrat']), float(res[-1]['Rgrat'])],
+            'api': 'run_tolerances(DevicePhotons, GpuSequence, wiggle, DeviceFacetPoses, params, '
+                   'CaptureResAeff)'}
 
 
 def adjoint_bench(args, torch):
@@ -627,6 +688,8 @@ def main():
         line['adjoint'] = adjoint_bench(args, torch)
     if rank == 0 and world == 1 and not args.no_design:
         line['design'] = design_bench(args, torch)
+    if rank == 0 and world == 1 and not args.no_tolerancing:
+        line['tolerancing'] = tolerancing_bench(args, torch)
     if rank == 0 and world == 1 and not args.no_cpu:
         line['cpu_baseline'] = cpu_baseline_single()
     if rank == 0:
