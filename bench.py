@@ -224,7 +224,7 @@ def source_pipeline_bench(args, torch, inst, n, head, row_base, dist):
     from marxs_gb300.sharding import max_over_ranks
     knots, dens = configs.spectrum_knots(2)
     ap = CircleAperture(position=[12000., 0, 0], zoom=[1, 500, 500], r_inner=300.)
-    src = DeviceSource(ap, energy={'energy': knots, 'fluxdensity': dens})
+    src = DeviceSource(ap, energy={'energy': knots, 'fluxdensity': dens}, precision=head)
     seq = GpuSequence(elements=inst.elements, precision=head, rng='philox', seed=12345)
     cols = ['det_phi', 'det_y', 'order', 'facet']
     out = simulate_events(src, seq, n, cols, seed=7, row_base=row_base)
@@ -240,6 +240,7 @@ def source_pipeline_bench(args, torch, inst, n, head, row_base, dist):
     world = dist.get_world_size() if dist is not None else 1
     return {'value': world * n / s, 'unit': UNIT, 'ms_per_step': s * 1e3,
             'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': d2h,
+            'source_precision': head,
             'api': 'simulate_events(DeviceSource(CircleAperture, spectrum), GpuSequence): '
                    'generate + trace + event columns to pinned host memory, chunks of 8e6 '
                    'on two streams'}

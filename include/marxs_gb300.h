@@ -355,7 +355,12 @@ int mgpu_device_sm_count(void);
  *            pos = centre + r cos(phi) v_y + r sin(phi) v_z
  *   prob     clip(dir . -e_x, 0, 1) (aperture.py:72-76)
  * Uniforms: Philox keyed by (seed, row_base + row, 0x5000 + k) or pre-drawn
- * (draws[k * n + row], k = 0..4). */
+ * (draws[k * n + row], k = 0..4).
+ * precision MGPU_FP32LOCAL (Philox only): the same distributions with the
+ * bin chosen by integer thresholds on a 32-bit draw, float32 sines,
+ * cosines and square root (24-bit uniforms, stages 0x5003-0x5004), and
+ * float-float sums for energy and position; no float64 arithmetic but the
+ * final float-float to float64 conversion (4 adds per photon). */
 typedef struct {
     int64_t n;
     uint64_t seed, row_base;
@@ -367,7 +372,7 @@ typedef struct {
     const double* e_cdf;     /* n_bins cumulative sum of the (sorted) pdf * width */
     const int32_t* e_index;  /* n_bins sort index (identity when unsorted) */
     int32_t pol_random;      /* 1: angle = 2 pi u2; 0: pol_angle */
-    int32_t pad;
+    int32_t precision;       /* MGPU_FP64 or MGPU_FP32LOCAL */
     double pol_angle;
     double dir[3];           /* unit direction of travel */
     double pol_v1[3], pol_v2[3];
@@ -375,6 +380,12 @@ typedef struct {
     double phi0, phi1, r_inner2;
     double prob;             /* probability of every photon */
     const double* draws;     /* RNG_PREDRAWN: 5 x n uniforms */
+    /* MGPU_FP32LOCAL energy tables, n_bins entries each */
+    const float* e_lo_ff;    /* 2 n_bins: the energy at u1 = 0 of bin j (x[j - 1], or x[j]
+                                without randomize_in_bin) as float-float (hi, lo) */
+    const float* e_width_f;  /* bin widths (0 without randomize_in_bin) */
+    const uint64_t* e_thresh;/* floor(cdf[i] / cdf[last] * 2^32) + 1: entry i is the first
+                                with U < e_thresh[i], U a 32-bit draw */
 } mgpu_source;
 
 int mgpu_generate_photons(const mgpu_source* src, mgpu_vec pos, mgpu_vec dir, mgpu_vec pol,

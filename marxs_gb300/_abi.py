@@ -156,11 +156,12 @@ class MgpuSource(C.Structure):
     _fields_ = [('n', C.c_int64), ('seed', C.c_uint64), ('row_base', C.c_uint64),
                 ('rng', C.c_int32), ('n_bins', C.c_int32), ('energy', C.c_double),
                 ('e_x', C.c_void_p), ('e_width', C.c_void_p), ('e_cdf', C.c_void_p),
-                ('e_index', C.c_void_p), ('pol_random', C.c_int32), ('pad', C.c_int32),
+                ('e_index', C.c_void_p), ('pol_random', C.c_int32), ('precision', C.c_int32),
                 ('pol_angle', C.c_double), ('dir', C.c_double * 3), ('pol_v1', C.c_double * 3),
                 ('pol_v2', C.c_double * 3), ('center', C.c_double * 3), ('v_y', C.c_double * 3),
                 ('v_z', C.c_double * 3), ('phi0', C.c_double), ('phi1', C.c_double),
-                ('r_inner2', C.c_double), ('prob', C.c_double), ('draws', C.c_void_p)]
+                ('r_inner2', C.c_double), ('prob', C.c_double), ('draws', C.c_void_p),
+                ('e_lo_ff', C.c_void_p), ('e_width_f', C.c_void_p), ('e_thresh', C.c_void_p)]
 
 
 class MgpuAdjointProblem(C.Structure):

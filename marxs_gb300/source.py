@@ -15,6 +15,11 @@ straight into device columns (``DevicePhotons``), ready for
 * ``polarization``: None (unpolarized: uniform angle in [0, 2 pi)) or an angle
   in rad.
 * ``direction``: unit direction of travel (default -x, an on-axis source).
+* ``precision``: 'fp64' (float64 arithmetic; with pre-drawn uniforms the
+  columns equal the reference's to rounding) or 'fp32local' (Philox only:
+  the same distributions with float32 trigonometry and integer bin
+  thresholds; positions, energies exact to float-float, ~1e-14, the
+  aperture offsets and polarization to float32).
 """
 import ctypes as C
 import math
@@ -90,7 +95,10 @@ def _energy_table(energy):
 
 class DeviceSource:
     def __init__(self, aperture, energy=1.0, polarization=None, direction=(-1., 0., 0.),
-                 device=None):
+                 device=None, precision='fp64'):
+        if precision not in ('fp64', 'fp32local'):
+            raise ValueError("precision must be 'fp64' or 'fp32local'")
+        self.precision = precision
         self.device = torch.device('cuda', torch.cuda.current_device()) if device is None \
             else torch.device(device)
         g = aperture.geometry
@@ -126,8 +134,18 @@ class DeviceSource:
                 w = np.zeros_like(w)
             idx = np.asarray(p.sortindex if getattr(p, 'sort', True) else np.arange(len(x)),
                              dtype=np.int32)
+            cdf = np.asarray(p.cdf, dtype=float)
+            # float32-local tables: the bin's energy at u = 0 (x[index - 1],
+            # numpy's x[-1] wrap included) as float-float, widths as float32,
+            # and 32-bit thresholds of the normalised cumulative masses
+            lo = np.roll(x, 1) if getattr(p, 'randomize_in_bin', True) else x
+            hi32 = lo.astype(np.float32)
+            lo32 = (lo - hi32.astype(np.float64)).astype(np.float32)
+            thresh = np.minimum(np.floor(cdf / cdf[-1] * 2.0 ** 32) + 1, 2.0 ** 32)
+            tabs32 = [np.ascontiguousarray(np.stack([hi32, lo32], axis=1).ravel()),
+                      w.astype(np.float32), thresh.astype(np.uint64).view(np.int64)]
             self._tables = [torch.from_numpy(np.ascontiguousarray(a)).to(self.device)
-                            for a in (x, w, np.asarray(p.cdf, dtype=float), idx)]
+                            for a in [x, w, cdf, idx] + tabs32]
         return self._tables
 
     def abi(self, n, seed=0, row_base=0, draws=None):
@@ -138,7 +156,9 @@ class DeviceSource:
         S.energy = self.energy_value
         tabs = self._device_tables()
         if tabs is not None:
-            S.e_x, S.e_width, S.e_cdf, S.e_index = [t.data_ptr() for t in tabs]
+            (S.e_x, S.e_width, S.e_cdf, S.e_index, S.e_lo_ff, S.e_width_f,
+             S.e_thresh) = [t.data_ptr() for t in tabs]
+        S.precision = _abi.FP64 if self.precision == 'fp64' else _abi.FP32LOCAL
         S.pol_random = 1 if self.polarization is None else 0
         S.pol_angle = 0.0 if self.polarization is None else float(self.polarization)
         for name, v in (('dir', self.direction), ('pol_v1', self.v1), ('pol_v2', self.v2),
@@ -156,6 +176,8 @@ class DeviceSource:
         optional (5, n) float64 device tensor of uniforms (energy choice,
         in-bin, polarization angle, phi, r) instead of Philox."""
         from .gpu import DevicePhotons
+        if draws is not None and self.precision != 'fp64':
+            raise ValueError('pre-drawn uniforms need precision="fp64"')
         out = DevicePhotons(n, self.device) if out is None else out
         if draws is not None:
             draws = torch.as_tensor(draws, dtype=torch.float64, device=self.device).contiguous()

@@ -136,3 +136,35 @@ def test_simulate_events_does_not_depend_on_chunking():
             assert np.array_equal(a, b, equal_nan=a.dtype.kind == 'f'), (chunk, c)
     with pytest.raises(ValueError):
         simulate_events(src, seq, 10, ('no_such_column',))
+
+
+def test_fp32local_generation_follows_the_same_distributions():
+    """precision='fp32local' (float32 trigonometry, integer energy bins):
+    KS against the float64 generator's samples, uniform aperture radius and
+    angle and polarization angle, unit polarization, keyed by photon id."""
+    g = load_golden('source')
+    n = 400_000
+    ref = _host(_source(g).generate(n, seed=11))
+    src = _source(g, precision='fp32local')
+    out = _host(src.generate(n, seed=12))
+    assert stats.ks_2samp(out['energy'], ref['energy']).pvalue > 1e-3
+    assert np.isin(np.unique(np.floor(out['energy'] * 1e3)), np.floor(ref['energy'] * 1e3)).mean() > 0.99
+    rel = out['pos'] - src.center
+    R = np.linalg.norm(src.v_y)
+    r = np.hypot(rel @ (src.v_y / R), rel @ (src.v_z / R)) / R
+    phi = np.arctan2(rel @ (src.v_z / R), rel @ (src.v_y / R)) % (2 * np.pi)
+    ri2 = src.r_inner_norm ** 2
+    assert stats.kstest((r ** 2 - ri2) / (1 - ri2), 'uniform').pvalue > 1e-3
+    assert stats.kstest((phi - src.phi[0]) / (src.phi[1] - src.phi[0]), 'uniform').pvalue > 1e-3
+    assert np.abs(rel @ src.e_x).max() < 1e-9                       # in the aperture plane
+    ang = np.arctan2(out['polarization'] @ src.v2, out['polarization'] @ src.v1) % (2 * np.pi)
+    assert stats.kstest(ang / (2 * np.pi), 'uniform').pvalue > 1e-3
+    assert np.max(np.abs(np.linalg.norm(out['polarization'], axis=1) - 1)) < 1e-6
+    assert np.array_equal(out['dir'], ref['dir']) and np.array_equal(out['probability'],
+                                                                      ref['probability'])
+    whole = src.generate(10_000, seed=3)
+    half = src.generate(5_000, seed=3, row_base=5_000)
+    assert torch.equal(whole.pos[:, 5000:], half.pos) and torch.equal(whole.energy[5000:],
+                                                                      half.energy)
+    with pytest.raises(ValueError):
+        src.generate(10, draws=torch.zeros((5, 10), dtype=torch.float64, device='cuda'))
