@@ -29,6 +29,7 @@
 #include <cuda_runtime.h>
 #include <math.h>
 #include "mgpu_device.cuh"
+#include "mgpu_ff.cuh"
 
 namespace {
 
@@ -36,7 +37,7 @@ constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 constexpr int kTileIn = 2048;                  // photons per classify / scatter tile
 constexpr int kPerLane = kTileIn / kThreads;   // 8: each warp owns 256 consecutive photons
-constexpr int kTileSeg = 4096;                 // segment values per clipping-pass tile
+constexpr int kTileSeg = 8192;                 // segment values per clipping-pass tile
 constexpr int kSegPerThread = kTileSeg / kThreads;
 constexpr int kRadixBits = 11;
 constexpr int kBins = 1 << kRadixBits;
@@ -55,6 +56,9 @@ struct GState {
     uint64_t klo, khi;                 // current bounds as keys: kept iff klo <= key <= khi
     uint64_t pref[2];
     int64_t rank[2];
+    unsigned long long n_cand;         // candidates of the median after the first digit
+    int32_t use_ff;                    // shifted sums in float-float (deviations of moderate size)
+    int32_t pad_;
     uint32_t aeff_flags;               // 1: NaN or |p| >= 2^62, 2: +inf, 4: -inf
     int32_t pb;        // leading key bits known for both selections
     int32_t two;       // even count: the median averages ranks n/2-1 and n/2
@@ -75,11 +79,13 @@ struct Work {
     double* parts;       // [max_tseg][3]: count, sum of (x - c), sum of (x - c)^2
     uint32_t* hist;      // [G][2][kBins]
     double* seg;         // [n]
+    uint64_t* cand;      // [n] keys of the median candidates, group g from seg_base[g]
+    int64_t* ctile_base; // [G + 1] tiles of the candidate lists
     int64_t n_tin;
 };
 
 struct Layout {
-    size_t gstate, cnt, off, seg_base, tile_base, parts, hist, seg, total;
+    size_t gstate, cnt, off, seg_base, tile_base, parts, hist, seg, cand, ctile_base, total;
     int64_t n_tin, max_tseg;
 };
 
@@ -98,6 +104,8 @@ Layout layout(int64_t n, int G) {
     L.parts = o;     o = align256(o + 24 * (size_t)L.max_tseg);
     L.hist = o;      o = align256(o + 4 * (size_t)G * 2 * kBins);
     L.seg = o;       o = align256(o + 8 * (size_t)(n > 0 ? n : 1));
+    L.cand = o;      o = align256(o + 8 * (size_t)(n > 0 ? n : 1));
+    L.ctile_base = o; o = align256(o + 8 * (size_t)(G + 1));
     L.total = o;
     return L;
 }
@@ -354,6 +362,44 @@ __device__ void write_result(const mgpu_stats_problem& P, const GState& s, int g
     r[MGPU_STATS_ROUNDS] = (double)s.round;
 }
 
+// int32 -> float32 by bit construction (truncated toward zero); the
+// hardware conversion issues on the FP64 pipe of this GPU
+__device__ __forceinline__ float i2f_int(int32_t v) {
+    if (v == 0) return 0.0f;
+    const uint32_t sign = v < 0 ? 0x80000000u : 0u;
+    const uint32_t m = v < 0 ? (uint32_t)(-(int64_t)v) : (uint32_t)v;
+    const int e = 31 - __clz(m);
+    const uint32_t mant = e > 23 ? (m >> (e - 23)) : (m << (23 - e));
+    return __uint_as_float(sign | ((uint32_t)(e + 127) << 23) | (mant & 0x7fffffu));
+}
+
+// float64 -> float-float on the integer pipe: hi = d rounded to float32,
+// lo = the rest truncated to float32 (2^-47 relative); d finite with
+// 2^-74 <= |d| < 2^127 (smaller magnitudes give lo = 0)
+__device__ __forceinline__ ff d2ff_int(double d) {
+    const float hi = d2f_bits(d);
+    const uint32_t dhi = mgpu_dhi(d), dlo = mgpu_dlo(d);
+    const uint32_t e = (dhi >> 20) & 0x7ffu;
+    if (e < 949u || e > 1150u) return ff{hi, 0.0f};
+    int32_t rem = (int32_t)(dlo & 0x1fffffffu);
+    const uint32_t trunc = (((dhi << 3) | (dlo >> 29)) - 0xC0000000u) & 0x7fffffffu;
+    if ((mgpu_f2u(hi) & 0x7fffffffu) != trunc) rem -= 0x20000000;   // hi was rounded up
+    float lo = i2f_int(rem) * __uint_as_float((e - 948u) << 23);      // 2^(e - 1075)
+    if (dhi & 0x80000000u) lo = -lo;
+    return ff{hi, lo};
+}
+
+// Shifted sums in float-float: d = x - c is formed in float64 (exact for
+// x within a factor two of c), split into float-float (2^-48 relative) and
+// summed on the float32 pipes.  Used when the kept deviations |x - c| <= D
+// satisfy D = 0 or 2^-60 <= D <= 2^60: the float32 parts neither overflow
+// nor drop deviations that matter next to D.
+__device__ void choose_sums(GState& s) {
+    const double a = fabs(from_okey(s.klo) - s.c), b = fabs(from_okey(s.khi) - s.c);
+    const double D = a > b ? a : b;
+    s.use_ff = (D == 0.0 || (D >= 0x1p-60 && D <= 0x1p60)) ? 1 : 0;
+}
+
 // the radix state for a round whose kept keys lie in [klo, khi]
 __device__ void start_selection(GState& s) {
     const uint64_t a = s.klo, b = s.khi;
@@ -463,6 +509,7 @@ __global__ void center_kernel(Work W) {
         v[k] = x;
     }
     s.c = v[m / 2];
+    choose_sums(s);
 }
 
 // ---------------------------------------------------------------- clipping
@@ -487,37 +534,17 @@ __device__ __forceinline__ T warp_sum(T v) {
     return v;
 }
 
-// Histogram of the next radix digit of the kept values that carry each
-// selection's prefix.  kStats: also the count and the shifted sums of the
-// kept values (the pass runs even when the selections are resolved).
-template <bool kStats>
-__global__ void __launch_bounds__(kThreads)
-round_pass(Work W, int G) {
-    __shared__ uint32_t h[2][kBins];
-    __shared__ double s_s1[kWarps], s_s2[kWarps];
-    __shared__ long long s_cnt[kWarps];
-    int g;
-    int64_t a, b;
-    if (!seg_tile(W, G, blockIdx.x, g, a, b)) return;
-    const GState& s = W.gs[g];
-    if (!s.active || (!kStats && s.sel_done)) return;
-    const bool sel = !s.sel_done;
-    const int pb = s.pb;
-    const int width = min(kRadixBits, 64 - pb);
-    const int shift = 64 - pb - width;
-    const uint64_t dmask = (1ull << width) - 1ull;
-    const uint64_t pa = pb ? (s.pref[0] >> (64 - pb)) : 0ull;
-    const uint64_t pbv = pb ? (s.pref[1] >> (64 - pb)) : 0ull;
-    const bool split = s.split != 0;
-    const uint64_t klo = s.klo, khi = s.khi;
-    const double c = s.c;
-    if (sel) {
-        for (int k = threadIdx.x; k < 2 * kBins; k += kThreads) (&h[0][0])[k] = 0u;
-        __syncthreads();
-    }
-    long long cnt = 0;
-    double s1 = 0.0, s2 = 0.0;
+// The kept values of one tile: count, shifted sums (float-float when kFF)
+// and the first-digit histogram (when sel).  The caller branches on the
+// group's mode outside the loop, so each loop carries one kind of sum.
+template <bool kFF>
+__device__ __forceinline__ void stats_loop(const Work& W, int64_t a, int64_t b, uint64_t klo,
+                                           uint64_t khi, double c, bool sel, int pb, int shift,
+                                           uint64_t dmask, uint64_t pa, uint64_t pbv, bool split,
+                                           uint32_t* h, long long& cnt, double& s1, double& s2) {
     const int lane = threadIdx.x & 31;
+    ff f1{0.0f, 0.0f}, f2{0.0f, 0.0f};
+#pragma unroll 4
     for (int k = 0; k < kSegPerThread; ++k) {
         const int64_t i = a + (int64_t)k * kThreads + threadIdx.x;
         int bin = -1;
@@ -525,9 +552,13 @@ round_pass(Work W, int G) {
             const double x = W.seg[i];
             const uint64_t key = okey(x);
             if (key >= klo && key <= khi) {
-                if (kStats) {
-                    const double d = x - c;
-                    ++cnt;
+                ++cnt;
+                const double d = x - c;
+                if (kFF) {
+                    const ff df = d2ff_int(d);
+                    f1 = ff_add(f1, df);
+                    f2 = ff_add(f2, ff_mul(df, df));
+                } else {
                     s1 += d;
                     s2 = fma(d, d, s2);
                 }
@@ -543,10 +574,50 @@ round_pass(Work W, int G) {
             const unsigned act = __ballot_sync(MGPU_FULL_MASK, bin >= 0);
             if (bin >= 0) {
                 const unsigned peers = __match_any_sync(act, bin);
-                if (lane == __ffs(peers) - 1) atomicAdd(&(&h[0][0])[bin], (uint32_t)__popc(peers));
+                if (lane == __ffs(peers) - 1) atomicAdd(h + bin, (uint32_t)__popc(peers));
             }
         }
     }
+    if (kFF) {
+        s1 = ff2d(f1);
+        s2 = ff2d(f2);
+    }
+}
+
+// One pass per clipping round over a tile of kept values: the count and the
+// shifted sums (for the mean and the variance) and the histogram of the
+// first radix digit of the kept values that carry each selection's prefix.
+__global__ void __launch_bounds__(kThreads)
+round_pass(Work W, int G) {
+    __shared__ uint32_t h[2][kBins];
+    __shared__ double s_s1[kWarps], s_s2[kWarps];
+    __shared__ long long s_cnt[kWarps];
+    int g;
+    int64_t a, b;
+    if (!seg_tile(W, G, blockIdx.x, g, a, b)) return;
+    const GState& s = W.gs[g];
+    if (!s.active) return;
+    const bool sel = !s.sel_done;
+    const int pb = s.pb;
+    const int width = min(kRadixBits, 64 - pb);
+    const int shift = 64 - pb - width;
+    const uint64_t dmask = (1ull << width) - 1ull;
+    const uint64_t pa = pb ? (s.pref[0] >> (64 - pb)) : 0ull;
+    const uint64_t pbv = pb ? (s.pref[1] >> (64 - pb)) : 0ull;
+    const bool split = s.split != 0;
+    if (sel) {
+        for (int k = threadIdx.x; k < 2 * kBins; k += kThreads) (&h[0][0])[k] = 0u;
+        __syncthreads();
+    }
+    long long cnt = 0;
+    double s1 = 0.0, s2 = 0.0;
+    if (s.use_ff)
+        stats_loop<true>(W, a, b, s.klo, s.khi, s.c, sel, pb, shift, dmask, pa, pbv, split,
+                         &h[0][0], cnt, s1, s2);
+    else
+        stats_loop<false>(W, a, b, s.klo, s.khi, s.c, sel, pb, shift, dmask, pa, pbv, split,
+                          &h[0][0], cnt, s1, s2);
+    const int lane = threadIdx.x & 31;
     if (sel) {
         __syncthreads();
         uint32_t* gh = W.hist + (int64_t)g * 2 * kBins;
@@ -555,27 +626,146 @@ round_pass(Work W, int G) {
             if (v) atomicAdd(gh + k, v);
         }
     }
-    if (kStats) {
-        cnt = warp_sum(cnt);
-        s1 = warp_sum(s1);
-        s2 = warp_sum(s2);
-        if (lane == 0) {
-            s_cnt[threadIdx.x >> 5] = cnt;
-            s_s1[threadIdx.x >> 5] = s1;
-            s_s2[threadIdx.x >> 5] = s2;
+    cnt = warp_sum(cnt);
+    s1 = warp_sum(s1);
+    s2 = warp_sum(s2);
+    if (lane == 0) {
+        s_cnt[threadIdx.x >> 5] = cnt;
+        s_s1[threadIdx.x >> 5] = s1;
+        s_s2[threadIdx.x >> 5] = s2;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 1; k < kWarps; ++k) {
+            cnt += s_cnt[k];
+            s1 += s_s1[k];
+            s2 += s_s2[k];
+        }
+        double* p = W.parts + 3 * (int64_t)blockIdx.x;
+        p[0] = (double)cnt;
+        p[1] = s1;
+        p[2] = s2;
+    }
+}
+
+// After the first digit: copy the keys of the kept values that still carry
+// either selection's prefix into the group's candidate list (order does not
+// matter to a selection; one atomic per warp).
+__global__ void __launch_bounds__(kThreads)
+compact_pass(Work W, int G) {
+    int g;
+    int64_t a, b;
+    if (!seg_tile(W, G, blockIdx.x, g, a, b)) return;
+    GState& s = W.gs[g];
+    if (!s.active || s.sel_done) return;
+    const int pb = s.pb;   // >= 1 after the first digit
+    const uint64_t pa = s.pref[0] >> (64 - pb), pbv = s.pref[1] >> (64 - pb);
+    const uint64_t klo = s.klo, khi = s.khi;
+    uint64_t* out = W.cand + W.seg_base[g];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    __shared__ unsigned long long s_base[kWarps];
+    // count (one bit per value of this thread), one atomic per tile, write
+    uint32_t mine = 0;
+    unsigned total = 0;
+#pragma unroll 8
+    for (int k = 0; k < kSegPerThread; ++k) {
+        const int64_t i = a + (int64_t)k * kThreads + threadIdx.x;
+        bool want = false;
+        if (i < b) {
+            const uint64_t key = okey(W.seg[i]);
+            if (key >= klo && key <= khi) {
+                const uint64_t top = key >> (64 - pb);
+                want = (top == pa) || (top == pbv);
+            }
+        }
+        mine |= (want ? 1u : 0u) << k;
+        total += __popc(__ballot_sync(MGPU_FULL_MASK, want));
+    }
+    if (lane == 0) s_base[w] = total;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long run = 0;
+        for (int k = 0; k < kWarps; ++k) {
+            const unsigned long long c = s_base[k];
+            s_base[k] = run;
+            run += c;
+        }
+        const unsigned long long base = run ? atomicAdd(&s.n_cand, run) : 0ull;
+        for (int k = 0; k < kWarps; ++k) s_base[k] += base;
+    }
+    __syncthreads();
+    unsigned long long pos = s_base[w];
+    const unsigned lt = lanemask_lt();
+    for (int k = 0; k < kSegPerThread; ++k) {
+        const bool want = (mine >> k) & 1u;
+        const unsigned m = __ballot_sync(MGPU_FULL_MASK, want);
+        if (want) {
+            const int64_t i = a + (int64_t)k * kThreads + threadIdx.x;
+            out[pos + __popc(m & lt)] = okey(W.seg[i]);
+        }
+        pos += __popc(m);
+    }
+}
+
+// tiles of the candidate lists (one thread)
+__global__ void cand_setup(Work W, int G) {
+    if (threadIdx.x != 0) return;
+    int64_t run = 0;
+    for (int g = 0; g < G; ++g) {
+        W.ctile_base[g] = run;
+        const GState& s = W.gs[g];
+        if (s.active && !s.sel_done) run += ((int64_t)s.n_cand + kTileSeg - 1) / kTileSeg;
+    }
+    W.ctile_base[G] = run;
+}
+
+// later digits over the candidate lists: a persistent grid walks the
+// candidate tiles of every group
+__global__ void __launch_bounds__(kThreads)
+cand_pass(Work W, int G) {
+    __shared__ uint32_t h[2][kBins];
+    const int64_t total = W.ctile_base[G];
+    const int lane = threadIdx.x & 31;
+    for (int64_t t = blockIdx.x; t < total; t += gridDim.x) {
+        int g = 0;
+        for (int k = 1; k < G; ++k)
+            if (W.ctile_base[k] <= t) g = k;
+        const GState& s = W.gs[g];
+        if (!s.active || s.sel_done) continue;
+        const int pb = s.pb;
+        const int width = min(kRadixBits, 64 - pb);
+        const int shift = 64 - pb - width;
+        const uint64_t dmask = (1ull << width) - 1ull;
+        const uint64_t pa = s.pref[0] >> (64 - pb), pbv = s.pref[1] >> (64 - pb);
+        const bool split = s.split != 0;
+        const int64_t a = W.seg_base[g] + (t - W.ctile_base[g]) * kTileSeg;
+        const int64_t b = min(W.seg_base[g] + (int64_t)s.n_cand, a + kTileSeg);
+        for (int k = threadIdx.x; k < 2 * kBins; k += kThreads) (&h[0][0])[k] = 0u;
+        __syncthreads();
+#pragma unroll 4
+        for (int k = 0; k < kSegPerThread; ++k) {
+            const int64_t i = a + (int64_t)k * kThreads + threadIdx.x;
+            int bin = -1;
+            if (i < b) {
+                const uint64_t key = W.cand[i];
+                const uint64_t top = key >> (64 - pb);
+                const int digit = (int)((key >> shift) & dmask);
+                if (top == pa) bin = digit;
+                else if (split && top == pbv) bin = kBins + digit;
+            }
+            const unsigned act = __ballot_sync(MGPU_FULL_MASK, bin >= 0);
+            if (bin >= 0) {
+                const unsigned peers = __match_any_sync(act, bin);
+                if (lane == __ffs(peers) - 1) atomicAdd(&(&h[0][0])[bin], (uint32_t)__popc(peers));
+            }
         }
         __syncthreads();
-        if (threadIdx.x == 0) {
-            for (int k = 1; k < kWarps; ++k) {
-                cnt += s_cnt[k];
-                s1 += s_s1[k];
-                s2 += s_s2[k];
-            }
-            double* p = W.parts + 3 * (int64_t)blockIdx.x;
-            p[0] = (double)cnt;
-            p[1] = s1;
-            p[2] = s2;
+        uint32_t* gh = W.hist + (int64_t)g * 2 * kBins;
+        for (int k = threadIdx.x; k < (split ? 2 : 1) * kBins; k += kThreads) {
+            const uint32_t v = (&h[0][0])[k];
+            if (v) atomicAdd(gh + k, v);
         }
+        __syncthreads();
     }
 }
 
@@ -667,6 +857,7 @@ radix_step(const __grid_constant__ mgpu_stats_problem P, Work W) {
                 s.two = (n % 2 == 0) ? 1 : 0;
                 s.rank[1] = n / 2;
                 s.rank[0] = s.two ? n / 2 - 1 : n / 2;
+                s.n_cand = 0ull;
             }
         }
         __syncthreads();
@@ -738,6 +929,7 @@ __global__ void finalize_round(const __grid_constant__ mgpu_stats_problem P, Wor
     }
     start_selection(s);
     s.c = isnan(med) ? 0.0 : med;
+    choose_sums(s);
     s.n_prev = s.n_cur;
     s.round += 1;
 }
@@ -773,6 +965,8 @@ extern "C" int mgpu_order_stats(const mgpu_stats_problem* prob, void* stream) {
     W.parts = (double*)(base + L.parts);
     W.hist = (uint32_t*)(base + L.hist);
     W.seg = (double*)(base + L.seg);
+    W.cand = (uint64_t*)(base + L.cand);
+    W.ctile_base = (int64_t*)(base + L.ctile_base);
     W.n_tin = L.n_tin;
     cudaStream_t st = (cudaStream_t)stream;
     cudaError_t e;
@@ -791,11 +985,14 @@ extern "C" int mgpu_order_stats(const mgpu_stats_problem* prob, void* stream) {
     scatter_kernel<<<cls_blocks, kThreads, 0, st>>>(P, W);
     center_kernel<<<G, 32, 0, st>>>(W);
     const unsigned tiles = (unsigned)L.max_tseg;
+    const unsigned persistent = (unsigned)(sms * 4);
     for (int r = 0; r <= P.maxiters; ++r) {
-        round_pass<true><<<tiles, kThreads, 0, st>>>(W, G);
+        round_pass<<<tiles, kThreads, 0, st>>>(W, G);
         radix_step<true><<<G, kThreads, 0, st>>>(P, W);
+        compact_pass<<<tiles, kThreads, 0, st>>>(W, G);
+        cand_setup<<<1, 32, 0, st>>>(W, G);
         for (int lvl = 1; lvl < kLevels; ++lvl) {
-            round_pass<false><<<tiles, kThreads, 0, st>>>(W, G);
+            cand_pass<<<persistent, kThreads, 0, st>>>(W, G);
             radix_step<false><<<G, kThreads, 0, st>>>(P, W);
         }
         finalize_round<<<1, kG, 0, st>>>(P, W);
