@@ -63,6 +63,9 @@ extern "C" {
 #define MGPU_STAGE_FLATDET  3  /* FlatDetector, optics/detector.py:72-75 */
 #define MGPU_STAGE_GRATINGS 4  /* Parallel of FlatGrating/CATGrating (or one grating) */
 #define MGPU_STAGE_CYLDET   5  /* CircularDetector on a Cylinder */
+#define MGPU_STAGE_SUPPORT  6  /* catsupportbars, missions/mitsnl/catgrating.py:314-324:
+                                  probability = 0 where the id column at id_out (the facet
+                                  column) is < 0, or for every photon when id_out is NULL */
 
 /* a float64 photon column: value of photon i at ptr[i * stride] */
 typedef struct {
@@ -244,7 +247,8 @@ typedef struct {
                                     zoom_z, R, b1, b2 (angle_between borders) */
     double p[8];                 /* kind parameters, see below */
     mgpu_col out[MGPU_MAX_OUT];  /* output columns (NULL ptr = not written) */
-    void* id_out;                /* id column (int32 or int64, bit 9) or NULL */
+    void* id_out;                /* id column (int32 or int64, first_writer bit 17) or NULL;
+                                    SUPPORT reads it */
     int64_t id_stride;
     const double* draw[MGPU_MAX_DRAWS]; /* pre-drawn per-photon values (RNG_PREDRAWN) */
     int64_t draw_stride;

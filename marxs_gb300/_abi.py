@@ -50,6 +50,7 @@ STAGE_SCATTER = 2
 STAGE_FLATDET = 3
 STAGE_GRATINGS = 4
 STAGE_CYLDET = 5
+STAGE_SUPPORT = 6
 
 
 class MgpuCol(C.Structure):

@@ -40,7 +40,7 @@ def native_namespace():
         FlatGrating=optics.FlatGrating, CATGrating=optics.CATGrating,
         OrderSelector=optics.OrderSelector, EfficiencyFile=optics.EfficiencyFile,
         InterpolateEfficiencyTable=optics.InterpolateEfficiencyTable.from_grid,
-        CATL1L2Stack=optics.CATL1L2Stack,
+        CATL1L2Stack=optics.CATL1L2Stack, catsupportbars=optics.catsupportbars,
         Cylinder=optics.Cylinder, Parallel=simulator.Parallel, Sequence=simulator.Sequence,
         angle=lambda rad: rad)
 
@@ -263,7 +263,8 @@ def build_c2(ns, seed=2, efficiency_file=None, n_facets=1000, interpolated=False
     """The CAT array; ``interpolated`` gives the lens a reflectivity
     interpolator and the facets an InterpolateEfficiencyTable selector;
     ``cat_stack`` makes every facet a CATL1L2Stack (grating, quality factor,
-    L1 and L2 supports)."""
+    L1 and L2 supports) and puts catsupportbars after the array, as the
+    Arcus design does (missions/arcus/arcus.py:263-278)."""
     lens_kw = {'reflectivity_interpolator': lens_reflectivity(seed)} if interpolated else {}
     lens = ns.PerfectLens(focallength=12000., position=[12000., 0, 0], zoom=[1, 600, 600],
                           **lens_kw)
@@ -296,7 +297,8 @@ def build_c2(ns, seed=2, efficiency_file=None, n_facets=1000, interpolated=False
     cyl = ns.Cylinder.from_rowland(torus, 50., rotation=np.pi,
                                    kwargs={'phi_lim': [-np.pi / 2, np.pi / 2]})
     det = ns.CircularDetector(geometry=cyl, pixsize=0.024)
-    return SimpleNamespace(elements=[lens, rms, gas, det], lens=lens, scatter=rms, gas=gas,
+    elements = [lens, rms, gas, ns.catsupportbars, det] if cat_stack else [lens, rms, gas, det]
+    return SimpleNamespace(elements=elements, lens=lens, scatter=rms, gas=gas,
                            detector=det, selector=eff, efficiency_table=table,
                            draw_slots=[(rms, 'scatter'), (gas, 'catstack' if cat_stack else 'order')],
                            aperture_x=12000.)

@@ -636,6 +636,17 @@ __device__ __forceinline__ bool run_stage_l(const mgpu_stage& st, PhotonL& ph, i
         return valid && stage_flatdet_l(st, ph, i);
     case MGPU_STAGE_CYLDET:
         return valid && stage_cyldet_l(st, ph, i);
+    case MGPU_STAGE_SUPPORT:
+        // catsupportbars (missions/mitsnl/catgrating.py:314-324)
+        if (valid) {
+            bool absorb = true;
+            if (st.id_out)
+                absorb = (((st.first_writer >> 17) & 1)
+                              ? ((const int64_t*)st.id_out)[i * st.id_stride]
+                              : (int64_t)((const int32_t*)st.id_out)[i * st.id_stride]) < 0;
+            if (absorb) ph.prob = 0.0f;
+        }
+        return false;
     default:
         if (valid) atomicOr(chain.status, MGPU_STATUS_BAD_STAGE);
         return false;
@@ -748,7 +759,7 @@ cudaError_t mgpu_launch_chain_fp32local(const mgpu_chain& chain, const mgpu_phot
     if (io.n <= 0) return cudaSuccess;
     for (int s = 0; s < chain.n_stages; ++s) {
         const mgpu_stage& st = chain.stages[s];
-        if (st.aux == nullptr) return cudaErrorInvalidValue;
+        if (st.aux == nullptr && st.kind != MGPU_STAGE_SUPPORT) return cudaErrorInvalidValue;
         if (st.kind == MGPU_STAGE_GRATINGS &&
             (st.facets32 == nullptr || st.cand32 == nullptr || ((uintptr_t)st.cand32 & 15u) != 0))
             return cudaErrorInvalidValue;

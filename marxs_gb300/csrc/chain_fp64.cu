@@ -77,6 +77,15 @@ __device__ __forceinline__ void write_miss_defaults(const mgpu_stage& st, int64_
     if (st.id_out && ((st.first_writer >> 16) & 1)) store_id(st, i, -1);
 }
 
+// catsupportbars (missions/mitsnl/catgrating.py:314-324): a photon that
+// passed no facet is absorbed by the support structure
+__device__ __forceinline__ bool support_absorbs(const mgpu_stage& st, int64_t i) {
+    if (!st.id_out) return true;
+    const int64_t v = ((st.first_writer >> 17) & 1) ? ((const int64_t*)st.id_out)[i * st.id_stride]
+                                                    : ((const int32_t*)st.id_out)[i * st.id_stride];
+    return v < 0;
+}
+
 __device__ __forceinline__ void check_prob(double f, uint32_t* status) {
     if (f < 0.0 || f > 1.0) atomicOr(status, MGPU_STATUS_PROB_RANGE);
 }
@@ -482,6 +491,9 @@ chain_fp64_kernel(const __grid_constant__ mgpu_chain chain, const __grid_constan
                 break;
             case MGPU_STAGE_CYLDET:
                 if (valid) hit = stage_cyldet(st, ph, i);
+                break;
+            case MGPU_STAGE_SUPPORT:
+                if (valid && support_absorbs(st, i)) ph.prob = 0.0;
                 break;
             default:
                 if (valid) atomicOr(chain.status, MGPU_STATUS_BAD_STAGE);

@@ -259,6 +259,9 @@ class ColumnPlan:
                     self.columns[st.id_col] = 'i4'
                     if st.id_col not in existing:
                         self.first_writer[st.id_col] = si
+            reads = getattr(st, 'reads', None)
+            if reads is not None and reads not in self.columns and reads in existing:
+                self.columns[reads] = 'i4'          # read from the table, never written
             self.order.append([c for c in st.new_col_order if c is not None])
 
 
@@ -344,6 +347,14 @@ class GpuSequence:
                 s.id_stride = 1
                 if plan.first_writer.get(st.id_col) == si:
                     fw |= 1 << 16
+                if idb.dtype == torch.int64:
+                    fw |= 1 << 17
+            if st.kind == _abi.STAGE_SUPPORT and st.reads in bufs:
+                idb = bufs[st.reads]
+                if idb.dtype not in (torch.int32, torch.int64):
+                    raise ValueError('catsupportbars needs an integer %r column' % st.reads)
+                s.id_out = idb.data_ptr()
+                s.id_stride = idb.stride(0)
                 if idb.dtype == torch.int64:
                     fw |= 1 << 17
             s.first_writer = fw

@@ -162,6 +162,7 @@ class StageSpec:
     grid: Optional[dict] = None
     spline: Optional[tuple] = None   # LENS reflectivity (tx, ty, c[1, ...])
     stack: Optional[dict] = None     # GRATINGS of CATL1L2Stack facets: layer constants
+    reads: Optional[str] = None      # SUPPORT: the id column it reads
 
 
 def _loc_names(elem):
@@ -382,7 +383,16 @@ def _cat_stack_stage(owner, stacks, id_col):
     return st
 
 
+def is_support_bars(e):
+    """catsupportbars (missions/mitsnl/catgrating.py:314-324), the reference's
+    function or this package's."""
+    return callable(e) and getattr(e, '__name__', None) == 'catsupportbars' and \
+        not hasattr(e, 'geometry')
+
+
 def _lower_one(e):
+    if is_support_bars(e):
+        return [StageSpec(kind=_abi.STAGE_SUPPORT, element=e, reads='facet')]
     names = classnames(e)
     if 'Parallel' in names:
         id_col = None

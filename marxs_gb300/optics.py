@@ -418,3 +418,16 @@ __all__ = ['GeometryError', 'FinitePlane', 'Cylinder', 'OrderSelector', 'Efficie
            'PerfectLens', 'RadialMirrorScatter', 'FlatDetector', 'CircularDetector',
            'FlatGrating', 'CATGrating', 'NonParallelCATGrating', 'QualityFactor', 'L1', 'L2Abs',
            'L2Diffraction', 'FlatStack', 'CATL1L2Stack', 'InterpolateEfficiencyTable']
+
+
+def catsupportbars(photons):
+    """Metal support of the CAT facets (missions/mitsnl/catgrating.py:314-324):
+    photons that passed no facet (``facet`` < 0) are absorbed; without a
+    ``facet`` column every photon is.  On the GPU it is a chain stage; this
+    host function acts on a photon table directly."""
+    if 'facet' in photons.colnames:
+        prob = photons['probability']
+        prob[np.asarray(photons['facet']) < 0] = 0.
+    else:
+        photons['probability'][...] = 0.
+    return photons

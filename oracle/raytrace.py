@@ -592,7 +592,20 @@ def run_sequence(elements, photons, draws=None, stats=None):
     return photons, stats
 
 
+def support_bars(photons):
+    """catsupportbars, missions/mitsnl/catgrating.py:314-324: probability 0
+    where facet < 0, or everywhere without a facet column."""
+    if 'facet' in photons:
+        photons['probability'][np.asarray(photons['facet']) < 0] = 0.
+    else:
+        photons['probability'][...] = 0.
+    return photons
+
+
 def _run_any(elem, photons, draws, stats):
+    if callable(elem) and getattr(elem, '__name__', None) == 'catsupportbars' and \
+            not hasattr(elem, 'geometry'):
+        return support_bars(photons)
     names = _classnames(elem)
     if 'Parallel' in names:
         return run_parallel(elem, photons, draws, stats)

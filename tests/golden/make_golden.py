@@ -150,8 +150,9 @@ def reference_namespace(marxs):
                     self.elements[2].transfunc = interp1d(*l1_transmission)
         return Stack
 
+    from marxs.missions.mitsnl.catgrating import catsupportbars
     return SimpleNamespace(PerfectLens=PerfectLens, RadialMirrorScatter=RadialMirrorScatter,
-                           CATL1L2Stack=cat_stack_class(),
+                           CATL1L2Stack=cat_stack_class(), catsupportbars=catsupportbars,
                            FlatDetector=FlatDetector, CircularDetector=CircularDetector,
                            FlatGrating=FlatGrating, CATGrating=CATGrating,
                            OrderSelector=OrderSelector, EfficiencyFile=eff,
@@ -180,7 +181,8 @@ def generate(name):
 
     rec = Recorder()
     for e in leaves(inst.elements):
-        rec.wrap(e)
+        if hasattr(e, 'specific_process_photons'):      # not the plain-function elements
+            rec.wrap(e)
     seq = ns.Sequence(elements=inst.elements)
     np.random.seed(GLOBAL_SEED + zlib.crc32(name.encode()) % 1000)
     rec.install()

@@ -111,3 +111,43 @@ def test_cat_stack_columns_and_fp32_local_refusal():
     with pytest.raises(NotImplementedError, match='fp64'):
         GpuSequence(inst.elements, precision='fp32local', rng='philox')(
             PhotonTable(golden_inputs(g)))
+
+
+def test_catsupportbars_stage():
+    """catsupportbars as a chain stage: probability 0 where facet < 0, the
+    rest unchanged (float64 and FP32-local, device and table paths); with
+    no facet column every photon is absorbed; an int64 facet column that
+    the input table already holds is read."""
+    from marxs_gb300 import configs, PhotonTable
+    from marxs_gb300.gpu import DevicePhotons, GpuSequence
+    from marxs_gb300.optics import catsupportbars
+    import torch
+    inst = configs.build('c2')
+    n = 50_000
+    host = configs.photons_for('c2', n, seed=3)
+    for prec in ('fp64', 'fp32local'):
+        res = {}
+        for key, elems in (('plain', inst.elements),
+                           ('bars', inst.elements[:3] + [catsupportbars] + inst.elements[3:])):
+            seq = GpuSequence(elems, precision=prec, rng='philox', seed=5)
+            ph = DevicePhotons.from_columns(host)
+            plan, bufs = seq.allocate_columns(n)
+            status, _ = seq.trace_device(ph, ph, plan, bufs)
+            torch.cuda.synchronize()
+            assert int(status.item()) == 0
+            res[key] = (ph.prob.cpu().numpy(), bufs['facet'].cpu().numpy())
+        (p0, f0), (p1, f1) = res['plain'], res['bars']
+        assert np.array_equal(f0, f1)
+        assert np.array_equal(p1[f1 >= 0], p0[f0 >= 0]) and np.all(p1[f1 < 0] == 0)
+        assert (f1 < 0).any() and (f1 >= 0).any()
+    # no facet column: everything absorbed
+    t = PhotonTable({k: np.array(v, copy=True) for k, v in host.items()})
+    GpuSequence([inst.lens, catsupportbars], precision='fp64', rng='philox')(t)
+    assert np.all(np.asarray(t['probability']) == 0)
+    # a facet column already in the table
+    t = PhotonTable({k: np.array(v, copy=True) for k, v in host.items()})
+    t['facet'] = np.where(np.arange(n) % 3 == 0, -1, 7).astype(np.int64)
+    GpuSequence([catsupportbars], precision='fp64', rng='philox')(t)
+    p = np.asarray(t['probability'])
+    assert np.all(p[np.arange(n) % 3 == 0] == 0)
+    assert np.array_equal(p[np.arange(n) % 3 != 0], host['probability'][np.arange(n) % 3 != 0])

@@ -98,3 +98,20 @@ def test_oracle_runs_reference_objects(reference_marxs, name):
     ref = golden_outputs(g)
     for col, b in ref.items():
         assert np.array_equal(out[col], b, equal_nan=True), col
+
+
+def test_catsupportbars_semantics():
+    """catsupportbars (missions/mitsnl/catgrating.py:314-324) in the oracle and
+    this package's host function: facet < 0 absorbs; no facet column
+    absorbs every photon."""
+    from marxs_gb300 import PhotonTable
+    from marxs_gb300.optics import catsupportbars
+    from oracle.raytrace import support_bars
+    prob = np.array([0.5, 1.0, 0.25, 0.75])
+    ph = {'probability': prob.copy(), 'facet': np.array([3, -1, 0, -1])}
+    assert np.array_equal(support_bars(ph)['probability'], [0.5, 0.0, 0.25, 0.0])
+    assert np.array_equal(support_bars({'probability': prob.copy()})['probability'], np.zeros(4))
+    t = PhotonTable({'probability': prob.copy(), 'facet': np.array([3, -1, 0, -1])})
+    assert np.array_equal(np.asarray(catsupportbars(t)['probability']), [0.5, 0.0, 0.25, 0.0])
+    t = PhotonTable({'probability': prob.copy()})
+    assert np.array_equal(np.asarray(catsupportbars(t)['probability']), np.zeros(4))
