@@ -25,7 +25,16 @@
 
 namespace {
 
-constexpr int kThreads = 256;
+// block size and the minimum resident blocks per SM the register
+// allocation is bounded for (compile-time; see the launch below)
+#ifndef MGPU_FP32L_THREADS
+#define MGPU_FP32L_THREADS 256
+#endif
+#ifndef MGPU_FP32L_MIN_BLOCKS
+#define MGPU_FP32L_MIN_BLOCKS 3
+#endif
+constexpr int kThreads = MGPU_FP32L_THREADS;
+constexpr int kMinBlocks = MGPU_FP32L_MIN_BLOCKS;
 
 struct PhotonL {
     ff3 pos;
@@ -696,8 +705,9 @@ struct FixedChain {
 
 template <class Chain>
 // 3 blocks of 256 per SM (<= 84 registers): measured 4 % faster than the
-// unconstrained allocation (100 registers, 2 blocks)
-__global__ void __launch_bounds__(kThreads, 3)
+// unconstrained allocation (100 registers, 2 blocks) and 5-15 % faster than
+// 128 x 6/7/8 or 256 x 4 (register spills)
+__global__ void __launch_bounds__(kThreads, kMinBlocks)
 chain_fp32local_kernel(const __grid_constant__ mgpu_chain chain, const __grid_constant__ mgpu_photons io) {
     __shared__ unsigned int s_hits[MGPU_MAX_STAGES];
     if (threadIdx.x < MGPU_MAX_STAGES) s_hits[threadIdx.x] = 0;
@@ -751,6 +761,9 @@ chain_fp32local_kernel(const __grid_constant__ mgpu_chain chain, const __grid_co
 using ChainCat = FixedChain<MGPU_STAGE_LENS, MGPU_STAGE_SCATTER, MGPU_STAGE_GRATINGS, MGPU_STAGE_CYLDET>;
 using ChainSpec = FixedChain<MGPU_STAGE_LENS, MGPU_STAGE_SCATTER, MGPU_STAGE_GRATINGS, MGPU_STAGE_FLATDET>;
 using ChainTel = FixedChain<MGPU_STAGE_LENS, MGPU_STAGE_SCATTER, MGPU_STAGE_FLATDET>;
+// the CAT array followed by its support structure (catsupportbars)
+using ChainCatBars = FixedChain<MGPU_STAGE_LENS, MGPU_STAGE_SCATTER, MGPU_STAGE_GRATINGS,
+                                MGPU_STAGE_SUPPORT, MGPU_STAGE_CYLDET>;
 
 }  // namespace
 
@@ -767,7 +780,7 @@ cudaError_t mgpu_launch_chain_fp32local(const mgpu_chain& chain, const mgpu_phot
     }
     int64_t warps = (io.n + 31) / 32;
     int64_t blocks = (warps * 32 + kThreads - 1) / kThreads;
-    int64_t cap = (int64_t)sm_count * 8;
+    int64_t cap = (int64_t)sm_count * 8 * (256 / kThreads);
     if (blocks > cap) blocks = cap;
     if (ChainCat::matches(chain))
         chain_fp32local_kernel<ChainCat><<<(unsigned)blocks, kThreads, 0, stream>>>(chain, io);
@@ -775,6 +788,8 @@ cudaError_t mgpu_launch_chain_fp32local(const mgpu_chain& chain, const mgpu_phot
         chain_fp32local_kernel<ChainSpec><<<(unsigned)blocks, kThreads, 0, stream>>>(chain, io);
     else if (ChainTel::matches(chain))
         chain_fp32local_kernel<ChainTel><<<(unsigned)blocks, kThreads, 0, stream>>>(chain, io);
+    else if (ChainCatBars::matches(chain))
+        chain_fp32local_kernel<ChainCatBars><<<(unsigned)blocks, kThreads, 0, stream>>>(chain, io);
     else
         chain_fp32local_kernel<GenericChain><<<(unsigned)blocks, kThreads, 0, stream>>>(chain, io);
     return cudaGetLastError();
