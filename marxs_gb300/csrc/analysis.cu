@@ -182,10 +182,24 @@ __device__ __forceinline__ double fixed_to_double(unsigned long long lo, unsigne
 
 // order keys of the requested groups: float64 bit patterns (-0.0 as 0.0)
 // for a float column, the integer value for an integer column (valid bit
-// clear for a non-integral order)
-__device__ void load_orders(const mgpu_stats_problem& P, uint64_t* s_key, uint64_t* s_valid) {
+// clear for a non-integral order).  Orders that are integers in
+// [-kLutHalf, kLutHalf] also go into a lookup table (first group wins);
+// *s_all_lut says that every valid order is there, so a photon whose order
+// is not a small integer matches no group.
+constexpr int kLutHalf = 64;
+
+struct OrderLut {
+    int16_t g[2 * kLutHalf + 1];
+    int all;
+};
+
+__device__ void load_orders(const mgpu_stats_problem& P, uint64_t* s_key, uint64_t* s_valid,
+                            OrderLut* lut) {
+    for (int k = threadIdx.x; k < 2 * kLutHalf + 1; k += blockDim.x) lut->g[k] = -1;
+    __syncthreads();
     if (threadIdx.x == 0) {
         uint64_t valid = 0;
+        int all = 1;
         for (int k = 0; k < P.n_groups; ++k) {
             const double o = P.orders[k];
             uint64_t key = 0;
@@ -199,11 +213,39 @@ __device__ void load_orders(const mgpu_stats_problem& P, uint64_t* s_key, uint64
                 key = ok ? (uint64_t)(long long)o : 0;
             }
             s_key[k] = key;
-            if (ok) valid |= 1ull << k;
+            if (ok) {
+                valid |= 1ull << k;
+                if (o == floor(o) && fabs(o) <= (double)kLutHalf) {
+                    const int idx = (int)o + kLutHalf;
+                    if (lut->g[idx] < 0) lut->g[idx] = (int16_t)k;
+                } else {
+                    all = 0;
+                }
+            }
         }
         *s_valid = valid;
+        lut->all = all;
     }
     __syncthreads();
+}
+
+// a float64 as an integer in [-kLutHalf, kLutHalf] (integer operations):
+// false when it is not such an integer
+__device__ __forceinline__ bool small_int_bits(uint64_t b, int* v) {
+    const uint64_t mag = b & ~kSign;
+    if (mag == 0) {
+        *v = 0;
+        return true;
+    }
+    const int e = (int)(mag >> 52) - 1023;
+    if (e < 0 || e > 6) return false;
+    const uint64_t m = (mag & 0xfffffffffffffull) | (1ull << 52);
+    const int sh = 52 - e;
+    if (m & ((1ull << sh) - 1ull)) return false;
+    int x = (int)(m >> sh);
+    if (x > kLutHalf) return false;
+    *v = (b >> 63) ? -x : x;
+    return true;
 }
 
 __device__ __forceinline__ uint64_t order_key(const mgpu_stats_problem& P, int64_t i) {
@@ -227,7 +269,8 @@ struct Photon {
 };
 
 __device__ __forceinline__ Photon classify(const mgpu_stats_problem& P, int64_t i,
-                                           const uint64_t* s_key, uint64_t valid) {
+                                           const uint64_t* s_key, uint64_t valid,
+                                           const OrderLut* lut) {
     Photon ph{-1, false, false, false, 0ull, 0ull};
     if (i >= P.n) return ph;
     int g = -1;
@@ -235,8 +278,22 @@ __device__ __forceinline__ Photon classify(const mgpu_stats_problem& P, int64_t 
         g = 0;
     } else {
         const uint64_t key = order_key(P, i);
-        for (int k = P.n_groups - 1; k >= 0; --k)
-            if (((valid >> k) & 1ull) && s_key[k] == key) g = k;
+        int v;
+        bool small;
+        if (P.order_type == MGPU_ORDER_F64) {
+            small = small_int_bits(key, &v);
+        } else {
+            const int64_t iv = (int64_t)key;
+            small = iv >= -kLutHalf && iv <= kLutHalf;
+            v = (int)iv;
+        }
+        // a small integer can only equal an order in the table
+        if (small) {
+            g = lut->g[v + kLutHalf];
+        } else if (!lut->all) {
+            for (int k = P.n_groups - 1; k >= 0; --k)
+                if (((valid >> k) & 1ull) && s_key[k] == key) g = k;
+        }
     }
     if (g < 0) return ph;
     ph.g = g;
@@ -263,6 +320,7 @@ __global__ void __launch_bounds__(kThreads)
 classify_kernel(const __grid_constant__ mgpu_stats_problem P, Work W) {
     __shared__ uint64_t s_key[kG];
     __shared__ uint64_t s_valid;
+    __shared__ OrderLut s_lut;
     __shared__ int32_t tcnt[kG];
     __shared__ unsigned long long s_mem[kG], s_lo[kG], s_hi[kG], s_kmin_inv[kG], s_kmax[kG];
     __shared__ uint32_t s_flags[kG];
@@ -273,12 +331,12 @@ classify_kernel(const __grid_constant__ mgpu_stats_problem P, Work W) {
         s_mem[k] = s_lo[k] = s_hi[k] = s_kmin_inv[k] = s_kmax[k] = 0ull;
         s_flags[k] = 0u;
     }
-    load_orders(P, s_key, &s_valid);
+    load_orders(P, s_key, &s_valid, &s_lut);
     const uint64_t valid = s_valid;
     for (int64_t t = blockIdx.x; t < W.n_tin; t += gridDim.x) {
         const int64_t base = t * kTileIn + (int64_t)w * (kPerLane * 32);
         for (int k = 0; k < kPerLane; ++k) {
-            const Photon ph = classify(P, base + k * 32 + lane, s_key, valid);
+            const Photon ph = classify(P, base + k * 32 + lane, s_key, valid, &s_lut);
             const unsigned sp = __match_any_sync(MGPU_FULL_MASK, ph.seg ? ph.g : -1);
             if (ph.seg && lane == __ffs(sp) - 1) atomicAdd(&tcnt[ph.g], __popc(sp));
             const unsigned mp = __match_any_sync(MGPU_FULL_MASK, ph.member ? ph.g : -1);
@@ -444,12 +502,13 @@ __global__ void __launch_bounds__(kThreads)
 scatter_kernel(const __grid_constant__ mgpu_stats_problem P, Work W) {
     __shared__ uint64_t s_key[kG];
     __shared__ uint64_t s_valid;
+    __shared__ OrderLut s_lut;
     __shared__ int32_t wcnt[kWarps][kG];
     __shared__ int64_t wbase[kWarps][kG];
     const int G = P.n_groups;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (int k = threadIdx.x; k < kWarps * kG; k += kThreads) (&wcnt[0][0])[k] = 0;
-    load_orders(P, s_key, &s_valid);
+    load_orders(P, s_key, &s_valid, &s_lut);
     const uint64_t valid = s_valid;
     for (int64_t t = blockIdx.x; t < W.n_tin; t += gridDim.x) {
         const int64_t base = t * kTileIn + (int64_t)w * (kPerLane * 32);
@@ -458,7 +517,7 @@ scatter_kernel(const __grid_constant__ mgpu_stats_problem P, Work W) {
         unsigned pk[kPerLane];
 #pragma unroll
         for (int k = 0; k < kPerLane; ++k) {
-            const Photon ph = classify(P, base + k * 32 + lane, s_key, valid);
+            const Photon ph = classify(P, base + k * 32 + lane, s_key, valid, &s_lut);
             gk[k] = ph.seg ? ph.g : -1;
             vk[k] = ph.vb;
             pk[k] = __match_any_sync(MGPU_FULL_MASK, gk[k]);

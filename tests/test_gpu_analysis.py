@@ -229,3 +229,22 @@ def test_capture_on_traced_device_columns():
         _close(np.atleast_1d(np.ma.filled(np.ma.asarray(out[k], dtype=float), np.nan)),
                np.atleast_1d(np.ma.filled(np.ma.asarray(ref[k], dtype=float), np.nan)), rel, 1e-12)
     assert np.nanmax(out['R']) > 100
+
+
+def test_order_matching_beyond_the_small_integer_table():
+    """Orders outside [-64, 64] and non-integral orders go through the
+    linear match; integer and float columns agree with the oracle."""
+    from marxs_gb300.analysis import order_stats
+    rng = np.random.default_rng(12)
+    n = 60_000
+    pool = np.array([-100., -3., 0., 2.5, 7., 64., 65., 1e6])
+    order = rng.choice(pool, n)
+    x = rng.normal(0, 1, n) + order
+    prob = rng.random(n)
+    orders = [65., -3., 2.5, 1e6, 64., 0., -100., 7., 8.]
+    got = order_stats(x, order, orders, probability=prob)
+    _compare(got, _oracle_rows(order, x, prob, orders))
+    iorder = np.where(np.isin(order, [2.5]), 99, order).astype(np.int64)
+    iorders = [65, -3, 99, 1000000, 64, 0, -100, 7, 2.5]
+    got = order_stats(x, iorder, iorders, probability=prob)
+    _compare(got, _oracle_rows(iorder, x, prob, iorders))
