@@ -41,6 +41,8 @@ constexpr int kTileSeg = 8192;                 // segment values per clipping-pa
 constexpr int kSegPerThread = kTileSeg / kThreads;
 constexpr int kRadixBits = 11;
 constexpr int kBins = 1 << kRadixBits;
+constexpr int kVBins = 8192;                   // value bins of the first level
+constexpr int kHist = kVBins > 2 * kBins ? kVBins : 2 * kBins;   // per-group histogram words
 constexpr int kLevels = 6;                     // ceil(64 / 11)
 constexpr int kCenterSample = 31;              // values whose median centres round 0's sums
 constexpr int kG = MGPU_STATS_MAX_GROUPS;
@@ -57,7 +59,10 @@ struct GState {
     uint64_t pref[2];
     int64_t rank[2];
     unsigned long long n_cand;         // candidates of the median after the first digit
+    unsigned long long cmin_inv, cmax; // key range of the candidates (~min, max)
     int32_t use_ff;                    // shifted sums in float-float (deviations of moderate size)
+    float voff, vinv;                  // first level: value bin of x from d = x - c (value_bin)
+    int32_t vb[2];                     // the value bins holding the two ranks
     int32_t pad_;
     uint32_t aeff_flags;               // 1: NaN or |p| >= 2^62, 2: +inf, 4: -inf
     int32_t pb;        // leading key bits known for both selections
@@ -77,7 +82,7 @@ struct Work {
     int64_t* seg_base;   // [G + 1]
     int64_t* tile_base;  // [G + 1]
     double* parts;       // [max_tseg][3]: count, sum of (x - c), sum of (x - c)^2
-    uint32_t* hist;      // [G][2][kBins]
+    uint32_t* hist;      // [G][kHist]: the value level, or two key-digit histograms
     double* seg;         // [n]
     uint64_t* cand;      // [n] keys of the median candidates, group g from seg_base[g]
     int64_t* ctile_base; // [G + 1] tiles of the candidate lists
@@ -102,7 +107,7 @@ Layout layout(int64_t n, int G) {
     L.seg_base = o;  o = align256(o + 8 * (size_t)(G + 1));
     L.tile_base = o; o = align256(o + 8 * (size_t)(G + 1));
     L.parts = o;     o = align256(o + 24 * (size_t)L.max_tseg);
-    L.hist = o;      o = align256(o + 4 * (size_t)G * 2 * kBins);
+    L.hist = o;      o = align256(o + 4 * (size_t)G * kHist);
     L.seg = o;       o = align256(o + 8 * (size_t)(n > 0 ? n : 1));
     L.cand = o;      o = align256(o + 8 * (size_t)(n > 0 ? n : 1));
     L.ctile_base = o; o = align256(o + 8 * (size_t)(G + 1));
@@ -458,15 +463,34 @@ __device__ void choose_sums(GState& s) {
     s.use_ff = (D == 0.0 || (D >= 0x1p-60 && D <= 0x1p60)) ? 1 : 0;
 }
 
-// the radix state for a round whose kept keys lie in [klo, khi]
+// First level of the median selection, in the value domain: bins linear
+// in x over [vlo, vhi] (kVBins - 2 inner bins; bin 0 and kVBins - 1 also take
+// what lies below and above).  The bin is formed in float32 from the
+// float64 deviation d = x - c, a monotone map of x, so the kept values of
+// a bin interval are a contiguous run of the sorted values.
+__device__ void set_value_bins(GState& s, double vlo, double vhi) {
+    const double range = vhi - vlo;
+    const double inv = (double)(kVBins - 2) / range;
+    const bool ok = isfinite(vlo) && isfinite(vhi) && range > 0.0 && isfinite(inv) &&
+                    inv < 1e37;
+    s.voff = ok ? __double2float_rn(vlo - s.c) : 0.0f;
+    s.vinv = ok ? __double2float_rn(inv) : 0.0f;
+}
+
+__device__ __forceinline__ int value_bin(double d, float voff, float vinv) {
+    if (vinv == 0.0f) return 1;
+    const float t = (d2f_bits(d) - voff) * vinv;
+    if (!(t >= 0.0f)) return 0;
+    if (t >= (float)(kVBins - 2)) return kVBins - 1;
+    return (int)t + 1;
+}
+
+// the selection state at the start of a round: the value level comes first
 __device__ void start_selection(GState& s) {
-    const uint64_t a = s.klo, b = s.khi;
-    const int cp = (a == b) ? 64 : __clzll((long long)(a ^ b));
-    const uint64_t mask = cp == 0 ? 0ull : (cp == 64 ? ~0ull : (~0ull << (64 - cp)));
-    s.pref[0] = s.pref[1] = a & mask;
-    s.pb = cp;
+    s.pref[0] = s.pref[1] = 0ull;
+    s.pb = 0;
     s.split = 0;
-    s.sel_done = cp == 64 ? 1 : 0;
+    s.sel_done = 0;
 }
 
 // segment bases, tile bases, effective areas and the round-0 state of every group
@@ -569,6 +593,11 @@ __global__ void center_kernel(Work W) {
     }
     s.c = v[m / 2];
     choose_sums(s);
+    // round 0's value bins: the sample median -/+ 4 interquartile ranges,
+    // or the group's whole range when the sample has no spread
+    const double w = 4.0 * (v[(3 * m) / 4] - v[m / 4]);
+    if (w > 0.0 && isfinite(w)) set_value_bins(s, s.c - w, s.c + w);
+    else set_value_bins(s, from_okey(s.klo), from_okey(s.khi));
 }
 
 // ---------------------------------------------------------------- clipping
@@ -598,9 +627,9 @@ __device__ __forceinline__ T warp_sum(T v) {
 // group's mode outside the loop, so each loop carries one kind of sum.
 template <bool kFF>
 __device__ __forceinline__ void stats_loop(const Work& W, int64_t a, int64_t b, uint64_t klo,
-                                           uint64_t khi, double c, bool sel, int pb, int shift,
-                                           uint64_t dmask, uint64_t pa, uint64_t pbv, bool split,
-                                           uint32_t* h, long long& cnt, double& s1, double& s2) {
+                                           uint64_t khi, double c, bool sel, float voff,
+                                           float vinv, uint32_t* h, long long& cnt, double& s1,
+                                           double& s2) {
     const int lane = threadIdx.x & 31;
     ff f1{0.0f, 0.0f}, f2{0.0f, 0.0f};
 #pragma unroll 4
@@ -621,12 +650,7 @@ __device__ __forceinline__ void stats_loop(const Work& W, int64_t a, int64_t b, 
                     s1 += d;
                     s2 = fma(d, d, s2);
                 }
-                if (sel) {
-                    const uint64_t top = pb ? (key >> (64 - pb)) : 0ull;
-                    const int digit = (int)((key >> shift) & dmask);
-                    if (top == pa) bin = digit;
-                    else if (split && top == pbv) bin = kBins + digit;
-                }
+                if (sel) bin = value_bin(d, voff, vinv);
             }
         }
         if (sel) {
@@ -648,7 +672,7 @@ __device__ __forceinline__ void stats_loop(const Work& W, int64_t a, int64_t b, 
 // first radix digit of the kept values that carry each selection's prefix.
 __global__ void __launch_bounds__(kThreads)
 round_pass(Work W, int G) {
-    __shared__ uint32_t h[2][kBins];
+    __shared__ uint32_t h[1][kVBins];
     __shared__ double s_s1[kWarps], s_s2[kWarps];
     __shared__ long long s_cnt[kWarps];
     int g;
@@ -657,30 +681,22 @@ round_pass(Work W, int G) {
     const GState& s = W.gs[g];
     if (!s.active) return;
     const bool sel = !s.sel_done;
-    const int pb = s.pb;
-    const int width = min(kRadixBits, 64 - pb);
-    const int shift = 64 - pb - width;
-    const uint64_t dmask = (1ull << width) - 1ull;
-    const uint64_t pa = pb ? (s.pref[0] >> (64 - pb)) : 0ull;
-    const uint64_t pbv = pb ? (s.pref[1] >> (64 - pb)) : 0ull;
-    const bool split = s.split != 0;
     if (sel) {
-        for (int k = threadIdx.x; k < 2 * kBins; k += kThreads) (&h[0][0])[k] = 0u;
+        for (int k = threadIdx.x; k < kVBins; k += kThreads) h[0][k] = 0u;
         __syncthreads();
     }
     long long cnt = 0;
     double s1 = 0.0, s2 = 0.0;
     if (s.use_ff)
-        stats_loop<true>(W, a, b, s.klo, s.khi, s.c, sel, pb, shift, dmask, pa, pbv, split,
-                         &h[0][0], cnt, s1, s2);
+        stats_loop<true>(W, a, b, s.klo, s.khi, s.c, sel, s.voff, s.vinv, &h[0][0], cnt, s1, s2);
     else
-        stats_loop<false>(W, a, b, s.klo, s.khi, s.c, sel, pb, shift, dmask, pa, pbv, split,
-                          &h[0][0], cnt, s1, s2);
+        stats_loop<false>(W, a, b, s.klo, s.khi, s.c, sel, s.voff, s.vinv, &h[0][0], cnt, s1,
+                          s2);
     const int lane = threadIdx.x & 31;
     if (sel) {
         __syncthreads();
-        uint32_t* gh = W.hist + (int64_t)g * 2 * kBins;
-        for (int k = threadIdx.x; k < (split ? 2 : 1) * kBins; k += kThreads) {
+        uint32_t* gh = W.hist + (int64_t)g * kHist;
+        for (int k = threadIdx.x; k < kVBins; k += kThreads) {
             const uint32_t v = (&h[0][0])[k];
             if (v) atomicAdd(gh + k, v);
         }
@@ -717,8 +733,9 @@ compact_pass(Work W, int G) {
     if (!seg_tile(W, G, blockIdx.x, g, a, b)) return;
     GState& s = W.gs[g];
     if (!s.active || s.sel_done) return;
-    const int pb = s.pb;   // >= 1 after the first digit
-    const uint64_t pa = s.pref[0] >> (64 - pb), pbv = s.pref[1] >> (64 - pb);
+    const int b0 = s.vb[0], b1 = s.vb[1];
+    const double c = s.c;
+    const float voff = s.voff, vinv = s.vinv;
     const uint64_t klo = s.klo, khi = s.khi;
     uint64_t* out = W.cand + W.seg_base[g];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -726,21 +743,38 @@ compact_pass(Work W, int G) {
     // count (one bit per value of this thread), one atomic per tile, write
     uint32_t mine = 0;
     unsigned total = 0;
+    unsigned long long kmn_inv = 0ull, kmx = 0ull;
 #pragma unroll 8
     for (int k = 0; k < kSegPerThread; ++k) {
         const int64_t i = a + (int64_t)k * kThreads + threadIdx.x;
         bool want = false;
         if (i < b) {
-            const uint64_t key = okey(W.seg[i]);
+            const double x = W.seg[i];
+            const uint64_t key = okey(x);
             if (key >= klo && key <= khi) {
-                const uint64_t top = key >> (64 - pb);
-                want = (top == pa) || (top == pbv);
+                const int vb = value_bin(x - c, voff, vinv);
+                want = vb >= b0 && vb <= b1;
+                if (want) {
+                    kmn_inv = max(kmn_inv, (unsigned long long)~key);
+                    kmx = max(kmx, (unsigned long long)key);
+                }
             }
         }
         mine |= (want ? 1u : 0u) << k;
         total += __popc(__ballot_sync(MGPU_FULL_MASK, want));
     }
-    if (lane == 0) s_base[w] = total;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+        kmn_inv = max(kmn_inv, __shfl_xor_sync(MGPU_FULL_MASK, kmn_inv, o));
+        kmx = max(kmx, __shfl_xor_sync(MGPU_FULL_MASK, kmx, o));
+    }
+    if (lane == 0) {
+        s_base[w] = total;
+        if (kmx) {
+            atomicMax(&s.cmin_inv, kmn_inv);
+            atomicMax(&s.cmax, kmx);
+        }
+    }
     __syncthreads();
     if (threadIdx.x == 0) {
         unsigned long long run = 0;
@@ -766,14 +800,120 @@ compact_pass(Work W, int G) {
     }
 }
 
-// tiles of the candidate lists (one thread)
+// Groups whose candidate list is short: one block runs every remaining
+// digit (shared-memory histogram with warp-aggregated updates, block-wide
+// rank search) and leaves the group resolved, with no launch per digit;
+// longer lists go through cand_pass + radix_step.  Runs after cand_setup
+// (the prefix already spans the candidates' common bits).
+constexpr int64_t kSmallCand = 3072;      // keys staged in shared memory (24 KB)
+
+__device__ void find_rank(const uint32_t* hist, int64_t r, int64_t* s_tot, int* out_bin,
+                          int64_t* out_below);
+
+__global__ void __launch_bounds__(kThreads)
+select_small(Work W) {
+    __shared__ uint32_t h[2][kBins];
+    __shared__ uint64_t keys[kSmallCand];
+    __shared__ int64_t s_tot[kThreads];
+    __shared__ int s_bin;
+    __shared__ int64_t s_below;
+    GState& s = W.gs[blockIdx.x];
+    if (!s.active || s.sel_done) return;
+    const int64_t nc = (int64_t)s.n_cand;
+    if (nc > kSmallCand) return;
+    {
+        const uint64_t* src = W.cand + W.seg_base[blockIdx.x];
+        for (int64_t j = threadIdx.x; j < nc; j += kThreads) keys[j] = src[j];
+        __syncthreads();
+    }
+    const int lane = threadIdx.x & 31;
+    for (int level = 0; level < kLevels; ++level) {
+        if (s.sel_done) break;                     // uniform: read after the barrier below
+        const int pb = s.pb;
+        const int width = min(kRadixBits, 64 - pb);
+        const int shift = 64 - pb - width;
+        const uint64_t dmask = (1ull << width) - 1ull;
+        const uint64_t pa = pb ? (s.pref[0] >> (64 - pb)) : 0ull;
+        const uint64_t pbv = pb ? (s.pref[1] >> (64 - pb)) : 0ull;
+        const bool split = s.split != 0;
+        for (int k = threadIdx.x; k < 2 * kBins; k += kThreads) (&h[0][0])[k] = 0u;
+        __syncthreads();
+        for (int64_t j0 = 0; j0 < nc; j0 += kThreads) {
+            const int64_t j = j0 + threadIdx.x;
+            int bin = -1;
+            if (j < nc) {
+                const uint64_t key = keys[j];
+                const uint64_t top = pb ? (key >> (64 - pb)) : 0ull;
+                const int digit = (int)((key >> shift) & dmask);
+                if (top == pa) bin = digit;
+                else if (split && top == pbv) bin = kBins + digit;
+            }
+            const unsigned act = __ballot_sync(MGPU_FULL_MASK, bin >= 0);
+            if (bin >= 0) {
+                const unsigned peers = __match_any_sync(act, bin);
+                if (lane == __ffs(peers) - 1) atomicAdd(&(&h[0][0])[bin], (uint32_t)__popc(peers));
+            }
+        }
+        __syncthreads();
+        int bins[2] = {0, 0};
+        bool lost = false;
+        for (int q = 0; q < (s.two ? 2 : 1); ++q) {
+            find_rank(&h[(split && q == 1) ? 1 : 0][0], s.rank[q], s_tot, &s_bin, &s_below);
+            bins[q] = s_bin;
+            lost = lost || s_bin < 0;
+            if (threadIdx.x == 0 && s_bin >= 0) {
+                s.rank[q] -= s_below;
+                s.pref[q] |= (uint64_t)s_bin << shift;
+            }
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) {
+            if (lost) {
+                s.bad = 1;
+                s.pb = 64;
+                s.sel_done = 1;
+            } else {
+                if (!s.two) {
+                    s.pref[1] = s.pref[0];
+                    s.rank[1] = s.rank[0];
+                } else if (!split && bins[0] != bins[1]) {
+                    s.split = 1;
+                }
+                s.pb = pb + width;
+                s.sel_done = s.pb >= 64 ? 1 : 0;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// tiles of the candidate lists (one thread); before them, every key bit
+// the candidates share is known: the prefix jumps to their common prefix
+// (one selection, or two not yet split), so the next digits split the
+// candidates' actual spread
 __global__ void cand_setup(Work W, int G) {
     if (threadIdx.x != 0) return;
     int64_t run = 0;
     for (int g = 0; g < G; ++g) {
         W.ctile_base[g] = run;
-        const GState& s = W.gs[g];
-        if (s.active && !s.sel_done) run += ((int64_t)s.n_cand + kTileSeg - 1) / kTileSeg;
+        GState& s = W.gs[g];
+        if (s.active && !s.sel_done) {
+            if (s.n_cand == 0) {
+                s.bad = 1;          // cannot happen for a consistent state
+                s.pb = 64;
+                s.sel_done = 1;
+            } else {
+                const uint64_t mn = ~s.cmin_inv, mx = s.cmax;
+                const int cp = (mn == mx) ? 64 : __clzll((long long)(mn ^ mx));
+                const uint64_t mask = cp == 0 ? 0ull : (cp == 64 ? ~0ull : (~0ull << (64 - cp)));
+                s.pref[0] = s.pref[1] = mn & mask;
+                s.pb = cp;
+                s.split = 0;
+                s.sel_done = cp == 64 ? 1 : 0;
+            }
+        }
+        if (s.active && !s.sel_done && (int64_t)s.n_cand > kSmallCand)
+            run += ((int64_t)s.n_cand + kTileSeg - 1) / kTileSeg;
     }
     W.ctile_base[G] = run;
 }
@@ -790,12 +930,13 @@ cand_pass(Work W, int G) {
         for (int k = 1; k < G; ++k)
             if (W.ctile_base[k] <= t) g = k;
         const GState& s = W.gs[g];
-        if (!s.active || s.sel_done) continue;
+        if (!s.active || s.sel_done || (int64_t)s.n_cand <= kSmallCand) continue;
         const int pb = s.pb;
         const int width = min(kRadixBits, 64 - pb);
         const int shift = 64 - pb - width;
         const uint64_t dmask = (1ull << width) - 1ull;
-        const uint64_t pa = s.pref[0] >> (64 - pb), pbv = s.pref[1] >> (64 - pb);
+        const uint64_t pa = pb ? (s.pref[0] >> (64 - pb)) : 0ull;
+        const uint64_t pbv = pb ? (s.pref[1] >> (64 - pb)) : 0ull;
         const bool split = s.split != 0;
         const int64_t a = W.seg_base[g] + (t - W.ctile_base[g]) * kTileSeg;
         const int64_t b = min(W.seg_base[g] + (int64_t)s.n_cand, a + kTileSeg);
@@ -807,7 +948,7 @@ cand_pass(Work W, int G) {
             int bin = -1;
             if (i < b) {
                 const uint64_t key = W.cand[i];
-                const uint64_t top = key >> (64 - pb);
+                const uint64_t top = pb ? (key >> (64 - pb)) : 0ull;
                 const int digit = (int)((key >> shift) & dmask);
                 if (top == pa) bin = digit;
                 else if (split && top == pbv) bin = kBins + digit;
@@ -819,7 +960,7 @@ cand_pass(Work W, int G) {
             }
         }
         __syncthreads();
-        uint32_t* gh = W.hist + (int64_t)g * 2 * kBins;
+        uint32_t* gh = W.hist + (int64_t)g * kHist;
         for (int k = threadIdx.x; k < (split ? 2 : 1) * kBins; k += kThreads) {
             const uint32_t v = (&h[0][0])[k];
             if (v) atomicAdd(gh + k, v);
@@ -828,12 +969,13 @@ cand_pass(Work W, int G) {
     }
 }
 
-// block-wide search of the bin holding rank r in a kBins histogram: returns
+// block-wide search of the bin holding rank r in an NB-bin histogram: returns
 // (bin, count of values in lower bins) through shared memory; bin -1 if the
 // histogram holds fewer than r + 1 values
-__device__ void find_rank(const uint32_t* hist, int64_t r, int64_t* s_tot, int* out_bin,
-                          int64_t* out_below) {
-    constexpr int per = kBins / kThreads;
+template <int NB>
+__device__ void find_rank_n(const uint32_t* hist, int64_t r, int64_t* s_tot, int* out_bin,
+                            int64_t* out_below) {
+    constexpr int per = NB / kThreads;
     if (threadIdx.x == 0) *out_bin = -1;
     int64_t loc = 0;
     uint32_t v[per];
@@ -863,6 +1005,11 @@ __device__ void find_rank(const uint32_t* hist, int64_t r, int64_t* s_tot, int* 
         below += v[k];
     }
     __syncthreads();
+}
+
+__device__ void find_rank(const uint32_t* hist, int64_t r, int64_t* s_tot, int* out_bin,
+                          int64_t* out_below) {
+    find_rank_n<kBins>(hist, r, s_tot, out_bin, out_below);
 }
 
 // one block per group: (kStats) count, mean and std of the kept values and
@@ -917,16 +1064,46 @@ radix_step(const __grid_constant__ mgpu_stats_problem P, Work W) {
                 s.rank[1] = n / 2;
                 s.rank[0] = s.two ? n / 2 - 1 : n / 2;
                 s.n_cand = 0ull;
+                s.cmin_inv = 0ull;
+                s.cmax = 0ull;
             }
         }
         __syncthreads();
         if (!s.active) return;
+        // the value level: the bins of both ranks, ranks counted from the
+        // first of them (the candidates are the kept values of bins
+        // vb[0]..vb[1]); the key digits follow on the candidates
+        uint32_t* gh = W.hist + (int64_t)g * kHist;
+        int vbs[2] = {0, 0};
+        int64_t below0 = 0;
+        bool lost = false;
+        for (int q = 0; q < (s.two ? 2 : 1); ++q) {
+            find_rank_n<kVBins>(gh, s.rank[q], s_tot, &s_bin, &s_below);
+            vbs[q] = s_bin;
+            if (q == 0) below0 = s_below;
+            lost = lost || s_bin < 0;
+            __syncthreads();       // every thread has read s_bin before the next search
+        }
+        if (threadIdx.x == 0) {
+            if (lost) {
+                s.bad = 1;
+                s.pb = 64;
+                s.sel_done = 1;
+            } else {
+                s.vb[0] = vbs[0];
+                s.vb[1] = s.two ? vbs[1] : vbs[0];
+                s.rank[0] -= below0;
+                s.rank[1] = s.two ? s.rank[1] - below0 : s.rank[0];
+            }
+        }
+        for (int k = threadIdx.x; k < kHist; k += kThreads) gh[k] = 0u;
+        return;
     }
     if (s.sel_done) return;
     const int pb = s.pb;
     const int width = min(kRadixBits, 64 - pb);
     const int shift = 64 - pb - width;
-    uint32_t* gh = W.hist + (int64_t)g * 2 * kBins;
+    uint32_t* gh = W.hist + (int64_t)g * kHist;
     const bool split = s.split != 0;
     int bins[2] = {0, 0};
     bool lost = false;
@@ -989,6 +1166,7 @@ __global__ void finalize_round(const __grid_constant__ mgpu_stats_problem P, Wor
     start_selection(s);
     s.c = isnan(med) ? 0.0 : med;
     choose_sums(s);
+    set_value_bins(s, lo, hi);
     s.n_prev = s.n_cur;
     s.round += 1;
 }
@@ -1034,7 +1212,7 @@ extern "C" int mgpu_order_stats(const mgpu_stats_problem* prob, void* stream) {
     if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
         return (int)e;
     if ((e = cudaMemsetAsync(W.gs, 0, sizeof(GState) * (size_t)G, st)) != cudaSuccess) return (int)e;
-    if ((e = cudaMemsetAsync(W.hist, 0, 4 * (size_t)G * 2 * kBins, st)) != cudaSuccess) return (int)e;
+    if ((e = cudaMemsetAsync(W.hist, 0, 4 * (size_t)G * kHist, st)) != cudaSuccess) return (int)e;
     const int64_t cap = (int64_t)sms * 8;
     const int cls_blocks = (int)(L.n_tin < cap ? L.n_tin : cap);
     if (cls_blocks > 0) classify_kernel<<<cls_blocks, kThreads, 0, st>>>(P, W);
@@ -1050,6 +1228,7 @@ extern "C" int mgpu_order_stats(const mgpu_stats_problem* prob, void* stream) {
         radix_step<true><<<G, kThreads, 0, st>>>(P, W);
         compact_pass<<<tiles, kThreads, 0, st>>>(W, G);
         cand_setup<<<1, 32, 0, st>>>(W, G);
+        select_small<<<G, kThreads, 0, st>>>(W);
         for (int lvl = 1; lvl < kLevels; ++lvl) {
             cand_pass<<<persistent, kThreads, 0, st>>>(W, G);
             radix_step<false><<<G, kThreads, 0, st>>>(P, W);
