@@ -621,7 +621,8 @@ def main():
     line = {
         'metric': METRIC, 'value': r['photons_per_s'], 'unit': UNIT, 'n_gpus': world,
         'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': r['wall_ms'] / args.steps,
-        'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64',
+        'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+        'dtype': 'f32' if head == 'fp32local' else 'f64', 'io_dtype': 'f64',
         'data': 'synthetic (seeded annulus aperture, piecewise-linear spectrum, seeded '
                 'facet jitter)',
         'config': {'workload': WORKLOAD, 'photons_per_gpu': n, 'n_facets': len(inst.gas.elements),

@@ -53,10 +53,16 @@ def _device():
 
 def _as_device(a, device, dtypes=(torch.float64,)):
     """A 1-D device tensor of one of ``dtypes`` (converted to the first if
-    needed); device tensors of a supported dtype are used in place."""
+    needed); device tensors of a supported dtype are used in place.  Masked
+    entries of a float column (astropy MaskedColumn, numpy masked array)
+    become NaN, which the reductions leave out as the reference's masked
+    statistics do."""
     if isinstance(a, torch.Tensor):
         t = a if a.device == device else a.to(device)
     else:
+        mask = getattr(a, 'mask', None)
+        if mask is not None and np.any(mask) and dtypes[0] == torch.float64:
+            a = np.ma.MaskedArray(np.asarray(a, dtype=np.float64), mask=mask).filled(np.nan)
         arr = np.asarray(a)
         if arr.dtype == np.bool_:
             arr = arr.astype(np.uint8)

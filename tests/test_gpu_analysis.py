@@ -248,3 +248,16 @@ def test_order_matching_beyond_the_small_integer_table():
     iorders = [65, -3, 99, 1000000, 64, 0, -100, 7, 2.5]
     got = order_stats(x, iorder, iorders, probability=prob)
     _compare(got, _oracle_rows(iorder, x, prob, iorders))
+
+
+def test_masked_columns_leave_out_masked_values():
+    """A masked dispersion column (astropy MaskedColumn semantics): masked
+    entries are left out of the statistics like non-finite ones, and still
+    count as order members without the resolving-power filter."""
+    from marxs_gb300.analysis import order_stats
+    order, x, prob = _event_list(13, 50_000)
+    mask = np.random.default_rng(14).random(len(x)) < 0.1
+    xm = np.ma.MaskedArray(x, mask=mask)
+    got = order_stats(xm, order, [-3, 0, 2], probability=prob)
+    ref = _oracle_rows(order, np.where(mask, np.nan, x), prob, [-3, 0, 2])
+    _compare(got, ref)
