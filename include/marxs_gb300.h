@@ -302,7 +302,7 @@ int mgpu_trace(const mgpu_chain* chain, const mgpu_photons* photons, void* strea
 
 /* Build the candidate lists of a grating stage's grid on the device:
  * grid->cell_start / cell_items are filled from the facet table.
- * ``counts`` is caller-provided scratch of nu*nv+1 int32. */
+ * ``counts`` is caller-provided scratch of nu*nv + 1 + ceil(nu*nv / 4096) int32. */
 int mgpu_facet_grid_build(const mgpu_facet* facets, int32_t n_facets, mgpu_grid* grid,
                           int32_t* counts, uint32_t* status, void* stream);
 

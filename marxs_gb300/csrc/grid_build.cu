@@ -48,58 +48,113 @@ __device__ CellRange facet_cells(const mgpu_facet& f, const mgpu_grid& g) {
     return r;
 }
 
+// one warp per facet: the lanes share the facet's cell rectangle
 __global__ void grid_count_kernel(const mgpu_facet* facets, int n_facets, mgpu_grid g,
                                   int* counts, uint32_t* status) {
-    int f = blockIdx.x * blockDim.x + threadIdx.x;
+    const int f = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (f >= n_facets) return;
     CellRange r = facet_cells(facets[f], g);
-    if (!r.inside) atomicOr(status, MGPU_STATUS_GRID_RANGE);
-    for (int iu = r.iu0; iu <= r.iu1; ++iu)
-        for (int iv = r.iv0; iv <= r.iv1; ++iv) atomicAdd(counts + iu * g.nv + iv, 1);
+    if (!r.inside && lane == 0) atomicOr(status, MGPU_STATUS_GRID_RANGE);
+    const int nv = r.iv1 - r.iv0 + 1, nu = r.iu1 - r.iu0 + 1;
+    if (nu <= 0 || nv <= 0) return;
+    for (int k = lane; k < nu * nv; k += 32)
+        atomicAdd(counts + (r.iu0 + k / nv) * g.nv + (r.iv0 + k % nv), 1);
 }
 
-// exclusive scan of n counts into start[0..n] by one block; counts is
-// overwritten with the start offsets (used as fill cursors)
-__global__ void grid_scan_kernel(int* counts, int n, int* start) {
-    __shared__ int s_part[1024];
-    const int t = threadIdx.x, T = blockDim.x;
-    const int chunk = (n + T - 1) / T;
-    const int lo = min(n, t * chunk), hi = min(n, lo + chunk);
-    int sum = 0;
-    for (int j = lo; j < hi; ++j) sum += counts[j];
-    s_part[t] = sum;
+// Exclusive scan of the n cell counts into start[0..n] in three steps: the
+// sum of every kScanChunk-cell chunk, a scan of those sums (one block), and
+// a block scan of each chunk from its offset.  counts is overwritten with
+// the start offsets (the fill cursors); sums is scratch of one int per chunk.
+constexpr int kScanThreads = 256;
+constexpr int kScanPer = 16;
+constexpr int kScanChunk = kScanThreads * kScanPer;
+
+__device__ __forceinline__ int block_exclusive_scan(int v, int* s_warp) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(MGPU_FULL_MASK, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_warp[w] = x;
     __syncthreads();
-    for (int off = 1; off < T; off <<= 1) {
-        int v = (t >= off) ? s_part[t - off] : 0;
-        __syncthreads();
-        s_part[t] += v;
+    if (threadIdx.x == 0) {
+        int run = 0;
+        for (int k = 0; k < kScanThreads / 32; ++k) {
+            const int t = s_warp[k];
+            s_warp[k] = run;
+            run += t;
+        }
+        s_warp[kScanThreads / 32] = run;
+    }
+    __syncthreads();
+    return s_warp[w] + x - v;
+}
+
+__global__ void __launch_bounds__(kScanThreads)
+grid_scan_sums(const int* counts, int n, int* sums) {
+    __shared__ int s_warp[kScanThreads / 32 + 1];
+    const int a = blockIdx.x * kScanChunk + threadIdx.x * kScanPer;
+    int v = 0;
+    for (int j = 0; j < kScanPer; ++j)
+        if (a + j < n) v += counts[a + j];
+    block_exclusive_scan(v, s_warp);
+    if (threadIdx.x == 0) sums[blockIdx.x] = s_warp[kScanThreads / 32];
+}
+
+__global__ void __launch_bounds__(kScanThreads)
+grid_scan_top(int* sums, int nb, int* total) {
+    __shared__ int s_warp[kScanThreads / 32 + 1];
+    // nb sums in chunks of kScanThreads, each scanned by the block and offset
+    int carry = 0;
+    for (int c0 = 0; c0 < nb; c0 += kScanThreads) {
+        const int i = c0 + threadIdx.x;
+        const int v = i < nb ? sums[i] : 0;
+        const int ex = block_exclusive_scan(v, s_warp);
+        if (i < nb) sums[i] = carry + ex;
+        carry += s_warp[kScanThreads / 32];
         __syncthreads();
     }
-    int run = s_part[t] - sum;
-    for (int j = lo; j < hi; ++j) {
-        int c = counts[j];
-        start[j] = run;
-        counts[j] = run;
-        run += c;
+    if (threadIdx.x == 0) *total = carry;
+}
+
+__global__ void __launch_bounds__(kScanThreads)
+grid_scan_apply(int* counts, int n, int* start, const int* sums) {
+    __shared__ int s_warp[kScanThreads / 32 + 1];
+    const int a = blockIdx.x * kScanChunk + threadIdx.x * kScanPer;
+    int c[kScanPer];
+    int v = 0;
+#pragma unroll
+    for (int j = 0; j < kScanPer; ++j) {
+        c[j] = (a + j < n) ? counts[a + j] : 0;
+        v += c[j];
     }
-    if (t == T - 1) start[n] = s_part[T - 1];
+    int run = sums[blockIdx.x] + block_exclusive_scan(v, s_warp);
+#pragma unroll
+    for (int j = 0; j < kScanPer; ++j) {
+        if (a + j < n) {
+            start[a + j] = run;
+            counts[a + j] = run;
+        }
+        run += c[j];
+    }
 }
 
 __global__ void grid_fill_kernel(const mgpu_facet* facets, int n_facets, mgpu_grid g,
                                  int* cursor, uint32_t* status) {
-    int f = blockIdx.x * blockDim.x + threadIdx.x;
+    const int f = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (f >= n_facets) return;
     CellRange r = facet_cells(facets[f], g);
-    for (int iu = r.iu0; iu <= r.iu1; ++iu)
-        for (int iv = r.iv0; iv <= r.iv1; ++iv) {
-            int slot = atomicAdd(cursor + iu * g.nv + iv, 1);
-            if (slot < g.capacity) g.cell_items[slot] = f;
-            else atomicOr(status, MGPU_STATUS_GRID_FULL);
-        }
+    const int nv = r.iv1 - r.iv0 + 1, nu = r.iu1 - r.iu0 + 1;
+    if (nu <= 0 || nv <= 0) return;
+    for (int k = lane; k < nu * nv; k += 32) {
+        const int slot = atomicAdd(cursor + (r.iu0 + k / nv) * g.nv + (r.iv0 + k % nv), 1);
+        if (slot < g.capacity) g.cell_items[slot] = f;
+        else atomicOr(status, MGPU_STATUS_GRID_FULL);
+    }
 }
 
-// candidate order inside a cell does not change results (ties resolve to
-// the lower facet index); sorting keeps the lists reproducible anyway
 __global__ void grid_sort_kernel(const int* start, int n_cells, int capacity, int* items) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= n_cells) return;
@@ -119,17 +174,24 @@ __global__ void grid_sort_kernel(const int* start, int n_cells, int capacity, in
 cudaError_t mgpu_launch_grid_build(const mgpu_facet* facets, int n_facets, const mgpu_grid& g,
                                    int* counts, uint32_t* status, cudaStream_t stream) {
     const int n_cells = g.nu * g.nv;
+    const int nb = (n_cells + kScanChunk - 1) / kScanChunk;
+    int* sums = counts + n_cells + 1;          // scratch after the counters
     cudaError_t e = cudaMemsetAsync(counts, 0, sizeof(int) * (size_t)(n_cells + 1), stream);
     if (e != cudaSuccess) return e;
-    const int T = 128;
+    const int T = 128;                         // 4 facets (warps) per block
+    const int fb = (int)(((int64_t)n_facets * 32 + T - 1) / T);
     if (n_facets > 0) {
-        grid_count_kernel<<<(n_facets + T - 1) / T, T, 0, stream>>>(facets, n_facets, g, counts, status);
+        grid_count_kernel<<<fb, T, 0, stream>>>(facets, n_facets, g, counts, status);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
-    grid_scan_kernel<<<1, 1024, 0, stream>>>(counts, n_cells, g.cell_start);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if (nb > 0) {
+        grid_scan_sums<<<nb, kScanThreads, 0, stream>>>(counts, n_cells, sums);
+        grid_scan_top<<<1, kScanThreads, 0, stream>>>(sums, nb, g.cell_start + n_cells);
+        grid_scan_apply<<<nb, kScanThreads, 0, stream>>>(counts, n_cells, g.cell_start, sums);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
     if (n_facets > 0) {
-        grid_fill_kernel<<<(n_facets + T - 1) / T, T, 0, stream>>>(facets, n_facets, g, counts, status);
+        grid_fill_kernel<<<fb, T, 0, stream>>>(facets, n_facets, g, counts, status);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
     grid_sort_kernel<<<(n_cells + T - 1) / T, T, 0, stream>>>(g.cell_start, n_cells, g.capacity,
@@ -137,19 +199,8 @@ cudaError_t mgpu_launch_grid_build(const mgpu_facet* facets, int n_facets, const
     return cudaGetLastError();
 }
 
-// ---------------------------------------------------------------------------
-// Allocation-free grid build.
-//
-// Some callers cannot allocate device memory when they (re)build the facet
-// candidate grid: a host application that has handed (nearly) all device
-// memory to its own pool, or a loop that must not call cudaMalloc/cudaFree
-// because those synchronise the device and stall its other streams.  This
-// variant keeps the build's scratch -- one counter per grid cell -- in the
-// fixed array below instead of caller-provided memory.  The array holds
-// MGPU_NOALLOC_MAX_CELLS + 1 int32 (256 KiB) on every GPU that loads the
-// library, for the life of the process.
-// ---------------------------------------------------------------------------
-static __device__ __align__(256) int32_t g_noalloc_counts[MGPU_NOALLOC_MAX_CELLS + 1];
+static __device__ __align__(256) int32_t
+    g_noalloc_counts[MGPU_NOALLOC_MAX_CELLS + 1 + (MGPU_NOALLOC_MAX_CELLS + kScanChunk - 1) / kScanChunk];
 
 namespace {
 constexpr int kNoallocMaxDevices = 64;

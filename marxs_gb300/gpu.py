@@ -187,7 +187,8 @@ class _Instrument:
                 ncell = g['nu'] * g['nv']
                 start = torch.zeros(ncell + 1, dtype=torch.int32, device=device)
                 items = torch.zeros(g['capacity'], dtype=torch.int32, device=device)
-                counts = torch.zeros(ncell + 1, dtype=torch.int32, device=device)
+                counts = torch.zeros(ncell + 1 + (ncell + 4095) // 4096, dtype=torch.int32,
+                                     device=device)
                 self.keep += [start, items]
                 grid = _abi.MgpuGrid()
                 for key in ('o', 'n', 'a', 'b'):

@@ -118,7 +118,8 @@ class DeviceFacetPoses:
         ncell = g['nu'] * g['nv']
         self._start = torch.zeros(ncell + 1, dtype=torch.int32, device=dev)
         self._items = torch.zeros(g['capacity'], dtype=torch.int32, device=dev)
-        self._counts = torch.zeros(ncell + 1, dtype=torch.int32, device=dev)
+        self._counts = torch.zeros(ncell + 1 + (ncell + 4095) // 4096, dtype=torch.int32,
+                                   device=dev)
         grid = _abi.MgpuGrid()
         for key in ('o', 'n', 'a', 'b'):
             getattr(grid, key)[:] = [float(x) for x in g[key]]

@@ -58,7 +58,7 @@ def _build(facets, g, noalloc):
         rc = lib.mgpu_facet_grid_build_noalloc(fac.data_ptr(), len(facets), C.byref(grid),
                                                status.data_ptr(), stream)
     else:
-        counts = torch.zeros(ncell + 1, dtype=torch.int32, device=dev)
+        counts = torch.zeros(ncell + 1 + (ncell + 4095) // 4096, dtype=torch.int32, device=dev)
         rc = lib.mgpu_facet_grid_build(fac.data_ptr(), len(facets), C.byref(grid),
                                        counts.data_ptr(), status.data_ptr(), stream)
     assert rc == 0, rc
