@@ -33,16 +33,11 @@ class AnalysisError(Exception):
     pass
 
 
-_work = {}
-
-
 def _workspace(device, nbytes):
-    """A 256-byte aligned device buffer of at least nbytes (cached per device)."""
-    key = (device.type, device.index)
-    buf = _work.get(key)
-    if buf is None or buf.numel() < nbytes + 256:
-        buf = torch.empty(int(nbytes) + 256, dtype=torch.uint8, device=device)
-        _work[key] = buf
+    """A 256-byte aligned device buffer of at least nbytes, allocated on the
+    current stream for this call (the caching allocator reuses it; calls on
+    different streams never share one)."""
+    buf = torch.empty(int(nbytes) + 256, dtype=torch.uint8, device=device)
     ptr = buf.data_ptr()
     return buf, (ptr + 255) & ~255
 
@@ -138,13 +133,15 @@ def order_stats(value, order=None, orders=(0,), probability=None, aeff_mask=None
         nbytes = lib.mgpu_order_stats_workspace(n, G)
         if nbytes < 0:
             raise ValueError('bad order_stats size')
-        with torch.cuda.device(dev):
+        with torch.cuda.device(dev), torch.cuda.stream(s):
             buf, ptr = _workspace(dev, nbytes)
             res = torch.empty(G * _abi.STATS_NRES, dtype=torch.float64, device=dev)
         P.work, P.work_bytes, P.result = ptr, nbytes, res.data_ptr()
         _abi.check(lib.mgpu_order_stats(C.byref(P), C.c_void_p(s.cuda_stream)),
                    'mgpu_order_stats')
-        host = res.cpu().numpy().reshape(G, _abi.STATS_NRES)   # synchronises the stream
+        with torch.cuda.stream(s):
+            host = res.cpu().numpy().reshape(G, _abi.STATS_NRES)   # synchronises the stream
+        del buf
         for k, x in enumerate(grp):
             out[x] = host[k]
     return np.stack([out[x] for x in wanted])

@@ -183,31 +183,48 @@ class _Instrument:
             self.keep.append(sel_dev)
             self.stage_selectors[si] = sel_dev
             if st.grid is not None:
-                g = st.grid
-                ncell = g['nu'] * g['nv']
-                start = torch.zeros(ncell + 1, dtype=torch.int32, device=device)
-                items = torch.zeros(g['capacity'], dtype=torch.int32, device=device)
-                counts = torch.zeros(ncell + 1 + (ncell + 4095) // 4096, dtype=torch.int32,
-                                     device=device)
-                self.keep += [start, items]
-                grid = _abi.MgpuGrid()
-                for key in ('o', 'n', 'a', 'b'):
-                    getattr(grid, key)[:] = [float(x) for x in g[key]]
-                grid.u0, grid.v0, grid.cell = g['u0'], g['v0'], g['cell']
-                grid.nu, grid.nv = g['nu'], g['nv']
-                grid.slope_max, grid.margin = g['slope_max'], g['margin']
-                grid.cell_start, grid.cell_items = start.data_ptr(), items.data_ptr()
-                grid.capacity = g['capacity']
-                _abi.check(lib.mgpu_facet_grid_build(fac.data_ptr(), len(st.facets), C.byref(grid),
-                                                     counts.data_ptr(), status.data_ptr(), stream),
-                           'mgpu_facet_grid_build')
-                self.stage_grid[si] = grid
-                self.keep.append(counts)
+                self.set_grid(si, st.grid, status, stream)
         if self.stage_grid:
             torch.cuda.current_stream().synchronize()
             code = int(status.item())
             if code & (_abi.STATUS_GRID_RANGE | _abi.STATUS_GRID_FULL):
                 raise RuntimeError('facet candidate grid build failed (status 0x%x)' % code)
+
+    def set_grid(self, si, g, status, stream):
+        """Allocate and build the candidate grid of grating stage ``si`` from
+        the parameters ``g`` (``lowering.grid_params``); the FP32-local
+        constants follow.  Returns a rebuild function (the same build on the
+        stage's current facet table, e.g. after the facets moved)."""
+        from . import lowering as L
+        lib = _abi.load()
+        dev = self.device
+        ncell = g['nu'] * g['nv']
+        start = torch.zeros(ncell + 1, dtype=torch.int32, device=dev)
+        items = torch.zeros(g['capacity'], dtype=torch.int32, device=dev)
+        counts = torch.zeros(ncell + 1 + (ncell + 4095) // 4096, dtype=torch.int32, device=dev)
+        self.keep += [start, items, counts]
+        grid = _abi.MgpuGrid()
+        for key in ('o', 'n', 'a', 'b'):
+            getattr(grid, key)[:] = [float(x) for x in g[key]]
+        grid.u0, grid.v0, grid.cell = g['u0'], g['v0'], g['cell']
+        grid.nu, grid.nv = g['nu'], g['nv']
+        grid.slope_max, grid.margin = g['slope_max'], g['margin']
+        grid.cell_start, grid.cell_items = start.data_ptr(), items.data_ptr()
+        grid.capacity = g['capacity']
+        self.stage_grid[si] = grid
+        if si in self.stage_facets32:
+            aux = torch.from_numpy(np.frombuffer(L.grid32_block(g), dtype=np.uint8).copy()).to(dev)
+            self.keep.append(aux)
+            self.stage_aux[si] = aux
+        fac = self.stage_facets[si]
+        n = len(self.stages[si].facets)
+
+        def rebuild(stream_handle):
+            _abi.check(lib.mgpu_facet_grid_build(fac.data_ptr(), n, C.byref(grid),
+                                                 counts.data_ptr(), status.data_ptr(),
+                                                 stream_handle), 'mgpu_facet_grid_build')
+        rebuild(stream)
+        return rebuild
 
     def fill_stage(self, si, s):
         st = self.stages[si]

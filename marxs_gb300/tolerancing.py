@@ -101,11 +101,9 @@ class DeviceFacetPoses:
     def _grid(self, pad):
         """Replace the stage's candidate grid by one padded by ``pad`` mm on
         every side, with twice the entry capacity."""
-        from . import lowering as L
-        inst, si = self.inst, self.si
-        st = inst.stages[si]
+        st = self.inst.stages[self.si]
         if st.grid is None:
-            self._grid_struct = None
+            self._rebuild_fn = None
             return
         g = dict(st.grid)
         extra = int(math.ceil(pad / g['cell']))
@@ -114,39 +112,14 @@ class DeviceFacetPoses:
         g['nu'] += 2 * extra
         g['nv'] += 2 * extra
         g['capacity'] = 2 * g['capacity'] + 64
-        dev = self.device
-        ncell = g['nu'] * g['nv']
-        self._start = torch.zeros(ncell + 1, dtype=torch.int32, device=dev)
-        self._items = torch.zeros(g['capacity'], dtype=torch.int32, device=dev)
-        self._counts = torch.zeros(ncell + 1 + (ncell + 4095) // 4096, dtype=torch.int32,
-                                   device=dev)
-        grid = _abi.MgpuGrid()
-        for key in ('o', 'n', 'a', 'b'):
-            getattr(grid, key)[:] = [float(x) for x in g[key]]
-        grid.u0, grid.v0, grid.cell = g['u0'], g['v0'], g['cell']
-        grid.nu, grid.nv = g['nu'], g['nv']
-        grid.slope_max, grid.margin = g['slope_max'], g['margin']
-        grid.cell_start, grid.cell_items = self._start.data_ptr(), self._items.data_ptr()
-        grid.capacity = g['capacity']
-        self._grid_struct = grid
-        inst.keep += [self._start, self._items, self._counts]
-        inst.stage_grid[si] = grid
-        if si in inst.stage_aux and si in inst.stage_facets32:
-            aux = torch.from_numpy(np.frombuffer(L.grid32_block(g), dtype=np.uint8).copy()).to(dev)
-            inst.keep.append(aux)
-            inst.stage_aux[si] = aux
-        self._rebuild(torch.cuda.current_stream(dev))
+        stream = torch.cuda.current_stream(self.device)
+        self._rebuild_fn = self.inst.set_grid(self.si, g, self._status,
+                                              C.c_void_p(stream.cuda_stream))
         self._check()
 
     def _rebuild(self, stream):
-        if self._grid_struct is None:
-            return
-        lib = _abi.load()
-        fac = self.inst.stage_facets[self.si]
-        _abi.check(lib.mgpu_facet_grid_build(fac.data_ptr(), self.n, C.byref(self._grid_struct),
-                                             self._counts.data_ptr(), self._status.data_ptr(),
-                                             C.c_void_p(stream.cuda_stream)),
-                   'mgpu_facet_grid_build')
+        if self._rebuild_fn is not None:
+            self._rebuild_fn(C.c_void_p(stream.cuda_stream))
 
     def _check(self):
         code = int(self._status.item())
