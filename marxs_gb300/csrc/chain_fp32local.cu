@@ -187,6 +187,15 @@ __device__ __forceinline__ void philox_u53(uint64_t seed, uint64_t row, uint32_t
     *U1 = (((uint64_t)r.z << 21) ^ (uint64_t)(r.w >> 11)) & ((1ull << 53) - 1);
 }
 
+// the same with a draw index (the float64 kernel's philox_uniform2 counters)
+__device__ __forceinline__ void philox_u53_draw(uint64_t seed, uint64_t row, uint32_t stage,
+                                                uint32_t draw, uint64_t* U0, uint64_t* U1) {
+    u4 c{(uint32_t)row, (uint32_t)(row >> 32), stage, draw};
+    u4 r = philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+    *U0 = (((uint64_t)r.x << 21) ^ (uint64_t)(r.y >> 11)) & ((1ull << 53) - 1);
+    *U1 = (((uint64_t)r.z << 21) ^ (uint64_t)(r.w >> 11)) & ((1ull << 53) - 1);
+}
+
 __device__ __forceinline__ float u53_to_f(uint64_t U) {
     return (float)(uint32_t)(U >> 29) * (1.0f / 16777216.0f);
 }
@@ -547,6 +556,87 @@ __device__ __forceinline__ int brute_force_nearest(const mgpu_stage& st, ff3 pos
     return mine;
 }
 
+// CATL1L2Stack layers after the membrane (missions/mitsnl/catgrating.py):
+// QualityFactor (:160-161), L1 (:196-207), L2Abs (:231-245), L2Diffraction
+// (:263-268) through RandomGaussianScatter (optics/scatter.py:109-150), in
+// FP32-local arithmetic: direction changes formed directly (the L1 grating
+// as the membrane, the L2 turn as two small rotations), probabilities in
+// float32, the L1 support transmission interpolated in float64.  Out of
+// line: only stages of stacked facets call it.
+__device__ __noinline__ void cat_stack_layers_l(const mgpu_stage& st, const mgpu_catstack& K,
+                                                int f, int m, float ly, float lz, uint64_t U1,
+                                                double u_sup, double z_l2, double u_phi,
+                                                PhotonL& ph, int64_t i, uint32_t* status) {
+    const mgpu_facet32* fc = st.facets32 + f;
+    const f3 n = ldf3(fc->ex);
+    // QualityFactor: factor ** (order ** 2)
+    const float q = powf(__double2float_rn(K.qf), (float)(m * m));
+    if (!(q >= 0.0f && q <= 1.0f)) atomicOr(status, MGPU_STATUS_PROB_RANGE);
+    ph.prob *= q;
+    // L1: a CAT grating with grooves at pi/2, or the support bars
+    const double* lv = K.l1_vec + 6 * (int64_t)f;
+    const f3 l1{__double2float_rn(lv[0]), __double2float_rn(lv[1]), __double2float_rn(lv[2])};
+    const f3 d1{__double2float_rn(lv[3]), __double2float_rn(lv[4]), __double2float_rn(lv[5])};
+    const f3 p = normf(ph.dir);
+    const float p_l = dotf(p, l1), p_d = dotf(p, d1), p_n = dotf(p, n);
+    const float blaze1 = atan2f(fabsf(p_d), fabsf(p_n));       // = arccos|p_perp . n|
+    float prob1;
+    int m1 = select_order_l(st.selectors[K.l1_selector], ph.energy_d, U1, &prob1, status);
+    if (u_sup > K.l1_open) {
+        m1 = 0;
+        const double t = np_interp(K.l1_trans_e, K.l1_trans_t, K.l1_n_trans, ph.energy_d, status);
+        if (t < 0.0 || t > 1.0) atomicOr(status, MGPU_STATUS_PROB_RANGE);
+        prob1 = __double2float_rn(t);
+    } else if (m1 != 0) {
+        const float sign = (p_d > 0.0f) ? 1.0f : ((p_d < 0.0f) ? -1.0f : 1.0f);
+        // sign * m * lambda / d in float-float
+        const double wd = 1.2398419292004202e-06 / K.l1_d;
+        const float wd_hi = __double2float_rn(wd);
+        ff term = ff_div(ff{wd_hi, __double2float_rn(wd - (double)wd_hi)}, ph.energy);
+        term = ff_mul_f(term, sign * (float)m1);
+        const float tf = ff_f(term);
+        const float pd2 = ff_f(ff_add_f(term, p_d));
+        const float p_n2 = sqrtf(1.0f - pd2 * pd2 - p_l * p_l);
+        const float sgn_n = (p_n > 0.0f) ? 1.0f : ((p_n < 0.0f) ? -1.0f : 0.0f);
+        const float dn_comp = sgn_n * (-tf * (2.0f * p_d + tf)) / (p_n2 + fabsf(p_n));
+        const f3 delta = tf * d1 + dn_comp * n;
+        ph.pol = transport_delta_f(p, delta, ph.pol);
+        ph.dir = p + delta;
+    }
+    if (!(prob1 >= 0.0f && prob1 <= 1.0f)) atomicOr(status, MGPU_STATUS_PROB_RANGE);
+    ph.prob *= prob1;
+    stored(st.out[6], i, (double)m1);
+    storef(st.out[7], i, blaze1);
+    // L2Abs: open fraction minus the shadow of the inclined hexagon walls;
+    // sin(arccos |p . n|) = |p x n| (no cancellation near normal incidence)
+    const f3 p3 = normf(ph.dir);
+    const f3 pxn = crossf(p3, n);
+    const float sin3 = fminf(sqrtf(dotf(pxn, pxn)), 1.0f);
+    const float a2 = __double2float_rn(K.l2_open) -
+                     __double2float_rn(K.l2_shadow / K.l2_total) * sin3;
+    if (!(a2 >= 0.0f && a2 <= 1.0f)) atomicOr(status, MGPU_STATUS_PROB_RANGE);
+    ph.prob *= a2;
+    // L2Diffraction: N(0,1) * sigma about dir x guess, then a uniform turn
+    // about the direction, both as direction changes
+    const f3 guess = (fabsf(p3.x) < 0.99999f) ? f3{1.0f, 0.0f, 0.0f} : f3{0.0f, 1.0f, 0.0f};
+    const f3 perp = crossf(p3, guess);
+    const float wave_mm = __double2float_rn(MGPU_HC_KEV_NM / ph.energy_d * 1e-6);
+    const float sigma = (1.22f * 0.4f) * asinf(wave_mm / __double2float_rn(K.l2_inner));
+    const float ang = __double2float_rn(z_l2) * sigma;
+    const f3 dl1 = rot_transpose_delta_f(perp, ang, p3);
+    const f3 dl2 = rot_transpose_delta_f(p3, __double2float_rn(u_phi) * 6.283185307179586f,
+                                         p3 + dl1);
+    const f3 delta2 = dl1 + dl2;
+    ph.pol = transport_delta_f(p3, delta2, ph.pol);
+    ph.dir = p3 + delta2;
+    storef(st.out[8], i, ang);
+    storef(st.out[4], i, ly);
+    storef(st.out[5], i, lz);
+}
+
+// kStack: compiled with the CATL1L2Stack layers (launches whose chain has a
+// stacked facet stage); plain facet chains leave them out entirely
+template <bool kStack>
 __device__ bool stage_gratings_l(const mgpu_stage& st, PhotonL& ph, int64_t i, bool valid,
                                  int rng, uint64_t seed, uint64_t row_base, int sidx,
                                  uint32_t* status) {
@@ -560,7 +650,7 @@ __device__ bool stage_gratings_l(const mgpu_stage& st, PhotonL& ph, int64_t i, b
     }
     if (!valid) return false;
     if (f < 0) {
-        write_miss_defaults(st, i, 4);
+        write_miss_defaults(st, i, kStack ? MGPU_MAX_OUT : 4);
         return false;
     }
     h = facet_hit(st.facets32 + f, ph.pos, ph.dir);
@@ -570,7 +660,11 @@ __device__ bool stage_gratings_l(const mgpu_stage& st, PhotonL& ph, int64_t i, b
     f3 p = normf(ph.dir);
     float p_l = dotf(p, l), p_d = dotf(p, dn), p_n = dotf(p, n);
     float blaze = atan2f(fabsf(p_d), fabsf(p_n));      // = arccos|p_perp . n|
-    uint64_t U;
+    // NonParallelCATGrating.blaze_angle_modifier (catgrating.py:324-333)
+    const double blaze_d = (kStack && st.stack) ? (double)blaze + (st.stack->blaze_center +
+                                                       (double)h.ly * st.stack->d_blaze_mm)
+                                                : (double)blaze;
+    uint64_t U, U1 = 0;
     double u_pre = 0.0;
     if (rng == MGPU_RNG_PREDRAWN) {
         if (st.draw[0] == nullptr) {
@@ -579,8 +673,8 @@ __device__ bool stage_gratings_l(const mgpu_stage& st, PhotonL& ph, int64_t i, b
         }
         u_pre = st.draw[0][i * st.draw_stride];
         U = (uint64_t)(u_pre * 9007199254740992.0);
+        if (kStack && st.draw[1]) U1 = (uint64_t)(st.draw[1][i * st.draw_stride] * 9007199254740992.0);
     } else {
-        uint64_t U1;
         philox_u53(seed, row_base + (uint64_t)i, (uint32_t)sidx, &U, &U1);
     }
     float selprob;
@@ -591,7 +685,7 @@ __device__ bool stage_gratings_l(const mgpu_stage& st, PhotonL& ph, int64_t i, b
         // float64 evaluation of the interpolated table (float32 blaze angle)
         double u = (rng == MGPU_RNG_PREDRAWN) ? u_pre : (double)U * (1.0 / 9007199254740992.0);
         double tot;
-        m = select_order_spline(sel, ph.energy_d, (double)blaze, u, &tot);
+        m = select_order_spline(sel, ph.energy_d, blaze_d, u, &tot);
         if (tot < 0.0 || tot > 1.0) atomicOr(status, MGPU_STATUS_PROB_RANGE);
         selprob = (float)tot;
     } else {
@@ -620,22 +714,45 @@ __device__ bool stage_gratings_l(const mgpu_stage& st, PhotonL& ph, int64_t i, b
     storef(st.out[0], i, h.ly);
     storef(st.out[1], i, h.lz);
     stored(st.out[2], i, f2d_bits((float)m));
-    storef(st.out[3], i, blaze);
+    if (kStack && st.stack) stored(st.out[3], i, blaze_d);
+    else storef(st.out[3], i, blaze);
     if (st.id_out) store_id(st, i, fc->id_num);
+    if (kStack && st.stack) {
+        double u_sup, u_phi, z;
+        if (rng == MGPU_RNG_PREDRAWN) {
+            if (!st.draw[1] || !st.draw[2] || !st.draw[3] || !st.draw[4]) {
+                atomicOr(status, MGPU_STATUS_BAD_STAGE);
+                return false;
+            }
+            u_sup = st.draw[2][i * st.draw_stride];
+            z = st.draw[3][i * st.draw_stride];
+            u_phi = st.draw[4][i * st.draw_stride];
+        } else {
+            // the float64 kernel's counters: draw 1 (u_sup, u_phi), draw 2 (normal)
+            const uint64_t row = row_base + (uint64_t)i;
+            uint64_t A, B;
+            philox_u53_draw(seed, row, (uint32_t)sidx, 1u, &A, &B);
+            u_sup = (double)A * (1.0 / 9007199254740992.0);
+            u_phi = (double)B * (1.0 / 9007199254740992.0);
+            double z1;
+            philox_normal2(seed, row, (uint32_t)sidx, 2u, &z, &z1);
+        }
+        cat_stack_layers_l(st, *st.stack, f, m, h.ly, h.lz, U1, u_sup, z, u_phi, ph, i, status);
+    }
     ph.pos = h.ip;
     return true;
 }
 
 // one stage, kind known at compile time (KIND > 0) or read from the
 // descriptor (KIND == 0, generic chains)
-template <int KIND>
+template <int KIND, bool kStack>
 __device__ __forceinline__ bool run_stage_l(const mgpu_stage& st, PhotonL& ph, int64_t i,
                                             bool valid, const mgpu_chain& chain, int s) {
     const int kind = KIND ? KIND : st.kind;
     switch (kind) {
     case MGPU_STAGE_GRATINGS:
-        return stage_gratings_l(st, ph, i, valid, chain.rng, chain.seed, chain.row_base, s,
-                                chain.status);
+        return stage_gratings_l<kStack>(st, ph, i, valid, chain.rng, chain.seed, chain.row_base,
+                                        s, chain.status);
     case MGPU_STAGE_LENS:
         return valid && stage_lens_l(st, ph, i, chain.status);
     case MGPU_STAGE_SCATTER:
@@ -669,10 +786,12 @@ __device__ __forceinline__ void count_hits(bool hit, unsigned* s_hits, int s, in
 
 // generic chain: stage loop over the descriptors
 struct GenericChain {
+    template <bool kStack>
     __device__ static void run(const mgpu_chain& chain, PhotonL& ph, int64_t i, bool valid,
                                unsigned* s_hits, int lane) {
         for (int s = 0; s < chain.n_stages; ++s)
-            count_hits(run_stage_l<0>(chain.stages[s], ph, i, valid, chain, s), s_hits, s, lane);
+            count_hits(run_stage_l<0, kStack>(chain.stages[s], ph, i, valid, chain, s), s_hits, s,
+                       lane);
     }
 };
 
@@ -680,19 +799,22 @@ struct GenericChain {
 // the per-stage constants are read straight from the parameter bank
 template <int... K>
 struct FixedChain {
-    template <int KIND, int S>
+    template <int KIND, int S, bool kStack>
     __device__ static void step(const mgpu_chain& chain, PhotonL& ph, int64_t i, bool valid,
                                 unsigned* s_hits, int lane) {
-        count_hits(run_stage_l<KIND>(chain.stages[S], ph, i, valid, chain, S), s_hits, S, lane);
+        count_hits(run_stage_l<KIND, kStack>(chain.stages[S], ph, i, valid, chain, S), s_hits, S,
+                   lane);
     }
-    template <int... S>
+    template <bool kStack, int... S>
     __device__ static void run_seq(const mgpu_chain& chain, PhotonL& ph, int64_t i, bool valid,
                                    unsigned* s_hits, int lane, std::integer_sequence<int, S...>) {
-        (step<K, S>(chain, ph, i, valid, s_hits, lane), ...);
+        (step<K, S, kStack>(chain, ph, i, valid, s_hits, lane), ...);
     }
+    template <bool kStack>
     __device__ static void run(const mgpu_chain& chain, PhotonL& ph, int64_t i, bool valid,
                                unsigned* s_hits, int lane) {
-        run_seq(chain, ph, i, valid, s_hits, lane, std::make_integer_sequence<int, sizeof...(K)>{});
+        run_seq<kStack>(chain, ph, i, valid, s_hits, lane,
+                        std::make_integer_sequence<int, sizeof...(K)>{});
     }
     static bool matches(const mgpu_chain& chain) {
         const int kinds[] = {K...};
@@ -703,7 +825,7 @@ struct FixedChain {
     }
 };
 
-template <class Chain>
+template <class Chain, bool kStack>
 // 3 blocks of 256 per SM (<= 84 registers): measured 4 % faster than the
 // unconstrained allocation (100 registers, 2 blocks) and 5-15 % faster than
 // 128 x 6/7/8 or 256 x 4 (register spills)
@@ -743,7 +865,7 @@ chain_fp32local_kernel(const __grid_constant__ mgpu_chain chain, const __grid_co
                 io.pol.ptr[i * io.pol.stride + 3 * io.pol.cstride] != 0.0)
                 atomicOr(chain.status, MGPU_STATUS_BAD_W);
         }
-        Chain::run(chain, ph, i, valid, s_hits, lane);
+        Chain::template run<kStack>(chain, ph, i, valid, s_hits, lane);
         if (valid) {
             store3(io.pos_out, i, d3{ff2d(ph.pos.x), ff2d(ph.pos.y), ff2d(ph.pos.z)});
             store3(io.dir_out, i, d3{f2d_bits(ph.dir.x), f2d_bits(ph.dir.y), f2d_bits(ph.dir.z)});
@@ -782,15 +904,24 @@ cudaError_t mgpu_launch_chain_fp32local(const mgpu_chain& chain, const mgpu_phot
     int64_t blocks = (warps * 32 + kThreads - 1) / kThreads;
     int64_t cap = (int64_t)sm_count * 8 * (256 / kThreads);
     if (blocks > cap) blocks = cap;
-    if (ChainCat::matches(chain))
-        chain_fp32local_kernel<ChainCat><<<(unsigned)blocks, kThreads, 0, stream>>>(chain, io);
-    else if (ChainSpec::matches(chain))
-        chain_fp32local_kernel<ChainSpec><<<(unsigned)blocks, kThreads, 0, stream>>>(chain, io);
-    else if (ChainTel::matches(chain))
-        chain_fp32local_kernel<ChainTel><<<(unsigned)blocks, kThreads, 0, stream>>>(chain, io);
-    else if (ChainCatBars::matches(chain))
-        chain_fp32local_kernel<ChainCatBars><<<(unsigned)blocks, kThreads, 0, stream>>>(chain, io);
-    else
-        chain_fp32local_kernel<GenericChain><<<(unsigned)blocks, kThreads, 0, stream>>>(chain, io);
+    bool stacked = false;
+    for (int s = 0; s < chain.n_stages; ++s) stacked = stacked || chain.stages[s].stack != nullptr;
+    const unsigned gb = (unsigned)blocks;
+    if (stacked) {
+        if (ChainCatBars::matches(chain))
+            chain_fp32local_kernel<ChainCatBars, true><<<gb, kThreads, 0, stream>>>(chain, io);
+        else
+            chain_fp32local_kernel<GenericChain, true><<<gb, kThreads, 0, stream>>>(chain, io);
+    } else if (ChainCat::matches(chain)) {
+        chain_fp32local_kernel<ChainCat, false><<<gb, kThreads, 0, stream>>>(chain, io);
+    } else if (ChainSpec::matches(chain)) {
+        chain_fp32local_kernel<ChainSpec, false><<<gb, kThreads, 0, stream>>>(chain, io);
+    } else if (ChainTel::matches(chain)) {
+        chain_fp32local_kernel<ChainTel, false><<<gb, kThreads, 0, stream>>>(chain, io);
+    } else if (ChainCatBars::matches(chain)) {
+        chain_fp32local_kernel<ChainCatBars, false><<<gb, kThreads, 0, stream>>>(chain, io);
+    } else {
+        chain_fp32local_kernel<GenericChain, false><<<gb, kThreads, 0, stream>>>(chain, io);
+    }
     return cudaGetLastError();
 }

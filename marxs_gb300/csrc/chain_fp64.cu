@@ -234,25 +234,6 @@ __device__ __forceinline__ int nearest_facet_grid(const mgpu_stage& st, const Ph
     return best;
 }
 
-// np.interp / scipy interp1d (linear): largest j <= n - 2 with x[j] <= v,
-// slope (y[j+1] - y[j]) / (x[j+1] - x[j]), slope * (v - x[j]) + y[j]; the
-// last knot maps to y[n-1]; outside the table interp1d raises (status bit)
-__device__ double np_interp(const double* x, const double* y, int n, double v, uint32_t* status) {
-    if (!(v >= x[0] && v <= x[n - 1])) {
-        atomicOr(status, MGPU_STATUS_TABLE_RANGE);
-        return kNaN;
-    }
-    if (v == x[n - 1]) return y[n - 1];
-    int lo = 0, hi = n - 1;
-    while (hi - lo > 1) {
-        int mid = (lo + hi) >> 1;
-        if (x[mid] <= v) lo = mid;
-        else hi = mid;
-    }
-    double slope = (y[lo + 1] - y[lo]) / (x[lo + 1] - x[lo]);
-    return __dadd_rn(__dmul_rn(slope, v - x[lo]), y[lo]);
-}
-
 // CATL1L2Stack layers after the membrane (missions/mitsnl/catgrating.py):
 // QualityFactor (:160-161), L1 (:196-207), L2Abs (:231-245), L2Diffraction
 // (:263-268) through RandomGaussianScatter (optics/scatter.py:109-150).

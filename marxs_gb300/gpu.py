@@ -135,7 +135,6 @@ class _Instrument:
                                        f64(k['l1_trans_t']), k['l2_open'], k['l2_shadow'],
                                        k['l2_total'], k['l2_inner'])
                 self.stage_stack[si] = dev_bytes(bytes(cs))
-                self.fp32_error = ('CATL1L2Stack facets are traced in precision="fp64" only')
             try:
                 if st.kind in (_abi.STAGE_LENS, _abi.STAGE_SCATTER, _abi.STAGE_FLATDET):
                     self.stage_aux[si] = dev_bytes(L.flat32_block(st))

@@ -98,19 +98,12 @@ def test_golden_hits_are_counted(name):
     assert (np.asarray(out['facet']) >= 0).sum() == (ref['facet'] >= 0).sum() > 0
 
 
-def test_cat_stack_columns_and_fp32_local_refusal():
+def test_cat_stack_l1_order_column():
     """CATL1L2Stack facets: the L1 order column is exact (the reference's
-    own L1 draws decide it) and the FP32-local mode says it is not
-    available for stacks."""
-    from marxs_gb300 import configs, PhotonTable
-    from marxs_gb300.gpu import GpuSequence
+    own L1 draws decide it)."""
     g, out = _run_gpu('c6')
     ref = golden_outputs(g)
     assert np.array_equal(np.asarray(out['order_L1']), ref['order_L1'], equal_nan=True)
-    inst = configs.build('c6')
-    with pytest.raises(NotImplementedError, match='fp64'):
-        GpuSequence(inst.elements, precision='fp32local', rng='philox')(
-            PhotonTable(golden_inputs(g)))
 
 
 def test_catsupportbars_stage():
