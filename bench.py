@@ -339,6 +339,40 @@ def tolerancing_bench(args, torch):
                    'CaptureResAeff)'}
 
 
+def cat_stack_bench(args, torch, dev_in, n, row_base):
+    """The Arcus-style chain: the same photons through lens, scatter, 1000
+    CATL1L2Stack facets (membrane, quality factor, L1 grating/support, L2
+    absorption and diffraction), catsupportbars and the circular detector,
+    FP32-local, Philox; CUDA events per step."""
+    from marxs_gb300 import configs
+    from marxs_gb300.gpu import DevicePhotons, GpuSequence
+    inst = configs.build('c6')
+    seq = GpuSequence(elements=inst.elements, precision='fp32local', rng='philox', seed=12345)
+    out = DevicePhotons(n)
+    plan, bufs = seq.allocate_columns(n)
+    stream = torch.cuda.current_stream()
+    for _ in range(2):
+        seq.trace_device(dev_in, out, plan, bufs, row_base=row_base)
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(3):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        status, _ = seq.trace_device(dev_in, out, plan, bufs, row_base=row_base)
+        b.record(stream)
+        torch.cuda.synchronize()
+        times.append(a.elapsed_time(b))
+    if int(status.item()):
+        raise RuntimeError('cat stack trace status 0x%x' % int(status.item()))
+    ms = sorted(times)[1]
+    hit = float((bufs['facet'] >= 0).float().mean().item())
+    del out, plan, bufs
+    torch.cuda.empty_cache()
+    return {'value': n / (ms / 1e3), 'unit': 'photons/s', 'ms_per_step': ms,
+            'precision': 'fp32local', 'facet_hit_fraction': hit,
+            'workload': 'c2 photons through 1000 CATL1L2Stack facets + catsupportbars'}
+
+
 def adjoint_bench(args, torch):
     """Pose gradients on the 200-facet spectrometer: hand-written adjoint vs
     central finite differences (h = 1e-4 mm / 1e-6 rad) over all 1,207
@@ -682,6 +716,12 @@ def main():
         line['source_pipeline'] = source_pipeline_bench(args, torch, inst, n, head, row_base, dist)
     if rank == 0 and world == 1:
         line['analysis'] = analysis_bench(args, torch, results[head], n)
+    if rank == 0 and world == 1 and head == 'fp32local':
+        for k in ('seq', 'plan', 'bufs', 'out'):
+            for rr in results.values():
+                rr.pop(k, None)
+        torch.cuda.empty_cache()
+        line['cat_stack'] = cat_stack_bench(args, torch, dev_in, n, row_base)
     if rank == 0 and world == 1 and not args.no_adjoint:
         for k in ('seq', 'plan', 'bufs', 'out'):
             for rr in results.values():

@@ -118,6 +118,7 @@ typedef struct {
     const double* tx;
     const double* ty;
     const double* c;
+    const float* c32;     /* the coefficients in float32, for FP32-local chains */
 } mgpu_spline1;
 
 #define MGPU_SEL_CDF    0  /* cumulative rows: OrderSelector, EfficiencyFile */
@@ -233,6 +234,9 @@ typedef struct mgpu_catstack {
     double l2_shadow;            /* bardepth * inner */
     double l2_total;             /* period^2 / 2 * sqrt(3) */
     double l2_inner;             /* period - barwidth, mm */
+    /* FP32-local constants */
+    const float* l1_vec32;       /* l1_vec in float32 */
+    float l1_wd_hi, l1_wd_lo;    /* energy2wave / L1 period as float-float (keV) */
 } mgpu_catstack;
 
 typedef struct {

@@ -71,7 +71,7 @@ class MgpuPhotons(C.Structure):
 
 class MgpuSpline1(C.Structure):
     _fields_ = [('nx', C.c_int32), ('ny', C.c_int32), ('n_surf', C.c_int32), ('pad', C.c_int32),
-                ('tx', C.c_void_p), ('ty', C.c_void_p), ('c', C.c_void_p)]
+                ('tx', C.c_void_p), ('ty', C.c_void_p), ('c', C.c_void_p), ('c32', C.c_void_p)]
 
 
 class MgpuSelector(C.Structure):
@@ -118,7 +118,8 @@ class MgpuCatStack(C.Structure):
                 ('l1_open', C.c_double), ('l1_d', C.c_double), ('l1_vec', C.c_void_p),
                 ('l1_selector', C.c_int32), ('l1_n_trans', C.c_int32), ('l1_trans_e', C.c_void_p),
                 ('l1_trans_t', C.c_void_p), ('l2_open', C.c_double), ('l2_shadow', C.c_double),
-                ('l2_total', C.c_double), ('l2_inner', C.c_double)]
+                ('l2_total', C.c_double), ('l2_inner', C.c_double), ('l1_vec32', C.c_void_p),
+                ('l1_wd_hi', C.c_float), ('l1_wd_lo', C.c_float)]
 
 
 class MgpuStage(C.Structure):

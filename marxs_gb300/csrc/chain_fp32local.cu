@@ -200,6 +200,79 @@ __device__ __forceinline__ float u53_to_f(uint64_t U) {
     return (float)(uint32_t)(U >> 29) * (1.0f / 16777216.0f);
 }
 
+// ------------------------------------------------------------ splines
+// Degree-1 spline (the FITPACK evaluation of spline1_at, mgpu_device.cuh)
+// in float32: knot intervals found on order-preserving integer keys of the
+// float64 knots, offsets from the knot formed in float64, weights and the
+// 2x2 coefficient sum in float32 (coefficients from the float32 copy).
+__device__ __forceinline__ uint64_t knot_key(double x) {
+    const uint64_t b = (uint64_t)__double_as_longlong(x);
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+
+__device__ __forceinline__ void spline1_axis_f(const double* t, int n, double a, int& l,
+                                               float& h0, float& h1) {
+    double arg = a;
+    const uint64_t ka = knot_key(a);
+    if (!isnan(a)) {
+        if (ka < knot_key(t[1])) arg = t[1];
+        else if (ka > knot_key(t[n - 2])) arg = t[n - 2];
+    }
+    const uint64_t karg = knot_key(arg);
+    int lo = 2, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (knot_key(t[mid]) > karg) hi = mid;
+        else lo = mid + 1;
+    }
+    l = lo - 1;
+    if (l > n - 3) l = n - 3;
+    const float inv = 1.0f / __double2float_rn(t[l + 1] - t[l]);
+    h0 = __double2float_rn(t[l + 1] - arg) * inv;
+    h1 = __double2float_rn(arg - t[l]) * inv;
+}
+
+struct Spline1Wf {
+    int base;
+    float hx0, hx1, hy0, hy1;
+};
+
+__device__ __forceinline__ Spline1Wf spline1_weights_f(const mgpu_spline1& S, double x, double y) {
+    Spline1Wf w;
+    int lx, ly;
+    spline1_axis_f(S.tx, S.nx, x, lx, w.hx0, w.hx1);
+    spline1_axis_f(S.ty, S.ny, y, ly, w.hy0, w.hy1);
+    w.base = (lx - 1) * (S.ny - 2) + (ly - 1);
+    return w;
+}
+
+__device__ __forceinline__ float spline1_value_f(const mgpu_spline1& S, int s, const Spline1Wf& w) {
+    const int nky1 = S.ny - 2;
+    const float* c = S.c32 + (size_t)s * (size_t)(S.nx - 2) * (size_t)nky1 + w.base;
+    return fmaf(__ldg(c) * w.hx0, w.hy0,
+                fmaf(__ldg(c + 1) * w.hx0, w.hy1,
+                     fmaf(__ldg(c + nky1) * w.hx1, w.hy0, __ldg(c + nky1 + 1) * w.hx1 * w.hy1)));
+}
+
+// InterpolateEfficiencyTable.__call__ (missions/mitsnl/catgrating.py:101-144)
+// in float32: the order whose running sum / total first exceeds u (index 0
+// when none does); the probability factor is the total
+__device__ __forceinline__ int select_order_spline_f(const mgpu_selector& sel, double energy,
+                                                     double blaze, float u, float* prob) {
+    const double wave = MGPU_HC_KEV_NM / energy;
+    const Spline1Wf w = spline1_weights_f(sel.spline, wave, blaze);
+    float total = 0.0f;
+    for (int k = 0; k < sel.n_orders; ++k) total += spline1_value_f(sel.spline, k, w);
+    float cum = 0.0f;
+    int pick = -1;
+    for (int k = 0; k < sel.n_orders && pick < 0; ++k) {
+        cum += spline1_value_f(sel.spline, k, w);
+        if (cum / total > u) pick = k;
+    }
+    *prob = total;
+    return sel.orders[pick < 0 ? 0 : pick];
+}
+
 // ------------------------------------------------------------------ stages
 __device__ bool stage_lens_l(const mgpu_stage& st, PhotonL& ph, int64_t i, uint32_t* status) {
     // PerfectLens.specific_process_photons, optics/mirror.py:53-82
@@ -218,10 +291,11 @@ __device__ bool stage_lens_l(const mgpu_stage& st, PhotonL& ph, int64_t i, uint3
         f3 od = normf(ph.dir);
         f3 cr = crossf(od, nd);
         float angle = atan2f(sqrtf(dotf(cr, cr)), fabsf(dotf(od, nd)));
-        double r = spline1_at(st.spline, ph.energy_d, 0.25 * (double)angle);
+        const Spline1Wf w = spline1_weights_f(st.spline, ph.energy_d, 0.25 * (double)angle);
+        float r = spline1_value_f(st.spline, 0, w);
         r = r * r;
-        if (r < 0.0 || r > 1.0) atomicOr(status, MGPU_STATUS_PROB_RANGE);
-        ph.prob = ph.prob * (float)r;
+        if (!(r >= 0.0f && r <= 1.0f)) atomicOr(status, MGPU_STATUS_PROB_RANGE);
+        ph.prob = ph.prob * r;
     }
     ph.pol = transport_f(ph.dir, nd, ph.pol);
     ph.dir = nd;
@@ -574,9 +648,9 @@ __device__ __noinline__ void cat_stack_layers_l(const mgpu_stage& st, const mgpu
     if (!(q >= 0.0f && q <= 1.0f)) atomicOr(status, MGPU_STATUS_PROB_RANGE);
     ph.prob *= q;
     // L1: a CAT grating with grooves at pi/2, or the support bars
-    const double* lv = K.l1_vec + 6 * (int64_t)f;
-    const f3 l1{__double2float_rn(lv[0]), __double2float_rn(lv[1]), __double2float_rn(lv[2])};
-    const f3 d1{__double2float_rn(lv[3]), __double2float_rn(lv[4]), __double2float_rn(lv[5])};
+    const float* lv = K.l1_vec32 + 6 * (int64_t)f;
+    const f3 l1{__ldg(lv), __ldg(lv + 1), __ldg(lv + 2)};
+    const f3 d1{__ldg(lv + 3), __ldg(lv + 4), __ldg(lv + 5)};
     const f3 p = normf(ph.dir);
     const float p_l = dotf(p, l1), p_d = dotf(p, d1), p_n = dotf(p, n);
     const float blaze1 = atan2f(fabsf(p_d), fabsf(p_n));       // = arccos|p_perp . n|
@@ -590,9 +664,7 @@ __device__ __noinline__ void cat_stack_layers_l(const mgpu_stage& st, const mgpu
     } else if (m1 != 0) {
         const float sign = (p_d > 0.0f) ? 1.0f : ((p_d < 0.0f) ? -1.0f : 1.0f);
         // sign * m * lambda / d in float-float
-        const double wd = 1.2398419292004202e-06 / K.l1_d;
-        const float wd_hi = __double2float_rn(wd);
-        ff term = ff_div(ff{wd_hi, __double2float_rn(wd - (double)wd_hi)}, ph.energy);
+        ff term = ff_div(ff{K.l1_wd_hi, K.l1_wd_lo}, ph.energy);
         term = ff_mul_f(term, sign * (float)m1);
         const float tf = ff_f(term);
         const float pd2 = ff_f(ff_add_f(term, p_d));
@@ -682,12 +754,9 @@ __device__ bool stage_gratings_l(const mgpu_stage& st, PhotonL& ph, int64_t i, b
     const mgpu_selector& sel = st.selectors[fc->selector];
     int m;
     if (sel.kind == MGPU_SEL_SPLINE) {
-        // float64 evaluation of the interpolated table (float32 blaze angle)
-        double u = (rng == MGPU_RNG_PREDRAWN) ? u_pre : (double)U * (1.0 / 9007199254740992.0);
-        double tot;
-        m = select_order_spline(sel, ph.energy_d, blaze_d, u, &tot);
-        if (tot < 0.0 || tot > 1.0) atomicOr(status, MGPU_STATUS_PROB_RANGE);
-        selprob = (float)tot;
+        // float32 evaluation of the interpolated table
+        m = select_order_spline_f(sel, ph.energy_d, blaze_d, u53_to_f(U), &selprob);
+        if (!(selprob >= 0.0f && selprob <= 1.0f)) atomicOr(status, MGPU_STATUS_PROB_RANGE);
     } else {
         m = select_order_l(sel, ph.energy_d, U, &selprob, status);
     }
@@ -728,14 +797,18 @@ __device__ bool stage_gratings_l(const mgpu_stage& st, PhotonL& ph, int64_t i, b
             z = st.draw[3][i * st.draw_stride];
             u_phi = st.draw[4][i * st.draw_stride];
         } else {
-            // the float64 kernel's counters: draw 1 (u_sup, u_phi), draw 2 (normal)
+            // the float64 kernel's counters: draw 1 (u_sup, u_phi), draw 2
+            // (the normal, by Box-Muller in float32 from the same uniforms)
             const uint64_t row = row_base + (uint64_t)i;
             uint64_t A, B;
             philox_u53_draw(seed, row, (uint32_t)sidx, 1u, &A, &B);
             u_sup = (double)A * (1.0 / 9007199254740992.0);
             u_phi = (double)B * (1.0 / 9007199254740992.0);
-            double z1;
-            philox_normal2(seed, row, (uint32_t)sidx, 2u, &z, &z1);
+            philox_u53_draw(seed, row, (uint32_t)sidx, 2u, &A, &B);
+            const float one_minus_u0 = (float)((1ull << 53) - A) * 1.1102230246251565e-16f;
+            float sn, cs;
+            sincospif(2.0f * u53_to_f(B), &sn, &cs);
+            z = (double)(sqrtf(-2.0f * logf(one_minus_u0)) * cs);   // accurate log: small u
         }
         cat_stack_layers_l(st, *st.stack, f, m, h.ly, h.lz, U1, u_sup, z, u_phi, ph, i, status);
     }

@@ -111,9 +111,11 @@ class _Instrument:
                 return out
             ts = [torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).to(device)
                   for a in sp]
-            self.keep += ts
+            c32 = torch.from_numpy(np.ascontiguousarray(sp[2], dtype=np.float32)).to(device)
+            self.keep += ts + [c32]
             out.nx, out.ny, out.n_surf = len(sp[0]), len(sp[1]), int(sp[2].shape[0])
             out.tx, out.ty, out.c = ts[0].data_ptr(), ts[1].data_ptr(), ts[2].data_ptr()
+            out.c32 = c32.data_ptr()
             return out
 
         self.stage_spline = {}
@@ -129,11 +131,16 @@ class _Instrument:
                 self.stage_spline[si] = spline_struct(st.spline)
             if st.stack is not None:
                 k = st.stack
+                l1v32 = torch.from_numpy(np.ascontiguousarray(k['l1_vec'], dtype=np.float32)).to(
+                    device)
+                self.keep.append(l1v32)
+                wd_hi, wd_lo = L.split_ff(1.2398419292004202e-06 / float(k['l1_d']))
                 cs = _abi.MgpuCatStack(k['blaze_center'], k['d_blaze_mm'], k['qf'], k['l1_open'],
                                        k['l1_d'], f64(k['l1_vec']), k['l1_selector'],
                                        len(k['l1_trans_e']), f64(k['l1_trans_e']),
                                        f64(k['l1_trans_t']), k['l2_open'], k['l2_shadow'],
-                                       k['l2_total'], k['l2_inner'])
+                                       k['l2_total'], k['l2_inner'], l1v32.data_ptr(),
+                                       float(wd_hi), float(wd_lo))
                 self.stage_stack[si] = dev_bytes(bytes(cs))
             try:
                 if st.kind in (_abi.STAGE_LENS, _abi.STAGE_SCATTER, _abi.STAGE_FLATDET):
