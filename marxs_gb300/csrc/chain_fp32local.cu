@@ -33,8 +33,13 @@ namespace {
 #ifndef MGPU_FP32L_MIN_BLOCKS
 #define MGPU_FP32L_MIN_BLOCKS 3
 #endif
+// grid cap in blocks of 256 threads per SM (0: one block per 256 photons)
+#ifndef MGPU_FP32L_GRID_PER_SM
+#define MGPU_FP32L_GRID_PER_SM 0
+#endif
 constexpr int kThreads = MGPU_FP32L_THREADS;
 constexpr int kMinBlocks = MGPU_FP32L_MIN_BLOCKS;
+constexpr int kGridPerSm = MGPU_FP32L_GRID_PER_SM;
 
 struct PhotonL {
     ff3 pos;
@@ -975,8 +980,11 @@ cudaError_t mgpu_launch_chain_fp32local(const mgpu_chain& chain, const mgpu_phot
     }
     int64_t warps = (io.n + 31) / 32;
     int64_t blocks = (warps * 32 + kThreads - 1) / kThreads;
-    int64_t cap = (int64_t)sm_count * 8 * (256 / kThreads);
-    if (blocks > cap) blocks = cap;
+    if (kGridPerSm > 0) {
+        const int64_t cap = (int64_t)sm_count * kGridPerSm * 256 / kThreads;
+        if (blocks > cap) blocks = cap;
+    }
+    if (blocks > (1 << 30)) blocks = 1 << 30;   // grid-stride beyond
     bool stacked = false;
     for (int s = 0; s < chain.n_stages; ++s) stacked = stacked || chain.stages[s].stack != nullptr;
     const unsigned gb = (unsigned)blocks;

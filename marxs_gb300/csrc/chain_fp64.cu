@@ -23,6 +23,11 @@
 namespace {
 
 constexpr int kThreads = 256;
+// grid cap in blocks per SM (0: one block per 256 photons)
+#ifndef MGPU_FP64_GRID_PER_SM
+#define MGPU_FP64_GRID_PER_SM 0
+#endif
+constexpr int kGridPerSm = MGPU_FP64_GRID_PER_SM;
 constexpr double kEnergy2Wave = 1.2398419292004202e-06;   // marxs/__init__.py:14
 
 __device__ __forceinline__ PlaneHit plane_intersect_frame(const double* f, d3 pos, d3 dir) {
@@ -501,8 +506,11 @@ cudaError_t mgpu_launch_chain_fp64(const mgpu_chain& chain, const mgpu_photons& 
     if (io.n <= 0) return cudaSuccess;
     int64_t warps = (io.n + 31) / 32;
     int64_t blocks = (warps * 32 + kThreads - 1) / kThreads;
-    int64_t cap = (int64_t)sm_count * 8;
-    if (blocks > cap) blocks = cap;
+    if (kGridPerSm > 0) {
+        const int64_t cap = (int64_t)sm_count * kGridPerSm;
+        if (blocks > cap) blocks = cap;
+    }
+    if (blocks > (1 << 30)) blocks = 1 << 30;   // grid-stride beyond
     chain_fp64_kernel<<<(unsigned)blocks, kThreads, 0, stream>>>(chain, io);
     return cudaGetLastError();
 }

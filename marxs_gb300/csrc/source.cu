@@ -12,6 +12,11 @@
 namespace {
 
 constexpr int kThreads = 256;
+// grid cap in blocks per SM (0: one block per 256 photons)
+#ifndef MGPU_SOURCE_GRID_PER_SM
+#define MGPU_SOURCE_GRID_PER_SM 8
+#endif
+constexpr int kGridPerSm = MGPU_SOURCE_GRID_PER_SM;
 constexpr double kTwoPi = 6.283185307179586;
 constexpr double kPi = 3.141592653589793;
 
@@ -180,8 +185,11 @@ extern "C" int mgpu_generate_photons(const mgpu_source* src, mgpu_vec pos, mgpu_
     if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
         return (int)e;
     int64_t blocks = (S.n + kThreads - 1) / kThreads;
-    const int64_t cap = (int64_t)sms * 8;
-    if (blocks > cap) blocks = cap;
+    if (kGridPerSm > 0) {
+        const int64_t cap = (int64_t)sms * kGridPerSm;
+        if (blocks > cap) blocks = cap;
+    }
+    if (blocks > (1 << 30)) blocks = 1 << 30;   // grid-stride beyond
     if (S.precision == MGPU_FP32LOCAL)
         generate_fast_kernel<<<(unsigned)blocks, kThreads, 0, (cudaStream_t)stream>>>(
             S, pos, dir, pol, energy, prob);
