@@ -56,6 +56,8 @@ def parse():
     p.add_argument('--no-tolerancing', action='store_true')
     p.add_argument('--tolerancing-photons', type=float, default=1e7)
     p.add_argument('--tolerancing-sets', type=int, default=10)
+    p.add_argument('--no-stages', action='store_true')
+    p.add_argument('--stage-photons', type=float, default=2e7)
     return p.parse_args()
 
 
@@ -371,6 +373,131 @@ def cat_stack_bench(args, torch, dev_in, n, row_base):
     return {'value': n / (ms / 1e3), 'unit': 'photons/s', 'ms_per_step': ms,
             'precision': 'fp32local', 'facet_hit_fraction': hit,
             'workload': 'c2 photons through 1000 CATL1L2Stack facets + catsupportbars'}
+
+
+def fma_peaks(torch):
+    """Measured FMA throughput (flop/s) of the FP32 and FP64 pipes: the
+    library's FMA-chain probe, 8 blocks of 256 threads per SM."""
+    import ctypes as C
+    from marxs_gb300 import _abi
+    lib = _abi.load()
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    blocks = sms * 8
+    out = {}
+    for name, prec, iters, dt in (('fp32', _abi.FP32LOCAL, 1 << 16, torch.float32),
+                                  ('fp64', _abi.FP64, 1 << 10, torch.float64)):
+        buf = torch.empty(blocks * 256, dtype=dt, device='cuda')
+        stream = torch.cuda.current_stream()
+
+        def run():
+            _abi.check(lib.mgpu_fma_probe(prec, blocks, iters, C.c_void_p(buf.data_ptr()),
+                                          C.c_void_p(stream.cuda_stream)), 'mgpu_fma_probe')
+        for _ in range(3):
+            run()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(5)]
+        for a, b in ev:
+            a.record(stream)
+            run()
+            b.record(stream)
+        torch.cuda.synchronize()
+        ms = sorted(a.elapsed_time(b) for a, b in ev)[2]
+        out[name] = 2.0 * 8 * iters * 256 * blocks / (ms / 1e3)
+    return out
+
+
+def grid_candidates(torch, seq, ph):
+    """Mean candidate-list length per photon at the facet stage's grid
+    lookup (the lookup's own arithmetic on the photons entering the stage;
+    0 outside the grid or beyond its slope limit)."""
+    from marxs_gb300 import _abi
+    low = seq.lower()
+    si = [k for k, st in enumerate(low.stages) if st.kind == _abi.STAGE_GRATINGS][0]
+    g = low.stages[si].grid
+    start = low.stage_grid_bufs[si][0].to(torch.int64)
+    vec = lambda x: torch.tensor([float(v) for v in x], dtype=torch.float64, device='cuda')[:, None]
+    o, nrm, a, b = vec(g['o']), vec(g['n']), vec(g['a']), vec(g['b'])
+    rel = ph.pos - o
+    dn = (ph.dir * nrm).sum(0)
+    da = (ph.dir * a).sum(0)
+    db = (ph.dir * b).sum(0)
+    t0 = -(rel * nrm).sum(0) / dn
+    u = (rel * a).sum(0) + t0 * da
+    v = (rel * b).sum(0) + t0 * db
+    iu = torch.floor((u - g['u0']) / g['cell'])
+    iv = torch.floor((v - g['v0']) / g['cell'])
+    ok = ((iu >= 0) & (iu < g['nu']) & (iv >= 0) & (iv < g['nv']) &
+          (da.abs() <= g['slope_max'] * dn.abs()) & (db.abs() <= g['slope_max'] * dn.abs()))
+    cell = (iu.clamp(0, g['nu'] - 1) * g['nv'] + iv.clamp(0, g['nv'] - 1)).to(torch.int64)
+    cnt = (start[cell + 1].clamp(max=g['capacity']) - start[cell]).clamp(min=0)
+    return float((cnt * ok).sum()) / ph.n
+
+
+def stages_bench(args, torch, inst, dev_in):
+    """Each stage of the workload's chain launched on its own (a one-stage
+    chain, generic kernel) on the photons the previous stages produced:
+    its own algorithmic bytes (state read 88 B, state written 80 B, its
+    columns) against the measured HBM peak, and for the facet stage the
+    intersect arithmetic against the measured FMA peak (per photon: 37 flops
+    per grid candidate, 153 per hit for diffraction and transport)."""
+    from marxs_gb300 import _abi
+    from marxs_gb300.gpu import DevicePhotons, GpuSequence
+    n = min(int(args.stage_photons), dev_in.n)
+    hbm, hbm_src = peaks()
+    fma = fma_peaks(torch)
+    src = dev_in
+    if n < dev_in.n:
+        src = DevicePhotons(n)
+        for k in ('pos', 'dir', 'pol'):
+            getattr(src, k).copy_(getattr(dev_in, k)[:, :n])
+        src.energy.copy_(dev_in.energy[:n])
+        src.prob.copy_(dev_in.prob[:n])
+    names = ['lens', 'scatter', 'facets', 'detector']
+    res = {'photons': n, 'fma_peak_flops': fma, 'hbm_peak_gbs': hbm, 'hbm_peak_source': hbm_src,
+           'kernel': 'chain kernels, generic one-stage chain'}
+    for prec in ('fp32local', 'fp64'):
+        cur = src
+        rows = {}
+        for k, elem in enumerate(inst.elements):
+            seq = GpuSequence(elements=[elem], precision=prec, rng='philox', seed=12345)
+            plan, bufs = seq.allocate_columns(n)
+            out = DevicePhotons(n)
+            hits = torch.zeros(_abi.MAX_STAGES, dtype=torch.int64, device='cuda')
+            seq.trace_device(cur, out, plan, bufs, hits=hits)
+            torch.cuda.synchronize()
+            n_hit = int(hits[0])
+            stream = torch.cuda.current_stream()
+            for _ in range(2):
+                seq.trace_device(cur, out, plan, bufs)
+            ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                  for _ in range(5)]
+            for a, b in ev:
+                a.record(stream)
+                seq.trace_device(cur, out, plan, bufs)
+                b.record(stream)
+            torch.cuda.synchronize()
+            ms = sorted(a.elapsed_time(b) for a, b in ev)[2]
+            B = algorithmic_bytes(seq)
+            gbs = B * n / (ms / 1e3) / 1e9
+            row = {'ms': ms, 'bytes_per_photon': B, 'achieved_gbs': gbs, 'hbm_frac': gbs / hbm,
+                   'hits': n_hit}
+            if names[k] == 'facets':
+                cand = grid_candidates(torch, seq, cur)
+                flops = 37.0 * cand * n + 153.0 * n_hit
+                rate = flops / (ms / 1e3)
+                peak = fma['fp32' if prec == 'fp32local' else 'fp64']
+                row.update({'candidates_per_photon': cand, 'flops': flops, 'flop_rate': rate,
+                            'fma_frac': rate / peak,
+                            'fma_pipe': 'fp32' if prec == 'fp32local' else 'fp64'})
+            rows[names[k]] = row
+            del plan, bufs
+            if cur is not src:
+                del cur
+            cur = out
+        res[prec] = rows
+    del cur
+    torch.cuda.empty_cache()
+    return res
 
 
 def adjoint_bench(args, torch):
@@ -722,6 +849,12 @@ def main():
                 rr.pop(k, None)
         torch.cuda.empty_cache()
         line['cat_stack'] = cat_stack_bench(args, torch, dev_in, n, row_base)
+    if rank == 0 and world == 1 and not args.no_stages:
+        for k in ('seq', 'plan', 'bufs', 'out'):
+            for rr in results.values():
+                rr.pop(k, None)
+        torch.cuda.empty_cache()
+        line['stages'] = stages_bench(args, torch, inst, dev_in)
     if rank == 0 and world == 1 and not args.no_adjoint:
         for k in ('seq', 'plan', 'bufs', 'out'):
             for rr in results.values():

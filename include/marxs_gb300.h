@@ -568,6 +568,15 @@ typedef struct {
 
 int mgpu_facet_poses(const mgpu_pose_update* update, void* stream);
 
+/* ---- measurement (no counterpart in the reference) ----
+ * FMA-chain throughput probe: ``blocks`` blocks of 256 threads, each thread
+ * running 8 independent chains of ``iters`` fused multiply-adds in float32
+ * (precision MGPU_FP32LOCAL) or float64 (MGPU_FP64); out receives one value
+ * per thread (blocks * 256 floats or doubles).  2 * 8 * iters * 256 * blocks
+ * flops per launch: the measured FMA peak of the pipe the intersect stage's
+ * arithmetic runs on. */
+int mgpu_fma_probe(int32_t precision, int32_t blocks, int32_t iters, void* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -14,7 +14,7 @@ CSRC = os.path.join(HERE, 'csrc')
 BUILD = os.path.join(HERE, '_build')
 LIB = os.path.join(HERE, 'libmarxs_gb300.so')
 SOURCES = ['chain_fp64.cu', 'chain_fp32local.cu', 'grid_build.cu', 'capi.cu', 'adjoint.cu',
-           'source.cu', 'analysis.cu', 'poses.cu']
+           'source.cu', 'analysis.cu', 'poses.cu', 'peaks.cu']
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 FLAGS = ['-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC', '--expt-relaxed-constexpr']
 

@@ -92,6 +92,7 @@ class _Instrument:
         self.stage_facets = {}
         self.stage_selectors = {}
         self.stage_grid = {}
+        self.stage_grid_bufs = {}     # si -> (cell_start, cell_items)
         self.stage_aux = {}       # FP32-local constant blocks
         self.stage_facets32 = {}
         self.stage_cand32 = {}
@@ -218,6 +219,7 @@ class _Instrument:
         grid.cell_start, grid.cell_items = start.data_ptr(), items.data_ptr()
         grid.capacity = g['capacity']
         self.stage_grid[si] = grid
+        self.stage_grid_bufs[si] = (start, items)
         if si in self.stage_facets32:
             aux = torch.from_numpy(np.frombuffer(L.grid32_block(g), dtype=np.uint8).copy()).to(dev)
             self.keep.append(aux)
