@@ -119,6 +119,8 @@ typedef struct {
     const double* ty;
     const double* c;
     const float* c32;     /* the coefficients in float32, for FP32-local chains */
+    const float* tx_ff;   /* FP32-local: the knots as float-float (hi, lo) pairs, nx x 2 */
+    const float* ty_ff;   /* ny x 2 */
 } mgpu_spline1;
 
 #define MGPU_SEL_CDF    0  /* cumulative rows: OrderSelector, EfficiencyFile */
@@ -144,6 +146,10 @@ typedef struct {
     mgpu_spline1 spline;  /* SPLINE: n_surf = n_orders surfaces */
     const uint8_t* guide; /* optional, sorted rows only: n_rows x 64, entry b = first order
                              index k with U < threshold[k] for U = b * 2^47 */
+    const double* e_mid;  /* optional, sorted energy rows (FP32-local): n_rows - 1 midpoints
+                             (E_j + E_j+1) / 2; row j+1 is nearer when e > e_mid[j] */
+    float e0_f;           /* FP32-local row guess: E_0 and (n_rows - 1) / (E_last - E_0) */
+    float e_scale_f;
 } mgpu_selector;
 
 /* FP32-local constants of a flat element (PerfectLens, RadialMirrorScatter,
@@ -237,6 +243,15 @@ typedef struct mgpu_catstack {
     /* FP32-local constants */
     const float* l1_vec32;       /* l1_vec in float32 */
     float l1_wd_hi, l1_wd_lo;    /* energy2wave / L1 period as float-float (keV) */
+    float qf32;                  /* qf */
+    float l2_open32;             /* l2_open */
+    float l2_absorb32;           /* l2_shadow / l2_total */
+    float l2_inv_inner32;        /* 1 / l2_inner, 1/mm */
+    float blaze_center32, d_blaze32;
+    int64_t l1_open_u53;         /* floor(l1_open * 2^53) (>= -1): a Philox draw U
+                                    (u = U 2^-53) takes the support when U > l1_open_u53 */
+    const float* l1_trans_e32;   /* l1_trans_e, l1_trans_t in float32 */
+    const float* l1_trans_t32;
 } mgpu_catstack;
 
 typedef struct {

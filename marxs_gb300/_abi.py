@@ -71,7 +71,8 @@ class MgpuPhotons(C.Structure):
 
 class MgpuSpline1(C.Structure):
     _fields_ = [('nx', C.c_int32), ('ny', C.c_int32), ('n_surf', C.c_int32), ('pad', C.c_int32),
-                ('tx', C.c_void_p), ('ty', C.c_void_p), ('c', C.c_void_p), ('c32', C.c_void_p)]
+                ('tx', C.c_void_p), ('ty', C.c_void_p), ('c', C.c_void_p), ('c32', C.c_void_p),
+                ('tx_ff', C.c_void_p), ('ty_ff', C.c_void_p)]
 
 
 class MgpuSelector(C.Structure):
@@ -79,7 +80,8 @@ class MgpuSelector(C.Structure):
                 ('sorted', C.c_int32), ('energy', C.c_void_p), ('cdf', C.c_void_p),
                 ('total', C.c_void_p), ('orders', C.c_void_p), ('thresholds', C.c_void_p),
                 ('kind', C.c_int32), ('pad', C.c_int32), ('spline', MgpuSpline1),
-                ('guide', C.c_void_p)]
+                ('guide', C.c_void_p), ('e_mid', C.c_void_p), ('e0_f', C.c_float),
+                ('e_scale_f', C.c_float)]
 
 
 class MgpuFlat32(C.Structure):
@@ -119,7 +121,11 @@ class MgpuCatStack(C.Structure):
                 ('l1_selector', C.c_int32), ('l1_n_trans', C.c_int32), ('l1_trans_e', C.c_void_p),
                 ('l1_trans_t', C.c_void_p), ('l2_open', C.c_double), ('l2_shadow', C.c_double),
                 ('l2_total', C.c_double), ('l2_inner', C.c_double), ('l1_vec32', C.c_void_p),
-                ('l1_wd_hi', C.c_float), ('l1_wd_lo', C.c_float)]
+                ('l1_wd_hi', C.c_float), ('l1_wd_lo', C.c_float), ('qf32', C.c_float),
+                ('l2_open32', C.c_float), ('l2_absorb32', C.c_float), ('l2_inv_inner32', C.c_float),
+                ('blaze_center32', C.c_float), ('d_blaze32', C.c_float),
+                ('l1_open_u53', C.c_int64), ('l1_trans_e32', C.c_void_p),
+                ('l1_trans_t32', C.c_void_p)]
 
 
 class MgpuStage(C.Structure):

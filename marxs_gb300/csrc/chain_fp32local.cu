@@ -207,34 +207,44 @@ __device__ __forceinline__ float u53_to_f(uint64_t U) {
 
 // ------------------------------------------------------------ splines
 // Degree-1 spline (the FITPACK evaluation of spline1_at, mgpu_device.cuh)
-// in float32: knot intervals found on order-preserving integer keys of the
-// float64 knots, offsets from the knot formed in float64, weights and the
-// 2x2 coefficient sum in float32 (coefficients from the float32 copy).
-__device__ __forceinline__ uint64_t knot_key(double x) {
-    const uint64_t b = (uint64_t)__double_as_longlong(x);
-    return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+// in float32: the knots as float-float pairs (tx_ff, ty_ff), the argument
+// as float-float, so the interval and the offsets from its knots match the
+// float64 evaluation to ~2^-44 relative; the weights and the 2x2
+// coefficient sum in float32 (coefficients from the float32 copy).
+__device__ __forceinline__ ff knot_ff(const float* t2, int j) {
+    return ff{__ldg(t2 + 2 * j), __ldg(t2 + 2 * j + 1)};
 }
 
-__device__ __forceinline__ void spline1_axis_f(const double* t, int n, double a, int& l,
-                                               float& h0, float& h1) {
-    double arg = a;
-    const uint64_t ka = knot_key(a);
-    if (!isnan(a)) {
-        if (ka < knot_key(t[1])) arg = t[1];
-        else if (ka > knot_key(t[n - 2])) arg = t[n - 2];
+__device__ __forceinline__ bool ff_gt(ff a, ff b) {
+    return a.hi > b.hi || (a.hi == b.hi && a.lo > b.lo);
+}
+
+__device__ __forceinline__ void spline1_axis_f(const float* t2, int n, ff a, int& l, float& h0,
+                                               float& h1) {
+    ff arg = a;
+    if (!isnan(a.hi)) {
+        const ff tb = knot_ff(t2, 1), te = knot_ff(t2, n - 2);
+        if (ff_gt(tb, a)) arg = tb;
+        else if (ff_gt(a, te)) arg = te;
     }
-    const uint64_t karg = knot_key(arg);
     int lo = 2, hi = n - 1;
     while (lo < hi) {
         const int mid = (lo + hi) >> 1;
-        if (knot_key(t[mid]) > karg) hi = mid;
+        if (ff_gt(knot_ff(t2, mid), arg)) hi = mid;
         else lo = mid + 1;
     }
     l = lo - 1;
     if (l > n - 3) l = n - 3;
-    const float inv = 1.0f / __double2float_rn(t[l + 1] - t[l]);
-    h0 = __double2float_rn(t[l + 1] - arg) * inv;
-    h1 = __double2float_rn(arg - t[l]) * inv;
+    const ff t0 = knot_ff(t2, l), t1 = knot_ff(t2, l + 1);
+    const float w = ff_f(ff_sub(t1, t0));
+    if (w > 0.0f) {
+        const float inv = 1.0f / w;
+        h0 = ff_f(ff_sub(t1, arg)) * inv;
+        h1 = ff_f(ff_sub(arg, t0)) * inv;
+    } else {   // knots closer than float-float resolution
+        h0 = 1.0f;
+        h1 = 0.0f;
+    }
 }
 
 struct Spline1Wf {
@@ -242,11 +252,11 @@ struct Spline1Wf {
     float hx0, hx1, hy0, hy1;
 };
 
-__device__ __forceinline__ Spline1Wf spline1_weights_f(const mgpu_spline1& S, double x, double y) {
+__device__ __forceinline__ Spline1Wf spline1_weights_f(const mgpu_spline1& S, ff x, ff y) {
     Spline1Wf w;
     int lx, ly;
-    spline1_axis_f(S.tx, S.nx, x, lx, w.hx0, w.hx1);
-    spline1_axis_f(S.ty, S.ny, y, ly, w.hy0, w.hy1);
+    spline1_axis_f(S.tx_ff, S.nx, x, lx, w.hx0, w.hx1);
+    spline1_axis_f(S.ty_ff, S.ny, y, ly, w.hy0, w.hy1);
     w.base = (lx - 1) * (S.ny - 2) + (ly - 1);
     return w;
 }
@@ -259,13 +269,19 @@ __device__ __forceinline__ float spline1_value_f(const mgpu_spline1& S, int s, c
                      fmaf(__ldg(c + nky1) * w.hx1, w.hy0, __ldg(c + nky1 + 1) * w.hx1 * w.hy1)));
 }
 
+// energy2wave (marxs/__init__.py:14) in nm keV as a float-float constant,
+// and in mm keV as a float
+constexpr float kHcNmHi = (float)MGPU_HC_KEV_NM;
+constexpr float kHcNmLo = (float)(MGPU_HC_KEV_NM - (double)kHcNmHi);
+constexpr float kHcMm = (float)(MGPU_HC_KEV_NM * 1e-6);
+
 // InterpolateEfficiencyTable.__call__ (missions/mitsnl/catgrating.py:101-144)
 // in float32: the order whose running sum / total first exceeds u (index 0
 // when none does); the probability factor is the total
-__device__ __forceinline__ int select_order_spline_f(const mgpu_selector& sel, double energy,
-                                                     double blaze, float u, float* prob) {
-    const double wave = MGPU_HC_KEV_NM / energy;
-    const Spline1Wf w = spline1_weights_f(sel.spline, wave, blaze);
+__device__ __forceinline__ int select_order_spline_f(const mgpu_selector& sel, ff energy,
+                                                     float blaze, float u, float* prob) {
+    const ff wave = ff_div(ff{kHcNmHi, kHcNmLo}, energy);
+    const Spline1Wf w = spline1_weights_f(sel.spline, wave, ff{blaze, 0.0f});
     float total = 0.0f;
     for (int k = 0; k < sel.n_orders; ++k) total += spline1_value_f(sel.spline, k, w);
     float cum = 0.0f;
@@ -296,7 +312,7 @@ __device__ bool stage_lens_l(const mgpu_stage& st, PhotonL& ph, int64_t i, uint3
         f3 od = normf(ph.dir);
         f3 cr = crossf(od, nd);
         float angle = atan2f(sqrtf(dotf(cr, cr)), fabsf(dotf(od, nd)));
-        const Spline1Wf w = spline1_weights_f(st.spline, ph.energy_d, 0.25 * (double)angle);
+        const Spline1Wf w = spline1_weights_f(st.spline, ph.energy, ff{0.25f * angle, 0.0f});
         float r = spline1_value_f(st.spline, 0, w);
         r = r * r;
         if (!(r >= 0.0f && r <= 1.0f)) atomicOr(status, MGPU_STATUS_PROB_RANGE);
@@ -474,8 +490,8 @@ __device__ bool stage_cyldet_l(const mgpu_stage& st, PhotonL& ph, int64_t i) {
 }
 
 // exact order selection (see the header comment)
-__device__ __forceinline__ int select_order_l(const mgpu_selector& sel, double e, uint64_t U,
-                                              float* prob, uint32_t* status) {
+__device__ __forceinline__ int select_order_l(const mgpu_selector& sel, double e, float ef,
+                                              uint64_t U, float* prob, uint32_t* status) {
     int row = 0;
     if (sel.by_energy) {
         const int n = sel.n_rows;
@@ -487,14 +503,21 @@ __device__ __forceinline__ int select_order_l(const mgpu_selector& sel, double e
                 row = 0;
             } else {
                 // guess from a uniform grid, then step to the largest j with E_j <= e
-                float g = __fdividef((float)(e - e0), (float)(e1 - e0)) * (float)(n - 1);
+                const float g = sel.e_mid ? (ef - sel.e0_f) * sel.e_scale_f
+                                          : __fdividef((float)(e - e0), (float)(e1 - e0)) *
+                                                (float)(n - 1);
                 int lo = min(max((int)g, 0), n - 1);
                 while (lo + 1 < n && __double_as_longlong(sel.energy[lo + 1]) <= key) ++lo;
                 while (lo > 0 && __double_as_longlong(sel.energy[lo]) > key) --lo;
                 row = lo;
                 if (row + 1 < n) {
-                    double d0 = fabs(sel.energy[row] - e), d1 = fabs(sel.energy[row + 1] - e);
-                    if (d1 < d0) row = row + 1;
+                    // the nearer row: past the midpoint (integer keys), or |E - e| in float64
+                    if (sel.e_mid) {
+                        if (key > __double_as_longlong(sel.e_mid[row])) row = row + 1;
+                    } else {
+                        double d0 = fabs(sel.energy[row] - e), d1 = fabs(sel.energy[row + 1] - e);
+                        if (d1 < d0) row = row + 1;
+                    }
                 }
             }
         } else {
@@ -635,21 +658,52 @@ __device__ __forceinline__ int brute_force_nearest(const mgpu_stage& st, ff3 pos
     return mine;
 }
 
+// order-preserving integer key of a float64 (all finite values and
+// infinities; NaN sorts above +inf)
+__device__ __forceinline__ uint64_t order_key(double x) {
+    const uint64_t b = (uint64_t)__double_as_longlong(x);
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+
+// np.interp (the L1 support transmission) with the interval found on the
+// float64 table's integer keys and the interpolation in float32 from the
+// float copies; outside the table: NaN and MGPU_STATUS_TABLE_RANGE, as the
+// float64 np_interp
+__device__ __forceinline__ float np_interp_f(const double* x, const float* x32, const float* y32,
+                                             int n, double v, float vf, uint32_t* status) {
+    const uint64_t kv = order_key(v);
+    if (!(kv >= order_key(x[0]) && kv <= order_key(x[n - 1]))) {
+        atomicOr(status, MGPU_STATUS_TABLE_RANGE);
+        return __int_as_float(0x7fc00000);
+    }
+    if (kv == order_key(x[n - 1])) return y32[n - 1];
+    int lo = 0, hi = n - 1;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (order_key(x[mid]) <= kv) lo = mid;
+        else hi = mid;
+    }
+    const float w = x32[lo + 1] - x32[lo];
+    if (!(w > 0.0f)) return y32[lo];
+    return fmaf((y32[lo + 1] - y32[lo]) / w, vf - x32[lo], y32[lo]);
+}
+
 // CATL1L2Stack layers after the membrane (missions/mitsnl/catgrating.py):
 // QualityFactor (:160-161), L1 (:196-207), L2Abs (:231-245), L2Diffraction
 // (:263-268) through RandomGaussianScatter (optics/scatter.py:109-150), in
 // FP32-local arithmetic: direction changes formed directly (the L1 grating
-// as the membrane, the L2 turn as two small rotations), probabilities in
-// float32, the L1 support transmission interpolated in float64.  Out of
-// line: only stages of stacked facets call it.
+// as the membrane, the L2 turn as two small rotations), probabilities and
+// the support transmission in float32 from host-made float constants, no
+// float64 arithmetic.  ``support``: the support draw exceeded the open
+// fraction.  Out of line: only stages of stacked facets call it.
 __device__ __noinline__ void cat_stack_layers_l(const mgpu_stage& st, const mgpu_catstack& K,
                                                 int f, int m, float ly, float lz, uint64_t U1,
-                                                double u_sup, double z_l2, double u_phi,
+                                                bool support, float z_l2, float u_phi,
                                                 PhotonL& ph, int64_t i, uint32_t* status) {
     const mgpu_facet32* fc = st.facets32 + f;
     const f3 n = ldf3(fc->ex);
     // QualityFactor: factor ** (order ** 2)
-    const float q = powf(__double2float_rn(K.qf), (float)(m * m));
+    const float q = powf(K.qf32, (float)(m * m));
     if (!(q >= 0.0f && q <= 1.0f)) atomicOr(status, MGPU_STATUS_PROB_RANGE);
     ph.prob *= q;
     // L1: a CAT grating with grooves at pi/2, or the support bars
@@ -660,12 +714,12 @@ __device__ __noinline__ void cat_stack_layers_l(const mgpu_stage& st, const mgpu
     const float p_l = dotf(p, l1), p_d = dotf(p, d1), p_n = dotf(p, n);
     const float blaze1 = atan2f(fabsf(p_d), fabsf(p_n));       // = arccos|p_perp . n|
     float prob1;
-    int m1 = select_order_l(st.selectors[K.l1_selector], ph.energy_d, U1, &prob1, status);
-    if (u_sup > K.l1_open) {
+    int m1 = select_order_l(st.selectors[K.l1_selector], ph.energy_d, ph.energy.hi, U1, &prob1,
+                            status);
+    if (support) {
         m1 = 0;
-        const double t = np_interp(K.l1_trans_e, K.l1_trans_t, K.l1_n_trans, ph.energy_d, status);
-        if (t < 0.0 || t > 1.0) atomicOr(status, MGPU_STATUS_PROB_RANGE);
-        prob1 = __double2float_rn(t);
+        prob1 = np_interp_f(K.l1_trans_e, K.l1_trans_e32, K.l1_trans_t32, K.l1_n_trans,
+                            ph.energy_d, ph.energy.hi, status);
     } else if (m1 != 0) {
         const float sign = (p_d > 0.0f) ? 1.0f : ((p_d < 0.0f) ? -1.0f : 1.0f);
         // sign * m * lambda / d in float-float
@@ -682,27 +736,25 @@ __device__ __noinline__ void cat_stack_layers_l(const mgpu_stage& st, const mgpu
     }
     if (!(prob1 >= 0.0f && prob1 <= 1.0f)) atomicOr(status, MGPU_STATUS_PROB_RANGE);
     ph.prob *= prob1;
-    stored(st.out[6], i, (double)m1);
+    stored(st.out[6], i, f2d_bits((float)m1));
     storef(st.out[7], i, blaze1);
     // L2Abs: open fraction minus the shadow of the inclined hexagon walls;
     // sin(arccos |p . n|) = |p x n| (no cancellation near normal incidence)
     const f3 p3 = normf(ph.dir);
     const f3 pxn = crossf(p3, n);
     const float sin3 = fminf(sqrtf(dotf(pxn, pxn)), 1.0f);
-    const float a2 = __double2float_rn(K.l2_open) -
-                     __double2float_rn(K.l2_shadow / K.l2_total) * sin3;
+    const float a2 = K.l2_open32 - K.l2_absorb32 * sin3;
     if (!(a2 >= 0.0f && a2 <= 1.0f)) atomicOr(status, MGPU_STATUS_PROB_RANGE);
     ph.prob *= a2;
     // L2Diffraction: N(0,1) * sigma about dir x guess, then a uniform turn
     // about the direction, both as direction changes
     const f3 guess = (fabsf(p3.x) < 0.99999f) ? f3{1.0f, 0.0f, 0.0f} : f3{0.0f, 1.0f, 0.0f};
     const f3 perp = crossf(p3, guess);
-    const float wave_mm = __double2float_rn(MGPU_HC_KEV_NM / ph.energy_d * 1e-6);
-    const float sigma = (1.22f * 0.4f) * asinf(wave_mm / __double2float_rn(K.l2_inner));
-    const float ang = __double2float_rn(z_l2) * sigma;
+    const float wave_mm = kHcMm / ph.energy.hi;
+    const float sigma = (1.22f * 0.4f) * asinf(wave_mm * K.l2_inv_inner32);
+    const float ang = z_l2 * sigma;
     const f3 dl1 = rot_transpose_delta_f(perp, ang, p3);
-    const f3 dl2 = rot_transpose_delta_f(p3, __double2float_rn(u_phi) * 6.283185307179586f,
-                                         p3 + dl1);
+    const f3 dl2 = rot_transpose_delta_f(p3, u_phi * 6.283185307179586f, p3 + dl1);
     const f3 delta2 = dl1 + dl2;
     ph.pol = transport_delta_f(p3, delta2, ph.pol);
     ph.dir = p3 + delta2;
@@ -738,9 +790,9 @@ __device__ bool stage_gratings_l(const mgpu_stage& st, PhotonL& ph, int64_t i, b
     float p_l = dotf(p, l), p_d = dotf(p, dn), p_n = dotf(p, n);
     float blaze = atan2f(fabsf(p_d), fabsf(p_n));      // = arccos|p_perp . n|
     // NonParallelCATGrating.blaze_angle_modifier (catgrating.py:324-333)
-    const double blaze_d = (kStack && st.stack) ? (double)blaze + (st.stack->blaze_center +
-                                                       (double)h.ly * st.stack->d_blaze_mm)
-                                                : (double)blaze;
+    const float blaze_s = (kStack && st.stack)
+                              ? blaze + (st.stack->blaze_center32 + h.ly * st.stack->d_blaze32)
+                              : blaze;
     uint64_t U, U1 = 0;
     double u_pre = 0.0;
     if (rng == MGPU_RNG_PREDRAWN) {
@@ -760,10 +812,10 @@ __device__ bool stage_gratings_l(const mgpu_stage& st, PhotonL& ph, int64_t i, b
     int m;
     if (sel.kind == MGPU_SEL_SPLINE) {
         // float32 evaluation of the interpolated table
-        m = select_order_spline_f(sel, ph.energy_d, blaze_d, u53_to_f(U), &selprob);
+        m = select_order_spline_f(sel, ph.energy, blaze_s, u53_to_f(U), &selprob);
         if (!(selprob >= 0.0f && selprob <= 1.0f)) atomicOr(status, MGPU_STATUS_PROB_RANGE);
     } else {
-        m = select_order_l(sel, ph.energy_d, U, &selprob, status);
+        m = select_order_l(sel, ph.energy_d, ph.energy.hi, U, &selprob, status);
     }
     float sign;
     if (flags & 1) sign = (p_d > 0.0f) ? 1.0f : ((p_d < 0.0f) ? -1.0f : 1.0f);
@@ -788,34 +840,36 @@ __device__ bool stage_gratings_l(const mgpu_stage& st, PhotonL& ph, int64_t i, b
     storef(st.out[0], i, h.ly);
     storef(st.out[1], i, h.lz);
     stored(st.out[2], i, f2d_bits((float)m));
-    if (kStack && st.stack) stored(st.out[3], i, blaze_d);
+    if (kStack && st.stack) storef(st.out[3], i, blaze_s);
     else storef(st.out[3], i, blaze);
     if (st.id_out) store_id(st, i, fc->id_num);
     if (kStack && st.stack) {
-        double u_sup, u_phi, z;
+        bool support;
+        float u_phi, z;
         if (rng == MGPU_RNG_PREDRAWN) {
             if (!st.draw[1] || !st.draw[2] || !st.draw[3] || !st.draw[4]) {
                 atomicOr(status, MGPU_STATUS_BAD_STAGE);
                 return false;
             }
-            u_sup = st.draw[2][i * st.draw_stride];
-            z = st.draw[3][i * st.draw_stride];
-            u_phi = st.draw[4][i * st.draw_stride];
+            support = st.draw[2][i * st.draw_stride] > st.stack->l1_open;
+            z = __double2float_rn(st.draw[3][i * st.draw_stride]);
+            u_phi = __double2float_rn(st.draw[4][i * st.draw_stride]);
         } else {
             // the float64 kernel's counters: draw 1 (u_sup, u_phi), draw 2
-            // (the normal, by Box-Muller in float32 from the same uniforms)
+            // (the normal, by Box-Muller in float32 from the same uniforms);
+            // u_sup > l1_open decided exactly on the 53-bit integer
             const uint64_t row = row_base + (uint64_t)i;
             uint64_t A, B;
             philox_u53_draw(seed, row, (uint32_t)sidx, 1u, &A, &B);
-            u_sup = (double)A * (1.0 / 9007199254740992.0);
-            u_phi = (double)B * (1.0 / 9007199254740992.0);
+            support = (int64_t)A > st.stack->l1_open_u53;
+            u_phi = u53_to_f(B);
             philox_u53_draw(seed, row, (uint32_t)sidx, 2u, &A, &B);
             const float one_minus_u0 = (float)((1ull << 53) - A) * 1.1102230246251565e-16f;
             float sn, cs;
             sincospif(2.0f * u53_to_f(B), &sn, &cs);
-            z = (double)(sqrtf(-2.0f * logf(one_minus_u0)) * cs);   // accurate log: small u
+            z = sqrtf(-2.0f * logf(one_minus_u0)) * cs;   // accurate log: small u
         }
-        cat_stack_layers_l(st, *st.stack, f, m, h.ly, h.lz, U1, u_sup, z, u_phi, ph, i, status);
+        cat_stack_layers_l(st, *st.stack, f, m, h.ly, h.lz, U1, support, z, u_phi, ph, i, status);
     }
     ph.pos = h.ip;
     return true;
@@ -977,6 +1031,9 @@ cudaError_t mgpu_launch_chain_fp32local(const mgpu_chain& chain, const mgpu_phot
             (st.facets32 == nullptr || st.cand32 == nullptr || ((uintptr_t)st.cand32 & 15u) != 0))
             return cudaErrorInvalidValue;
         if (st.kind == MGPU_STAGE_CYLDET && st.table == nullptr) return cudaErrorInvalidValue;
+        if (st.kind == MGPU_STAGE_LENS && st.spline.n_surf > 0 &&
+            (st.spline.tx_ff == nullptr || st.spline.ty_ff == nullptr || st.spline.c32 == nullptr))
+            return cudaErrorInvalidValue;
     }
     int64_t warps = (io.n + 31) / 32;
     int64_t blocks = (warps * 32 + kThreads - 1) / kThreads;

@@ -113,10 +113,12 @@ class _Instrument:
             ts = [torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).to(device)
                   for a in sp]
             c32 = torch.from_numpy(np.ascontiguousarray(sp[2], dtype=np.float32)).to(device)
-            self.keep += ts + [c32]
+            tff = [torch.from_numpy(L.split_ff_array(a)).to(device) for a in sp[:2]]
+            self.keep += ts + [c32] + tff
             out.nx, out.ny, out.n_surf = len(sp[0]), len(sp[1]), int(sp[2].shape[0])
             out.tx, out.ty, out.c = ts[0].data_ptr(), ts[1].data_ptr(), ts[2].data_ptr()
             out.c32 = c32.data_ptr()
+            out.tx_ff, out.ty_ff = tff[0].data_ptr(), tff[1].data_ptr()
             return out
 
         self.stage_spline = {}
@@ -136,12 +138,23 @@ class _Instrument:
                     device)
                 self.keep.append(l1v32)
                 wd_hi, wd_lo = L.split_ff(1.2398419292004202e-06 / float(k['l1_d']))
+                te32, tt32 = [torch.from_numpy(np.ascontiguousarray(k[c], dtype=np.float32)).to(
+                    device) for c in ('l1_trans_e', 'l1_trans_t')]
+                self.keep += [te32, tt32]
                 cs = _abi.MgpuCatStack(k['blaze_center'], k['d_blaze_mm'], k['qf'], k['l1_open'],
                                        k['l1_d'], f64(k['l1_vec']), k['l1_selector'],
                                        len(k['l1_trans_e']), f64(k['l1_trans_e']),
                                        f64(k['l1_trans_t']), k['l2_open'], k['l2_shadow'],
                                        k['l2_total'], k['l2_inner'], l1v32.data_ptr(),
                                        float(wd_hi), float(wd_lo))
+                cs.qf32 = float(np.float32(k['qf']))
+                cs.l2_open32 = float(np.float32(k['l2_open']))
+                cs.l2_absorb32 = float(np.float32(k['l2_shadow'] / k['l2_total']))
+                cs.l2_inv_inner32 = float(np.float32(1.0 / k['l2_inner']))
+                cs.blaze_center32 = float(np.float32(k['blaze_center']))
+                cs.d_blaze32 = float(np.float32(k['d_blaze_mm']))
+                cs.l1_open_u53 = L.u53_threshold(k['l1_open'])
+                cs.l1_trans_e32, cs.l1_trans_t32 = te32.data_ptr(), tt32.data_ptr()
                 self.stage_stack[si] = dev_bytes(bytes(cs))
             try:
                 if st.kind in (_abi.STAGE_LENS, _abi.STAGE_SCATTER, _abi.STAGE_FLATDET):
@@ -185,6 +198,12 @@ class _Instrument:
                                                    cdf.data_ptr(), tot.data_ptr(), ords.data_ptr(),
                                                    thr.data_ptr(), s.kind, 0,
                                                    spline_struct(s.spline), gd_ptr)
+                rows = L.selector_rows32(s)
+                if rows is not None:
+                    mid = torch.from_numpy(rows[0]).to(device)
+                    self.keep.append(mid)
+                    sel_structs[k].e_mid = mid.data_ptr()
+                    sel_structs[k].e0_f, sel_structs[k].e_scale_f = rows[1], rows[2]
             raw = np.frombuffer(bytes(sel_structs), dtype=np.uint8).copy()
             sel_dev = torch.from_numpy(raw).to(device)
             self.keep.append(sel_dev)

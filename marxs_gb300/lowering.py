@@ -496,6 +496,31 @@ def split_ff(x):
     return hi, lo
 
 
+def split_ff_array(x):
+    """float64 array -> float32 array of (hi, lo) pairs, shape (n, 2)."""
+    hi, lo = split_ff(np.ravel(x))
+    return np.ascontiguousarray(np.stack([hi, lo], axis=1))
+
+
+def u53_threshold(x):
+    """floor(x * 2^53), at least -1: for a 53-bit draw U (u = U * 2^-53),
+    u > x exactly when U > this value."""
+    v = math.floor(float(x) * 2.0 ** 53) if math.isfinite(float(x)) else (
+        2 ** 62 if float(x) > 0 else -1)
+    return int(min(max(v, -1), 2 ** 62))
+
+
+def selector_rows32(sel):
+    """FP32-local row lookup of a sorted energy-row selector: the midpoints
+    of adjacent rows (float64) and the float32 guess constants E_0 and
+    (n - 1) / (E_last - E_0); None when the selector has no such rows."""
+    e = np.asarray(sel.energy, dtype=np.float64)
+    if not (sel.by_energy and selector_sorted(sel) and len(e) >= 2):
+        return None
+    mid = np.ascontiguousarray(0.5 * (e[:-1] + e[1:]))
+    return mid, float(np.float32(e[0])), float(np.float32((len(e) - 1) / (e[-1] - e[0])))
+
+
 def flat32_block(st):
     b = _abi.MgpuFlat32()
     hi, lo = split_ff(st.frame[0:3])
