@@ -23,7 +23,7 @@ import numpy as np
 import torch
 
 from . import _abi
-from .lowering import lower_elements, classnames
+from .lowering import ChangeWatch, lower_elements, classnames
 
 _PRECISIONS = {'fp64': _abi.FP64, 'fp32local': _abi.FP32LOCAL}
 _RNGS = {'predrawn': _abi.RNG_PREDRAWN, 'philox': _abi.RNG_PHILOX}
@@ -328,36 +328,19 @@ class GpuSequence:
         self.seed = int(seed)
         self.device = _device(device)
         self._inst = None
-        self._key = None
+        self._watch = None
         self.last_hits = None
         self.last_status = 0
 
     # ------------------------------------------------------------ lowering
-    def _raw_key(self):
-        parts = []
-
-        def walk(e):
-            parts.append(id(e))
-            g = getattr(e, 'geometry', None)
-            if g is not None and hasattr(g, 'pos4d'):
-                parts.append(np.asarray(g.pos4d, dtype=float).tobytes())
-            for attr in ('order_selector', 'focallength', 'inplanescatter', 'perpplanescatter',
-                         'pixsize', '_d', 'd_center_optax', 'transmission', 'id_num'):
-                if hasattr(e, attr):
-                    v = getattr(e, attr)
-                    parts.append(id(v) if attr == 'order_selector' else repr(v))
-            for sub in getattr(e, 'elements', []) or []:
-                walk(sub)
-        for e in self.elements:
-            walk(e)
-        return hash(tuple(parts))
-
     def lower(self, stream=None):
-        key = self._raw_key()
-        if self._inst is None or key != self._key:
+        """The lowered chain, rebuilt when an element, a pose or a watched
+        parameter changed since the last call."""
+        if self._inst is None or self._watch.changed(self.elements):
+            watch = ChangeWatch(self.elements)
             stages = lower_elements(self.elements)
             self._inst = _Instrument(stages, self.device, _stream_handle(stream))
-            self._key = key
+            self._watch = watch
         return self._inst
 
     @property

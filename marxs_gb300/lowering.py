@@ -10,6 +10,7 @@ from ``pos4d`` with the same numpy expressions as Geometry.__getitem__
 Unsupported elements raise ``NotImplementedError``: there is no CPU path.
 """
 import math
+import operator
 from dataclasses import dataclass, field
 from typing import Any, List, Optional
 
@@ -278,6 +279,112 @@ def _grid_params(facets, slope_max, margin, cells_per_facet):
     capacity = int(np.sum((iu1 - iu0 + 2) * (iv1 - iv0 + 2))) + 16
     return dict(o=o, n=nrm, a=a, b=b, u0=u0, v0=v0, cell=cell, nu=nu, nv=nv,
                 slope_max=slope_max, margin=margin, capacity=capacity, n_facets=F)
+
+
+# element attributes whose change makes a chain lower again (the geometry's
+# pos4d is watched separately)
+WATCHED_ATTRS = ('order_selector', 'focallength', 'inplanescatter', 'perpplanescatter',
+                 'pixsize', '_d', 'd_center_optax', 'transmission', 'id_num')
+
+
+def _same(a, b):
+    if a is b:
+        return True
+    if isinstance(a, np.ndarray) or isinstance(b, np.ndarray):
+        return (isinstance(a, np.ndarray) and isinstance(b, np.ndarray) and a.shape == b.shape
+                and bool(np.array_equal(a, b)))
+    try:
+        return bool(a == b)
+    except Exception:
+        return False
+
+
+def _snapshot(v):
+    return np.array(v, copy=True) if isinstance(v, np.ndarray) else v
+
+
+class ChangeWatch:
+    """What a lowered chain was built from, for a cheap check on every call.
+
+    MARXS users move elements by assigning or editing ``geometry.pos4d`` in
+    place (design/tolerancing.py:133) and swap order selectors on facets
+    (analysis/gratings.py:117-124), so every call must notice such changes.
+    The element tree is walked once; a call then compares the containers'
+    element lists and the geometry objects by identity, all pos4d matrices
+    (assigned or edited in place) as one stacked array, and the watched
+    attributes by identity (by value where the identity changed, and always
+    for array values).
+    """
+
+    def __init__(self, elements):
+        self.top = tuple(elements)
+        containers, holders, geoms = [], [], []
+        objs = {name: [] for name in WATCHED_ATTRS}
+
+        def walk(e):
+            g = getattr(e, 'geometry', None)
+            if g is not None and hasattr(g, 'pos4d'):
+                holders.append(e)
+                geoms.append(g)
+            for name in WATCHED_ATTRS:
+                if hasattr(e, name):
+                    objs[name].append(e)
+            sub = getattr(e, 'elements', None)
+            if sub:
+                containers.append((e, tuple(sub)))
+                for x in sub:
+                    walk(x)
+        for e in elements:
+            walk(e)
+        self.containers = containers
+        self.holders = holders
+        self.geoms = geoms
+        self.geom_ids = [id(g) for g in geoms]
+        self.pos = self._stack(list(map(_POS4D, geoms)))
+        self.attrs = []
+        for name, ol in objs.items():
+            if not ol:
+                continue
+            vals = list(map(operator.attrgetter(name), ol))
+            arrays = [k for k, v in enumerate(vals) if isinstance(v, np.ndarray)]
+            self.attrs.append((operator.attrgetter(name), ol, [id(v) for v in vals],
+                               [_snapshot(v) for v in vals], arrays))
+
+    @staticmethod
+    def _stack(mats):
+        if not mats:
+            return np.zeros((0, 4, 4))
+        try:
+            return np.array(mats, dtype=float)
+        except ValueError:
+            return np.array([np.asarray(m, dtype=float) for m in mats])
+
+    def changed(self, elements):
+        """True when ``elements`` no longer match what was watched."""
+        if tuple(elements) != self.top:
+            return True
+        for c, snap in self.containers:
+            if tuple(getattr(c, 'elements', ()) or ()) != snap:
+                return True
+        if list(map(id, map(_GEOMETRY, self.holders))) != self.geom_ids:
+            return True
+        stacked = self._stack(list(map(_POS4D, self.geoms)))
+        if stacked.shape != self.pos.shape or not np.array_equal(stacked, self.pos):
+            return True
+        for get, ol, ids, snaps, arrays in self.attrs:
+            vals = list(map(get, ol))
+            if list(map(id, vals)) != ids:
+                for v, i0, s0 in zip(vals, ids, snaps):
+                    if id(v) != i0 and not _same(v, s0):
+                        return True
+            for k in arrays:
+                if not _same(vals[k], snaps[k]):
+                    return True
+        return False
+
+
+_POS4D = operator.attrgetter('pos4d')
+_GEOMETRY = operator.attrgetter('geometry')
 
 
 def lower_elements(elements):

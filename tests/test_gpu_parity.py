@@ -144,3 +144,47 @@ def test_catsupportbars_stage():
     p = np.asarray(t['probability'])
     assert np.all(p[np.arange(n) % 3 == 0] == 0)
     assert np.array_equal(p[np.arange(n) % 3 != 0], host['probability'][np.arange(n) % 3 != 0])
+
+
+def test_host_changes_reach_the_device():
+    """One GpuSequence traced, then facets moved the way the reference's
+    tolerancing moves them (a new pos4d assigned, design/tolerancing.py:133),
+    one edited in place, an order selector swapped (as
+    analysis/gratings.py:117-124 does) and the lens refocused: the next call
+    must trace the changed instrument, equal to the oracle on it."""
+    from marxs_gb300 import configs, PhotonTable
+    from marxs_gb300.gpu import GpuSequence
+    from marxs_gb300.optics import OrderSelector
+    from oracle.raytrace import run_sequence
+    n = 20000
+    inst = configs.build('c1')
+    photons = configs.photons_for('c1', n, seed=31)
+    draws = configs.draws_for(inst.draw_slots, n, seed=31)
+    seq = GpuSequence(elements=inst.elements, precision='fp64', rng='predrawn')
+    first = seq(PhotonTable(photons), draws=draws)
+    hits0 = np.bincount(np.asarray(first['facet'])[np.asarray(first['facet']) >= 0],
+                        minlength=200)
+    busy = np.argsort(hits0)[::-1][:3]
+    facets = inst.elements[2].elements
+    # moves inside the 2 mm gaps of the 22 mm pitch: facets never overlap,
+    # where the sequential Parallel and the nearest hit would differ
+    move = np.eye(4)
+    move[1, 3] = 1.5
+    g = facets[busy[0]].geometry
+    g.pos4d = move @ g.pos4d
+    facets[busy[1]].geometry.pos4d[2, 3] -= 1.5
+    facets[busy[2]].order_selector = OrderSelector([2])
+    inst.elements[0].focallength = inst.elements[0].focallength + 25.0
+    out = seq(PhotonTable(photons), draws=draws)
+    ref, stats = run_sequence(inst.elements, photons, draws)
+    ok = ~stats.get('multi_hit_mask', np.zeros(n, dtype=bool))
+    fa, fr = np.asarray(out['facet']), ref['facet']
+    assert np.array_equal(fa[ok], fr[ok])
+    assert np.array_equal(np.asarray(out['order'])[ok], ref['order'][ok], equal_nan=True)
+    assert not np.array_equal(np.asarray(first['facet']), fa)
+    assert np.all(np.asarray(out['order'])[fa == busy[2]] == 2)
+    for key in ('pos', 'dir'):
+        a, b = np.asarray(out[key])[ok], ref[key][ok]
+        assert np.array_equal(np.isnan(a), np.isnan(b))
+        m = ~np.isnan(b)
+        assert np.all(np.abs(a[m] - b[m]) <= 1e-9 * np.maximum(np.abs(b[m]), 1.0)), key
