@@ -15,10 +15,17 @@
 //     angle resolved as (reference angle k/1024 from a float-float table) +
 //     (small float32 residual), so det_phi keeps ~1e-11 rad;
 //   * order selection is exact: a 53-bit draw U against integer thresholds
-//     ceil(cdf * 2^53), and the nearest energy row decided in float64.
-// float64 inputs/outputs are converted on the integer pipe (mgpu_ff.cuh);
-// the FP64 pipe only sees a handful of adds per photon for the final
-// float64 detector coordinates.
+//     ceil(cdf * 2^53); the nearest energy row by integer keys against the
+//     rows' float64 midpoints (made on the host);
+//   * interpolated tables (efficiency splines, lens reflectivity, the L1
+//     support transmission) and the CAT stack layers run in float32 /
+//     float-float from host-made float constants.
+// The float64 inputs are converted by the FP64 pipe's conversion
+// instructions (about 23 per photon; measured faster than integer-pipe
+// routines), the outputs on the integer pipe (mgpu_bits.cuh) with one
+// float64 add per float-float value; in Philox mode no other float64
+// arithmetic runs, except the float64 scan of an energy table whose rows
+// are not increasing.
 #include <cuda_runtime.h>
 #include <utility>
 #include "mgpu_ff.cuh"
