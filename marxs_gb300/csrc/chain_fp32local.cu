@@ -702,8 +702,9 @@ __device__ __forceinline__ float np_interp_f(const double* x, const float* x32, 
 // as the membrane, the L2 turn as two small rotations), probabilities and
 // the support transmission in float32 from host-made float constants, no
 // float64 arithmetic.  ``support``: the support draw exceeded the open
-// fraction.  Out of line: only stages of stacked facets call it.
-__device__ __noinline__ void cat_stack_layers_l(const mgpu_stage& st, const mgpu_catstack& K,
+// fraction.  Inlined into the stacked-chain kernels only (kStack), which
+// then fit 80 registers without spills.
+__device__ __forceinline__ void cat_stack_layers_l(const mgpu_stage& st, const mgpu_catstack& K,
                                                 int f, int m, float ly, float lz, uint64_t U1,
                                                 bool support, float z_l2, float u_phi,
                                                 PhotonL& ph, int64_t i, uint32_t* status) {
