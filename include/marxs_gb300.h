@@ -118,7 +118,8 @@ typedef struct {
     const double* tx;
     const double* ty;
     const double* c;
-    const float* c32;     /* the coefficients in float32, for FP32-local chains */
+    const float* c32;     /* FP32-local: the coefficients in float32, n_surf + 1 surfaces,
+                             the last one the sum of the others */
     const float* tx_ff;   /* FP32-local: the knots as float-float (hi, lo) pairs, nx x 2 */
     const float* ty_ff;   /* ny x 2 */
 } mgpu_spline1;

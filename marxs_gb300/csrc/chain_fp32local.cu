@@ -289,8 +289,8 @@ __device__ __forceinline__ int select_order_spline_f(const mgpu_selector& sel, f
                                                      float blaze, float u, float* prob) {
     const ff wave = ff_div(ff{kHcNmHi, kHcNmLo}, energy);
     const Spline1Wf w = spline1_weights_f(sel.spline, wave, ff{blaze, 0.0f});
-    float total = 0.0f;
-    for (int k = 0; k < sel.n_orders; ++k) total += spline1_value_f(sel.spline, k, w);
+    // the total from the summed surface (the last one of the float copy)
+    const float total = spline1_value_f(sel.spline, sel.n_orders, w);
     float cum = 0.0f;
     int pick = -1;
     for (int k = 0; k < sel.n_orders && pick < 0; ++k) {

@@ -112,7 +112,11 @@ class _Instrument:
                 return out
             ts = [torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).to(device)
                   for a in sp]
-            c32 = torch.from_numpy(np.ascontiguousarray(sp[2], dtype=np.float32)).to(device)
+            # float copy of the coefficients plus one more surface: their sum
+            # over the surfaces (an order selector's total, in one evaluation)
+            c = np.asarray(sp[2], dtype=np.float64)
+            c32 = torch.from_numpy(np.ascontiguousarray(
+                np.concatenate([c, c.sum(axis=0, keepdims=True)]), dtype=np.float32)).to(device)
             tff = [torch.from_numpy(L.split_ff_array(a)).to(device) for a in sp[:2]]
             self.keep += ts + [c32] + tff
             out.nx, out.ny, out.n_surf = len(sp[0]), len(sp[1]), int(sp[2].shape[0])
