@@ -281,10 +281,14 @@ def _grid_params(facets, slope_max, margin, cells_per_facet):
                 slope_max=slope_max, margin=margin, capacity=capacity, n_facets=F)
 
 
-# element attributes whose change makes a chain lower again (the geometry's
-# pos4d is watched separately)
+# element attributes the lowering reads, so a change makes a chain lower
+# again (the geometry's pos4d is watched separately)
 WATCHED_ATTRS = ('order_selector', 'focallength', 'inplanescatter', 'perpplanescatter',
-                 'pixsize', '_d', 'd_center_optax', 'transmission', 'id_num')
+                 'pixsize', 'centerpix', '_d', 'd_center_optax', 'transmission', 'id_num',
+                 'id_col', 'reflectivity_interpolator', 'order_name', 'blaze_name',
+                 'detpix_name', 'inplanescattercol', 'perpplanescattercol', 'scattername',
+                 'blaze_center', 'd_blaze_mm', 'factor', 'openfraction', 'bardepth', 'period',
+                 'innerfree')
 
 
 def _same(a, b):

@@ -81,3 +81,25 @@ def test_stack_layer_moved():
     assert not w.changed(chain)                      # identity changed, same values
     layers[1].geometry.pos4d[0, 3] += 1e-6
     assert w.changed(chain)
+
+
+def test_stack_layer_parameters():
+    chain = configs.build('c6').elements
+    facet = chain[2].elements[4]
+    qf = facet.elements[1]
+    w = ChangeWatch(chain)
+    qf.factor = qf.factor * 0.99
+    assert w.changed(chain)
+    w = ChangeWatch(chain)
+    facet.elements[2].openfraction = facet.elements[2].openfraction * 0.99
+    assert w.changed(chain)
+
+
+def test_lens_reflectivity_and_detector_pixels():
+    chain = configs.build('c5').elements
+    w = ChangeWatch(chain)
+    chain[0].reflectivity_interpolator = configs.lens_reflectivity(99)
+    assert w.changed(chain)
+    w = ChangeWatch(chain)
+    chain[-1].pixsize = chain[-1].pixsize * 2
+    assert w.changed(chain)
