@@ -467,14 +467,17 @@ class GpuSequence:
         return cols, draws
 
     def trace_device(self, inp, out, plan, bufs, draws=None, stream=None, status=None, hits=None,
-                     row_base=0):
+                     row_base=0, lowered=None):
         """Trace device-resident photons (asynchronous on ``stream``).
 
         ``inp``/``out`` are DevicePhotons (may be the same object); ``plan``
         and ``bufs`` come from ``allocate_columns``.  Returns the device
         status word and hit counters (read them after synchronising).
+        ``lowered``: the result of ``lower()`` earlier in the same call, for
+        callers that trace many chunks of one call and check the elements
+        once.
         """
-        inst = self.lower(stream)
+        inst = self.lower(stream) if lowered is None else lowered
         n = inp.n
         if status is None:
             status = torch.zeros(1, dtype=torch.int32, device=self.device)

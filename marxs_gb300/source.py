@@ -235,7 +235,7 @@ def simulate_events(source, seq, n, columns=('det_phi', 'det_y', 'order', 'facet
             source.generate(m, seed=seed, row_base=row_base + start, out=ph, stream=s)
             seq.trace_device(ph, ph, sl['plan'], {c: b[:m] for c, b in sl['bufs'].items()},
                              stream=s, status=sl['status'], hits=sl['hits'],
-                             row_base=row_base + start)
+                             row_base=row_base + start, lowered=inst)
             for c in columns:
                 out[c][start:start + m].copy_(sl['bufs'][c][:m], non_blocking=True)
     for s in streams:
