@@ -90,6 +90,11 @@ int mgpu_device_sm_count(void) { return sm_count_cached(); }
 int mgpu_trace(const mgpu_chain* chain, const mgpu_photons* photons, void* stream) {
     if (chain == nullptr || photons == nullptr) return (int)cudaErrorInvalidValue;
     if (chain->n_stages < 0 || chain->n_stages > MGPU_MAX_STAGES) return (int)cudaErrorInvalidValue;
+    if (chain->precision != MGPU_FP64 && chain->precision != MGPU_FP32LOCAL)
+        return (int)cudaErrorInvalidValue;
+    if (chain->rng != MGPU_RNG_PREDRAWN && chain->rng != MGPU_RNG_PHILOX)
+        return (int)cudaErrorInvalidValue;
+    if (photons->n < 0) return (int)cudaErrorInvalidValue;
     cudaStream_t s = (cudaStream_t)stream;
     cudaError_t e;
     if (chain->precision == MGPU_FP32LOCAL)

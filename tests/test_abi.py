@@ -140,3 +140,37 @@ def test_order_guide_table_gives_the_linear_search_result():
             while k[j] < th.shape[1] and not (U[j] < th[r][k[j]]):
                 k[j] += 1
         assert np.array_equal(k, ref)
+
+
+def test_entry_points_reject_bad_descriptors_without_a_gpu():
+    """Every entry point checks its descriptor on the host and returns
+    cudaErrorInvalidValue (1) before any CUDA call, so the checks run here."""
+    import ctypes as C
+    lib = _abi.load()
+    bad = 1
+    ph = _abi.MgpuPhotons()
+    assert lib.mgpu_trace(None, C.byref(ph), None) == bad
+    ch = _abi.MgpuChain()
+    ch.n_stages = _abi.MAX_STAGES + 1
+    assert lib.mgpu_trace(C.byref(ch), C.byref(ph), None) == bad
+    ch.n_stages, ch.precision = 1, 7
+    assert lib.mgpu_trace(C.byref(ch), C.byref(ph), None) == bad
+    ch.precision, ch.rng = _abi.FP32LOCAL, 9
+    assert lib.mgpu_trace(C.byref(ch), C.byref(ph), None) == bad
+    ch.rng, ph.n = _abi.RNG_PHILOX, -1
+    assert lib.mgpu_trace(C.byref(ch), C.byref(ph), None) == bad
+    g = _abi.MgpuGrid()
+    assert lib.mgpu_facet_grid_build(None, 0, C.byref(g), None, None, None) == bad
+    assert lib.mgpu_facet_grid_build(None, 0, C.byref(g), C.c_void_p(16), C.c_void_p(16),
+                                     None) == bad                      # nu = nv = 0
+    assert lib.mgpu_plane_intersect(None, 5, _abi.MgpuVec(), _abi.MgpuVec(), None,
+                                    _abi.MgpuVec(), _abi.MgpuCol(), _abi.MgpuCol(), None) == bad
+    assert lib.mgpu_order_stats(None, None) == bad
+    assert lib.mgpu_facet_poses(None, None) == bad
+    src = _abi.MgpuSource()
+    src.n, src.rng, src.precision = 10, 5, _abi.FP64
+    v = _abi.MgpuVec()
+    c = _abi.MgpuCol()
+    assert lib.mgpu_generate_photons(C.byref(src), v, v, v, c, c, None) == bad
+    assert lib.mgpu_pose_adjoint(None, None, 0, None, None, None, None) == bad
+    assert lib.mgpu_fma_probe(_abi.FP32LOCAL, 0, 1, None, None) == bad
