@@ -210,12 +210,16 @@ class PoseModel:
 
     # --------------------------------------------------------- frozen photons
     def trace(self, photons, orders, draws=None, precision='fp64', rng=None, seed=0,
-              theta=None, energy_range=None, device=None, freeze=True):
+              theta=None, energy_range=None, device=None, freeze=True, process_group=None,
+              row_base=0):
         """Trace ``photons`` (host columns or DevicePhotons) through the
         elements as they are posed now and freeze the result.
 
         Returns (FrozenPhotons or None if not ``freeze``, trace) with trace =
-        (sequence, input, output, column buffers) of the device run.
+        (sequence, input, output, column buffers) of the device run.  For
+        photons sharded over a process group, ``row_base`` is the global id
+        of this rank's first photon (its Philox streams) and the frozen
+        photons sum their moments and gradients over ``process_group``.
         """
         from .gpu import DevicePhotons, GpuSequence
         rng = rng or ('predrawn' if draws is not None else 'philox')
@@ -224,14 +228,16 @@ class PoseModel:
             DevicePhotons.from_columns(photons, seq.device)
         out = DevicePhotons(inp.n, seq.device)
         plan, bufs = seq.allocate_columns(inp.n)
-        status, _ = seq.trace_device(inp, out, plan, bufs, draws=draws)
+        status, _ = seq.trace_device(inp, out, plan, bufs, draws=draws, row_base=row_base)
         seq._raise_status(int(status.item()))
         if not freeze:
             return None, (seq, inp, out, bufs)
-        frozen = self.freeze_trace(seq, inp, out, bufs, orders, energy_range, theta)
+        frozen = self.freeze_trace(seq, inp, out, bufs, orders, energy_range, theta,
+                                   process_group)
         return frozen, (seq, inp, out, bufs)
 
-    def freeze_trace(self, seq, inp, out, bufs, orders, energy_range=None, theta=None):
+    def freeze_trace(self, seq, inp, out, bufs, orders, energy_range=None, theta=None,
+                     process_group=None):
         """Frozen photons of a device trace ``seq.trace_device(inp, out, ...)``.
 
         Photons count when they met a facet and the detector; group g holds
@@ -268,18 +274,21 @@ class PoseModel:
             self, pos=inp.pos[:, sel], dir=inp.dir[:, sel], energy=inp.energy[sel],
             weight=out.prob[sel], alpha=alpha[sel], beta=beta[sel], facet=lut[fid],
             order=order[sel].to(torch.int32), group=group[sel].to(torch.int32),
-            n_groups=len(orders), theta=theta, rows=sel)
+            n_groups=len(orders), theta=theta, rows=sel, process_group=process_group)
 
 
 class FrozenPhotons:
     """Device arrays of the frozen photons and the C-ABI problem over them."""
 
     def __init__(self, model, pos, dir, energy, weight, alpha, beta, facet, order, group,
-                 n_groups, theta=None, stream=None, rows=None):
+                 n_groups, theta=None, stream=None, rows=None, process_group=None):
         if n_groups < 1 or n_groups > _abi.ADJ_MAX_GROUPS:
             raise ValueError('pose adjoint: 1..%d groups' % _abi.ADJ_MAX_GROUPS)
         self.model = model
         self.rows = rows            # indices of the frozen photons in the traced table
+        # photons sharded over the ranks of this torch.distributed group: the
+        # moments and the gradient are summed over it (None: one process)
+        self.process_group = process_group
         dev = pos.device
         self.device = dev
         f64 = dict(dtype=torch.float64, device=dev)
@@ -309,9 +318,9 @@ class FrozenPhotons:
         self._run(self.theta_frozen, _abi.ADJ_FREEZE)
         self.check()
         # moments are taken about the group centres at the frozen parameters
-        m = self.moments(self.theta_frozen)
-        W = m[:, 0].clamp_min(1e-300)
-        self.ref = torch.stack([m[:, 1] / W, m[:, 2] / W], 1).contiguous()
+        # (over all shards)
+        m = sum_over_shards(self.moments(self.theta_frozen), process_group)
+        self.ref = group_centres(m)
         self._P = None
 
     # ------------------------------------------------------------- launches
@@ -456,20 +465,44 @@ class FrozenPhotons:
         return d
 
 
+def sum_over_shards(t, process_group=None):
+    """In-place sum of ``t`` over the ranks of ``process_group`` (one
+    all-reduce; the identity for None)."""
+    if process_group is not None:
+        import torch.distributed as dist
+        dist.all_reduce(t, op=dist.ReduceOp.SUM, group=process_group)
+    return t
+
+
+def group_centres(m):
+    """(G, 2) weighted centroids from (G, 5) moments taken about the origin."""
+    W = m[:, 0].clamp_min(1e-300)
+    return torch.stack([m[:, 1] / W, m[:, 2] / W], 1).contiguous()
+
+
 class PoseMoments(torch.autograd.Function):
     """theta -> (G, 5) detector moments of frozen photons; the backward is
-    one launch of the hand-written adjoint."""
+    one launch of the hand-written adjoint.
+
+    Data-parallel over photon shards (``frozen.process_group``): moments are
+    sums over photons, so the forward sums them over the ranks; the loss
+    and its seeds dL/dmoments are then the same on every rank, each rank's
+    backward runs the adjoint on its own photons, and the gradient is
+    summed over the ranks -- one all-reduce of G x 5 values and one of the
+    parameter vector per gradient."""
 
     @staticmethod
     def forward(ctx, theta, frozen):
         ctx.frozen = frozen
         ctx.save_for_backward(theta)
-        return frozen.moments(theta.detach())
+        return sum_over_shards(frozen.moments(theta.detach()),
+                               getattr(frozen, 'process_group', None))
 
     @staticmethod
     def backward(ctx, grad_moments):
         (theta,) = ctx.saved_tensors
-        return ctx.frozen.vjp(theta.detach(), grad_moments), None
+        g = ctx.frozen.vjp(theta.detach(), grad_moments)
+        return sum_over_shards(g, getattr(ctx.frozen, 'process_group', None)), None
 
 
 def moment_stats(m, ref):
@@ -504,9 +537,14 @@ def resolving_power(zero_group, groups):
 def design_loop(model, photons, orders, zero_order=0, steps=50, lr=0.2, rot_scale=1e-4,
                 trans_scale=0.5, optimise=('facet_rotation', 'detector_translation',
                                            'detector_rotation'),
-                precision='fp32local', seed=0, min_photons=20, theta_init=None, callback=None):
+                precision='fp32local', seed=0, min_photons=20, theta_init=None, callback=None,
+                process_group=None, row_base=0):
     """Adam on the poses of the chain, maximising the mean resolving power of
     ``orders`` (distance from the ``zero_order`` centroid over FWHM).
+
+    With ``process_group`` every rank holds a shard of the photons (global
+    ids from ``row_base``): moments, gradients and the per-order photon
+    counts are summed over the ranks, so all ranks take the same steps.
 
     Every step re-poses the elements at the current parameters, traces
     ``photons`` (host columns or DevicePhotons) with fresh Philox draws, freezes
@@ -543,8 +581,10 @@ def design_loop(model, photons, orders, zero_order=0, steps=50, lr=0.2, rot_scal
             theta[idx] += scale * u.detach()
             model.apply(theta)
             fr, _ = model.trace(photons, all_orders, precision=precision, rng='philox',
-                                seed=seed + step, theta=theta, device=dev)
-            counts = torch.bincount(fr.group.long(), minlength=len(all_orders)).cpu().numpy()
+                                seed=seed + step, theta=theta, device=dev,
+                                process_group=process_group, row_base=row_base)
+            counts = sum_over_shards(torch.bincount(fr.group.long(), minlength=len(all_orders)),
+                                     process_group).cpu().numpy()
             groups = [g for g in range(len(orders)) if counts[g] >= min_photons]
             rp = resolving_power(len(orders), groups)
             th = theta.detach().requires_grad_(True)
@@ -579,6 +619,9 @@ class GraphedGradient:
     """
 
     def __init__(self, frozen, loss_fn, theta=None, warmup=3):
+        if getattr(frozen, 'process_group', None) is not None:
+            raise ValueError('GraphedGradient captures one process; call loss_and_grad for '
+                             'photons sharded over a process group')
         self.frozen = frozen
         dev = frozen.device
         self.theta = (frozen.model.theta0(dev) if theta is None else
