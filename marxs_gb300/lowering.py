@@ -93,10 +93,16 @@ def spline1_arrays(ip, what):
         raise NotImplementedError('%s: only degree-1 RectBivariateSpline (kx = ky = 1) is '
                                   'supported on the GPU' % what)
     tx, ty = ip.get_knots()
+    tx, ty = np.asarray(tx, dtype=float), np.asarray(ty, dtype=float)
+    # the kernels index the interval below a knot and its coefficients:
+    # at least two grid points (four knots) per axis, knots non-decreasing
+    if len(tx) < 4 or len(ty) < 4 or np.any(np.diff(tx) < 0) or np.any(np.diff(ty) < 0):
+        raise NotImplementedError('%s: a degree-1 spline needs at least two grid points per '
+                                  'axis and sorted knots' % what)
     c = np.asarray(ip.get_coeffs(), dtype=float)
     if c.size != (len(tx) - 2) * (len(ty) - 2):
         raise NotImplementedError('%s: unexpected spline coefficient layout' % what)
-    return np.asarray(tx, dtype=float), np.asarray(ty, dtype=float), c
+    return tx, ty, c
 
 
 def lens_spline(lens):

@@ -76,3 +76,30 @@ def test_split_ff_array_round_trip():
     ps = L.split_ff_array(xs)
     key = [(a, b) for a, b in ps]
     assert key == sorted(key)
+
+
+class _FakeSpline:
+    degrees = (1, 1)
+
+    def __init__(self, tx, ty):
+        self.tx, self.ty = np.asarray(tx, float), np.asarray(ty, float)
+
+    def get_knots(self):
+        return self.tx, self.ty
+
+    def get_coeffs(self):
+        return np.zeros((len(self.tx) - 2) * (len(self.ty) - 2))
+
+
+def test_spline_tables_need_two_grid_points_per_axis():
+    ok = _FakeSpline([0, 0, 1, 1], [0, 0, 2, 2])
+    tx, ty, c = L.spline1_arrays(ok, 'test')
+    assert len(tx) == 4 and c.size == 4
+    with pytest.raises(NotImplementedError):
+        L.spline1_arrays(_FakeSpline([0, 0, 0], [0, 0, 1, 1]), 'test')
+    with pytest.raises(NotImplementedError):
+        L.spline1_arrays(_FakeSpline([0, 0, 2, 1, 1], [0, 0, 1, 1]), 'test')
+    from scipy.interpolate import RectBivariateSpline
+    sp = RectBivariateSpline([0., 1.], [0., 1., 2.], np.ones((2, 3)), kx=1, ky=1)
+    tx, ty, c = L.spline1_arrays(sp, 'scipy')
+    assert len(tx) == 4 and len(ty) == 5 and c.size == 6
