@@ -119,7 +119,20 @@ def lens_spline(lens):
 
 
 def lower_selector(sel):
-    """Tables of an order selector, computed with the reference's numpy ops."""
+    """Tables of an order selector, computed with the reference's numpy ops;
+    checked so the kernels never index an empty table."""
+    spec = _lower_selector(sel)
+    n_rows, n_orders = spec.cdf.shape
+    if n_rows < 1 or n_orders < 1 or len(spec.orders) != n_orders or len(spec.total) != n_rows:
+        raise ValueError('order selector %s: needs at least one order and one row, and '
+                         'matching table shapes' % type(sel).__name__)
+    if spec.by_energy and len(spec.energy) != n_rows:
+        raise ValueError('order selector %s: %d energies for %d table rows'
+                         % (type(sel).__name__, len(spec.energy), n_rows))
+    return spec
+
+
+def _lower_selector(sel):
     names = classnames(sel)
     if hasattr(sel, 'interpolators') and hasattr(sel, 'orders'):
         # InterpolateEfficiencyTable (missions/mitsnl/catgrating.py:63-144)
@@ -142,6 +155,8 @@ def lower_selector(sel):
                             total=np.asarray(sel.totalprob, dtype=float),
                             orders=np.asarray(sel.orders).astype(np.int32), by_energy=True)
     if 'OrderSelector' in names:
+        if len(sel.p) == 0 or len(sel.orderlist) != len(sel.p):
+            raise ValueError('OrderSelector: needs at least one order, one probability each')
         p_sum = sel.p.sum()
         p = sel.p / p_sum
         cdf = p.cumsum()
@@ -170,6 +185,15 @@ class StageSpec:
     spline: Optional[tuple] = None   # LENS reflectivity (tx, ty, c[1, ...])
     stack: Optional[dict] = None     # GRATINGS of CATL1L2Stack facets: layer constants
     reads: Optional[str] = None      # SUPPORT: the id column it reads
+
+
+def _interp_table(x, y):
+    """(x, y) of an np.interp table: at least one point, x increasing."""
+    x, y = np.asarray(x, dtype=float), np.asarray(y, dtype=float)
+    if x.ndim != 1 or len(x) < 1 or x.shape != y.shape or np.any(np.diff(x) < 0):
+        raise ValueError('interpolation table: needs at least one point, matching x and y, '
+                         'and increasing x')
+    return x, y
 
 
 def _loc_names(elem):
@@ -484,8 +508,8 @@ def _cat_stack_stage(owner, stacks, id_col):
         qf=_value(qf.factor), l1_open=_value(l1.openfraction), l1_d=float(l1tab['dgrat'][0]),
         l1_vec=np.ascontiguousarray(np.concatenate([l1tab['l'], l1tab['dneg']], axis=1)),
         l1_selector=int(l1tab['selector'][0]),
-        l1_trans_e=np.asarray(l1.transfunc.x, dtype=float),
-        l1_trans_t=np.asarray(l1.transfunc.y, dtype=float),
+        l1_trans_e=_interp_table(l1.transfunc.x, l1.transfunc.y)[0],
+        l1_trans_t=_interp_table(l1.transfunc.x, l1.transfunc.y)[1],
         l2_open=(inner / period) ** 2, l2_shadow=_value(l2abs.bardepth) * inner,
         l2_total=period ** 2 / 2 * np.sqrt(3), l2_inner=_value(l2diff.innerfree))
     loc_stack = _loc_names(stacks[0])

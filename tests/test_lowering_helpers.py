@@ -103,3 +103,17 @@ def test_spline_tables_need_two_grid_points_per_axis():
     sp = RectBivariateSpline([0., 1.], [0., 1., 2.], np.ones((2, 3)), kx=1, ky=1)
     tx, ty, c = L.spline1_arrays(sp, 'scipy')
     assert len(tx) == 4 and len(ty) == 5 and c.size == 6
+
+
+def test_order_selectors_and_tables_are_checked():
+    from marxs_gb300.optics import OrderSelector, EfficiencyFile
+    spec = L.lower_selector(OrderSelector([0, 1, 2], p=[0.2, 0.3, 0.5]))
+    assert spec.cdf.shape == (1, 3) and spec.total[0] == pytest.approx(1.0)
+    with pytest.raises(ValueError):
+        L.lower_selector(OrderSelector([]))
+    with pytest.raises(ValueError):
+        L._interp_table([], [])
+    with pytest.raises(ValueError):
+        L._interp_table([1.0, 0.5], [0.1, 0.2])
+    x, y = L._interp_table([0.5], [0.3])
+    assert x[0] == 0.5 and y[0] == 0.3
