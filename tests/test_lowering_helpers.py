@@ -117,3 +117,18 @@ def test_order_selectors_and_tables_are_checked():
         L._interp_table([1.0, 0.5], [0.1, 0.2])
     x, y = L._interp_table([0.5], [0.3])
     assert x[0] == 0.5 and y[0] == 0.3
+
+
+@pytest.mark.parametrize('name, kinds', [('c0', [1, 2, 3]), ('c1', [1, 2, 4, 3]),
+                                         ('c2', [1, 2, 4, 5]), ('c5', [1, 2, 4, 5]),
+                                         ('c6', [1, 2, 4, 6, 5])])
+def test_every_workload_lowers_on_the_host(name, kinds):
+    """Lowering (stage descriptors, facet tables, candidate grid parameters,
+    selector and stack tables) is host work and runs without a GPU."""
+    from marxs_gb300 import configs
+    stages = L.lower_elements(configs.build(name).elements)
+    assert [s.kind for s in stages] == kinds
+    for st in stages:
+        if st.facets is not None:
+            assert len(st.facets) > 0 and st.grid is not None
+            assert st.grid['nu'] * st.grid['nv'] <= 1 << 20
