@@ -132,3 +132,31 @@ def test_every_workload_lowers_on_the_host(name, kinds):
         if st.facets is not None:
             assert len(st.facets) > 0 and st.grid is not None
             assert st.grid['nu'] * st.grid['nv'] <= 1 << 20
+
+
+@pytest.mark.parametrize('name', ['c0', 'c1', 'c2', 'c5', 'c6'])
+def test_column_plan_reproduces_the_reference_columns(name):
+    """The column plan (which stage creates which column, in which order,
+    float or id) gives the reference's own output table: the column names in
+    the order MARXS created them (add_output_cols, base/base.py:249-286) and
+    their kinds, as recorded in the golden fixture."""
+    import sys
+    import os
+    sys.path.insert(0, os.path.dirname(__file__))
+    from conftest import load_golden, golden_inputs, golden_outputs
+    from marxs_gb300 import configs
+    from marxs_gb300.gpu import ColumnPlan
+    g = load_golden(name)
+    inputs = list(golden_inputs(g))
+    stages = L.lower_elements(configs.build(name).elements)
+    plan = ColumnPlan(stages, existing=set(inputs))
+    cols = list(inputs)
+    for names in plan.order:            # every stage hits photons in the fixture
+        for c in names:
+            if c not in cols:
+                cols.append(c)
+    assert cols == [str(c) for c in g['colnames']]
+    out = golden_outputs(g)
+    for c, kind in plan.columns.items():
+        want = np.float64 if kind == 'f8' else np.integer
+        assert np.issubdtype(out[c].dtype, want), (c, kind, out[c].dtype)
