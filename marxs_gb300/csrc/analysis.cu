@@ -44,7 +44,7 @@ constexpr int kBins = 1 << kRadixBits;
 constexpr int kVBins = 8192;                   // value bins of the first level
 constexpr int kHist = kVBins > 2 * kBins ? kVBins : 2 * kBins;   // per-group histogram words
 constexpr int kLevels = 6;                     // ceil(64 / 11)
-constexpr int kCenterSample = 31;              // values whose median centres round 0's sums
+constexpr int kCenterSample = 31;              // values whose median centres the first clipping round's sums
 constexpr int kG = MGPU_STATS_MAX_GROUPS;
 constexpr uint64_t kSign = 0x8000000000000000ull;
 constexpr uint64_t kExp = 0x7ff0000000000000ull;
@@ -573,7 +573,7 @@ scatter_kernel(const __grid_constant__ mgpu_stats_problem P, Work W) {
     }
 }
 
-// round 0's centre: the median of the group's first values (a robust
+// the first clipping round's centre: the median of the group's first values (a robust
 // guess of the mean keeps the shifted sums well conditioned)
 __global__ void center_kernel(Work W) {
     if (threadIdx.x != 0) return;
@@ -593,7 +593,7 @@ __global__ void center_kernel(Work W) {
     }
     s.c = v[m / 2];
     choose_sums(s);
-    // round 0's value bins: the sample median -/+ 4 interquartile ranges,
+    // the first clipping round's value bins: the sample median -/+ 4 interquartile ranges,
     // or the group's whole range when the sample has no spread
     const double w = 4.0 * (v[(3 * m) / 4] - v[m / 4]);
     if (w > 0.0 && isfinite(w)) set_value_bins(s, s.c - w, s.c + w);
