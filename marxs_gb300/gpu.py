@@ -317,16 +317,20 @@ class ColumnPlan:
 class GpuSequence:
     """GPU backend for ``Sequence(elements=[...])`` on supported elements."""
 
-    def __init__(self, elements, precision='fp64', rng='predrawn', seed=0, device=None):
+    def __init__(self, elements, precision='fp64', rng='predrawn', seed=0, device=None,
+                 preprocess_steps=None, postprocess_steps=None):
         if precision not in _PRECISIONS:
             raise ValueError('precision must be one of %s' % list(_PRECISIONS))
         if rng not in _RNGS:
             raise ValueError('rng must be one of %s' % list(_RNGS))
-        for e in elements:
+        self.preprocess_steps = list(preprocess_steps or [])
+        self.postprocess_steps = list(postprocess_steps or [])
+        for e in list(elements) + self.preprocess_steps + self.postprocess_steps:
             if not callable(e):
                 from .simulator import SimulationSetupError
                 raise SimulationSetupError('{0} is not callable.'.format(str(e)))
         self.elements = list(elements)
+        self._stepwise = None
         self.precision = precision
         self.rng = rng
         self.seed = int(seed)
@@ -496,6 +500,34 @@ class GpuSequence:
         return status, hits
 
     # ------------------------------------------------------------ table path
+    def _element_sequence(self, k, elem):
+        """One-element chain for element ``k`` of a sequence with steps; its
+        Philox streams get their own seed (a one-element chain numbers its
+        stage 0, so a shared seed would repeat the draws of other elements)."""
+        seed = (self.seed * 1000003 + 7919 * (k + 1)) & 0xffffffffffffffff
+        return GpuSequence([elem], precision=self.precision, rng=self.rng, seed=seed,
+                           device=self.device)
+
+    def _call_stepwise(self, photons, draws, row_base, chunk):
+        """BaseContainer.__call__ (simulator/simulator.py:42-49) with
+        ``preprocess_steps`` / ``postprocess_steps``: the steps see the photon
+        table before and after every element, so each element runs as its own
+        GPU chain on the table (in place) with the steps on the host between."""
+        if isinstance(photons, dict):
+            from .table import PhotonTable
+            photons = PhotonTable(photons)
+        if self._stepwise is None or len(self._stepwise) != len(self.elements) or any(
+                sub[0] is not e for sub, e in zip(self._stepwise, self.elements)):
+            self._stepwise = [(e, self._element_sequence(k, e))
+                              for k, e in enumerate(self.elements)]
+        for _, sub in self._stepwise:
+            for p in self.preprocess_steps:
+                p(photons)
+            photons = sub(photons, draws=draws, row_base=row_base, chunk=chunk)
+            for p in self.postprocess_steps:
+                p(photons)
+        return photons
+
     def __call__(self, photons, draws=None, row_base=0, chunk=8_000_000):
         """Trace a photon table (astropy Table, PhotonTable or dict) in place.
 
@@ -507,8 +539,12 @@ class GpuSequence:
         arrays in pinned memory (``pinned_photons``) make the copies true DMA.
         On an error (raised after the whole call) the table content is
         unspecified, as in MARXS where earlier elements have already written
-        their columns when a later one raises.
+        their columns when a later one raises.  With ``preprocess_steps`` or
+        ``postprocess_steps`` the elements run one at a time, the steps
+        between them (``_call_stepwise``).
         """
+        if self.preprocess_steps or self.postprocess_steps:
+            return self._call_stepwise(photons, draws, row_base, chunk)
         import time as _time
         tm = {}
         t0 = _time.perf_counter()
