@@ -14,6 +14,16 @@ Prints one JSON line on rank 0.  ``value`` is device-resident throughput
 ``GpuSequence(...)(table)`` call with pinned host buffers, host<->device
 copies included.  ``--impl reference`` times the CPU oracle (the reference
 algorithm restated in numpy) on all host cores on a bounded sample.
+
+Sub-lines of the same JSON line (each can be switched off by a --no-* flag):
+``fp32local_*`` / ``fp64_*`` and ``um_error`` (the two precisions and the
+FP32-local error against float64), ``roofline`` (the chain kernel against
+the measured HBM copy bandwidth), ``e2e``, ``source_pipeline`` (photons
+generated on the device, event columns to the host), ``analysis``
+(CaptureResAeff on the device columns), ``cat_stack`` (CATL1L2Stack facets),
+``stages`` (each stage alone, against HBM and the measured FMA peaks),
+``adjoint`` and ``design`` (pose gradients, design loop), ``tolerancing``
+and ``cpu_baseline`` (the oracle on one core).
 """
 import argparse
 import json
@@ -33,8 +43,8 @@ WORKLOAD = 'cat_rowland_1000facets_circular_detector'
 # DRAM bytes (read + write) per photon of the chain kernel, from the ncu
 # captures of a 4e6-photon launch (profiles/chain_fp64_c2.md,
 # profiles/chain_fp32local_c2.md), scaled to the launch by photon count
-NCU_TRAFFIC_BYTES_PER_PHOTON = {'fp64': (353.9e6 + 727.0e6) / 4e6,
-                                'fp32local': (355.9e6 + 732.1e6) / 4e6}
+NCU_TRAFFIC_BYTES_PER_PHOTON = {'fp64': (358.2e6 + 735.3e6) / 4e6,
+                                'fp32local': (354.1e6 + 725.2e6) / 4e6}
 
 
 def parse():
