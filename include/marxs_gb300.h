@@ -184,16 +184,19 @@ typedef struct {
 } mgpu_grid32;
 
 /* FP32-local constants of a circular cylinder detector.  e1, e2, a are the
- * unit local axes; angles are resolved against a table of reference angles
- * k / 1024 rad, k = k0 .. k0 + nk - 1, holding cos and sin as float-float. */
+ * unit local axes.  Hits are resolved around reference points on the
+ * cylinder at the angles k / 1024 rad, k = k0 .. k0 + nk - 1: the stage's
+ * table holds per k three float4, (P_k hi, u.x), (P_k lo, u.y), (t_k, u.z),
+ * with P_k = c + R u_k the global reference point as float-float,
+ * u_k = cos e1 + sin e2 the radial and t_k = -sin e1 + cos e2 the tangential
+ * unit vector. */
 typedef struct {
     float c_hi[3], c_lo[3];
-    float e1_hi[3], e1_lo[3];
-    float e2_hi[3], e2_lo[3];
-    float a_hi[3], a_lo[3];
-    float R_hi, R_lo;      /* radius (x zoom) */
+    float e1[3], e2[3], a[3];
+    float R;               /* radius (x zoom) */
     float Rz;              /* half length (z zoom) */
-    float b1, b2;          /* reduced phi_lim borders */
+    float w1[2], w2[2];    /* phi_lim borders as unit vectors in the (e1, e2) plane */
+    int32_t arc;           /* 0: arc w1 -> w2 spans <= pi, 1: > pi, 2: full circle */
     float rpix_hi, rpix_lo;/* R / pixsize */
     float inv_pix;
     float cp0, cp1;        /* centerpix */
@@ -280,7 +283,8 @@ typedef struct {
     const void* aux;             /* FP32-local constants: mgpu_flat32 (flat kinds),
                                     mgpu_grid32 (GRATINGS), mgpu_cyl32 (CYLDET) */
     const mgpu_facet32* facets32;/* GRATINGS, FP32-local */
-    const float* table;          /* CYLDET, FP32-local: nk x (cos hi, cos lo, sin hi, sin lo) */
+    const float* table;          /* CYLDET, FP32-local: nk x 12 floats, 16-byte aligned
+                                    (see mgpu_cyl32) */
     const float* cand32;         /* GRATINGS, FP32-local: 16 floats per facet, 16-byte aligned:
                                     (c_hi, hy), (e_x, hz), (e_y, e_z.x), (e_z.y, e_z.z, 0, 0) */
     mgpu_spline1 spline;         /* LENS: reflectivity_interpolator(energy, angle / 4), squared
@@ -322,6 +326,7 @@ int mgpu_trace(const mgpu_chain* chain, const mgpu_photons* photons, void* strea
 
 /* Build the candidate lists of a grating stage's grid on the device:
  * grid->cell_start / cell_items are filled from the facet table.
+ * n_facets < 0, or facets NULL with n_facets > 0, is cudaErrorInvalidValue.
  * ``counts`` is caller-provided scratch of nu*nv + 1 + ceil(nu*nv / 4096) int32. */
 int mgpu_facet_grid_build(const mgpu_facet* facets, int32_t n_facets, mgpu_grid* grid,
                           int32_t* counts, uint32_t* status, void* stream);
@@ -330,14 +335,18 @@ int mgpu_facet_grid_build(const mgpu_facet* facets, int32_t n_facets, mgpu_grid*
  * the reference.  For callers that cannot allocate device memory when they
  * rebuild the grid (a host whose own pool owns the device memory, or a loop
  * where cudaMalloc/cudaFree would synchronise the device): the per-cell
- * scratch lives in a fixed device array of MGPU_NOALLOC_MAX_CELLS + 1 int32
- * (256 KiB, held on every GPU that loads the library until the process
- * exits), and the entry point calls no allocator.  The caller still passes
+ * scratch lives in a fixed device array of MGPU_NOALLOC_MAX_CELLS + 1 cell
+ * counters plus one int32 scan sum per 4096 cells (65,553 int32 = 262,212 B,
+ * held on every GPU that loads the library until the process exits), and
+ * the entry point calls no allocator.  The caller still passes
  * the facets, the grid with its cell_start / cell_items outputs, and the
  * status word.  Grids with nu * nv > MGPU_NOALLOC_MAX_CELLS are rejected with
  * MGPU_ERR_NOALLOC_LIMIT before anything is launched.  The first call on a
  * device looks up the array's device address with that device current; make
- * that first call before any stream capture.  All calls share the array:
+ * that first call before any stream capture.  The address is kept for the
+ * life of the process: after cudaDeviceReset, or with another context made
+ * current on the same device, it is stale, so do not call this entry point
+ * across a reset.  All calls share the array:
  * each call clears it before use, and calls that overlap on the GPU (other
  * streams, other host threads) race on it. */
 #define MGPU_NOALLOC_MAX_CELLS 65536

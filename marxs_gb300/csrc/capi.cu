@@ -107,6 +107,7 @@ int mgpu_trace(const mgpu_chain* chain, const mgpu_photons* photons, void* strea
 int mgpu_facet_grid_build(const mgpu_facet* facets, int32_t n_facets, mgpu_grid* grid,
                           int32_t* counts, uint32_t* status, void* stream) {
     if (grid == nullptr || counts == nullptr || status == nullptr) return (int)cudaErrorInvalidValue;
+    if (n_facets < 0 || (n_facets > 0 && facets == nullptr)) return (int)cudaErrorInvalidValue;
     if (grid->nu <= 0 || grid->nv <= 0 || grid->cell_start == nullptr || grid->cell_items == nullptr)
         return (int)cudaErrorInvalidValue;
     return (int)mgpu_launch_grid_build(facets, n_facets, *grid, counts, status, (cudaStream_t)stream);

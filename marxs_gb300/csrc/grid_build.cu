@@ -210,6 +210,7 @@ std::atomic<void*> g_noalloc_addr[kNoallocMaxDevices];
 extern "C" int mgpu_facet_grid_build_noalloc(const mgpu_facet* facets, int32_t n_facets,
                                              mgpu_grid* grid, uint32_t* status, void* stream) {
     if (grid == nullptr || status == nullptr) return (int)cudaErrorInvalidValue;
+    if (n_facets < 0 || (n_facets > 0 && facets == nullptr)) return (int)cudaErrorInvalidValue;
     if (grid->nu <= 0 || grid->nv <= 0 || grid->cell_start == nullptr || grid->cell_items == nullptr)
         return (int)cudaErrorInvalidValue;
     if ((long long)grid->nu * (long long)grid->nv > MGPU_NOALLOC_MAX_CELLS)

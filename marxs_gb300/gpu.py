@@ -516,11 +516,15 @@ class GpuSequence:
         if isinstance(photons, dict):
             from .table import PhotonTable
             photons = PhotonTable(photons)
-        if self._stepwise is None or len(self._stepwise) != len(self.elements) or any(
-                sub[0] is not e for sub, e in zip(self._stepwise, self.elements)):
-            self._stepwise = [(e, self._element_sequence(k, e))
-                              for k, e in enumerate(self.elements)]
-        for _, sub in self._stepwise:
+        # the one-element chains carry this sequence's settings: rebuild them
+        # when an element or any of precision, rng, seed, device changed
+        key = (self.precision, self.rng, self.seed, str(self.device))
+        if self._stepwise is None or self._stepwise[0] != key or \
+                len(self._stepwise[1]) != len(self.elements) or any(
+                    sub[0] is not e for sub, e in zip(self._stepwise[1], self.elements)):
+            self._stepwise = (key, [(e, self._element_sequence(k, e))
+                                    for k, e in enumerate(self.elements)])
+        for _, sub in self._stepwise[1]:
             for p in self.preprocess_steps:
                 p(photons)
             photons = sub(photons, draws=draws, row_base=row_base, chunk=chunk)
@@ -541,7 +545,10 @@ class GpuSequence:
         unspecified, as in MARXS where earlier elements have already written
         their columns when a later one raises.  With ``preprocess_steps`` or
         ``postprocess_steps`` the elements run one at a time, the steps
-        between them (``_call_stepwise``).
+        between them (``_call_stepwise``); with ``rng='philox'`` each element
+        then draws from its own seed, so the draws (and results) differ from
+        the fused chain's for the same seed -- the same distributions, a
+        different stream.  Pre-drawn randomness gives identical results.
         """
         if self.preprocess_steps or self.postprocess_steps:
             return self._call_stepwise(photons, draws, row_base, chunk)

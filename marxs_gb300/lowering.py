@@ -206,6 +206,18 @@ def _norms(v):
     return np.sqrt(np.einsum('ij,ij->i', v, v))
 
 
+def default_blaze_modifier(g):
+    """True when ``g.blaze_angle_modifier`` is FlatGrating's own (zero,
+    optics/grating.py:222-231): the class that defines it, found along the
+    MRO, is FlatGrating, and the instance does not override it."""
+    if 'blaze_angle_modifier' in getattr(g, '__dict__', {}):
+        return False
+    for klass in type(g).__mro__:
+        if 'blaze_angle_modifier' in vars(klass):
+            return klass.__name__ == 'FlatGrating'
+    return True
+
+
 def _grating_facets(gratings, selectors, sel_index):
     """Facet table of a list of gratings (vectorised over the facets): the
     frame of Geometry.__getitem__ (math/geometry.py:108-160) and the groove
@@ -216,7 +228,7 @@ def _grating_facets(gratings, selectors, sel_index):
         if callable(g._d):
             raise NotImplementedError('position-dependent grating constant (callable d) is not '
                                       'supported on the GPU')
-        if 'blaze_angle_modifier' in type(g).__dict__ and not hasattr(g, 'd_blaze_mm'):
+        if not default_blaze_modifier(g) and not hasattr(g, 'd_blaze_mm'):
             raise NotImplementedError('custom blaze_angle_modifier is not supported on the GPU')
     P = np.stack([np.asarray(g.geometry.pos4d, dtype=float) for g in gratings])   # (F, 4, 4)
     vx, vy, vz = P[:, :, 0], P[:, :, 1], P[:, :, 2]
@@ -337,6 +349,29 @@ def _snapshot(v):
     return np.array(v, copy=True) if isinstance(v, np.ndarray) else v
 
 
+def _inner_arrays(obj, depth=2):
+    """The ndarrays an object holds (in its ``__dict__``, in lists and tuples
+    there, and in the objects it holds, ``depth`` levels down): the tables of
+    an order selector or an interpolator (a scipy spline keeps its knots and
+    coefficients in ``tck``)."""
+    out, seen = [], set()
+
+    def visit(o, d):
+        if id(o) in seen:
+            return
+        seen.add(id(o))
+        if isinstance(o, np.ndarray):
+            out.append(o)
+        elif isinstance(o, (list, tuple)):
+            for x in o:
+                visit(x, d)
+        elif d > 0 and isinstance(getattr(o, '__dict__', None), dict):
+            for v in vars(o).values():
+                visit(v, d - 1)
+    visit(obj, depth)
+    return out
+
+
 class ChangeWatch:
     """What a lowered chain was built from, for a cheap check on every call.
 
@@ -347,7 +382,9 @@ class ChangeWatch:
     element lists and the geometry objects by identity, all pos4d matrices
     (assigned or edited in place) as one stacked array, and the watched
     attributes by identity (by value where the identity changed, and always
-    for array values).
+    for array values).  Objects held in watched attributes (order selectors,
+    interpolators) are also compared by the values of the tables they hold,
+    so a selector's probability table edited in place is noticed too.
     """
 
     def __init__(self, elements):
@@ -383,6 +420,15 @@ class ChangeWatch:
             arrays = [k for k, v in enumerate(vals) if isinstance(v, np.ndarray)]
             self.attrs.append((operator.attrgetter(name), ol, [id(v) for v in vals],
                                [_snapshot(v) for v in vals], arrays))
+        # tables inside the distinct objects held by watched attributes
+        held = {}
+        for _, ol, _, snaps, _ in self.attrs:
+            for v in snaps:
+                if not isinstance(v, (np.ndarray, str, bytes, int, float, bool, type(None))) and \
+                        isinstance(getattr(v, '__dict__', None), dict):
+                    held[id(v)] = v
+        self.held = [(o, [np.array(a, copy=True) for a in _inner_arrays(o)])
+                     for o in held.values()]
 
     @staticmethod
     def _stack(mats):
@@ -414,6 +460,10 @@ class ChangeWatch:
             for k in arrays:
                 if not _same(vals[k], snaps[k]):
                     return True
+        for o, tables in self.held:
+            now = _inner_arrays(o)
+            if len(now) != len(tables) or not all(map(_same, now, tables)):
+                return True
         return False
 
 
@@ -730,7 +780,9 @@ PHI_TABLE_STEP = 1024
 
 
 def cyl32_block(st):
-    """Cylinder constants and the cos/sin table of reference angles k/1024."""
+    """Cylinder constants and the table of reference points k/1024 rad:
+    per k the global point P_k = c + R u_k (float-float), the radial u_k and
+    the tangent t_k, as three float4 (P_k hi, u.x), (P_k lo, u.y), (t_k, u.z)."""
     from .geomath import decompose44
     e = st.element
     pos4d = np.asarray(e.geometry.pos4d, dtype=float)
@@ -738,15 +790,18 @@ def cyl32_block(st):
     if not np.isclose(Z[0], Z[1], rtol=1e-12, atol=0) or not np.allclose(S, 0, atol=1e-12):
         raise NotImplementedError('fp32local supports circular, unsheared cylinders only')
     b = _abi.MgpuCyl32()
-    for name, vec in (('c', T), ('e1', R[:, 0]), ('e2', R[:, 1]), ('a', R[:, 2])):
-        hi, lo = split_ff(vec)
-        getattr(b, name + '_hi')[:] = [float(v) for v in hi]
-        getattr(b, name + '_lo')[:] = [float(v) for v in lo]
-    rhi, rlo = split_ff(Z[0])
-    b.R_hi, b.R_lo = float(rhi), float(rlo)
+    hi, lo = split_ff(T)
+    b.c_hi[:] = [float(v) for v in hi]
+    b.c_lo[:] = [float(v) for v in lo]
+    for name, vec in (('e1', R[:, 0]), ('e2', R[:, 1]), ('a', R[:, 2])):
+        getattr(b, name)[:] = [float(v) for v in np.float32(vec)]
+    b.R = float(np.float32(Z[0]))
     b.Rz = float(Z[2])
-    b.b1 = float(st.cyl[26])
-    b.b2 = float(st.cyl[27])
+    b1, b2 = float(st.cyl[26]), float(st.cyl[27])
+    b.w1[:] = [float(np.float32(np.cos(b1))), float(np.float32(np.sin(b1)))]
+    b.w2[:] = [float(np.float32(np.cos(b2))), float(np.float32(np.sin(b2)))]
+    arc = (b2 - b1) if b1 < b2 else (2 * np.pi - b1 + b2)
+    b.arc = 2 if b1 == b2 else (0 if arc <= np.pi else 1)
     ph, pl = split_ff(Z[0] / st.p[0])
     b.rpix_hi, b.rpix_lo = float(ph), float(pl)
     b.inv_pix = float(1.0 / st.p[0])
@@ -755,9 +810,14 @@ def cyl32_block(st):
     kmax = int(np.ceil((np.pi + 0.01) * PHI_TABLE_STEP))
     k = np.arange(-kmax, kmax + 1)
     ang = k / PHI_TABLE_STEP
-    ch, cl = split_ff(np.cos(ang))
-    sh, sl = split_ff(np.sin(ang))
-    table = np.stack([ch, cl, sh, sl], axis=1).astype(np.float32)
+    u = np.cos(ang)[:, None] * R[:, 0] + np.sin(ang)[:, None] * R[:, 1]
+    tg = -np.sin(ang)[:, None] * R[:, 0] + np.cos(ang)[:, None] * R[:, 1]
+    P = T + Z[0] * u
+    phi_, plo = split_ff(P)
+    table = np.empty((len(k), 12), dtype=np.float32)
+    table[:, 0:3], table[:, 3] = phi_, u[:, 0]
+    table[:, 4:7], table[:, 7] = plo, u[:, 1]
+    table[:, 8:11], table[:, 11] = tg, u[:, 2]
     b.k0 = int(k[0])
     b.nk = int(len(k))
     return bytes(b), table

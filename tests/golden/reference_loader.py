@@ -9,7 +9,11 @@ this module.
 import os
 import sys
 
-REFERENCE_ROOT = os.environ.get('MARXS_REFERENCE_ROOT', '/root/reference')
+# MARXS_REFERENCE_ROOT, else a MARXS checkout named ``reference`` beside
+# this repository; the tests that need it skip when neither exists
+_REPO = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+REFERENCE_ROOT = os.environ.get('MARXS_REFERENCE_ROOT',
+                                os.path.join(os.path.dirname(_REPO), 'reference'))
 _SHIM = os.path.join(os.path.dirname(os.path.abspath(__file__)), 'refshim')
 
 

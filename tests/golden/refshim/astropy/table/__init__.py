@@ -129,10 +129,11 @@ class Table:
         else:
             raise NotImplementedError('row assignment not supported by the shim')
 
-    def add_column(self, col, name=None, index=None):
+    def add_column(self, col, name=None, index=None, copy=True):
         name = name or col.name
         if not isinstance(col, Column):
-            col = self._as_column(name, col)
+            # copy=False keeps the caller's array (a view, no copy), as astropy
+            col = self._as_column(name, col) if copy else np.asarray(col).view(Column)
         col.name = name
         self.columns[name] = col
 

@@ -163,6 +163,14 @@ def test_entry_points_reject_bad_descriptors_without_a_gpu():
     assert lib.mgpu_facet_grid_build(None, 0, C.byref(g), None, None, None) == bad
     assert lib.mgpu_facet_grid_build(None, 0, C.byref(g), C.c_void_p(16), C.c_void_p(16),
                                      None) == bad                      # nu = nv = 0
+    g.nu = g.nv = 1
+    g.cell_start = g.cell_items = 16
+    for build in (lambda f, n: lib.mgpu_facet_grid_build(f, n, C.byref(g), C.c_void_p(16),
+                                                           C.c_void_p(16), None),
+                  lambda f, n: lib.mgpu_facet_grid_build_noalloc(f, n, C.byref(g),
+                                                                   C.c_void_p(16), None)):
+        assert build(None, 3) == bad                  # facets NULL with n_facets > 0
+        assert build(C.c_void_p(16), -1) == bad       # negative facet count
     assert lib.mgpu_plane_intersect(None, 5, _abi.MgpuVec(), _abi.MgpuVec(), None,
                                     _abi.MgpuVec(), _abi.MgpuCol(), _abi.MgpuCol(), None) == bad
     assert lib.mgpu_order_stats(None, None) == bad

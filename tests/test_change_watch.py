@@ -103,3 +103,33 @@ def test_lens_reflectivity_and_detector_pixels():
     w = ChangeWatch(chain)
     chain[-1].pixsize = chain[-1].pixsize * 2
     assert w.changed(chain)
+
+
+def test_order_selector_table_edited_in_place(chain):
+    """A selector's probability table edited in place (same object, same
+    array) must make the chain lower again."""
+    w = ChangeWatch(chain)
+    f = chain[2].elements[0]
+    if not hasattr(f, 'order_selector'):
+        f = f.elements[0]
+    sel = f.order_selector
+    if hasattr(sel, 'cumprob'):                      # EfficiencyFile
+        sel.cumprob[..., 0] *= 0.5
+    else:                                            # InterpolateEfficiencyTable
+        spl = sel.interpolators[3]
+        coeff = spl.tck[2] if hasattr(spl, 'tck') else spl.get_coeffs()
+        coeff[0] += 1e-3
+    assert w.changed(chain)
+
+
+def test_reflectivity_coefficients_edited_in_place():
+    chain = configs.build('c5').elements
+    w = ChangeWatch(chain)
+    assert not w.changed(chain)
+    spl = chain[0].reflectivity_interpolator
+    arrays = [a for a in vars(spl).values() if isinstance(a, np.ndarray)]
+    arrays += [a for t in vars(spl).values() if isinstance(t, (list, tuple))
+               for a in t if isinstance(a, np.ndarray)]
+    assert arrays, 'the interpolator keeps its tables as arrays'
+    max(arrays, key=lambda a: a.size).flat[0] += 1e-3
+    assert w.changed(chain)

@@ -98,3 +98,16 @@ def test_noalloc_build_rejects_grid_beyond_its_limit():
     assert rc == _abi.ERR_NOALLOC_LIMIT
     torch.cuda.synchronize()
     assert int(status.item()) == 0
+
+
+def test_noalloc_build_rejects_bad_facet_arguments():
+    """NULL facets with a positive count, or a negative count, are refused
+    on the host with cudaErrorInvalidValue (1); nothing is launched."""
+    from marxs_gb300 import _abi
+    lib = _abi.load()
+    grid = _abi.MgpuGrid()
+    grid.nu = grid.nv = 1
+    grid.cell_start = grid.cell_items = 16
+    assert lib.mgpu_facet_grid_build_noalloc(None, 3, C.byref(grid), C.c_void_p(16), None) == 1
+    assert lib.mgpu_facet_grid_build_noalloc(C.c_void_p(16), -1, C.byref(grid), C.c_void_p(16),
+                                             None) == 1
