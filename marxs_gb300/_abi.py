@@ -98,12 +98,12 @@ class MgpuGrid32(C.Structure):
 
 
 class MgpuCyl32(C.Structure):
-    _fields_ = [('c_hi', C.c_float * 3), ('c_lo', C.c_float * 3), ('e1_hi', C.c_float * 3),
-                ('e1_lo', C.c_float * 3), ('e2_hi', C.c_float * 3), ('e2_lo', C.c_float * 3),
-                ('a_hi', C.c_float * 3), ('a_lo', C.c_float * 3), ('R_hi', C.c_float),
-                ('R_lo', C.c_float), ('Rz', C.c_float), ('b1', C.c_float), ('b2', C.c_float),
-                ('rpix_hi', C.c_float), ('rpix_lo', C.c_float), ('inv_pix', C.c_float),
-                ('cp0', C.c_float), ('cp1', C.c_float), ('k0', C.c_int32), ('nk', C.c_int32)]
+    _fields_ = [('c_hi', C.c_float * 3), ('c_lo', C.c_float * 3), ('e1', C.c_float * 3),
+                ('e2', C.c_float * 3), ('a', C.c_float * 3), ('R', C.c_float),
+                ('Rz', C.c_float), ('w1', C.c_float * 2), ('w2', C.c_float * 2),
+                ('arc', C.c_int32), ('rpix_hi', C.c_float), ('rpix_lo', C.c_float),
+                ('inv_pix', C.c_float), ('cp0', C.c_float), ('cp1', C.c_float),
+                ('k0', C.c_int32), ('nk', C.c_int32)]
 
 
 class MgpuGrid(C.Structure):

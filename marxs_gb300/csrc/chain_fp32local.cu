@@ -5,15 +5,18 @@
 // arithmetic split by what each quantity needs:
 //   * photon positions are float-float (hi + lo) in the global frame, so a
 //     ray is re-centred on each element exactly (pos - centre) and the
-//     element's own arithmetic runs in float32 on small local numbers;
-//   * every ray/plane parameter k is refined once against the plane so the
-//     stored position lies on the element (the float32 solve alone leaves it
-//     ~1e-7 k off along the ray);
+//     element's own arithmetic runs in float32 on small local numbers: the
+//     intersection's local offset is formed inside FMAs, where the large
+//     parts of (pos - centre) and k dir cancel exactly, and the parameter k
+//     is refined once against the element so the stored position lies on it
+//     (the float32 solve alone leaves it ~1e-7 k off along the ray);
 //   * directions, polarization, probability and local coordinates are
 //     float32; the grating term m * lambda / d is formed in float-float;
-//   * the cylinder hit is refined by one float-float Newton step and its
-//     angle resolved as (reference angle k/1024 from a float-float table) +
-//     (small float32 residual), so det_phi keeps ~1e-11 rad;
+//   * the cylinder hit is solved in float32 around the tabulated reference
+//     point at the nearest angle k/1024 (global float-float point, radial
+//     and tangential unit vectors): one Newton step on the small offset from
+//     that point, and det_phi = k/1024 + a small float32 residual angle, so
+//     det_phi keeps ~1e-11 rad;
 //   * order selection is exact: a 53-bit draw U against integer thresholds
 //     ceil(cdf * 2^53); the nearest energy row by integer keys against the
 //     rows' float64 midpoints (made on the host);
@@ -89,36 +92,36 @@ __device__ __forceinline__ void write_miss_defaults(const mgpu_stage& st, int64_
 struct HitL {
     bool hit;
     float k;
-    ff3 ip;
+    ff3 ip;      // intersection point, global (float-float)
+    f3 v;        // intersection point - element centre
+    f3 r0;       // ray start - element centre
     float ly, lz;
 };
 
-// FinitePlane.intersect in the element frame: float32 solve, one
-// refinement against the plane, local coordinates from the exact offset
+// FinitePlane.intersect in the element frame.  The ray start is re-centred
+// once on the element (pos - c as an unnormalised pair s + e, exact to
+// ~2^-46); the parameter k comes from a float32 solve, and the local offset
+// v = (s + k dir) + e is formed inside FMAs, where the large parts of s and
+// k dir cancel exactly, so v carries only its own rounding (~2^-24 |v|)
+// plus an offset along the ray from the error of k, which one refinement
+// against the plane removes.  The global point is c + v in float-float.
 __device__ __forceinline__ HitL plane_hit_l(ff3 c, f3 n, f3 ey, f3 ez, float hy, float hz,
                                             const ff3& pos, f3 dir) {
     HitL h;
-    // first solve from a float32 offset (error ~2^-24 |pos|, removed by the
-    // refinement against the float-float offset below)
-    f3 rel{(pos.x.hi - c.x.hi) + (pos.x.lo - c.x.lo), (pos.y.hi - c.y.hi) + (pos.y.lo - c.y.lo),
-           (pos.z.hi - c.z.hi) + (pos.z.lo - c.z.lo)};
-    float kd = dotf(dir, n);
-    float k = -dotf(rel, n) / kd;
-    ff3 ip = pos;
-    f3 v = rel;
-    if (k != 0.0f) {            // rays that start on the plane (k == 0) need no update
-        ip = ff3_axpy(pos, k, dir);
-        v = ff3_f(ff3_sub(ip, c));
-        float dk = -dotf(v, n) / kd;
-        if (kd != 0.0f && dk != 0.0f && isfinite(dk)) {
-            // |dk| ~ float32 error of k: dk * dir is exact to ~1e-10 mm in float32
-            k += dk;
-            ip = ff3_add_f3(ip, dk * dir);
-            v = v + dk * dir;
-        }
+    f3 s, e;
+    ff3_rel(pos, c, s, e);
+    const float kd = dotf(dir, n);
+    float k = -(dotf(s, n) + dotf(e, n)) / kd;
+    f3 v{fmaf(k, dir.x, s.x) + e.x, fmaf(k, dir.y, s.y) + e.y, fmaf(k, dir.z, s.z) + e.z};
+    const float dk = -dotf(v, n) / kd;
+    if (isfinite(dk)) {
+        k += dk;
+        v = f3{fmaf(dk, dir.x, v.x), fmaf(dk, dir.y, v.y), fmaf(dk, dir.z, v.z)};
     }
     h.k = k;
-    h.ip = ip;
+    h.v = v;
+    h.r0 = s + e;
+    h.ip = ff3{ff_add_f(c.x, v.x), ff_add_f(c.y, v.y), ff_add_f(c.z, v.z)};
     h.ly = dotf(v, ey);
     h.lz = dotf(v, ez);
     h.hit = (kd != 0.0f) && (k >= 0.0f) && (fabsf(h.ly) <= hy) && (fabsf(h.lz) <= hz);
@@ -310,8 +313,8 @@ __device__ bool stage_lens_l(const mgpu_stage& st, PhotonL& ph, int64_t i, uint3
         write_miss_defaults(st, i, 2);
         return false;
     }
-    f3 cm = ff3_f(ff3_sub(ldff3(F->c_hi, F->c_lo), h.ip));     // centre - interpos
-    f3 v = cm - F->p[1] * ldf3(F->ez) + F->p[0] * normf(ph.dir);
+    // focus - interpos = (centre - interpos) - d_off e_z + f norm(dir)
+    f3 v = (F->p[0] * normf(ph.dir) - F->p[1] * ldf3(F->ez)) - h.v;
     f3 nd = normf(v);
     if (st.spline.n_surf > 0) {
         // probability *= reflectivity_interpolator(E, angle / 4) ** 2 (mirror.py:73-79);
@@ -369,7 +372,7 @@ __device__ bool stage_scatter_l(const mgpu_stage& st, PhotonL& ph, int64_t i, in
         a_in = sig_in * (r * cs);
         a_perp = sig_perp * (r * sn);
     }
-    f3 radial = ff3_f(ff3_sub(ph.pos, ldff3(F->c_hi, F->c_lo)));   // previous position
+    const f3 radial = h.r0;   // previous position - centre
     f3 perpplane = crossf(ph.dir, radial);
     f3 delta{0.0f, 0.0f, 0.0f};
     if (sig_in != 0.0f) delta = rot_transpose_delta_f(perpplane, a_in, ph.dir);
@@ -406,93 +409,96 @@ __device__ bool stage_flatdet_l(const mgpu_stage& st, PhotonL& ph, int64_t i) {
     return true;
 }
 
-__device__ __forceinline__ bool angle_between_f(float angle, float b1, float b2) {
-    const float twopi = 6.283185307179586f;
-    float a = fmodf(angle, twopi);
-    if (a < 0.0f) a += twopi;
-    if (b1 < b2) return (b1 <= a) && (a <= b2);
-    return (b1 <= a) || (a <= b2);
+// phi_lim test of a point (x, y) of the cylinder's (e1, e2) plane against
+// the borders as unit vectors w1, w2 (angle_between, math/utils.py:180-215,
+// as half-plane tests: the arc from w1 counter-clockwise to w2 is the
+// intersection of two half-planes when it spans at most pi, their union
+// otherwise)
+__device__ __forceinline__ bool in_arc(const mgpu_cyl32* K, float x, float y) {
+    const bool s1 = K->w1[0] * y - K->w1[1] * x >= 0.0f;     // w1 x p >= 0
+    const bool s2 = x * K->w2[1] - y * K->w2[0] >= 0.0f;     // p x w2 >= 0
+    return K->arc == 2 || (K->arc == 0 ? (s1 && s2) : (s1 || s2));
 }
 
 __device__ bool stage_cyldet_l(const mgpu_stage& st, PhotonL& ph, int64_t i) {
     // Cylinder.intersect (math/geometry.py:470-564) + CircularDetector
     // (optics/detector.py:115-118) for a circular tube
     const mgpu_cyl32* K = (const mgpu_cyl32*)st.aux;
-    ff3 e1 = ldff3(K->e1_hi, K->e1_lo), e2 = ldff3(K->e2_hi, K->e2_lo), ax = ldff3(K->a_hi, K->a_lo);
-    f3 e1f = ldf3(K->e1_hi), e2f = ldf3(K->e2_hi), af = ldf3(K->a_hi);
-    ff R{K->R_hi, K->R_lo};
-    ff3 q = ff3_sub(ph.pos, ldff3(K->c_hi, K->c_lo));
-    // the root is found in float32 (error ~1e-3 mm from the cancellation in
-    // c at |q_perp| ~ R), the float-float Newton step below makes it exact
-    const f3 qf = ff3_f(q);
-    const float q1f = dotf(qf, e1f), q2f = dotf(qf, e2f), q3 = dotf(qf, af);
-    f3 d = ph.dir;
-    float d1 = dotf(d, e1f), d2 = dotf(d, e2f), d3 = dotf(d, af);
-    float a = d1 * d1 + d2 * d2;
-    float b = q1f * d1 + q2f * d2;                                  // half of the linear term
-    float c = (q1f - K->R_hi) * (q1f + K->R_hi) + q2f * q2f;
-    float disc = b * b - a * c;
+    const f3 e1 = ldf3(K->e1), e2 = ldf3(K->e2), ax = ldf3(K->a);
+    const float R = K->R;
+    // approximate root in float32 from q = pos - c (error ~1e-3 mm from the
+    // cancellation in c at |q_perp| ~ R; the Newton step below removes it)
+    f3 qs, qe;
+    ff3_rel(ph.pos, ldff3(K->c_hi, K->c_lo), qs, qe);
+    const f3 qf = qs + qe;
+    const float q1 = dotf(qf, e1), q2 = dotf(qf, e2), q3 = dotf(qf, ax);
+    const f3 d = ph.dir;
+    const float d1 = dotf(d, e1), d2 = dotf(d, e2), d3 = dotf(d, ax);
+    const float a = d1 * d1 + d2 * d2;
+    const float b = q1 * d1 + q2 * d2;                              // half of the linear term
+    const float c = (q1 - R) * (q1 + R) + q2 * q2;
+    const float disc = b * b - a * c;
     bool hit = false;
     float t = 0.0f;
     if (disc >= 0.0f && a > 0.0f) {
-        float sq = sqrtf(disc);
-        float qq = -(b + copysignf(sq, b));
-        float tA = qq / a, tB = c / qq;
-        float a1 = (b < 0.0f) ? tA : tB;     // (-b + sq) / a
-        float a2 = (b < 0.0f) ? tB : tA;     // (-b - sq) / a
-        float z1 = q3 + a1 * d3, z2 = q3 + a2 * d3;
-        bool h1 = (a1 >= 0.0f) && (fabsf(z1) <= K->Rz) &&
-                  angle_between_f(atan2f(q2f + a1 * d2, q1f + a1 * d1), K->b1, K->b2);
-        bool h2 = (a2 >= 0.0f) && (fabsf(z2) <= K->Rz) &&
-                  angle_between_f(atan2f(q2f + a2 * d2, q1f + a2 * d1), K->b1, K->b2);
+        const float sq = sqrtf(disc);
+        const float qq = -(b + copysignf(sq, b));
+        const float tA = qq / a, tB = c / qq;
+        const float a1 = (b < 0.0f) ? tA : tB;     // (-b + sq) / a
+        const float a2 = (b < 0.0f) ? tB : tA;     // (-b - sq) / a
+        bool h1 = (a1 >= 0.0f) && (fabsf(q3 + a1 * d3) <= K->Rz) &&
+                  in_arc(K, q1 + a1 * d1, q2 + a1 * d2);
+        bool h2 = (a2 >= 0.0f) && (fabsf(q3 + a2 * d3) <= K->Rz) &&
+                  in_arc(K, q1 + a2 * d1, q2 + a2 * d2);
         if (h1 && h2) {
             if (a2 < a1) h1 = false;
             else h2 = false;
         }
-        if (h1) {
-            hit = true;
-            t = a1;
-        } else if (h2) {
-            hit = true;
-            t = a2;
-        }
+        hit = h1 || h2;
+        t = h1 ? a1 : a2;
     }
     if (!hit) {
         write_miss_defaults(st, i, 4);
         return false;
     }
-    // one float-float Newton step on |H_perp|^2 = R^2; the correction dt is
-    // ~1e-3 mm, so the projections are updated by dt * d_i in float32
-    ff3 H = ff3_axpy(q, t, d);
-    ff h1 = ff_dot(H, e1), h2 = ff_dot(H, e2);
-    ff g = ff_sub(ff_add(ff_mul(h1, h1), ff_mul(h2, h2)), ff_mul(R, R));
-    float dg = 2.0f * (ff_f(h1) * d1 + ff_f(h2) * d2);
-    float dt = -ff_f(g) / dg;
-    if (isfinite(dt) && dt != 0.0f) {
-        H = ff3_add_f3(H, dt * d);
-        h1 = ff_add_f(h1, dt * d1);
-        h2 = ff_add_f(h2, dt * d2);
-    }
-    float h3 = ff_f(ff_dot(H, ax));
-    // angle: reference k/1024 from the table, then the small residual
-    float phi_a = atan2f(h2.hi, h1.hi);
-    int kk = __float2int_rn(phi_a * 1024.0f);
-    int idx = min(max(kk - K->k0, 0), K->nk - 1);
+    // reference point P_k = c + R u_k on the cylinder at the angle k/1024
+    // nearest the approximate hit; table row: (P_k hi, u.x), (P_k lo, u.y),
+    // (tangent t_k, u.z), P_k global
+    int kk = __float2int_rn(atan2f(q2 + t * d2, q1 + t * d1) * 1024.0f);
+    const int idx = min(max(kk - K->k0, 0), K->nk - 1);
     kk = idx + K->k0;
-    const float* tb = st.table + 4 * idx;
-    ff cr{__ldg(tb), __ldg(tb + 1)}, sr{__ldg(tb + 2), __ldg(tb + 3)};
-    ff cp = ff_add(ff_mul(h1, cr), ff_mul(h2, sr));
-    ff sp = ff_sub(ff_mul(h2, cr), ff_mul(h1, sr));
-    float psi = atan2f(ff_f(sp), ff_f(cp));
-    ff phi = fast_two_sum((float)kk * (1.0f / 1024.0f), psi);
+    const float4* tb = reinterpret_cast<const float4*>(st.table) + 3 * idx;
+    const float4 T0 = __ldg(tb), T1 = __ldg(tb + 1), T2 = __ldg(tb + 2);
+    const ff3 P{ff{T0.x, T1.x}, ff{T0.y, T1.y}, ff{T0.z, T1.z}};
+    const f3 u{T0.w, T1.w, T2.w}, tg{T2.x, T2.y, T2.z};
+    // w = pos + t d - P_k, a few mm: the large parts cancel inside the FMAs
+    f3 ws, we;
+    ff3_rel(ph.pos, P, ws, we);
+    f3 w{fmaf(t, d.x, ws.x) + we.x, fmaf(t, d.y, ws.y) + we.y, fmaf(t, d.z, ws.z) + we.z};
+    float wu = dotf(w, u), wt = dotf(w, tg), wa = dotf(w, ax);
+    // one Newton step along the ray on |R u_k + w_perp|^2 = R^2:
+    // g = wu (2R + wu) + wt^2, g' = 2 ((R + wu) d.u + wt d.t)
+    const float du = dotf(d, u), dtg = dotf(d, tg);
+    const float g = fmaf(wu, 2.0f * R + wu, wt * wt);
+    const float dt = -g / (2.0f * fmaf(R + wu, du, wt * dtg));
+    if (isfinite(dt)) {
+        w = f3{fmaf(dt, d.x, w.x), fmaf(dt, d.y, w.y), fmaf(dt, d.z, w.z)};
+        wu = fmaf(dt, du, wu);
+        wt = fmaf(dt, dtg, wt);
+        wa = fmaf(dt, d3, wa);
+    }
+    // det_phi = k/1024 + atan(wt / (R + wu)); |ratio| < 6e-4, so two terms
+    // of the series (next term r^5/5 < 2e-17)
+    const float r = wt / (R + wu);
+    const float psi = fmaf(-(1.0f / 3.0f) * r * r, r, r);
+    const ff phi = fast_two_sum((float)kk * (1.0f / 1024.0f), psi);
     stored(st.out[0], i, ff2d(phi));
-    storef(st.out[1], i, h3);
-    ff px = ff_add_f(ff_mul(phi, ff{K->rpix_hi, K->rpix_lo}), K->cp0);
+    storef(st.out[1], i, wa);                      // P_k - c is perpendicular to the axis
+    const ff px = ff_add_f(ff_mul(phi, ff{K->rpix_hi, K->rpix_lo}), K->cp0);
     stored(st.out[2], i, ff2d(px));
-    storef(st.out[3], i, h3 * K->inv_pix + K->cp1);
+    storef(st.out[3], i, wa * K->inv_pix + K->cp1);
     if (st.id_out) store_id(st, i, st.id_num);
-    ph.pos = ff3{ff_add(H.x, ff{K->c_hi[0], K->c_lo[0]}), ff_add(H.y, ff{K->c_hi[1], K->c_lo[1]}),
-                 ff_add(H.z, ff{K->c_hi[2], K->c_lo[2]})};
+    ph.pos = ff3{ff_add_f(P.x, w.x), ff_add_f(P.y, w.y), ff_add_f(P.z, w.z)};
     return true;
 }
 
@@ -575,7 +581,9 @@ __device__ __forceinline__ int nearest_facet_grid_l(const mgpu_stage& st, const 
         *need_brute = true;
         return -1;
     }
-    f3 rel = ff3_f(ff3_sub(ph.pos, ldff3(G->o_hi, G->o_lo)));
+    f3 rs, re;
+    ff3_rel(ph.pos, ldff3(G->o_hi, G->o_lo), rs, re);
+    const f3 rel = rs + re;
     f3 n = ldf3(G->n), a = ldf3(G->a), b = ldf3(G->b);
     float dn = dotf(ph.dir, n), da = dotf(ph.dir, a), db = dotf(ph.dir, b);
     if (!(fabsf(da) <= G->slope_max * fabsf(dn)) || !(fabsf(db) <= G->slope_max * fabsf(dn)) ||
@@ -1038,7 +1046,8 @@ cudaError_t mgpu_launch_chain_fp32local(const mgpu_chain& chain, const mgpu_phot
         if (st.kind == MGPU_STAGE_GRATINGS &&
             (st.facets32 == nullptr || st.cand32 == nullptr || ((uintptr_t)st.cand32 & 15u) != 0))
             return cudaErrorInvalidValue;
-        if (st.kind == MGPU_STAGE_CYLDET && st.table == nullptr) return cudaErrorInvalidValue;
+        if (st.kind == MGPU_STAGE_CYLDET && (st.table == nullptr || ((uintptr_t)st.table & 15u) != 0))
+            return cudaErrorInvalidValue;
         if (st.kind == MGPU_STAGE_LENS && st.spline.n_surf > 0 &&
             (st.spline.tx_ff == nullptr || st.spline.ty_ff == nullptr || st.spline.c32 == nullptr))
             return cudaErrorInvalidValue;

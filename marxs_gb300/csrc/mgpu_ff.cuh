@@ -86,6 +86,21 @@ __device__ __forceinline__ ff ff_div(ff a, ff b) {
 }
 __device__ __forceinline__ float ff_f(ff a) { return a.hi + a.lo; }
 
+// a - b as an unnormalised pair s + e: s = a.hi - b.hi rounded, e its exact
+// rounding error (TwoSum) plus the low words; |e| is a few ulp of s, so
+// s + e carries a - b to ~2^-46 relative.  The cheap entry to an element's
+// frame: 8 flops instead of the 20 of ff_sub.
+__device__ __forceinline__ void ff_rel(ff a, ff b, float& s, float& e) {
+    s = a.hi - b.hi;
+    const float bb = s - a.hi;
+    e = ((a.hi - (s - bb)) + (-b.hi - bb)) + (a.lo - b.lo);
+}
+__device__ __forceinline__ void ff3_rel(const ff3& a, const ff3& b, f3& s, f3& e) {
+    ff_rel(a.x, b.x, s.x, e.x);
+    ff_rel(a.y, b.y, s.y, e.y);
+    ff_rel(a.z, b.z, s.z, e.z);
+}
+
 __device__ __forceinline__ ff3 ff3_add_f3(ff3 a, f3 b) {
     return ff3{ff_add_f(a.x, b.x), ff_add_f(a.y, b.y), ff_add_f(a.z, b.z)};
 }
