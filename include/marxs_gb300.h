@@ -162,17 +162,22 @@ typedef struct {
     float p[6];            /* kind parameters as in mgpu_stage.p */
 } mgpu_flat32;
 
-/* FP32-local facet record */
+/* FP32-local facet record: 128 bytes, read by the kernels as eight float4
+ * rows from a 16-byte aligned table:
+ *   (c_hi, hy) (c_lo, hz) (ex, ey.x) (ey.y, ey.z, ez.x, ez.y)
+ *   (ez.z, l) (dneg, wd_hi) (wd_lo, id_num, selector, flags) (pad) */
 typedef struct {
-    float c_hi[3], c_lo[3];
+    float c_hi[3];
+    float hy;
+    float c_lo[3];
+    float hz;
     float ex[3], ey[3], ez[3];
-    float hy, hz;
     float l[3], dneg[3];
     float wd_hi, wd_lo;    /* energy2wave / d as float-float (keV) */
     int32_t id_num;
     int32_t selector;
     int32_t flags;         /* bit 0: CAT sign convention, bit 1: transmission */
-    int32_t pad;
+    int32_t pad[4];
 } mgpu_facet32;
 
 /* FP32-local constants of a grating stage's candidate grid */
@@ -282,11 +287,9 @@ typedef struct {
     mgpu_grid grid;              /* GRATINGS: candidate grid (cell_start NULL = brute force) */
     const void* aux;             /* FP32-local constants: mgpu_flat32 (flat kinds),
                                     mgpu_grid32 (GRATINGS), mgpu_cyl32 (CYLDET) */
-    const mgpu_facet32* facets32;/* GRATINGS, FP32-local */
+    const mgpu_facet32* facets32;/* GRATINGS, FP32-local, 16-byte aligned */
     const float* table;          /* CYLDET, FP32-local: nk x 12 floats, 16-byte aligned
                                     (see mgpu_cyl32) */
-    const float* cand32;         /* GRATINGS, FP32-local: 16 floats per facet, 16-byte aligned:
-                                    (c_hi, hy), (e_x, hz), (e_y, e_z.x), (e_z.y, e_z.z, 0, 0) */
     mgpu_spline1 spline;         /* LENS: reflectivity_interpolator(energy, angle / 4), squared
                                     into the probability (optics/mirror.py:73-79); n_surf 0 = 1 */
     const struct mgpu_catstack* stack; /* GRATINGS: facets are CATL1L2Stacks (NULL: plain) */
@@ -588,7 +591,6 @@ typedef struct {
     const double* groove;       /* device, n_facets x 2: sin(-groove angle), cos(-groove angle) */
     mgpu_facet* facets;         /* device, rewritten in place */
     mgpu_facet32* facets32;     /* optional, device: FP32-local records rewritten */
-    float* cand32;              /* optional, device, 16-B aligned, n_facets x 16 floats */
 } mgpu_pose_update;
 
 int mgpu_facet_poses(const mgpu_pose_update* update, void* stream);

@@ -136,7 +136,7 @@ class MgpuStage(C.Structure):
                 ('draw_stride', C.c_int64),
                 ('facets', C.c_void_p), ('selectors', C.c_void_p), ('n_selectors', C.c_int32),
                 ('pad', C.c_int32), ('grid', MgpuGrid), ('aux', C.c_void_p),
-                ('facets32', C.c_void_p), ('table', C.c_void_p), ('cand32', C.c_void_p),
+                ('facets32', C.c_void_p), ('table', C.c_void_p),
                 ('spline', MgpuSpline1), ('stack', C.c_void_p)]
 
 
@@ -153,11 +153,12 @@ FACET_DTYPE = np.dtype([('c', '<f8', 3), ('ex', '<f8', 3), ('ey', '<f8', 3), ('e
                         ('dgrat', '<f8'), ('id_num', '<i4'), ('selector', '<i4'),
                         ('cat', '<i4'), ('transmission', '<i4')], align=True)
 
-FACET32_DTYPE = np.dtype([('c_hi', '<f4', 3), ('c_lo', '<f4', 3), ('ex', '<f4', 3),
-                          ('ey', '<f4', 3), ('ez', '<f4', 3), ('hy', '<f4'), ('hz', '<f4'),
+FACET32_DTYPE = np.dtype([('c_hi', '<f4', 3), ('hy', '<f4'), ('c_lo', '<f4', 3), ('hz', '<f4'),
+                          ('ex', '<f4', 3), ('ey', '<f4', 3), ('ez', '<f4', 3),
                           ('l', '<f4', 3), ('dneg', '<f4', 3), ('wd_hi', '<f4'), ('wd_lo', '<f4'),
                           ('id_num', '<i4'), ('selector', '<i4'), ('flags', '<i4'),
-                          ('pad', '<i4')], align=True)
+                          ('pad', '<i4', 4)], align=True)
+assert FACET32_DTYPE.itemsize == 128
 
 # name -> (restype, argtypes) of every exported entry point
 class MgpuSource(C.Structure):
@@ -210,8 +211,7 @@ class MgpuPoseUpdate(C.Structure):
     _fields_ = [('n_facets', C.c_int32), ('mode', C.c_int32), ('seed', C.c_uint64),
                 ('sigma', C.c_double * 6), ('offset', C.c_double * 6), ('given', C.c_void_p),
                 ('perturb_out', C.c_void_p), ('outer', C.c_double * 16), ('local', C.c_void_p),
-                ('groove', C.c_void_p), ('facets', C.c_void_p), ('facets32', C.c_void_p),
-                ('cand32', C.c_void_p)]
+                ('groove', C.c_void_p), ('facets', C.c_void_p), ('facets32', C.c_void_p)]
 
 
 SIGNATURES = {

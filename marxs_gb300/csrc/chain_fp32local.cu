@@ -133,9 +133,36 @@ __device__ __forceinline__ HitL flat_hit(const mgpu_flat32* F, const ff3& pos, f
                        pos, dir);
 }
 
+// the plane of an FP32-local facet record, from its first five float4 rows
+struct FacetPlane {
+    ff3 c;
+    f3 n, ey, ez;
+    float hy, hz;
+};
+__device__ __forceinline__ const float4* facet_rows(const mgpu_facet32* fc) {
+    return reinterpret_cast<const float4*>(fc);
+}
+__device__ __forceinline__ ff3 facet_centre(const mgpu_facet32* fc) {
+    const float4 A = __ldg(facet_rows(fc)), B = __ldg(facet_rows(fc) + 1);
+    return ff3{ff{A.x, B.x}, ff{A.y, B.y}, ff{A.z, B.z}};
+}
+__device__ __forceinline__ FacetPlane facet_plane(const mgpu_facet32* fc) {
+    const float4* r = facet_rows(fc);
+    const float4 A = __ldg(r), B = __ldg(r + 1), E = __ldg(r + 2), D = __ldg(r + 3);
+    const float G = __ldg(reinterpret_cast<const float*>(r + 4));
+    FacetPlane P;
+    P.c = ff3{ff{A.x, B.x}, ff{A.y, B.y}, ff{A.z, B.z}};
+    P.hy = A.w;
+    P.hz = B.w;
+    P.n = f3{E.x, E.y, E.z};
+    P.ey = f3{E.w, D.x, D.y};
+    P.ez = f3{D.z, D.w, G};
+    return P;
+}
+
 __device__ __forceinline__ HitL facet_hit(const mgpu_facet32* fc, const ff3& pos, f3 dir) {
-    return plane_hit_l(ldff3(fc->c_hi, fc->c_lo), ldf3(fc->ex), ldf3(fc->ey), ldf3(fc->ez),
-                       fc->hy, fc->hz, pos, dir);
+    const FacetPlane P = facet_plane(fc);
+    return plane_hit_l(P.c, P.n, P.ey, P.ez, P.hy, P.hz, pos, dir);
 }
 
 // parallel_transport (polarization.py:90-170) in float32
@@ -570,6 +597,10 @@ __device__ __forceinline__ int select_order_l(const mgpu_selector& sel, double e
     return sel.orders[k];
 }
 
+// nearest facet through the candidate grid: every candidate gets the full
+// FP32-local plane test (re-centring, float32 solve, one refinement), the
+// nearest hit (smallest k, then lowest index) keeps its local offset, so the
+// winner needs no second test; its global point is c + v.
 __device__ __forceinline__ int nearest_facet_grid_l(const mgpu_stage& st, const PhotonL& ph,
                                                     bool valid, HitL* best_hit, bool* need_brute) {
     const mgpu_grid32* G = (const mgpu_grid32*)st.aux;
@@ -600,34 +631,15 @@ __device__ __forceinline__ int nearest_facet_grid_l(const mgpu_stage& st, const 
     int cell = (int)fu * G->nv + (int)fv;
     const mgpu_grid& g = st.grid;
     int s0 = __ldg(g.cell_start + cell), s1 = min(__ldg(g.cell_start + cell + 1), g.capacity);
-    float best_k = 0.0f;
     for (int q = s0; q < s1; ++q) {
-        int f = __ldg(g.cell_items + q);
-        // plain float32 test on the packed record first (centre without its
-        // low word, <= 2^-25 |c|); the exact float-float test only when the
-        // ray passes within the error band of an edge
-        const float4* cr = reinterpret_cast<const float4*>(st.cand32) + 4 * f;
-        const float4 A = __ldg(cr), B = __ldg(cr + 1), E = __ldg(cr + 2), D = __ldg(cr + 3);
-        f3 r{(ph.pos.x.hi - A.x) + ph.pos.x.lo, (ph.pos.y.hi - A.y) + ph.pos.y.lo,
-             (ph.pos.z.hi - A.z) + ph.pos.z.lo};
-        f3 nx{B.x, B.y, B.z};
-        float kd = dotf(ph.dir, nx);
-        float k = -dotf(r, nx) / kd;
-        f3 v = r + k * ph.dir;
-        float ly = dotf(v, f3{E.x, E.y, E.z}), lz = dotf(v, f3{E.w, D.x, D.y});
-        float tol = 1e-6f * (fabsf(ph.pos.x.hi) + fabsf(ph.pos.y.hi) + fabsf(ph.pos.z.hi) +
-                             fabsf(r.x) + fabsf(r.y) + fabsf(r.z) + fabsf(k)) + 1e-5f;
-        float my = fabsf(ly) - A.w, mz = fabsf(lz) - B.w;
-        if (!(kd != 0.0f) || !(k >= -tol) || !(my <= tol) || !(mz <= tol)) continue;
-        bool hit = true;
-        if (!(k > tol) || !(my < -tol) || !(mz < -tol)) {
-            HitL h = facet_hit(st.facets32 + f, ph.pos, ph.dir);
-            hit = h.hit;
-            k = h.k;
-        }
-        if (hit && (best < 0 || k < best_k || (k == best_k && f < best))) {
+        const int f = __ldg(g.cell_items + q);
+        const HitL h = facet_hit(st.facets32 + f, ph.pos, ph.dir);
+        if (h.hit && (best < 0 || h.k < best_hit->k || (h.k == best_hit->k && f < best))) {
             best = f;
-            best_k = k;
+            best_hit->k = h.k;
+            best_hit->v = h.v;
+            best_hit->ly = h.ly;
+            best_hit->lz = h.lz;
         }
     }
     return best;
@@ -791,17 +803,26 @@ __device__ bool stage_gratings_l(const mgpu_stage& st, PhotonL& ph, int64_t i, b
     unsigned bm = __ballot_sync(MGPU_FULL_MASK, brute);
     if (bm) {
         int bf = brute_force_nearest(st, ph.pos, ph.dir, bm);
-        if (brute) f = bf;
+        if (brute) {
+            f = bf;
+            if (f >= 0) h = facet_hit(st.facets32 + f, ph.pos, ph.dir);
+        }
     }
     if (!valid) return false;
     if (f < 0) {
         write_miss_defaults(st, i, kStack ? MGPU_MAX_OUT : 4);
         return false;
     }
-    h = facet_hit(st.facets32 + f, ph.pos, ph.dir);
-    // FlatGrating.diffract_photons (grating.py:233-266) in the facet frame
+    {
+        const ff3 c = facet_centre(st.facets32 + f);
+        h.ip = ff3{ff_add_f(c.x, h.v.x), ff_add_f(c.y, h.v.y), ff_add_f(c.z, h.v.z)};
+    }
+    // FlatGrating.diffract_photons (grating.py:233-266) in the facet frame;
+    // rows (ex, ey.x), (ez.z, l), (dneg, wd_hi), (wd_lo, id, selector, flags)
     const mgpu_facet32* fc = st.facets32 + f;
-    f3 l = ldf3(fc->l), dn = ldf3(fc->dneg), n = ldf3(fc->ex);
+    const float4* fr = facet_rows(fc);
+    const float4 R2 = __ldg(fr + 2), R4 = __ldg(fr + 4), R5 = __ldg(fr + 5), R6 = __ldg(fr + 6);
+    f3 l{R4.y, R4.z, R4.w}, dn{R5.x, R5.y, R5.z}, n{R2.x, R2.y, R2.z};
     f3 p = normf(ph.dir);
     float p_l = dotf(p, l), p_d = dotf(p, dn), p_n = dotf(p, n);
     float blaze = atan2f(fabsf(p_d), fabsf(p_n));      // = arccos|p_perp . n|
@@ -823,8 +844,8 @@ __device__ bool stage_gratings_l(const mgpu_stage& st, PhotonL& ph, int64_t i, b
         philox_u53(seed, row_base + (uint64_t)i, (uint32_t)sidx, &U, &U1);
     }
     float selprob;
-    const int flags = fc->flags;
-    const mgpu_selector& sel = st.selectors[fc->selector];
+    const int flags = __float_as_int(R6.w);
+    const mgpu_selector& sel = st.selectors[__float_as_int(R6.z)];
     int m;
     if (sel.kind == MGPU_SEL_SPLINE) {
         // float32 evaluation of the interpolated table
@@ -837,7 +858,7 @@ __device__ bool stage_gratings_l(const mgpu_stage& st, PhotonL& ph, int64_t i, b
     if (flags & 1) sign = (p_d > 0.0f) ? 1.0f : ((p_d < 0.0f) ? -1.0f : 1.0f);
     else sign = -1.0f;
     // sign * m * lambda / d in float-float
-    ff term = ff_div(ff{fc->wd_hi, fc->wd_lo}, ph.energy);
+    ff term = ff_div(ff{R5.w, R6.x}, ph.energy);
     term = ff_mul_f(term, sign * (float)m);
     float tf = ff_f(term);
     float pd2 = ff_f(ff_add_f(term, p_d));
@@ -858,7 +879,7 @@ __device__ bool stage_gratings_l(const mgpu_stage& st, PhotonL& ph, int64_t i, b
     stored(st.out[2], i, f2d_bits((float)m));
     if (kStack && st.stack) storef(st.out[3], i, blaze_s);
     else storef(st.out[3], i, blaze);
-    if (st.id_out) store_id(st, i, fc->id_num);
+    if (st.id_out) store_id(st, i, __float_as_int(R6.y));
     if (kStack && st.stack) {
         bool support;
         float u_phi, z;
@@ -1044,7 +1065,7 @@ cudaError_t mgpu_launch_chain_fp32local(const mgpu_chain& chain, const mgpu_phot
         const mgpu_stage& st = chain.stages[s];
         if (st.aux == nullptr && st.kind != MGPU_STAGE_SUPPORT) return cudaErrorInvalidValue;
         if (st.kind == MGPU_STAGE_GRATINGS &&
-            (st.facets32 == nullptr || st.cand32 == nullptr || ((uintptr_t)st.cand32 & 15u) != 0))
+            (st.facets32 == nullptr || ((uintptr_t)st.facets32 & 15u) != 0))
             return cudaErrorInvalidValue;
         if (st.kind == MGPU_STAGE_CYLDET && (st.table == nullptr || ((uintptr_t)st.table & 15u) != 0))
             return cudaErrorInvalidValue;

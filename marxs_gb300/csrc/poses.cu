@@ -10,7 +10,7 @@
 // common rotation and zooms.  The caller passes O = G U and the
 // uncertainty-free local poses (c_i, M_i); this kernel draws or takes
 // (t_i, a_i), composes the pose and rewrites the facet's frame in the
-// float64 table, the FP32-local table and the packed candidate records,
+// float64 table and the FP32-local table,
 // exactly as the host lowering derives them from pos4d (frame of
 // Geometry.__getitem__, math/geometry.py:108-160; groove frame of
 // FlatGrating.e_groove_coos, optics/grating.py:186-207).  The candidate
@@ -105,14 +105,6 @@ pose_kernel(const __grid_constant__ mgpu_pose_update P) {
             for (int k = 0; k < 3; ++k) dst[v][k] = __double2float_rn(src[v][k]);
         g.hy = __double2float_rn(ny);
         g.hz = __double2float_rn(nz);
-        if (P.cand32) {
-            // (c_hi, hy), (e_x, hz), (e_y, e_z.x), (e_z.y, e_z.z, 0, 0)
-            float4* c4 = reinterpret_cast<float4*>(P.cand32) + 4 * (int64_t)i;
-            c4[0] = make_float4(g.c_hi[0], g.c_hi[1], g.c_hi[2], g.hy);
-            c4[1] = make_float4(g.ex[0], g.ex[1], g.ex[2], g.hz);
-            c4[2] = make_float4(g.ey[0], g.ey[1], g.ey[2], g.ez[0]);
-            c4[3] = make_float4(g.ez[1], g.ez[2], 0.0f, 0.0f);
-        }
     }
 }
 
@@ -125,8 +117,7 @@ extern "C" int mgpu_facet_poses(const mgpu_pose_update* p, void* stream) {
     if (p->mode != MGPU_POSE_ZERO && p->mode != MGPU_POSE_DRAW && p->mode != MGPU_POSE_GIVEN)
         return (int)cudaErrorInvalidValue;
     if (p->mode == MGPU_POSE_GIVEN && !p->given) return (int)cudaErrorInvalidValue;
-    if (p->cand32 && (!p->facets32 || ((uintptr_t)p->cand32 & 15u) != 0))
-        return (int)cudaErrorInvalidValue;
+    if (p->facets32 && ((uintptr_t)p->facets32 & 15u) != 0) return (int)cudaErrorInvalidValue;
     const int blocks = (p->n_facets + kThreads - 1) / kThreads;
     pose_kernel<<<blocks, kThreads, 0, (cudaStream_t)stream>>>(*p);
     return (int)cudaGetLastError();

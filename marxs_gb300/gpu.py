@@ -95,7 +95,6 @@ class _Instrument:
         self.stage_grid_bufs = {}     # si -> (cell_start, cell_items)
         self.stage_aux = {}       # FP32-local constant blocks
         self.stage_facets32 = {}
-        self.stage_cand32 = {}
         self.stage_table = {}
         self.fp32_error = None
         lib = _abi.load()
@@ -170,7 +169,6 @@ class _Instrument:
                 elif st.kind == _abi.STAGE_GRATINGS:
                     t32 = L.facets32_table(st.facets)
                     self.stage_facets32[si] = dev_bytes(t32.tobytes())
-                    self.stage_cand32[si] = dev_bytes(L.facets_cand32(t32).tobytes())
                     if st.grid is not None:
                         self.stage_aux[si] = dev_bytes(L.grid32_block(st.grid))
                     else:
@@ -275,7 +273,6 @@ class _Instrument:
             s.aux = self.stage_aux[si].data_ptr()
         if si in self.stage_facets32:
             s.facets32 = self.stage_facets32[si].data_ptr()
-            s.cand32 = self.stage_cand32[si].data_ptr()
         if si in self.stage_table:
             s.table = self.stage_table[si].data_ptr()
         if si in self.stage_spline:

@@ -745,21 +745,6 @@ def facets32_table(facets):
     return out
 
 
-def facets_cand32(table32):
-    """Candidate-test records of the FP32-local facet search: per facet four
-    float4 (c_hi, hy), (e_x, hz), (e_y, e_z.x), (e_z.y, e_z.z, 0, 0)."""
-    t = table32
-    out = np.zeros((len(t), 16), dtype=np.float32)
-    out[:, 0:3] = t['c_hi']
-    out[:, 3] = t['hy']
-    out[:, 4:7] = t['ex']
-    out[:, 7] = t['hz']
-    out[:, 8:11] = t['ey']
-    out[:, 11] = t['ez'][:, 0]
-    out[:, 12:14] = t['ez'][:, 1:3]
-    return out
-
-
 def grid32_block(g):
     b = _abi.MgpuGrid32()
     hi, lo = split_ff(g['o'])

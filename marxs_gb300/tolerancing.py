@@ -151,7 +151,6 @@ class DeviceFacetPoses:
         U.facets = self.inst.stage_facets[self.si].data_ptr()
         if self.si in self.inst.stage_facets32:
             U.facets32 = self.inst.stage_facets32[self.si].data_ptr()
-            U.cand32 = self.inst.stage_cand32[self.si].data_ptr()
         stream = torch.cuda.current_stream(dev)
         lib = _abi.load()
         _abi.check(lib.mgpu_facet_poses(C.byref(U), C.c_void_p(stream.cuda_stream)),

@@ -81,8 +81,6 @@ def test_device_poses_match_reference_tolerancing():
     ref32 = L.facets32_table(tab)
     for k in ('c_hi', 'c_lo', 'ex', 'ey', 'ez', 'l', 'dneg', 'hy', 'hz'):
         assert np.array_equal(t32[k], ref32[k]), k
-    c32 = poses.inst.stage_cand32[poses.si].cpu().numpy().view(np.float32).reshape(-1, 16)
-    assert np.array_equal(c32, L.facets_cand32(ref32))
     poses.reset()
     _check(_table(poses), g['base_pos4d'], groove)
 

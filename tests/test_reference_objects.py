@@ -72,7 +72,7 @@ def lowered(stages):
             rec['fp32'] = _arrays([blk, table])
         elif st.kind == _abi.STAGE_GRATINGS:
             t32 = L.facets32_table(st.facets)
-            rec['fp32'] = _arrays([t32.view(np.uint8), L.facets_cand32(t32)])
+            rec['fp32'] = _arrays(t32.view(np.uint8))
             if st.grid is not None:
                 rec['grid32'] = L.grid32_block(st.grid)
         out.append(rec)
