@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define MGPU_ABI_VERSION 1
+#define MGPU_ABI_VERSION 2
 #define MGPU_MAX_STAGES 16
 #define MGPU_MAX_OUT 10
 #define MGPU_MAX_DRAWS 6
@@ -283,16 +283,21 @@ typedef struct {
     const mgpu_facet* facets;    /* GRATINGS */
     const mgpu_selector* selectors;
     int32_t n_selectors;
-    int32_t pad;
+    int32_t facet_sel0;          /* GRATINGS: 1 when every facet uses selectors[0] */
     mgpu_grid grid;              /* GRATINGS: candidate grid (cell_start NULL = brute force) */
-    const void* aux;             /* FP32-local constants: mgpu_flat32 (flat kinds),
-                                    mgpu_grid32 (GRATINGS), mgpu_cyl32 (CYLDET) */
+    int32_t aux_size;            /* bytes of aux32 in use (0: none) */
+    int32_t pad2;
+    uint8_t aux32[128];          /* FP32-local constants inline, so the kernel reads them from
+                                    its parameter bank: mgpu_flat32 (flat kinds), mgpu_grid32
+                                    (GRATINGS), mgpu_cyl32 (CYLDET) */
     const mgpu_facet32* facets32;/* GRATINGS, FP32-local, 16-byte aligned */
     const float* table;          /* CYLDET, FP32-local: nk x 12 floats, 16-byte aligned
                                     (see mgpu_cyl32) */
     mgpu_spline1 spline;         /* LENS: reflectivity_interpolator(energy, angle / 4), squared
                                     into the probability (optics/mirror.py:73-79); n_surf 0 = 1 */
     const struct mgpu_catstack* stack; /* GRATINGS: facets are CATL1L2Stacks (NULL: plain) */
+    mgpu_selector sel0;          /* GRATINGS: a copy of selectors[0]; with facet_sel0 the
+                                    FP32-local kernel reads it from its parameter bank */
 } mgpu_stage;
 /* p[] per kind:
  *   LENS:    p[0] focal length, p[1] d_center_optical_axis

@@ -13,7 +13,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, 'libmarxs_gb300.so')
 
-MGPU_ABI_VERSION = 1
+MGPU_ABI_VERSION = 2
 MAX_STAGES = 16
 MAX_OUT = 10
 MAX_DRAWS = 6
@@ -135,9 +135,10 @@ class MgpuStage(C.Structure):
                 ('id_stride', C.c_int64), ('draw', C.c_void_p * MAX_DRAWS),
                 ('draw_stride', C.c_int64),
                 ('facets', C.c_void_p), ('selectors', C.c_void_p), ('n_selectors', C.c_int32),
-                ('pad', C.c_int32), ('grid', MgpuGrid), ('aux', C.c_void_p),
+                ('facet_sel0', C.c_int32), ('grid', MgpuGrid), ('aux_size', C.c_int32),
+                ('pad2', C.c_int32), ('aux32', C.c_uint8 * 128),
                 ('facets32', C.c_void_p), ('table', C.c_void_p),
-                ('spline', MgpuSpline1), ('stack', C.c_void_p)]
+                ('spline', MgpuSpline1), ('stack', C.c_void_p), ('sel0', MgpuSelector)]
 
 
 class MgpuChain(C.Structure):

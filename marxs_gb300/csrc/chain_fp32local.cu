@@ -36,12 +36,17 @@
 namespace {
 
 // block size and the minimum resident blocks per SM the register
-// allocation is bounded for (compile-time; see the launch below)
+// allocation is bounded for (compile-time; see the launch below): 4 blocks
+// of 256 (64 registers) for the fixed plain chains, 3 (80 registers) for
+// the generic and the CAT-stack chains, which spill at 64
 #ifndef MGPU_FP32L_THREADS
 #define MGPU_FP32L_THREADS 256
 #endif
 #ifndef MGPU_FP32L_MIN_BLOCKS
-#define MGPU_FP32L_MIN_BLOCKS 3
+#define MGPU_FP32L_MIN_BLOCKS 4
+#endif
+#ifndef MGPU_FP32L_MIN_BLOCKS_WIDE
+#define MGPU_FP32L_MIN_BLOCKS_WIDE 3
 #endif
 // grid cap in blocks of 256 threads per SM (0: one block per 256 photons)
 #ifndef MGPU_FP32L_GRID_PER_SM
@@ -49,6 +54,7 @@ namespace {
 #endif
 constexpr int kThreads = MGPU_FP32L_THREADS;
 constexpr int kMinBlocks = MGPU_FP32L_MIN_BLOCKS;
+constexpr int kMinBlocksWide = MGPU_FP32L_MIN_BLOCKS_WIDE;
 constexpr int kGridPerSm = MGPU_FP32L_GRID_PER_SM;
 
 struct PhotonL {
@@ -334,7 +340,7 @@ __device__ __forceinline__ int select_order_spline_f(const mgpu_selector& sel, f
 // ------------------------------------------------------------------ stages
 __device__ bool stage_lens_l(const mgpu_stage& st, PhotonL& ph, int64_t i, uint32_t* status) {
     // PerfectLens.specific_process_photons, optics/mirror.py:53-82
-    const mgpu_flat32* F = (const mgpu_flat32*)st.aux;
+    const mgpu_flat32* F = reinterpret_cast<const mgpu_flat32*>(st.aux32);
     HitL h = flat_hit(F, ph.pos, ph.dir);
     if (!h.hit) {
         write_miss_defaults(st, i, 2);
@@ -366,7 +372,7 @@ __device__ bool stage_lens_l(const mgpu_stage& st, PhotonL& ph, int64_t i, uint3
 __device__ bool stage_scatter_l(const mgpu_stage& st, PhotonL& ph, int64_t i, int rng,
                                 uint64_t seed, uint64_t row_base, int sidx, uint32_t* status) {
     // RadialMirrorScatter.specific_process_photons, optics/scatter.py:49-77
-    const mgpu_flat32* F = (const mgpu_flat32*)st.aux;
+    const mgpu_flat32* F = reinterpret_cast<const mgpu_flat32*>(st.aux32);
     HitL h = flat_hit(F, ph.pos, ph.dir);
     if (!h.hit) {
         write_miss_defaults(st, i, 4);
@@ -421,7 +427,7 @@ __device__ bool stage_scatter_l(const mgpu_stage& st, PhotonL& ph, int64_t i, in
 
 __device__ bool stage_flatdet_l(const mgpu_stage& st, PhotonL& ph, int64_t i) {
     // FlatDetector.specific_process_photons, optics/detector.py:72-75
-    const mgpu_flat32* F = (const mgpu_flat32*)st.aux;
+    const mgpu_flat32* F = reinterpret_cast<const mgpu_flat32*>(st.aux32);
     HitL h = flat_hit(F, ph.pos, ph.dir);
     if (!h.hit) {
         write_miss_defaults(st, i, 4);
@@ -450,7 +456,7 @@ __device__ __forceinline__ bool in_arc(const mgpu_cyl32* K, float x, float y) {
 __device__ bool stage_cyldet_l(const mgpu_stage& st, PhotonL& ph, int64_t i) {
     // Cylinder.intersect (math/geometry.py:470-564) + CircularDetector
     // (optics/detector.py:115-118) for a circular tube
-    const mgpu_cyl32* K = (const mgpu_cyl32*)st.aux;
+    const mgpu_cyl32* K = reinterpret_cast<const mgpu_cyl32*>(st.aux32);
     const f3 e1 = ldf3(K->e1), e2 = ldf3(K->e2), ax = ldf3(K->a);
     const float R = K->R;
     // approximate root in float32 from q = pos - c (error ~1e-3 mm from the
@@ -603,7 +609,7 @@ __device__ __forceinline__ int select_order_l(const mgpu_selector& sel, double e
 // winner needs no second test; its global point is c + v.
 __device__ __forceinline__ int nearest_facet_grid_l(const mgpu_stage& st, const PhotonL& ph,
                                                     bool valid, HitL* best_hit, bool* need_brute) {
-    const mgpu_grid32* G = (const mgpu_grid32*)st.aux;
+    const mgpu_grid32* G = reinterpret_cast<const mgpu_grid32*>(st.aux32);
     *need_brute = false;
     int best = -1;
     best_hit->k = 0.0f;
@@ -792,8 +798,10 @@ __device__ __forceinline__ void cat_stack_layers_l(const mgpu_stage& st, const m
 }
 
 // kStack: compiled with the CATL1L2Stack layers (launches whose chain has a
-// stacked facet stage); plain facet chains leave them out entirely
-template <bool kStack>
+// stacked facet stage); plain facet chains leave them out entirely.
+// kSel0: every facet uses the stage's first selector, read from the inline
+// copy in the parameter bank
+template <bool kStack, bool kSel0>
 __device__ bool stage_gratings_l(const mgpu_stage& st, PhotonL& ph, int64_t i, bool valid,
                                  int rng, uint64_t seed, uint64_t row_base, int sidx,
                                  uint32_t* status) {
@@ -845,7 +853,7 @@ __device__ bool stage_gratings_l(const mgpu_stage& st, PhotonL& ph, int64_t i, b
     }
     float selprob;
     const int flags = __float_as_int(R6.w);
-    const mgpu_selector& sel = st.selectors[__float_as_int(R6.z)];
+    const mgpu_selector& sel = kSel0 ? st.sel0 : st.selectors[__float_as_int(R6.z)];
     int m;
     if (sel.kind == MGPU_SEL_SPLINE) {
         // float32 evaluation of the interpolated table
@@ -914,13 +922,13 @@ __device__ bool stage_gratings_l(const mgpu_stage& st, PhotonL& ph, int64_t i, b
 
 // one stage, kind known at compile time (KIND > 0) or read from the
 // descriptor (KIND == 0, generic chains)
-template <int KIND, bool kStack>
+template <int KIND, bool kStack, bool kSel0>
 __device__ __forceinline__ bool run_stage_l(const mgpu_stage& st, PhotonL& ph, int64_t i,
                                             bool valid, const mgpu_chain& chain, int s) {
     const int kind = KIND ? KIND : st.kind;
     switch (kind) {
     case MGPU_STAGE_GRATINGS:
-        return stage_gratings_l<kStack>(st, ph, i, valid, chain.rng, chain.seed, chain.row_base,
+        return stage_gratings_l<kStack, kSel0>(st, ph, i, valid, chain.rng, chain.seed, chain.row_base,
                                         s, chain.status);
     case MGPU_STAGE_LENS:
         return valid && stage_lens_l(st, ph, i, chain.status);
@@ -955,11 +963,12 @@ __device__ __forceinline__ void count_hits(bool hit, unsigned* s_hits, int s, in
 
 // generic chain: stage loop over the descriptors
 struct GenericChain {
+    static constexpr bool kFixed = false;
     template <bool kStack>
     __device__ static void run(const mgpu_chain& chain, PhotonL& ph, int64_t i, bool valid,
                                unsigned* s_hits, int lane) {
         for (int s = 0; s < chain.n_stages; ++s)
-            count_hits(run_stage_l<0, kStack>(chain.stages[s], ph, i, valid, chain, s), s_hits, s,
+            count_hits(run_stage_l<0, kStack, false>(chain.stages[s], ph, i, valid, chain, s), s_hits, s,
                        lane);
     }
 };
@@ -968,10 +977,11 @@ struct GenericChain {
 // the per-stage constants are read straight from the parameter bank
 template <int... K>
 struct FixedChain {
+    static constexpr bool kFixed = true;
     template <int KIND, int S, bool kStack>
     __device__ static void step(const mgpu_chain& chain, PhotonL& ph, int64_t i, bool valid,
                                 unsigned* s_hits, int lane) {
-        count_hits(run_stage_l<KIND, kStack>(chain.stages[S], ph, i, valid, chain, S), s_hits, S,
+        count_hits(run_stage_l<KIND, kStack, true>(chain.stages[S], ph, i, valid, chain, S), s_hits, S,
                    lane);
     }
     template <bool kStack, int... S>
@@ -985,20 +995,26 @@ struct FixedChain {
         run_seq<kStack>(chain, ph, i, valid, s_hits, lane,
                         std::make_integer_sequence<int, sizeof...(K)>{});
     }
+    // the stage kinds match, and every facet stage reads its first selector
     static bool matches(const mgpu_chain& chain) {
         const int kinds[] = {K...};
         if (chain.n_stages != (int)sizeof...(K)) return false;
-        for (int s = 0; s < chain.n_stages; ++s)
+        for (int s = 0; s < chain.n_stages; ++s) {
             if (chain.stages[s].kind != kinds[s]) return false;
+            if (kinds[s] == MGPU_STAGE_GRATINGS && !chain.stages[s].facet_sel0) return false;
+        }
         return true;
     }
 };
 
 template <class Chain, bool kStack>
-// 3 blocks of 256 per SM (<= 84 registers): measured 4 % faster than the
-// unconstrained allocation (100 registers, 2 blocks) and 5-15 % faster than
-// 128 x 6/7/8 or 256 x 4 (register spills)
-__global__ void __launch_bounds__(kThreads, kMinBlocks)
+// fixed plain chains: 4 blocks of 256 per SM (64 registers, no spills; the
+// stage constants come from the parameter bank), measured 6 % faster than
+// 3 blocks (80 registers) on the CAT chain at 1e8 photons; the others keep
+// 3 blocks (at 64 registers they spill), which measured 4 % faster than
+// the unconstrained allocation (100 registers, 2 blocks); 128-thread
+// blocks and a capped (persistent) grid measured no faster
+__global__ void __launch_bounds__(kThreads, (Chain::kFixed && !kStack) ? kMinBlocks : kMinBlocksWide)
 chain_fp32local_kernel(const __grid_constant__ mgpu_chain chain, const __grid_constant__ mgpu_photons io) {
     __shared__ unsigned int s_hits[MGPU_MAX_STAGES];
     if (threadIdx.x < MGPU_MAX_STAGES) s_hits[threadIdx.x] = 0;
@@ -1063,7 +1079,7 @@ cudaError_t mgpu_launch_chain_fp32local(const mgpu_chain& chain, const mgpu_phot
     if (io.n <= 0) return cudaSuccess;
     for (int s = 0; s < chain.n_stages; ++s) {
         const mgpu_stage& st = chain.stages[s];
-        if (st.aux == nullptr && st.kind != MGPU_STAGE_SUPPORT) return cudaErrorInvalidValue;
+        if (st.aux_size <= 0 && st.kind != MGPU_STAGE_SUPPORT) return cudaErrorInvalidValue;
         if (st.kind == MGPU_STAGE_GRATINGS &&
             (st.facets32 == nullptr || ((uintptr_t)st.facets32 & 15u) != 0))
             return cudaErrorInvalidValue;

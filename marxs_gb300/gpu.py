@@ -93,7 +93,8 @@ class _Instrument:
         self.stage_selectors = {}
         self.stage_grid = {}
         self.stage_grid_bufs = {}     # si -> (cell_start, cell_items)
-        self.stage_aux = {}       # FP32-local constant blocks
+        self.stage_aux = {}       # FP32-local constant blocks (bytes, inline in the stage)
+        self.stage_sel0 = {}      # first selector of a facet stage (inline copy)
         self.stage_facets32 = {}
         self.stage_table = {}
         self.fp32_error = None
@@ -161,18 +162,18 @@ class _Instrument:
                 self.stage_stack[si] = dev_bytes(bytes(cs))
             try:
                 if st.kind in (_abi.STAGE_LENS, _abi.STAGE_SCATTER, _abi.STAGE_FLATDET):
-                    self.stage_aux[si] = dev_bytes(L.flat32_block(st))
+                    self.stage_aux[si] = L.flat32_block(st)
                 elif st.kind == _abi.STAGE_CYLDET:
                     blk, table = L.cyl32_block(st)
-                    self.stage_aux[si] = dev_bytes(blk)
+                    self.stage_aux[si] = blk
                     self.stage_table[si] = dev_bytes(table.tobytes())
                 elif st.kind == _abi.STAGE_GRATINGS:
                     t32 = L.facets32_table(st.facets)
                     self.stage_facets32[si] = dev_bytes(t32.tobytes())
                     if st.grid is not None:
-                        self.stage_aux[si] = dev_bytes(L.grid32_block(st.grid))
+                        self.stage_aux[si] = L.grid32_block(st.grid)
                     else:
-                        self.stage_aux[si] = dev_bytes(bytes(_abi.MgpuGrid32()))
+                        self.stage_aux[si] = bytes(_abi.MgpuGrid32())
             except NotImplementedError as exc:
                 self.fp32_error = str(exc)
             if st.kind != _abi.STAGE_GRATINGS:
@@ -206,6 +207,8 @@ class _Instrument:
                     self.keep.append(mid)
                     sel_structs[k].e_mid = mid.data_ptr()
                     sel_structs[k].e0_f, sel_structs[k].e_scale_f = rows[1], rows[2]
+            if len(st.selectors):
+                self.stage_sel0[si] = sel_structs[0]
             raw = np.frombuffer(bytes(sel_structs), dtype=np.uint8).copy()
             sel_dev = torch.from_numpy(raw).to(device)
             self.keep.append(sel_dev)
@@ -242,9 +245,7 @@ class _Instrument:
         self.stage_grid[si] = grid
         self.stage_grid_bufs[si] = (start, items)
         if si in self.stage_facets32:
-            aux = torch.from_numpy(np.frombuffer(L.grid32_block(g), dtype=np.uint8).copy()).to(dev)
-            self.keep.append(aux)
-            self.stage_aux[si] = aux
+            self.stage_aux[si] = L.grid32_block(g)
         fac = self.stage_facets[si]
         n = len(self.stages[si].facets)
 
@@ -267,10 +268,17 @@ class _Instrument:
             s.facets = self.stage_facets[si].data_ptr()
             s.selectors = self.stage_selectors[si].data_ptr()
             s.n_selectors = len(st.selectors)
+            s.facet_sel0 = int(len(st.selectors) > 0 and int(np.max(st.facets['selector'])) <= 0)
             if si in self.stage_grid:
                 s.grid = self.stage_grid[si]
         if si in self.stage_aux:
-            s.aux = self.stage_aux[si].data_ptr()
+            blk = self.stage_aux[si]
+            if len(blk) > len(s.aux32):
+                raise RuntimeError('FP32-local constant block of %d bytes' % len(blk))
+            C.memmove(C.addressof(s.aux32), blk, len(blk))
+            s.aux_size = len(blk)
+        if si in self.stage_sel0:
+            s.sel0 = self.stage_sel0[si]
         if si in self.stage_facets32:
             s.facets32 = self.stage_facets32[si].data_ptr()
         if si in self.stage_table:
