@@ -66,6 +66,12 @@ extern "C" {
 #define MGPU_STAGE_SUPPORT  6  /* catsupportbars, missions/mitsnl/catgrating.py:314-324:
                                   probability = 0 where the id column at id_out (the facet
                                   column) is < 0, or for every photon when id_out is NULL */
+#define MGPU_STAGE_DETARRAY 7  /* Parallel of FlatDetectors (a CCD array), simulator.py:206-441
+                                  over optics/detector.py:18-75: the nearest element the ray
+                                  crosses, found like the facets of GRATINGS (facets, grid,
+                                  facets32); per element the pixel size in mgpu_facet.dgrat and
+                                  the centre pixel in l[0], l[1] (FP32-local: mgpu_facet32.l =
+                                  1 / pixel size, centre x, centre y) */
 
 /* a float64 photon column: value of photon i at ptr[i * stride] */
 typedef struct {
@@ -289,7 +295,7 @@ typedef struct {
     int32_t pad2;
     uint8_t aux32[128];          /* FP32-local constants inline, so the kernel reads them from
                                     its parameter bank: mgpu_flat32 (flat kinds), mgpu_grid32
-                                    (GRATINGS), mgpu_cyl32 (CYLDET) */
+                                    (GRATINGS, DETARRAY), mgpu_cyl32 (CYLDET) */
     const mgpu_facet32* facets32;/* GRATINGS, FP32-local, 16-byte aligned */
     const float* table;          /* CYLDET, FP32-local: nk x 12 floats, 16-byte aligned
                                     (see mgpu_cyl32) */
@@ -308,6 +314,7 @@ typedef struct {
  *   SCATTER:  loc0, loc1, inplanescatter, perpplanescatter
  *   FLATDET:  loc0 (det_x), loc1 (det_y), detpix_x, detpix_y
  *   GRATINGS: loc0 (grat_y), loc1 (grat_z), order, blaze   (+ id_out: facet)
+ *   DETARRAY: loc0 (det_x), loc1 (det_y), detpix_x, detpix_y (+ id_out: e.g. CCD_ID)
  *   CYLDET:   loc0 (det_phi), loc1 (det_y), detpix_x, detpix_y
  */
 

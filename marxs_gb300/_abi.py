@@ -51,6 +51,9 @@ STAGE_FLATDET = 3
 STAGE_GRATINGS = 4
 STAGE_CYLDET = 5
 STAGE_SUPPORT = 6
+STAGE_DETARRAY = 7
+# stages that search a table of plane elements through a candidate grid
+FACET_STAGES = (4, 7)
 
 
 class MgpuCol(C.Structure):

@@ -18,6 +18,15 @@ travel from large x towards the focus at the origin.
   blaze 1.8 deg (rotation about the groove axis), N(0, 30") pose jitter
   about three axes; energies from a piecewise-linear spectrum on 200 knots
   in [0.2, 2] keV; CircularDetector (R=5900) on the Rowland circle.
+* ``C7`` CCD array: the reference's own Parallel test layout
+  (simulator/tests/test_parallel.py:11-23), four 10x10 mm FlatDetectors
+  (0.01 mm pixels, 0.2 mm gaps) in one Parallel with id column CCD_ID,
+  photons spread over the four chips, the gaps and beyond.
+* ``C8`` CAT array + CCD strip: C2 with the CircularDetector replaced by
+  16 FlatDetectors of 24.576 mm (0.024 mm pixels, 2.4 mm gaps) tangent to
+  the Rowland circle, chip 7 on the focus, placed by ParallelCalculated
+  (normals from the circle centre, one side parallel to the circle's axis),
+  id column CCD.
 
 The builders take a namespace of element classes so the same instrument
 can be assembled from this package's classes or from MARXS itself.
@@ -42,7 +51,7 @@ def native_namespace():
         InterpolateEfficiencyTable=optics.InterpolateEfficiencyTable.from_grid,
         CATL1L2Stack=optics.CATL1L2Stack, catsupportbars=optics.catsupportbars,
         Cylinder=optics.Cylinder, Parallel=simulator.Parallel, Sequence=simulator.Sequence,
-        angle=lambda rad: rad)
+        ParallelCalculated=simulator.ParallelCalculated, angle=lambda rad: rad)
 
 
 # ---------------------------------------------------------------------------
@@ -304,8 +313,59 @@ def build_c2(ns, seed=2, efficiency_file=None, n_facets=1000, interpolated=False
                            aperture_x=12000.)
 
 
+def ccd_test_photons(n, seed):
+    """Rays towards the C7 chips (the x = 0 plane): starts at x = 100 with
+    (y, z) uniform in [-16, 6] mm (chips, gaps and the surroundings),
+    directions (-1, N(0, 0.01), N(0, 0.01)) normalised, energies U(0.3, 2)
+    keV, random linear polarization, probability 1."""
+    rng = np.random.default_rng(seed + 300)
+    pos = np.zeros((n, 4))
+    pos[:, 0] = 100.
+    pos[:, 1:3] = rng.uniform(-16., 6., size=(n, 2))
+    pos[:, 3] = 1.
+    d = np.column_stack([-np.ones(n), rng.normal(0, 0.01, n), rng.normal(0, 0.01, n)])
+    d /= np.sqrt(np.sum(d * d, axis=1))[:, None]
+    dirs = geomath.e2h(d, 0)
+    pol = geomath.polarization_vectors(dirs, rng.uniform(0, np.pi, n))
+    return {'pos': pos, 'dir': dirs, 'energy': rng.uniform(0.3, 2.0, n),
+            'polarization': pol, 'probability': np.ones(n)}
+
+
+def build_c7(ns):
+    pos = [[0, -10.1, -10.1], [0, .1, -10.1], [0, -10.1, .1], [0, .1, .1]]
+    det = ns.Parallel(elem_class=ns.FlatDetector, elem_args={'pixsize': 0.01, 'zoom': 5},
+                      elem_pos={'position': pos}, id_col='CCD_ID')
+    return SimpleNamespace(elements=[det], detector=det, draw_slots=[])
+
+
+def rowland_ccd_centres(cyl_pos4d, n_ccd=16, pitch=27.0):
+    """Centres (homogeneous) of n_ccd chips at ``pitch`` mm of arc along the
+    circle of a Rowland cylinder, chip n_ccd / 2 - 1 centred on the focus
+    (the origin), and the circle's centre and axis."""
+    T, R, Z, _ = geomath.decompose44(cyl_pos4d)
+    r = Z[0]
+    phi_f = math.atan2(np.dot(-T, R[:, 1]), np.dot(-T, R[:, 0]))
+    phis = phi_f + (np.arange(n_ccd) - n_ccd // 2 + 1) * (pitch / r)      # chip 7 on the focus
+    cen = T + r * (np.cos(phis)[:, None] * R[:, 0] + np.sin(phis)[:, None] * R[:, 1])
+    return geomath.e2h(cen, 1), T, R[:, 2]
+
+
+def build_c8(ns, seed=8):
+    inst = build_c2(ns, seed=seed)
+    xyzw, centre, axis = rowland_ccd_centres(inst.detector.geometry.pos4d)
+    ccds = ns.ParallelCalculated(pos_spec=xyzw, normal_spec=geomath.e2h(centre, 1),
+                                 parallel_spec=geomath.e2h(axis, 0), elem_class=ns.FlatDetector,
+                                 elem_args={'pixsize': 0.024, 'zoom': [1, 12.288, 12.288]},
+                                 id_col='CCD')
+    return SimpleNamespace(elements=[inst.lens, inst.scatter, inst.gas, ccds], lens=inst.lens,
+                           scatter=inst.scatter, gas=inst.gas, detector=ccds,
+                           selector=inst.selector, draw_slots=inst.draw_slots)
+
+
 def photons_for(config_name, n, seed):
-    if config_name in ('c2', 'c5', 'c6'):
+    if config_name == 'c7':
+        return ccd_test_photons(n, seed)
+    if config_name in ('c2', 'c5', 'c6', 'c8'):
         e = piecewise_linear_energies(n, seed)
         return annulus_photons(n, seed, 12000., energies=e)
     return annulus_photons(n, seed, 10000.)
@@ -323,4 +383,8 @@ def build(config_name, ns=None, seed=None):
         return build_c2(ns, seed=5 if seed is None else seed, interpolated=True)
     if config_name == 'c6':
         return build_c2(ns, seed=6 if seed is None else seed, interpolated=True, cat_stack=True)
+    if config_name == 'c7':
+        return build_c7(ns)
+    if config_name == 'c8':
+        return build_c8(ns, seed=8 if seed is None else seed)
     raise ValueError(config_name)

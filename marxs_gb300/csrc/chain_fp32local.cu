@@ -920,6 +920,38 @@ __device__ bool stage_gratings_l(const mgpu_stage& st, PhotonL& ph, int64_t i, b
     return true;
 }
 
+// Parallel of FlatDetectors (a CCD array): FlatDetector.specific_process_photons
+// (optics/detector.py:72-75) on the nearest element the ray crosses; record
+// row (ez.z, l) holds 1 / pixel size and the centre pixel
+__device__ bool stage_detarray_l(const mgpu_stage& st, PhotonL& ph, int64_t i, bool valid) {
+    HitL h;
+    bool brute;
+    int f = nearest_facet_grid_l(st, ph, valid, &h, &brute);
+    const unsigned bm = __ballot_sync(MGPU_FULL_MASK, brute);
+    if (bm) {
+        const int bf = brute_force_nearest(st, ph.pos, ph.dir, bm);
+        if (brute) {
+            f = bf;
+            if (f >= 0) h = facet_hit(st.facets32 + f, ph.pos, ph.dir);
+        }
+    }
+    if (!valid) return false;
+    if (f < 0) {
+        write_miss_defaults(st, i, 4);
+        return false;
+    }
+    const mgpu_facet32* fc = st.facets32 + f;
+    const ff3 c = facet_centre(fc);
+    const float4 R4 = __ldg(facet_rows(fc) + 4), R6 = __ldg(facet_rows(fc) + 6);
+    storef(st.out[0], i, h.ly);
+    storef(st.out[1], i, h.lz);
+    storef(st.out[2], i, fmaf(h.ly, R4.y, R4.z));
+    storef(st.out[3], i, fmaf(h.lz, R4.y, R4.w));
+    if (st.id_out) store_id(st, i, __float_as_int(R6.y));
+    ph.pos = ff3{ff_add_f(c.x, h.v.x), ff_add_f(c.y, h.v.y), ff_add_f(c.z, h.v.z)};
+    return true;
+}
+
 // one stage, kind known at compile time (KIND > 0) or read from the
 // descriptor (KIND == 0, generic chains)
 template <int KIND, bool kStack, bool kSel0>
@@ -930,6 +962,8 @@ __device__ __forceinline__ bool run_stage_l(const mgpu_stage& st, PhotonL& ph, i
     case MGPU_STAGE_GRATINGS:
         return stage_gratings_l<kStack, kSel0>(st, ph, i, valid, chain.rng, chain.seed, chain.row_base,
                                         s, chain.status);
+    case MGPU_STAGE_DETARRAY:
+        return stage_detarray_l(st, ph, i, valid);
     case MGPU_STAGE_LENS:
         return valid && stage_lens_l(st, ph, i, chain.status);
     case MGPU_STAGE_SCATTER:
@@ -1080,7 +1114,7 @@ cudaError_t mgpu_launch_chain_fp32local(const mgpu_chain& chain, const mgpu_phot
     for (int s = 0; s < chain.n_stages; ++s) {
         const mgpu_stage& st = chain.stages[s];
         if (st.aux_size <= 0 && st.kind != MGPU_STAGE_SUPPORT) return cudaErrorInvalidValue;
-        if (st.kind == MGPU_STAGE_GRATINGS &&
+        if ((st.kind == MGPU_STAGE_GRATINGS || st.kind == MGPU_STAGE_DETARRAY) &&
             (st.facets32 == nullptr || ((uintptr_t)st.facets32 & 15u) != 0))
             return cudaErrorInvalidValue;
         if (st.kind == MGPU_STAGE_CYLDET && (st.table == nullptr || ((uintptr_t)st.table & 15u) != 0))

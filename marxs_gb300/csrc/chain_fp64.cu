@@ -307,9 +307,12 @@ __device__ __noinline__ void cat_stack_layers(const mgpu_stage& st, const mgpu_c
     store_col(st.out[5], i, h.lz);
 }
 
-__device__ bool stage_gratings(const mgpu_stage& st, Photon& ph, int64_t i, bool valid,
-                               int rng, uint64_t seed, uint64_t row_base, int sidx,
-                               uint32_t* status) {
+// nearest element of a facet stage (gratings or detectors) the ray crosses:
+// the candidate grid, and for photons the grid cannot bound a whole-warp scan
+// of all facets with a warp min-reduction on (k, index).  Every lane of the
+// warp must call it (the scan is warp-cooperative).
+__device__ __forceinline__ int nearest_facet(const mgpu_stage& st, const Photon& ph, bool valid,
+                                             PlaneHit* hit) {
     PlaneHit h;
     bool brute;
     int f = nearest_facet_grid(st, ph, valid, &h, &brute);
@@ -348,6 +351,37 @@ __device__ bool stage_gratings(const mgpu_stage& st, Photon& ph, int64_t i, bool
             h = facet_intersect(st.facets + bf, ph.pos, ph.dir);
         }
     }
+    *hit = h;
+    return f;
+}
+
+// Parallel of FlatDetectors (a CCD array): FlatDetector.specific_process_photons
+// (optics/detector.py:72-75) on the nearest element the ray crosses; per
+// element pixel size (dgrat) and centre pixel (l[0], l[1])
+__device__ bool stage_detarray(const mgpu_stage& st, Photon& ph, int64_t i, bool valid) {
+    PlaneHit h;
+    const int f = nearest_facet(st, ph, valid, &h);
+    if (!valid) return false;
+    if (f < 0) {
+        write_miss_defaults(st, i, 4);
+        return false;
+    }
+    const mgpu_facet* fc = st.facets + f;
+    const double pix = __ldg(&fc->dgrat);
+    store_col(st.out[0], i, h.ly);
+    store_col(st.out[1], i, h.lz);
+    store_col(st.out[2], i, h.ly / pix + __ldg(&fc->l[0]));
+    store_col(st.out[3], i, h.lz / pix + __ldg(&fc->l[1]));
+    if (st.id_out) store_id(st, i, __ldg(&fc->id_num));
+    ph.pos = h.ip;
+    return true;
+}
+
+__device__ bool stage_gratings(const mgpu_stage& st, Photon& ph, int64_t i, bool valid,
+                               int rng, uint64_t seed, uint64_t row_base, int sidx,
+                               uint32_t* status) {
+    PlaneHit h;
+    const int f = nearest_facet(st, ph, valid, &h);
     if (!valid) return false;
     if (f < 0) {
         write_miss_defaults(st, i, MGPU_MAX_OUT);
@@ -464,6 +498,9 @@ chain_fp64_kernel(const __grid_constant__ mgpu_chain chain, const __grid_constan
             case MGPU_STAGE_GRATINGS:
                 hit = stage_gratings(st, ph, i, valid, chain.rng, chain.seed, chain.row_base, s,
                                      chain.status);
+                break;
+            case MGPU_STAGE_DETARRAY:
+                hit = stage_detarray(st, ph, i, valid);
                 break;
             case MGPU_STAGE_LENS:
                 if (valid) hit = stage_lens(st, ph, i, chain.status);

@@ -167,8 +167,8 @@ class _Instrument:
                     blk, table = L.cyl32_block(st)
                     self.stage_aux[si] = blk
                     self.stage_table[si] = dev_bytes(table.tobytes())
-                elif st.kind == _abi.STAGE_GRATINGS:
-                    t32 = L.facets32_table(st.facets)
+                elif st.kind in _abi.FACET_STAGES:
+                    t32 = L.facets32_table(st.facets, detectors=st.kind == _abi.STAGE_DETARRAY)
                     self.stage_facets32[si] = dev_bytes(t32.tobytes())
                     if st.grid is not None:
                         self.stage_aux[si] = L.grid32_block(st.grid)
@@ -176,7 +176,7 @@ class _Instrument:
                         self.stage_aux[si] = bytes(_abi.MgpuGrid32())
             except NotImplementedError as exc:
                 self.fp32_error = str(exc)
-            if st.kind != _abi.STAGE_GRATINGS:
+            if st.kind not in _abi.FACET_STAGES:
                 continue
             fac = torch.from_numpy(st.facets.view(np.uint8).copy()).to(device)
             self.keep.append(fac)
@@ -263,7 +263,7 @@ class _Instrument:
         s.frame[:] = [float(x) for x in st.frame]
         s.cyl[:] = [float(x) for x in st.cyl]
         s.p[:] = [float(x) for x in st.p]
-        if st.kind == _abi.STAGE_GRATINGS:
+        if st.kind in _abi.FACET_STAGES:
             s.n_facets = len(st.facets)
             s.facets = self.stage_facets[si].data_ptr()
             s.selectors = self.stage_selectors[si].data_ptr()

@@ -218,6 +218,25 @@ def default_blaze_modifier(g):
     return True
 
 
+def _plane_frames(elems, out):
+    """Frames of flat elements into a facet table (vectorised over the
+    elements): centre, unit e_x/e_y/e_z and half sizes as
+    Geometry.__getitem__ derives them (math/geometry.py:108-160), and the id
+    numbers.  Returns the homogeneous e_y, e_z (F, 4)."""
+    P = np.stack([np.asarray(g.geometry.pos4d, dtype=float) for g in elems])   # (F, 4, 4)
+    vx, vy, vz = P[:, :, 0], P[:, :, 1], P[:, :, 2]
+    nx, ny, nz = _norms(vx), _norms(vy), _norms(vz)
+    ex4, ey4, ez4 = vx / nx[:, None], vy / ny[:, None], vz / nz[:, None]
+    out['c'] = P[:, :3, 3]
+    out['ex'] = ex4[:, :3]
+    out['ey'] = ey4[:, :3]
+    out['ez'] = ez4[:, :3]
+    out['hy'] = ny
+    out['hz'] = nz
+    out['id_num'] = [int(g.id_num) for g in elems]
+    return ey4, ez4
+
+
 def _grating_facets(gratings, selectors, sel_index):
     """Facet table of a list of gratings (vectorised over the facets): the
     frame of Geometry.__getitem__ (math/geometry.py:108-160) and the groove
@@ -230,16 +249,7 @@ def _grating_facets(gratings, selectors, sel_index):
                                       'supported on the GPU')
         if not default_blaze_modifier(g) and not hasattr(g, 'd_blaze_mm'):
             raise NotImplementedError('custom blaze_angle_modifier is not supported on the GPU')
-    P = np.stack([np.asarray(g.geometry.pos4d, dtype=float) for g in gratings])   # (F, 4, 4)
-    vx, vy, vz = P[:, :, 0], P[:, :, 1], P[:, :, 2]
-    nx, ny, nz = _norms(vx), _norms(vy), _norms(vz)
-    ex4, ey4, ez4 = vx / nx[:, None], vy / ny[:, None], vz / nz[:, None]
-    out['c'] = P[:, :3, 3]
-    out['ex'] = ex4[:, :3]
-    out['ey'] = ey4[:, :3]
-    out['ez'] = ez4[:, :3]
-    out['hy'] = ny
-    out['hz'] = nz
+    ey4, ez4 = _plane_frames(gratings, out)
     # FlatGrating.e_groove_coos on the flat bases (e_y, e_z, e_x): math.sin /
     # math.cos of each distinct groove angle, as the reference evaluates them
     groove = np.array([float(g.geometry._geometry.get('groove_angle', 0.)) for g in gratings])
@@ -254,7 +264,6 @@ def _grating_facets(gratings, selectors, sel_index):
     out['l'] = e_groove[:, :3]
     out['dneg'] = (-e_perp)[:, :3]
     out['dgrat'] = [float(g._d) for g in gratings]
-    out['id_num'] = [int(g.id_num) for g in gratings]
     sel = np.empty(n, dtype=np.int32)
     for i, g in enumerate(gratings):
         key = id(g.order_selector)
@@ -501,6 +510,38 @@ def _grating_stage(owner, gratings, id_col):
     return st
 
 
+def _detector_array_stage(owner, dets, id_col):
+    """Stage for a Parallel of FlatDetectors, a CCD array
+    (simulator/tests/test_parallel.py:11-23; the cameras of
+    missions/arcus/arcus.py:342-360): the element table of the grating stages
+    with each element's pixel size and centre pixel (FlatDetector,
+    optics/detector.py:18-75) in place of the groove constants."""
+    first = dets[0]
+    loc = _loc_names(first)
+    dp = list(getattr(first, 'detpix_name', ['detpix_x', 'detpix_y']))
+    for d in dets:
+        if 'FlatDetector' not in classnames(d):
+            raise NotImplementedError('a Parallel mixing %s with FlatDetectors' % type(d).__name__)
+        if _loc_names(d) != loc or list(getattr(d, 'detpix_name', dp)) != dp:
+            raise NotImplementedError('a Parallel of FlatDetectors with different column names')
+    facets = np.zeros(len(dets), dtype=_abi.FACET_DTYPE)
+    _plane_frames(dets, facets)
+    facets['dgrat'] = [float(d.pixsize) for d in dets]
+    facets['l'][:, 0] = [float(d.centerpix[0]) for d in dets]
+    facets['l'][:, 1] = [float(d.centerpix[1]) for d in dets]
+    facets['selector'] = -1
+    st = StageSpec(kind=_abi.STAGE_DETARRAY, element=owner,
+                   out_names=[loc[0], loc[1], dp[0], dp[1]], id_col=id_col, facets=facets)
+    st.new_col_order = dp + ([id_col] if id_col else []) + [n for n in loc if n is not None]
+    if len(dets) > 1:
+        st.grid = grid_params(facets)
+    return st
+
+
+def _is_detector(e):
+    return 'FlatDetector' in classnames(e)
+
+
 _STACK_LAYERS = ('CATGrating', 'QualityFactor', 'L1', 'L2Abs', 'L2Diffraction')
 
 
@@ -593,6 +634,8 @@ def _lower_one(e):
             return []
         if all(_is_cat_stack(x) for x in e.elements):
             return [_cat_stack_stage(e, list(e.elements), id_col)]
+        if _is_detector(e.elements[0]):
+            return [_detector_array_stage(e, list(e.elements), id_col)]
         return [_grating_stage(e, list(e.elements), id_col)]
     if 'FlatGrating' in names:
         return [_grating_stage(e, [e], getattr(e, 'id_col', None))]
@@ -729,18 +772,28 @@ def flat32_block(st):
     return bytes(b)
 
 
-def facets32_table(facets):
+def facets32_table(facets, detectors=False):
+    """FP32-local element records of a facet table: the centre as
+    float-float, frame, half sizes; for gratings the groove vectors and
+    energy2wave / d as float-float, for detectors (``detectors``) in l the
+    inverse pixel size and the centre pixel."""
     out = np.zeros(len(facets), dtype=_abi.FACET32_DTYPE)
     hi, lo = split_ff(facets['c'])
     out['c_hi'], out['c_lo'] = hi, lo
-    for k in ('ex', 'ey', 'ez', 'l', 'dneg'):
+    for k in ('ex', 'ey', 'ez'):
         out[k] = facets[k].astype(np.float32)
     out['hy'] = facets['hy'].astype(np.float32)
     out['hz'] = facets['hz'].astype(np.float32)
-    wd = 1.2398419292004202e-06 / facets['dgrat']
-    out['wd_hi'], out['wd_lo'] = split_ff(wd)
     out['id_num'] = facets['id_num']
     out['selector'] = facets['selector']
+    if detectors:
+        out['l'][:, 0] = 1.0 / facets['dgrat']
+        out['l'][:, 1:3] = facets['l'][:, 0:2]
+        return out
+    for k in ('l', 'dneg'):
+        out[k] = facets[k].astype(np.float32)
+    wd = 1.2398419292004202e-06 / facets['dgrat']
+    out['wd_hi'], out['wd_lo'] = split_ff(wd)
     out['flags'] = facets['cat'] | (facets['transmission'] << 1)
     return out
 

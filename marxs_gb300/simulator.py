@@ -1,4 +1,5 @@
-"""Containers mirroring ``marxs.simulator``: ``Sequence`` and ``Parallel``.
+"""Containers mirroring ``marxs.simulator``: ``Sequence``, ``Parallel`` and
+``ParallelCalculated``.
 
 ``Parallel.generate_elements`` restates the FP64 pose composition of
 marxs/simulator/simulator.py:384-440 (11-matrix chain, :424-437): global
@@ -9,7 +10,7 @@ common rotation, uncertainty zoom, element zoom, common zoom.
 import numpy as np
 
 from .geomath import (parse_position_keywords, decompose44, translation2aff,
-                      mat2aff, zoom2aff)
+                      mat2aff, zoom2aff, compose, e2h, h2e)
 from .optics import BaseContainer, FinitePlane, Geometry
 
 
@@ -105,3 +106,62 @@ class Parallel(BaseContainer):
                 f_pos4d = np.dot(m, f_pos4d)
             self.elements.append(self.elem_class(pos4d=f_pos4d, id_num=self.id_num_offset + i,
                                                  **specific))
+
+
+def _normalized(vec):
+    # transforms3d.utils.normalized_vector: vec / sqrt(sum(vec ** 2))
+    vec = np.asarray(vec, dtype=float)
+    return vec / np.sqrt(np.sum(vec * vec))
+
+
+def _ex2vec_fix(e1, efix):
+    """Rotation taking x to ``e1`` with the new y coplanar with ``efix``
+    (marxs/math/rotations.py:8-47, vectors normalised as transforms3d does)."""
+    e1 = _normalized(e1)
+    efix = _normalized(efix)
+    if np.allclose(e1, efix) or np.allclose(e1, -efix):
+        raise ValueError('Input vectors are parallel - Rotation matrix is ambiguous.')
+    rot = np.empty((3, 3))
+    rot[:, 0] = e1
+    rot[:, 1] = _normalized(efix - np.dot(efix, e1) * e1)
+    rot[:, 2] = np.cross(rot[:, 0], rot[:, 1])
+    return rot
+
+
+class ParallelCalculated(Parallel):
+    """Parallel whose element poses are computed from three specifications
+    (marxs/simulator/simulator.py:443-541): ``pos_spec`` the centres
+    ((n, 4) homogeneous points, or a callable returning them),
+    ``normal_spec`` the element normals (a homogeneous direction shared by
+    all, a point they all face away from, or a callable of the centres) and
+    ``parallel_spec`` a direction one element side stays parallel to (same
+    forms; a callable gets the centres and the normals).  Element i is posed
+    as compose(centre_i, ex2vec_fix(normal_i, parallel_i), 1).
+    """
+
+    def __init__(self, **kwargs):
+        self.pos_spec = kwargs.pop('pos_spec')
+        self.normal_spec = kwargs.pop('normal_spec')
+        self.parallel_spec = kwargs.pop('parallel_spec')
+        kwargs['elem_pos'] = self.calculate_elempos()
+        super().__init__(**kwargs)
+
+    def calculate_elempos(self):
+        xyzw = self.get_elemxyzw()
+        normals = self.get_spec('normal_spec', xyzw)
+        parallels = self.get_spec('parallel_spec', xyzw, normals)
+        return [compose(h2e(xyzw[i, :]), _ex2vec_fix(h2e(normals[i, :]), h2e(parallels[i, :])),
+                        np.ones(3)) for i in range(xyzw.shape[0])]
+
+    def get_elemxyzw(self):
+        return self.pos_spec() if callable(self.pos_spec) else self.pos_spec
+
+    def get_spec(self, specname, xyzw, *args, **kwargs):
+        spec = getattr(self, specname)
+        if callable(spec):
+            return spec(xyzw, *args, **kwargs)
+        if len(spec) == 4:
+            if spec[3] == 0:          # a direction shared by all elements
+                return np.tile(spec, (xyzw.shape[0], 1))
+            return e2h(h2e(xyzw) - h2e(spec)[None, :], 1)   # away from a point
+        raise ValueError(specname + 'must be callable or homogeneous coordinate.')

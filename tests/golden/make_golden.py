@@ -32,7 +32,7 @@ sys.path.insert(0, ROOT)
 import reference_loader  # noqa: E402
 from marxs_gb300 import configs  # noqa: E402
 
-N_PHOTONS = {'c0': 2000, 'c1': 3000, 'c2': 3000, 'c5': 3000, 'c6': 3000}
+N_PHOTONS = {'c0': 2000, 'c1': 3000, 'c2': 3000, 'c5': 3000, 'c6': 3000, 'c7': 2000, 'c8': 3000}
 GLOBAL_SEED = 20261203
 
 
@@ -116,7 +116,7 @@ def reference_namespace(marxs):
     from marxs.optics import (PerfectLens, RadialMirrorScatter, FlatDetector, CircularDetector,
                               FlatGrating, CATGrating, OrderSelector, EfficiencyFile)
     from marxs.math.geometry import Cylinder
-    from marxs.simulator import Parallel, Sequence
+    from marxs.simulator import Parallel, ParallelCalculated, Sequence
 
     def interpolated(wave_nm, blaze_deg, probs, orders):
         # the reference class reads a flattened (wavelength, blaze) table
@@ -157,7 +157,8 @@ def reference_namespace(marxs):
                            FlatGrating=FlatGrating, CATGrating=CATGrating,
                            OrderSelector=OrderSelector, EfficiencyFile=eff,
                            InterpolateEfficiencyTable=interpolated, Cylinder=Cylinder,
-                           Parallel=Parallel, Sequence=Sequence, angle=lambda r: r * u.rad)
+                           Parallel=Parallel, ParallelCalculated=ParallelCalculated,
+                           Sequence=Sequence, angle=lambda r: r * u.rad)
 
 
 def leaves(elements):
@@ -176,7 +177,7 @@ def generate(name):
     ns = reference_namespace(marxs)
     inst = configs.build(name, ns)
     n = N_PHOTONS[name]
-    ph = configs.photons_for(name, n, seed={'c0': 0, 'c1': 1, 'c2': 2, 'c5': 5, 'c6': 6}[name])
+    ph = configs.photons_for(name, n, seed=int(name[1:]))
     table = Table({k: v.copy() for k, v in ph.items()})
 
     rec = Recorder()
@@ -239,6 +240,8 @@ def generate(name):
         res['out_' + k] = np.asarray(out[k])
     if hasattr(inst, 'gas'):
         res['facet_pos4d'] = np.array([e.geometry.pos4d for e in inst.gas.elements])
+    if hasattr(getattr(inst, 'detector', None), 'elements'):
+        res['ccd_pos4d'] = np.array([e.geometry.pos4d for e in inst.detector.elements])
     res['colnames'] = np.array(out.colnames)
     np.savez_compressed(os.path.join(HERE, name + '.npz'), **res)
     print(name, 'n=%d' % n, 'columns:', out.colnames, 'multi-hit:', int(multi.sum()))
@@ -434,7 +437,8 @@ def generate_poses():
 if __name__ == '__main__':
     check_choice_restatement()
     check_uniform_restatement()
-    names = sys.argv[1:] or ['c0', 'c1', 'c2', 'c5', 'c6', 'source', 'analysis', 'poses']
+    names = sys.argv[1:] or ['c0', 'c1', 'c2', 'c5', 'c6', 'c7', 'c8', 'source', 'analysis',
+                             'poses']
     for name in names:
         if name == 'source':
             generate_source()

@@ -5,7 +5,8 @@ reference made, and every output column of the reference's own Sequence
 (see tests/golden/make_golden.py).  The float64 GPU chain, fed the same
 draws, must reproduce them:
 
-* ``facet``, ``order`` (and ``order_L1`` of CAT stacks) bit-exact for every photon;
+* ``facet``, ``order`` (and ``order_L1`` of CAT stacks) and the CCD id
+  columns of detector arrays bit-exact for every photon;
 * every float column within 1e-9 relative, |a - b| <= 1e-9 * max(|b|, s)
   with s the column's natural scale (1 mm, 1 for unit vectors, 1 pixel,
   1e-3 rad), and NaN exactly where the reference has NaN;
@@ -54,7 +55,7 @@ def _column_report(out, ref, ok):
         if a.dtype != b.dtype:
             report[col] = (False, 'dtype %s vs %s' % (a.dtype, b.dtype))
             continue
-        if col in ('facet', 'order', 'order_L1'):
+        if col in ('facet', 'order', 'order_L1', 'CCD_ID', 'CCD'):
             same = np.array_equal(a[ok], b[ok], equal_nan=True)
             report[col] = (same, int(np.sum(~((a[ok] == b[ok]) | (np.isnan(a[ok].astype(float)) &
                                                                  np.isnan(b[ok].astype(float)))))))
@@ -79,7 +80,7 @@ def _column_report(out, ref, ok):
 BLAZE_ABS = 5e-8
 
 
-@pytest.mark.parametrize('name', ['c0', 'c1', 'c2', 'c5', 'c6'])
+@pytest.mark.parametrize('name', ['c0', 'c1', 'c2', 'c5', 'c6', 'c7', 'c8'])
 def test_golden_parity_fp64(name):
     g, out = _run_gpu(name)
     ref = golden_outputs(g)
@@ -96,6 +97,22 @@ def test_golden_hits_are_counted(name):
     g, out = _run_gpu(name)
     ref = golden_outputs(g)
     assert (np.asarray(out['facet']) >= 0).sum() == (ref['facet'] >= 0).sum() > 0
+
+
+@pytest.mark.parametrize('name,idc', [('c7', 'CCD_ID'), ('c8', 'CCD')])
+def test_ccd_array_ids_and_misses(name, idc):
+    """A Parallel of FlatDetectors: the chip each photon lands on is the
+    reference's (bit-exact, -1 for gaps and misses), per-chip hit counts
+    match, and the C7 layout numbers its chips 0..3 as the reference's own
+    Parallel test requires (simulator/tests/test_parallel.py:11-23)."""
+    g, out = _run_gpu(name)
+    ref = golden_outputs(g)
+    ids = np.asarray(out[idc])
+    assert ids.dtype == ref[idc].dtype
+    assert np.array_equal(ids, ref[idc])
+    assert np.array_equal(np.bincount(ids[ids >= 0]), np.bincount(ref[idc][ref[idc] >= 0]))
+    miss = ids < 0
+    assert miss.any() and np.all(np.isnan(np.asarray(out['det_x'])[miss]))
 
 
 def test_cat_stack_l1_order_column():

@@ -28,7 +28,7 @@ def _draws(inst, g):
     return draws
 
 
-@pytest.mark.parametrize('name', ['c0', 'c1', 'c2', 'c5', 'c6'])
+@pytest.mark.parametrize('name', ['c0', 'c1', 'c2', 'c5', 'c6', 'c7', 'c8'])
 def test_oracle_reproduces_reference_bitwise(name):
     g = load_golden(name)
     inst = configs.build(name)
@@ -42,13 +42,37 @@ def test_oracle_reproduces_reference_bitwise(name):
     assert stats.get('multi_hit', 0) == int(g['multi_hit'].sum())
 
 
-@pytest.mark.parametrize('name', ['c1', 'c2', 'c5', 'c6'])
+@pytest.mark.parametrize('name', ['c1', 'c2', 'c5', 'c6', 'c8'])
 def test_native_facet_poses_equal_reference(name):
     """Parallel.generate_elements restated on the host gives the same poses."""
     g = load_golden(name)
     inst = configs.build(name)
     mine = np.array([e.geometry.pos4d for e in inst.gas.elements])
     assert np.array_equal(mine, g['facet_pos4d'])
+
+
+@pytest.mark.parametrize('name', ['c7', 'c8'])
+def test_native_ccd_poses_equal_reference(name):
+    """The CCD poses of Parallel (C7, the reference's test layout) and of
+    ParallelCalculated (C8, centres on the Rowland circle) equal the
+    reference's."""
+    g = load_golden(name)
+    inst = configs.build(name)
+    mine = np.array([e.geometry.pos4d for e in inst.detector.elements])
+    assert np.array_equal(mine, g['ccd_pos4d'])
+
+
+def test_ccd_workloads_are_nontrivial():
+    """Every C7 chip is hit and some photons fall in the gaps; C8's strip
+    catches dispersed orders on several chips."""
+    ref = golden_outputs(load_golden('c7'))
+    ids = ref['CCD_ID']
+    assert np.array_equal(np.unique(ids), [-1, 0, 1, 2, 3])
+    assert (ids == -1).mean() > 0.05
+    ref = golden_outputs(load_golden('c8'))
+    hit = ref['CCD'] >= 0
+    assert len(np.unique(ref['CCD'][hit])) >= 10
+    assert len(np.unique(ref['order'][hit & np.isfinite(ref['order'])])) >= 5
 
 
 def test_golden_workloads_are_nontrivial():

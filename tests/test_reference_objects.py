@@ -6,6 +6,7 @@ the same instruments are built from the reference's own classes (its
 ``PerfectLens``, ``RadialMirrorScatter``, ``FlatGrating``, ``CATGrating``,
 ``CATL1L2Stack``, ``Parallel``, ``EfficiencyFile``,
 ``InterpolateEfficiencyTable``, ``FlatDetector``, ``CircularDetector``,
+``ParallelCalculated``,
 imported from the MARXS source tree under the test stand-ins for astropy
 and transforms3d), and everything the lowering derives from them -- stage
 specs, facet records, order tables, splines, stack constants, candidate
@@ -70,8 +71,8 @@ def lowered(stages):
         elif st.kind == _abi.STAGE_CYLDET:
             blk, table = L.cyl32_block(st)
             rec['fp32'] = _arrays([blk, table])
-        elif st.kind == _abi.STAGE_GRATINGS:
-            t32 = L.facets32_table(st.facets)
+        elif st.kind in _abi.FACET_STAGES:
+            t32 = L.facets32_table(st.facets, detectors=st.kind == _abi.STAGE_DETARRAY)
             rec['fp32'] = _arrays(t32.view(np.uint8))
             if st.grid is not None:
                 rec['grid32'] = L.grid32_block(st.grid)
@@ -80,7 +81,7 @@ def lowered(stages):
     return out, (repr(plan.columns), repr(plan.first_writer), repr(plan.order))
 
 
-@pytest.mark.parametrize('name', ['c0', 'c1', 'c2', 'c5', 'c6'])
+@pytest.mark.parametrize('name', ['c0', 'c1', 'c2', 'c5', 'c6', 'c7', 'c8'])
 def test_reference_objects_lower_like_the_lookalikes(name, reference_marxs):
     import make_golden
     ns = make_golden.reference_namespace(reference_marxs)
