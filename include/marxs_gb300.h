@@ -616,6 +616,14 @@ int mgpu_facet_poses(const mgpu_pose_update* update, void* stream);
  * arithmetic runs on. */
 int mgpu_fma_probe(int32_t precision, int32_t blocks, int32_t iters, void* out, void* stream);
 
+/* The Philox4x32-10 generator every stochastic stage draws from, evaluated
+ * on caller-given inputs; it has no counterpart in the reference (whose
+ * draws come from numpy's global Mersenne Twister) and exists so that tests
+ * can hold the device generator to the published Random123 known-answer
+ * vectors.  in: n x 6 uint32 (counter words 0..3, key words 0..1), out:
+ * n x 4 uint32, both device memory. */
+int mgpu_philox4x32_10(const uint32_t* in, uint32_t* out, int64_t n, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -240,6 +240,7 @@ SIGNATURES = {
     'mgpu_order_stats': (C.c_int, [C.POINTER(MgpuStatsProblem), C.c_void_p]),
     'mgpu_facet_poses': (C.c_int, [C.POINTER(MgpuPoseUpdate), C.c_void_p]),
     'mgpu_fma_probe': (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
+    'mgpu_philox4x32_10': (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
 }
 
 _lib = None

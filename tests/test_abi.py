@@ -182,3 +182,5 @@ def test_entry_points_reject_bad_descriptors_without_a_gpu():
     assert lib.mgpu_generate_photons(C.byref(src), v, v, v, c, c, None) == bad
     assert lib.mgpu_pose_adjoint(None, None, 0, None, None, None, None) == bad
     assert lib.mgpu_fma_probe(_abi.FP32LOCAL, 0, 1, None, None) == bad
+    assert lib.mgpu_philox4x32_10(None, None, 5, None) == bad
+    assert lib.mgpu_philox4x32_10(None, None, -1, None) == bad
