@@ -50,3 +50,36 @@ def test_design_loop_raises_resolving_power():
     r0 = _resolving_power(model, photons, start, seed=999)
     r1 = _resolving_power(model, photons, res['theta'], seed=999)
     assert r1 > 1.05 * r0, (r0, r1, [h['resolving_power'] for h in res['history']])
+
+
+def test_design_gradient_matches_finite_differences():
+    """The gradient the design loop steps along, at matched accuracy: the
+    adjoint gradient of the mean resolving power of orders -8..-3 with
+    respect to a sample of the optimised parameters (facet tilts, detector
+    translation and rotation) equals central differences of the same loss
+    on the frozen float64 forward (h = 1e-4 mm / 1e-6 rad) within 1e-4
+    relative."""
+    from marxs_gb300 import configs
+    from marxs_gb300.adjoint import PoseModel, resolving_power
+    from marxs_gb300.gpu import DevicePhotons
+    inst = configs.build('c2')
+    n = 400_000
+    host = configs.annulus_photons(n, 5, inst.aperture_x, energies=np.full(n, 0.5))
+    photons = DevicePhotons.from_columns(host)
+    model = PoseModel(inst.elements)
+    theta = model.theta0('cuda')
+    fr, _ = model.trace(photons, ORDERS + [0], precision='fp32local', rng='philox', seed=7,
+                        theta=theta)
+    counts = torch.bincount(fr.group.long(), minlength=len(ORDERS) + 1).cpu().numpy()
+    groups = [g for g in range(len(ORDERS)) if counts[g] >= 20]
+    assert len(groups) >= 4
+    loss = resolving_power(len(ORDERS), groups)
+    sl = model.param_slices()
+    opt = np.concatenate([sl['facet_rotation'], sl['detector_translation'],
+                          sl['detector_rotation']])
+    sub = opt[:: max(1, len(opt) // 60)]
+    fd = fr.finite_differences(theta, loss, params=sub)
+    _, g = fr.loss_and_grad(theta, loss)
+    g = g[torch.from_numpy(sub).to(g.device)]
+    rel = float(torch.linalg.norm(g - fd) / torch.linalg.norm(fd))
+    assert rel <= 1e-4, rel
