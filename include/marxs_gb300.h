@@ -304,6 +304,12 @@ typedef struct {
     const struct mgpu_catstack* stack; /* GRATINGS: facets are CATL1L2Stacks (NULL: plain) */
     mgpu_selector sel0;          /* GRATINGS: a copy of selectors[0]; with facet_sel0 the
                                     FP32-local kernel reads it from its parameter bank */
+    mgpu_col grating_d;          /* GRATINGS, optional: per-photon grating constant (mm) where
+                                    it depends on the position on the facet (FlatGrating.d with
+                                    a callable _d, optics/grating.py:209-220); NaN = the
+                                    facet's own dgrat */
+    mgpu_col blaze_add;          /* GRATINGS, optional: per-photon addend to the blaze angle
+                                    (a custom blaze_angle_modifier, grating.py:222-231) */
 } mgpu_stage;
 /* p[] per kind:
  *   LENS:    p[0] focal length, p[1] d_center_optical_axis

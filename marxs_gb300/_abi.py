@@ -141,7 +141,8 @@ class MgpuStage(C.Structure):
                 ('facet_sel0', C.c_int32), ('grid', MgpuGrid), ('aux_size', C.c_int32),
                 ('pad2', C.c_int32), ('aux32', C.c_uint8 * 128),
                 ('facets32', C.c_void_p), ('table', C.c_void_p),
-                ('spline', MgpuSpline1), ('stack', C.c_void_p), ('sel0', MgpuSelector)]
+                ('spline', MgpuSpline1), ('stack', C.c_void_p), ('sel0', MgpuSelector),
+                ('grating_d', MgpuCol), ('blaze_add', MgpuCol)]
 
 
 class MgpuChain(C.Structure):

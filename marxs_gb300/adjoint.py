@@ -30,7 +30,7 @@ import torch
 
 from . import _abi
 from .geomath import euler2mat
-from .lowering import _grating_facets, classnames, cylinder_block
+from .lowering import _grating_facets, classnames, cylinder_block, host_evaluated
 
 FWHM_PER_SIGMA = 2.0 * math.sqrt(2.0 * math.log(2.0))
 
@@ -129,6 +129,10 @@ class PoseModel:
                                           [float(getattr(self.lens, 'd_center_optax', 0.))]])
         sp = np.asarray(self.scatter.geometry.pos4d, dtype=float)
         self.scatter_block = np.concatenate([sp[:3, 3], _unit(sp[:, 0])])
+        hd, hb = host_evaluated(self.gratings)
+        if hd or hb:
+            raise NotImplementedError('pose gradients of gratings with a position-dependent '
+                                      'grating constant or blaze modifier')
         fac = _grating_facets(self.gratings, [], {})
         base = np.empty((self.n_facets, 13))
         base[:, 0:3] = fac['c']

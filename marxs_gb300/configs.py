@@ -22,6 +22,12 @@ travel from large x towards the focus at the origin.
   (simulator/tests/test_parallel.py:11-23), four 10x10 mm FlatDetectors
   (0.01 mm pixels, 0.2 mm gaps) in one Parallel with id column CCD_ID,
   photons spread over the four chips, the gaps and beyond.
+* ``C9`` chirped spectrometer: C1 with every facet's grating constant a
+  function of the position on the facet, installed as
+  design/bendgratings.py:180-192 does (a RectBivariateSpline, kx = ky = 2,
+  of d * corr(y) over the facet, bound as the facet's ``_d``; corr within
+  +-1 %), and every third facet with a blaze_angle_modifier linear in the
+  local y.
 * ``C8`` CAT array + CCD strip: C2 with the CircularDetector replaced by
   16 FlatDetectors of 24.576 mm (0.024 mm pixels, 2.4 mm gaps) tangent to
   the Rowland circle, chip 7 on the focus, placed by ParallelCalculated
@@ -362,6 +368,42 @@ def build_c8(ns, seed=8):
                            selector=inst.selector, draw_slots=inst.draw_slots)
 
 
+def chirp_facets(gratings, seed, d=2e-4):
+    """Position-dependent grating constants and blaze modifiers on the
+    facets of a grating array (any MARXS-like FlatGrating objects): the
+    chirp as design/bendgratings.py:180-192 installs it, with a seeded
+    correction instead of the optimiser's; a linear blaze modifier on every
+    third facet."""
+    import types
+    from scipy.interpolate import RectBivariateSpline
+    rng = np.random.default_rng(seed + 900)
+    uarray = np.array([-.999, 0, .999])
+    for k, g in enumerate(gratings):
+        pos4d = np.asarray(g.geometry.pos4d, dtype=float)
+        ly = np.linalg.norm(pos4d[:3, 1])
+        lz = np.linalg.norm(pos4d[:3, 2])
+        corr = 1.0 + 0.01 * np.tanh(rng.standard_normal(3))
+        corr = np.tile(corr, (3, 1)).T
+        g.spline = RectBivariateSpline(ly * uarray, lz * uarray, d * corr,
+                                       bbox=[-ly, ly, -lz, lz], kx=2, ky=2)
+
+        def func(self, intercoos):
+            return self.spline(intercoos[:, 0], intercoos[:, 1], grid=False)
+        g._d = types.MethodType(func, g)
+        if k % 3 == 0:
+            a, b = 1e-3 * rng.standard_normal(), 1e-4 * rng.standard_normal()
+
+            def modifier(self, intercoos, a=a, b=b):
+                return a + b * intercoos[:, 0]
+            g.blaze_angle_modifier = types.MethodType(modifier, g)
+
+
+def build_c9(ns, seed=9):
+    inst = build_c1(ns, seed=seed)
+    chirp_facets(inst.gas.elements, seed)
+    return inst
+
+
 def photons_for(config_name, n, seed):
     if config_name == 'c7':
         return ccd_test_photons(n, seed)
@@ -387,4 +429,6 @@ def build(config_name, ns=None, seed=None):
         return build_c7(ns)
     if config_name == 'c8':
         return build_c8(ns, seed=8 if seed is None else seed)
+    if config_name == 'c9':
+        return build_c9(ns, seed=9 if seed is None else seed)
     raise ValueError(config_name)

@@ -317,6 +317,10 @@ __device__ __forceinline__ float spline1_value_f(const mgpu_spline1& S, int s, c
 constexpr float kHcNmHi = (float)MGPU_HC_KEV_NM;
 constexpr float kHcNmLo = (float)(MGPU_HC_KEV_NM - (double)kHcNmHi);
 constexpr float kHcMm = (float)(MGPU_HC_KEV_NM * 1e-6);
+// energy2wave of the grating equation (marxs/__init__.py:14), mm keV, as float-float
+constexpr double kE2w = 1.2398419292004202e-06;
+constexpr float kE2wHi = (float)kE2w;
+constexpr float kE2wLo = (float)(kE2w - (double)kE2wHi);
 
 // InterpolateEfficiencyTable.__call__ (missions/mitsnl/catgrating.py:101-144)
 // in float32: the order whose running sum / total first exceeds u (index 0
@@ -835,9 +839,14 @@ __device__ bool stage_gratings_l(const mgpu_stage& st, PhotonL& ph, int64_t i, b
     float p_l = dotf(p, l), p_d = dotf(p, dn), p_n = dotf(p, n);
     float blaze = atan2f(fabsf(p_d), fabsf(p_n));      // = arccos|p_perp . n|
     // NonParallelCATGrating.blaze_angle_modifier (catgrating.py:324-333)
-    const float blaze_s = (kStack && st.stack)
-                              ? blaze + (st.stack->blaze_center32 + h.ly * st.stack->d_blaze32)
-                              : blaze;
+    float blaze_s = (kStack && st.stack)
+                        ? blaze + (st.stack->blaze_center32 + h.ly * st.stack->d_blaze32)
+                        : blaze;
+    // a custom blaze_angle_modifier, evaluated on the host (grating.py:255)
+    if (st.blaze_add.ptr) {
+        blaze_s += d2f_bits(st.blaze_add.ptr[i * st.blaze_add.stride]);
+        blaze = blaze_s;
+    }
     uint64_t U, U1 = 0;
     double u_pre = 0.0;
     if (rng == MGPU_RNG_PREDRAWN) {
@@ -866,7 +875,13 @@ __device__ bool stage_gratings_l(const mgpu_stage& st, PhotonL& ph, int64_t i, b
     if (flags & 1) sign = (p_d > 0.0f) ? 1.0f : ((p_d < 0.0f) ? -1.0f : 1.0f);
     else sign = -1.0f;
     // sign * m * lambda / d in float-float
-    ff term = ff_div(ff{R5.w, R6.x}, ph.energy);
+    ff wd{R5.w, R6.x};
+    if (st.grating_d.ptr) {
+        // a position-dependent grating constant: energy2wave / d per photon
+        const double v = st.grating_d.ptr[i * st.grating_d.stride];
+        if (!isnan(v)) wd = ff_div(ff{kE2wHi, kE2wLo}, d2ff_hw(v));
+    }
+    ff term = ff_div(wd, ph.energy);
     term = ff_mul_f(term, sign * (float)m);
     float tf = ff_f(term);
     float pd2 = ff_f(ff_add_f(term, p_d));

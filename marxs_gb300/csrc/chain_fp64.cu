@@ -401,6 +401,9 @@ __device__ bool stage_gratings(const mgpu_stage& st, Photon& ph, int64_t i, bool
         blaze = __dadd_rn(blaze, __dadd_rn(st.stack->blaze_center,
                                            __dmul_rn(h.ly, st.stack->d_blaze_mm)));
     }
+    // a custom blaze_angle_modifier, evaluated on the host at this photon's
+    // local coordinates (grating.py:255)
+    if (st.blaze_add.ptr) blaze = __dadd_rn(blaze, st.blaze_add.ptr[i * st.blaze_add.stride]);
     double u, u1;
     if (rng == MGPU_RNG_PREDRAWN) {
         if (st.draw[0] == nullptr) {
@@ -425,7 +428,14 @@ __device__ bool stage_gratings(const mgpu_stage& st, Photon& ph, int64_t i, bool
     } else {
         sign = -1.0;
     }
-    double p_d = pd0 + sign * (double)m * wave / __ldg(&fc->dgrat);
+    // FlatGrating.d (grating.py:209-220): the facet's constant, or the value
+    // of its callable at this photon's local coordinates
+    double dgr = __ldg(&fc->dgrat);
+    if (st.grating_d.ptr) {
+        const double v = st.grating_d.ptr[i * st.grating_d.stride];
+        if (!isnan(v)) dgr = v;
+    }
+    double p_d = pd0 + sign * (double)m * wave / dgr;
     double p_l = dot3(p, l);
     double p_n = sqrt(1.0 - p_d * p_d - p_l * p_l);
     double pn = dot3(p, n);

@@ -495,14 +495,83 @@ class GpuSequence:
         draws_dev = draws if isinstance(draws, dict) and all(isinstance(k, int) for k in draws) \
             else self._draws_to_device(inst, draws, n)
         chain = self._chain(inst, plan, bufs, draws_dev, n, status, hits, row_base)
+        lib = _abi.load()
         ph = _abi.MgpuPhotons()
         ph.n = n
         ph.pos, ph.dir, ph.pol, ph.energy, ph.prob = inp.abi()
         ph.pos_out, ph.dir_out, ph.pol_out, _, ph.prob_out = out.abi()
-        lib = _abi.load()
+        keep = []
+        if any(st.host_eval for st in inst.stages):
+            keep = self._host_evaluate(inst, chain, ph, bufs, n, stream)
         _abi.check(lib.mgpu_trace(C.byref(chain), C.byref(ph), _stream_handle(stream)),
                    'mgpu_trace')
+        if keep:
+            # the per-photon columns must outlive the launch
+            (stream or torch.cuda.current_stream()).synchronize()
         return status, hits
+
+    def _host_evaluate(self, inst, chain, ph_in, bufs, n, stream):
+        """Position-dependent grating constants and blaze modifiers
+        (FlatGrating.d with a callable _d and custom blaze_angle_modifier,
+        optics/grating.py:209-231): MARXS evaluates these Python callables at
+        each photon's local coordinates on the facet it hit.  For every such
+        grating stage, the chain up to and including that stage is traced
+        once (same draws: Philox streams are keyed by photon and stage, so the
+        final trace reproduces these hits), the facets' own callables are
+        evaluated on the host at the recorded local coordinates, and the
+        results go to the stage as per-photon columns (grating_d, blaze_add)
+        of the final trace.  Returns the device columns (keep them alive
+        until the final trace has run)."""
+        lib = _abi.load()
+        keep = []
+        tmp = DevicePhotons(n, device=self.device)
+        # the locate passes count hits and report status into scratch words:
+        # the final trace reports both
+        scratch_status = torch.zeros(1, dtype=torch.int32, device=self.device)
+        scratch_hits = torch.zeros(_abi.MAX_STAGES, dtype=torch.int64, device=self.device)
+        for si, st in enumerate(inst.stages):
+            if not st.host_eval:
+                continue
+            prefix = _abi.MgpuChain.from_buffer_copy(chain)
+            prefix.n_stages = si + 1
+            prefix.status = scratch_status.data_ptr()
+            prefix.hits = scratch_hits.data_ptr()
+            # the final trace's input state, the locate pass's own output
+            ph = _abi.MgpuPhotons.from_buffer_copy(ph_in)
+            ph.pos_out, ph.dir_out, ph.pol_out, _, ph.prob_out = tmp.abi()
+            _abi.check(lib.mgpu_trace(C.byref(prefix), C.byref(ph), _stream_handle(stream)),
+                       'mgpu_trace')
+            (stream or torch.cuda.current_stream()).synchronize()
+            y = bufs[st.out_names[0]].cpu().numpy()
+            z = bufs[st.out_names[1]].cpu().numpy()
+            hit = ~np.isnan(y)
+            if st.id_col is not None and len(st.facets) > 1:
+                ids = bufs[st.id_col].cpu().numpy()
+                index = {int(v): k for k, v in enumerate(st.facets['id_num'])}
+                fidx = np.full(n, -1, dtype=np.int64)
+                fidx[hit] = [index.get(int(v), -1) for v in ids[hit]]
+            else:
+                fidx = np.where(hit, 0, -1)
+            dcol = np.full(n, np.nan)
+            bcol = np.zeros(n)
+            for k, g in st.host_eval['d'].items():
+                m = fidx == k
+                if m.any():
+                    dcol[m] = g._d(np.column_stack([y[m], z[m]]))
+            for k, g in st.host_eval['blaze'].items():
+                m = fidx == k
+                if m.any():
+                    bcol[m] = g.blaze_angle_modifier(np.column_stack([y[m], z[m]]))
+            s = chain.stages[si]
+            if st.host_eval['d']:
+                t = torch.from_numpy(dcol).to(self.device)
+                keep.append(t)
+                s.grating_d = _abi.col(t)
+            if st.host_eval['blaze']:
+                t = torch.from_numpy(bcol).to(self.device)
+                keep.append(t)
+                s.blaze_add = _abi.col(t)
+        return keep
 
     # ------------------------------------------------------------ table path
     def _element_sequence(self, k, elem):
@@ -606,6 +675,7 @@ class GpuSequence:
                                             pin_memory=True)
         tm['setup'] = _time.perf_counter() - t0
         lib = _abi.load()
+        keep_cols = []            # per-photon columns of host-evaluated gratings
         streams = self._side_streams(dev)
         for st_ in streams:
             st_.wait_stream(main)
@@ -628,6 +698,8 @@ class GpuSequence:
                 ph.pol = ph.pol_out = _abi.vec_aos(dstate['polarization'][a:b])
                 ph.energy = _abi.col(dstate['energy'][a:b])
                 ph.prob = ph.prob_out = _abi.col(dstate['probability'][a:b])
+                if any(st.host_eval for st in inst.stages):
+                    keep_cols += self._host_evaluate(inst, chain, ph, sub_bufs, b - a, side)
                 _abi.check(lib.mgpu_trace(C.byref(chain), C.byref(ph), _stream_handle(side)),
                            'mgpu_trace')
                 for key in ('pos', 'dir', 'polarization', 'probability'):

@@ -185,6 +185,7 @@ class StageSpec:
     spline: Optional[tuple] = None   # LENS reflectivity (tx, ty, c[1, ...])
     stack: Optional[dict] = None     # GRATINGS of CATL1L2Stack facets: layer constants
     reads: Optional[str] = None      # SUPPORT: the id column it reads
+    host_eval: Optional[dict] = None # GRATINGS: facets with callable d / blaze modifier
 
 
 def _interp_table(x, y):
@@ -237,18 +238,25 @@ def _plane_frames(elems, out):
     return ey4, ez4
 
 
+def host_evaluated(gratings):
+    """The facets whose grating constant or blaze modifier depends on the
+    position on the facet through a Python callable: FlatGrating.d with a
+    callable _d (optics/grating.py:209-220, e.g. the chirped facets of
+    design/bendgratings.py:180-192) and an overridden blaze_angle_modifier
+    (grating.py:222-231).  Returns ({facet index: grating} for d, the same
+    for the blaze modifier)."""
+    d = {i: g for i, g in enumerate(gratings) if callable(g._d)}
+    blaze = {i: g for i, g in enumerate(gratings)
+             if not default_blaze_modifier(g) and not hasattr(g, 'd_blaze_mm')}
+    return d, blaze
+
+
 def _grating_facets(gratings, selectors, sel_index):
     """Facet table of a list of gratings (vectorised over the facets): the
     frame of Geometry.__getitem__ (math/geometry.py:108-160) and the groove
     frame of FlatGrating.e_groove_coos (optics/grating.py:186-207)."""
     n = len(gratings)
     out = np.zeros(n, dtype=_abi.FACET_DTYPE)
-    for g in gratings:
-        if callable(g._d):
-            raise NotImplementedError('position-dependent grating constant (callable d) is not '
-                                      'supported on the GPU')
-        if not default_blaze_modifier(g) and not hasattr(g, 'd_blaze_mm'):
-            raise NotImplementedError('custom blaze_angle_modifier is not supported on the GPU')
     ey4, ez4 = _plane_frames(gratings, out)
     # FlatGrating.e_groove_coos on the flat bases (e_y, e_z, e_x): math.sin /
     # math.cos of each distinct groove angle, as the reference evaluates them
@@ -263,7 +271,8 @@ def _grating_facets(gratings, selectors, sel_index):
     e_perp = cs[:, None] * ey4 - sn[:, None] * ez4
     out['l'] = e_groove[:, :3]
     out['dneg'] = (-e_perp)[:, :3]
-    out['dgrat'] = [float(g._d) for g in gratings]
+    # a callable grating constant is evaluated per photon (host_evaluated)
+    out['dgrat'] = [float('nan') if callable(g._d) else float(g._d) for g in gratings]
     sel = np.empty(n, dtype=np.int32)
     for i, g in enumerate(gratings):
         key = id(g.order_selector)
@@ -507,6 +516,18 @@ def _grating_stage(owner, gratings, id_col):
         [n for n in loc if n is not None]
     if len(gratings) > 1:
         st.grid = grid_params(facets)
+    hd, hb = host_evaluated(gratings)
+    if hd or hb:
+        # the callables take the photons' local coordinates, which the stage
+        # writes to its loc columns; facets are told apart by id number
+        if loc[0] is None or loc[1] is None:
+            raise NotImplementedError('a position-dependent grating needs its local '
+                                      'coordinate columns (loc_coos_name)')
+        if len(gratings) > 1 and (id_col is None or
+                                  len(set(facets['id_num'].tolist())) != len(gratings)):
+            raise NotImplementedError('position-dependent facets need an id column with a '
+                                      'distinct id number per facet')
+        st.host_eval = {'d': hd, 'blaze': hb}
     return st
 
 

@@ -321,6 +321,17 @@ def e_groove_coos(pos4d, groove):
     return e_groove, e_perp_groove, en
 
 
+def _custom_blaze_modifier(g):
+    """blaze_angle_modifier overridden on the instance or by a subclass of
+    FlatGrating (whose own returns zeros, grating.py:222-231)."""
+    if 'blaze_angle_modifier' in vars(g):
+        return True
+    for klass in type(g).__mro__:
+        if 'blaze_angle_modifier' in vars(klass):
+            return klass.__name__ != 'FlatGrating'
+    return False
+
+
 def flat_grating_process(g, photons, intersect, intercoos, u):
     """FlatGrating.diffract_photons + specific_process_photons, grating.py:233-277"""
     n_hit = intersect.sum()
@@ -336,6 +347,9 @@ def flat_grating_process(g, photons, intersect, intercoos, u):
     if hasattr(g, 'd_blaze_mm'):
         # NonParallelCATGrating.blaze_angle_modifier, missions/mitsnl/catgrating.py:324-333
         blazeangle += g.blaze_center + intercoos[intersect, 0] * g.d_blaze_mm
+    elif _custom_blaze_modifier(g):
+        # an overridden blaze_angle_modifier, called as grating.py:255 does
+        blazeangle += g.blaze_angle_modifier(intercoos[intersect, :])
     else:
         blazeangle += np.zeros(n_hit)
     m, prob = order_select(g.order_selector, photons['energy'][intersect], u[intersect],

@@ -332,4 +332,34 @@ def case_scatter_zero_sigma(r):
     assert np.all(out['det_y'] == 0)
 
 
+def case_grating_d_callable(r):
+    """marxs/optics/tests/test_grating.py:297-311: d can be a function of the
+    local coordinates; the photon at local y < 0 sees half the grating
+    constant and leaves at twice the angle."""
+    photons = test_photons(5)
+    photons['pos'][0, 1] = 1.
+    photons['pos'][1, 1] = -1.
+
+    def dfunc(intercoos):
+        darr = np.ones(intercoos.shape[0]) * 2e-4
+        return np.where(intercoos[:, 0] >= 0, darr, darr / 2.)
+
+    grat = FlatGrating(order_selector=OrderSelector([1]), zoom=2, d=dfunc)
+    p = r.trace([grat], photons, {grat: {'order_u': np.full(5, 0.5)}})
+    assert np.abs(p['dir'][1, 1] / p['dir'][0, 1] - 2) < 0.00001
+
+
+def case_grating_blaze_angle_modifier(r):
+    """An overridden blaze_angle_modifier (grating.py:222-231) adds to the
+    blaze angle at each photon's local coordinates: at normal incidence the
+    blaze column is the modifier itself."""
+    photons = test_photons(4)
+    photons['pos'][:, 1] = [-1.5, -0.5, 0.5, 1.5]
+    grat = FlatGrating(order_selector=OrderSelector([0]), zoom=2, d=2e-4)
+    grat.blaze_angle_modifier = lambda intercoos: 0.01 + 0.001 * intercoos[:, 0]
+    p = r.trace([grat], photons, {grat: {'order_u': np.full(4, 0.5)}})
+    assert np.allclose(p['blaze'], 0.01 + 0.001 * np.array([-1.5, -0.5, 0.5, 1.5]),
+                       rtol=0, atol=1e-12)
+
+
 CASES = [v for k, v in sorted(globals().items()) if k.startswith('case_')]

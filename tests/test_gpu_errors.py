@@ -58,10 +58,20 @@ def test_missing_predrawn_draws_raise():
 
 
 def test_unsupported_element_raises_not_implemented():
+    """An element class the backend does not implement is refused before
+    anything runs (there is no CPU fallback); so is a position-dependent
+    grating without local coordinate columns to evaluate its callable on."""
     from marxs_gb300 import FlatGrating, OrderSelector
+    from marxs_gb300.optics import FlatOpticalElement
     from marxs_gb300.gpu import GpuSequence
+
+    class Baffle(FlatOpticalElement):
+        pass
+    with pytest.raises(NotImplementedError):
+        GpuSequence([Baffle(zoom=5)], rng='philox')(_table(_photons()))
     g = FlatGrating(d=lambda intercoos: np.full(len(intercoos), 1e-3),
                     order_selector=OrderSelector([1]), zoom=5)
+    g.loc_coos_name = None
     with pytest.raises(NotImplementedError):
         GpuSequence([g], rng='philox')(_table(_photons()))
 

@@ -141,7 +141,7 @@ def test_fp32local_vs_fp64_cat_array(n):
     print('columns:', check_columns(a, b, agree, inst))
 
 
-@pytest.mark.parametrize('name', ['c0', 'c1', 'c2', 'c5', 'c6', 'c7', 'c8'])
+@pytest.mark.parametrize('name', ['c0', 'c1', 'c2', 'c5', 'c6', 'c7', 'c8', 'c9'])
 def test_fp32local_golden(name):
     from marxs_gb300 import configs
     g = load_golden(name)

@@ -80,7 +80,7 @@ def _column_report(out, ref, ok):
 BLAZE_ABS = 5e-8
 
 
-@pytest.mark.parametrize('name', ['c0', 'c1', 'c2', 'c5', 'c6', 'c7', 'c8'])
+@pytest.mark.parametrize('name', ['c0', 'c1', 'c2', 'c5', 'c6', 'c7', 'c8', 'c9'])
 def test_golden_parity_fp64(name):
     g, out = _run_gpu(name)
     ref = golden_outputs(g)
@@ -91,7 +91,7 @@ def test_golden_parity_fp64(name):
     assert not bad, 'columns out of tolerance: %s (all: %s)' % (bad, report)
 
 
-@pytest.mark.parametrize('name', ['c1', 'c2', 'c5', 'c6'])
+@pytest.mark.parametrize('name', ['c1', 'c2', 'c5', 'c6', 'c9'])
 def test_golden_hits_are_counted(name):
     from marxs_gb300 import configs
     g, out = _run_gpu(name)
@@ -229,3 +229,28 @@ def test_sequence_with_steps_equals_the_fused_chain():
     assert sorted(a.colnames) == sorted(b.colnames)
     for col in a.colnames:
         assert np.array_equal(np.asarray(a[col]), np.asarray(b[col]), equal_nan=True), col
+
+
+def test_chirped_facets_use_their_callables():
+    """C9: the facets' own callables decide the diffraction.  The golden
+    parity above holds; here the same trace with the chirp removed (every
+    facet's constant d) must move the dispersed photons, and the blaze
+    column of the facets with a modifier carries it."""
+    from marxs_gb300 import configs, PhotonTable
+    from marxs_gb300.gpu import GpuSequence
+    g, out = _run_gpu('c9')
+    inst = configs.build('c9')
+    ref = golden_outputs(g)
+    disp = np.isfinite(ref['order']) & (ref['order'] != 0) & np.isfinite(ref['det_x'])
+    assert disp.sum() > 100
+    plain = configs.build('c1', seed=9)
+    draws = {plain.scatter: {'inplanescatter': g['draw_inplanescatter'],
+                             'perpplanescatter': g['draw_perpplanescatter']},
+             plain.gas: {'order_u': g['draw_order_u']}}
+    flat = GpuSequence(elements=plain.elements, precision='fp64', rng='predrawn')(
+        PhotonTable(golden_inputs(g)), draws=draws)
+    moved = np.abs(np.asarray(flat['det_x'])[disp] - np.asarray(out['det_x'])[disp])
+    assert np.median(moved) > 1e-3
+    facet = np.asarray(out['facet'])
+    mod = np.isin(facet, [e.id_num for k, e in enumerate(inst.gas.elements) if k % 3 == 0])
+    assert np.any(np.asarray(out['blaze'])[mod] != np.asarray(flat['blaze'])[mod])

@@ -28,7 +28,7 @@ def _draws(inst, g):
     return draws
 
 
-@pytest.mark.parametrize('name', ['c0', 'c1', 'c2', 'c5', 'c6', 'c7', 'c8'])
+@pytest.mark.parametrize('name', ['c0', 'c1', 'c2', 'c5', 'c6', 'c7', 'c8', 'c9'])
 def test_oracle_reproduces_reference_bitwise(name):
     g = load_golden(name)
     inst = configs.build(name)
@@ -42,7 +42,7 @@ def test_oracle_reproduces_reference_bitwise(name):
     assert stats.get('multi_hit', 0) == int(g['multi_hit'].sum())
 
 
-@pytest.mark.parametrize('name', ['c1', 'c2', 'c5', 'c6', 'c8'])
+@pytest.mark.parametrize('name', ['c1', 'c2', 'c5', 'c6', 'c8', 'c9'])
 def test_native_facet_poses_equal_reference(name):
     """Parallel.generate_elements restated on the host gives the same poses."""
     g = load_golden(name)

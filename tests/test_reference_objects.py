@@ -60,7 +60,9 @@ def lowered(stages):
                'cyl': _arrays(st.cyl), 'p': _arrays(st.p),
                'out_names': repr(st.out_names), 'id_col': repr(st.id_col),
                'new_col_order': repr(st.new_col_order), 'draw_names': repr(st.draw_names),
-               'reads': repr(st.reads)}
+               'reads': repr(st.reads),
+               'host_eval': None if st.host_eval is None else
+               (sorted(st.host_eval['d']), sorted(st.host_eval['blaze']))}
         rec['facets'] = _arrays(None if st.facets is None else st.facets.view(np.uint8))
         rec['selectors'] = [_selector(s) for s in st.selectors]
         rec['spline'] = _arrays(st.spline)
@@ -81,7 +83,7 @@ def lowered(stages):
     return out, (repr(plan.columns), repr(plan.first_writer), repr(plan.order))
 
 
-@pytest.mark.parametrize('name', ['c0', 'c1', 'c2', 'c5', 'c6', 'c7', 'c8'])
+@pytest.mark.parametrize('name', ['c0', 'c1', 'c2', 'c5', 'c6', 'c7', 'c8', 'c9'])
 def test_reference_objects_lower_like_the_lookalikes(name, reference_marxs):
     import make_golden
     ns = make_golden.reference_namespace(reference_marxs)
