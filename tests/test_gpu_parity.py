@@ -250,7 +250,9 @@ def test_chirped_facets_use_their_callables():
     flat = GpuSequence(elements=plain.elements, precision='fp64', rng='predrawn')(
         PhotonTable(golden_inputs(g)), draws=draws)
     moved = np.abs(np.asarray(flat['det_x'])[disp] - np.asarray(out['det_x'])[disp])
-    assert np.median(moved) > 1e-3
+    # photons the unchirped gratings send off the detector are NaN there
+    assert np.isfinite(moved).mean() > 0.5
+    assert np.nanmedian(moved) > 1e-3
     facet = np.asarray(out['facet'])
     mod = np.isin(facet, [e.id_num for k, e in enumerate(inst.gas.elements) if k % 3 == 0])
     assert np.any(np.asarray(out['blaze'])[mod] != np.asarray(flat['blaze'])[mod])
