@@ -23,10 +23,10 @@
 //   * interpolated tables (efficiency splines, lens reflectivity, the L1
 //     support transmission) and the CAT stack layers run in float32 /
 //     float-float from host-made float constants.
-// The float64 inputs are converted by the FP64 pipe's conversion
-// instructions (about 23 per photon; measured faster than integer-pipe
-// routines), the outputs on the integer pipe (mgpu_bits.cuh) with one
-// float64 add per float-float value; in Philox mode no other float64
+// The float64 positions are converted on the integer pipe (mgpu_bits.cuh),
+// the other inputs by the FP64 pipe's conversion instructions (this split
+// measured faster than either pipe alone), the outputs on the integer pipe
+// with one float64 add per float-float value; in Philox mode no other float64
 // arithmetic runs, except the float64 scan of an energy table whose rows
 // are not increasing.
 #include <cuda_runtime.h>
@@ -969,20 +969,22 @@ __device__ bool stage_detarray_l(const mgpu_stage& st, PhotonL& ph, int64_t i, b
 
 // one stage, kind known at compile time (KIND > 0) or read from the
 // descriptor (KIND == 0, generic chains)
-template <int KIND, bool kStack, bool kSel0>
+template <int KIND, bool kStack, bool kSel0, bool kPhilox>
 __device__ __forceinline__ bool run_stage_l(const mgpu_stage& st, PhotonL& ph, int64_t i,
                                             bool valid, const mgpu_chain& chain, int s) {
+    // fixed chains run Philox only: the pre-drawn branches fold away
+    const int rng = kPhilox ? MGPU_RNG_PHILOX : chain.rng;
     const int kind = KIND ? KIND : st.kind;
     switch (kind) {
     case MGPU_STAGE_GRATINGS:
-        return stage_gratings_l<kStack, kSel0>(st, ph, i, valid, chain.rng, chain.seed, chain.row_base,
+        return stage_gratings_l<kStack, kSel0>(st, ph, i, valid, rng, chain.seed, chain.row_base,
                                         s, chain.status);
     case MGPU_STAGE_DETARRAY:
         return stage_detarray_l(st, ph, i, valid);
     case MGPU_STAGE_LENS:
         return valid && stage_lens_l(st, ph, i, chain.status);
     case MGPU_STAGE_SCATTER:
-        return valid && stage_scatter_l(st, ph, i, chain.rng, chain.seed, chain.row_base, s,
+        return valid && stage_scatter_l(st, ph, i, rng, chain.seed, chain.row_base, s,
                                         chain.status);
     case MGPU_STAGE_FLATDET:
         return valid && stage_flatdet_l(st, ph, i);
@@ -1017,7 +1019,7 @@ struct GenericChain {
     __device__ static void run(const mgpu_chain& chain, PhotonL& ph, int64_t i, bool valid,
                                unsigned* s_hits, int lane) {
         for (int s = 0; s < chain.n_stages; ++s)
-            count_hits(run_stage_l<0, kStack, false>(chain.stages[s], ph, i, valid, chain, s), s_hits, s,
+            count_hits(run_stage_l<0, kStack, false, false>(chain.stages[s], ph, i, valid, chain, s), s_hits, s,
                        lane);
     }
 };
@@ -1030,7 +1032,7 @@ struct FixedChain {
     template <int KIND, int S, bool kStack>
     __device__ static void step(const mgpu_chain& chain, PhotonL& ph, int64_t i, bool valid,
                                 unsigned* s_hits, int lane) {
-        count_hits(run_stage_l<KIND, kStack, true>(chain.stages[S], ph, i, valid, chain, S), s_hits, S,
+        count_hits(run_stage_l<KIND, kStack, true, true>(chain.stages[S], ph, i, valid, chain, S), s_hits, S,
                    lane);
     }
     template <bool kStack, int... S>
@@ -1044,10 +1046,11 @@ struct FixedChain {
         run_seq<kStack>(chain, ph, i, valid, s_hits, lane,
                         std::make_integer_sequence<int, sizeof...(K)>{});
     }
-    // the stage kinds match, and every facet stage reads its first selector
+    // the stage kinds match, every facet stage reads its first selector, and
+    // the draws come from Philox (the pre-drawn code is compiled out)
     static bool matches(const mgpu_chain& chain) {
         const int kinds[] = {K...};
-        if (chain.n_stages != (int)sizeof...(K)) return false;
+        if (chain.n_stages != (int)sizeof...(K) || chain.rng != MGPU_RNG_PHILOX) return false;
         for (int s = 0; s < chain.n_stages; ++s) {
             if (chain.stages[s].kind != kinds[s]) return false;
             if (kinds[s] == MGPU_STAGE_GRATINGS && !chain.stages[s].facet_sel0) return false;
@@ -1080,7 +1083,9 @@ chain_fp32local_kernel(const __grid_constant__ mgpu_chain chain, const __grid_co
             // input conversions on the (otherwise idle) FP64 pipe: measured
             // 4 % faster than the integer-pipe routines used for the outputs
             d3 p = load3(io.pos, i), d = load3(io.dir, i), q = load3(io.pol, i);
-            ph.pos = ff3{d2ff_hw(p.x), d2ff_hw(p.y), d2ff_hw(p.z)};
+            // positions on the integer pipe, the rest on the FP64 pipe's
+            // conversions: measured 1.2 % faster than all of them on either
+            ph.pos = ff3{d2ff_bits(p.x), d2ff_bits(p.y), d2ff_bits(p.z)};
             ph.dir = f3{__double2float_rn(d.x), __double2float_rn(d.y), __double2float_rn(d.z)};
             ph.pol = f3{__double2float_rn(q.x), __double2float_rn(q.y), __double2float_rn(q.z)};
             ph.energy_d = io.energy.ptr[i * io.energy.stride];
