@@ -310,7 +310,14 @@ typedef struct {
                                     facet's own dgrat */
     mgpu_col blaze_add;          /* GRATINGS, optional: per-photon addend to the blaze angle
                                     (a custom blaze_angle_modifier, grating.py:222-231) */
+    const double* facet_cyl;     /* GRATINGS, optional (float64 kernel): the facets are gratings
+                                    on Cylinder surfaces, MGPU_FACET_CYL doubles each: the
+                                    cylinder block of mgpu_stage.cyl (pos4d rows, inverse rows,
+                                    zoom_z, R, reduced phi borders; 32) and sin(-groove),
+                                    cos(-groove); the facet table then holds each patch's
+                                    tangent plane for the candidate grid.  NULL: flat facets */
 } mgpu_stage;
+#define MGPU_FACET_CYL 34
 /* p[] per kind:
  *   LENS:    p[0] focal length, p[1] d_center_optical_axis
  *   SCATTER: p[0] sigma in-plane (rad), p[1] sigma perpendicular (rad)

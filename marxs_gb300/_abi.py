@@ -16,6 +16,7 @@ LIB_PATH = os.path.join(HERE, 'libmarxs_gb300.so')
 MGPU_ABI_VERSION = 2
 MAX_STAGES = 16
 MAX_OUT = 10
+FACET_CYL = 34
 MAX_DRAWS = 6
 
 STATUS_PROB_RANGE = 0x1
@@ -142,7 +143,7 @@ class MgpuStage(C.Structure):
                 ('pad2', C.c_int32), ('aux32', C.c_uint8 * 128),
                 ('facets32', C.c_void_p), ('table', C.c_void_p),
                 ('spline', MgpuSpline1), ('stack', C.c_void_p), ('sel0', MgpuSelector),
-                ('grating_d', MgpuCol), ('blaze_add', MgpuCol)]
+                ('grating_d', MgpuCol), ('blaze_add', MgpuCol), ('facet_cyl', C.c_void_p)]
 
 
 class MgpuChain(C.Structure):

@@ -130,6 +130,8 @@ class PoseModel:
         sp = np.asarray(self.scatter.geometry.pos4d, dtype=float)
         self.scatter_block = np.concatenate([sp[:3, 3], _unit(sp[:, 0])])
         hd, hb = host_evaluated(self.gratings)
+        if any('Cylinder' in classnames(g.geometry) for g in self.gratings):
+            raise NotImplementedError('pose gradients of gratings on Cylinder surfaces')
         if hd or hb:
             raise NotImplementedError('pose gradients of gratings with a position-dependent '
                                       'grating constant or blaze modifier')

@@ -28,6 +28,11 @@ travel from large x towards the focus at the origin.
   of d * corr(y) over the facet, bound as the facet's ``_d``; corr within
   +-1 %), and every third facet with a blaze_angle_modifier linear in the
   local y.
+* ``C10`` bent gratings: C1 (facet tilts seeded 10) with every facet bent
+  onto a cylinder of radius 1500 mm along its local y, as
+  design/bendgratings.py:24-60 bends a facet (the facet's geometry becomes
+  a Cylinder whose axis lies 1500 mm behind the facet centre, phi limits
+  +-arctan(half width / radius), keeping the groove angle).
 * ``C8`` CAT array + CCD strip: C2 with the CircularDetector replaced by
   16 FlatDetectors of 24.576 mm (0.024 mm pixels, 2.4 mm gaps) tangent to
   the Rowland circle, chip 7 on the focus, placed by ParallelCalculated
@@ -398,6 +403,28 @@ def chirp_facets(gratings, seed, d=2e-4):
             g.blaze_angle_modifier = types.MethodType(modifier, g)
 
 
+def bend_facets(gratings, radius, ns):
+    """Each flat grating's geometry replaced by a Cylinder through its
+    centre, curved along the local y, as design/bendgratings.py:24-60 does
+    for a facet: axis ``radius`` behind the centre along e_x, zoom
+    [radius, radius, z], phi limits +-arctan(half width / radius), the
+    geometry dict (groove angle) kept."""
+    for e in gratings:
+        t, rot, z, _ = geomath.decompose44(np.asarray(e.geometry.pos4d, dtype=float))
+        d_phi = np.arctan(z[1] / radius)
+        c = ns.Cylinder({'position': t - radius * geomath.h2e(e.geometry['e_x']),
+                         'orientation': rot, 'zoom': [radius, radius, z[2]],
+                         'phi_lim': [-d_phi, d_phi]})
+        c._geometry = e.geometry._geometry
+        e.geometry = c
+
+
+def build_c10(ns, seed=10, radius=1500.):
+    inst = build_c1(ns, seed=seed)
+    bend_facets(inst.gas.elements, radius, ns)
+    return inst
+
+
 def build_c9(ns, seed=9):
     inst = build_c1(ns, seed=seed)
     chirp_facets(inst.gas.elements, seed)
@@ -431,4 +458,6 @@ def build(config_name, ns=None, seed=None):
         return build_c8(ns, seed=8 if seed is None else seed)
     if config_name == 'c9':
         return build_c9(ns, seed=9 if seed is None else seed)
+    if config_name == 'c10':
+        return build_c10(ns, seed=10 if seed is None else seed)
     raise ValueError(config_name)

@@ -39,6 +39,21 @@ __device__ __forceinline__ PlaneHit facet_intersect(const mgpu_facet* fc, d3 pos
                            __ldg(&fc->hy), __ldg(&fc->hz), pos, dir);
 }
 
+// facet f of a facet stage: a flat facet, or a grating on a Cylinder
+// surface (Cylinder.intersect, math/geometry.py:470-564; local coordinates
+// (phi, z), k the ray parameter of the hit for the nearest-hit order)
+__device__ __forceinline__ PlaneHit stage_facet_hit(const mgpu_stage& st, int f, d3 pos, d3 dir) {
+    if (st.facet_cyl == nullptr) return facet_intersect(st.facets + f, pos, dir);
+    const CylHit ch = cylinder_intersect_dev(st.facet_cyl + (int64_t)MGPU_FACET_CYL * f, pos, dir);
+    PlaneHit h;
+    h.hit = ch.hit;
+    h.ip = ch.ip;
+    h.ly = ch.phi;
+    h.lz = ch.zl;
+    h.k = dot3(ch.ip - pos, dir);
+    return h;
+}
+
 // order selection: first order whose cumulative probability exceeds u, on
 // the nearest-energy row for EfficiencyFile (grating.py:88-96) or the only
 // row for OrderSelector (np.random.choice, grating.py:51-57)
@@ -230,7 +245,7 @@ __device__ __forceinline__ int nearest_facet_grid(const mgpu_stage& st, const Ph
     int s0 = __ldg(g.cell_start + cell), s1 = min(__ldg(g.cell_start + cell + 1), g.capacity);
     for (int q = s0; q < s1; ++q) {
         int f = __ldg(g.cell_items + q);
-        PlaneHit h = facet_intersect(st.facets + f, ph.pos, ph.dir);
+        PlaneHit h = stage_facet_hit(st, f, ph.pos, ph.dir);
         if (h.hit && (best < 0 || h.k < best_hit->k || (h.k == best_hit->k && f < best))) {
             best = f;
             *best_hit = h;
@@ -330,7 +345,7 @@ __device__ __forceinline__ int nearest_facet(const mgpu_stage& st, const Photon&
         double bk = 0.0;
         int bf = -1;
         for (int q = lane; q < st.n_facets; q += 32) {
-            PlaneHit hq = facet_intersect(st.facets + q, p, d);
+            PlaneHit hq = stage_facet_hit(st, q, p, d);
             if (hq.hit && (bf < 0 || hq.k < bk)) {
                 bf = q;
                 bk = hq.k;
@@ -348,7 +363,7 @@ __device__ __forceinline__ int nearest_facet(const mgpu_stage& st, const Photon&
         }
         if (lane == src && bf >= 0) {
             f = bf;
-            h = facet_intersect(st.facets + bf, ph.pos, ph.dir);
+            h = stage_facet_hit(st, bf, ph.pos, ph.dir);
         }
     }
     *hit = h;
@@ -390,6 +405,27 @@ __device__ bool stage_gratings(const mgpu_stage& st, Photon& ph, int64_t i, bool
     // FlatGrating.diffract_photons + specific_process_photons (grating.py:233-277)
     const mgpu_facet* fc = st.facets + f;
     d3 l = ldg3(fc->l), dn = ldg3(fc->dneg), n = ldg3(fc->ex);
+    if (st.facet_cyl) {
+        // on a Cylinder: the groove frame of e_groove_coos (grating.py:186-207)
+        // on Cylinder.get_local_euklid_bases at the hit angle phi
+        // (math/geometry.py:602-626): e_phi = M (-sin, cos, 0), e_n = M (cos, sin, 0)
+        const double* M = st.facet_cyl + (int64_t)MGPU_FACET_CYL * f;
+        double sp, cp;
+        sincos(h.ly, &sp, &cp);
+        d3 ephi{__dadd_rn(__dmul_rn(M[0], -sp), __dmul_rn(M[1], cp)),
+                __dadd_rn(__dmul_rn(M[4], -sp), __dmul_rn(M[5], cp)),
+                __dadd_rn(__dmul_rn(M[8], -sp), __dmul_rn(M[9], cp))};
+        d3 en{__dadd_rn(__dmul_rn(M[0], cp), __dmul_rn(M[1], sp)),
+              __dadd_rn(__dmul_rn(M[4], cp), __dmul_rn(M[5], sp)),
+              __dadd_rn(__dmul_rn(M[8], cp), __dmul_rn(M[9], sp))};
+        ephi = normalize3(ephi);
+        en = normalize3(en);
+        const d3 ez = ldg3(fc->ez);
+        const double sg = M[32], cg = M[33];            // sin(-groove), cos(-groove)
+        l = sg * ephi + cg * ez;
+        dn = -1.0 * (cg * ephi - sg * ez);
+        n = en;
+    }
     d3 p = normalize3(ph.dir);
     double wave = kEnergy2Wave / ph.energy;
     d3 pp = normalize3(p - dot3(p, l) * l);

@@ -95,6 +95,7 @@ class _Instrument:
         self.stage_grid_bufs = {}     # si -> (cell_start, cell_items)
         self.stage_aux = {}       # FP32-local constant blocks (bytes, inline in the stage)
         self.stage_sel0 = {}      # first selector of a facet stage (inline copy)
+        self.stage_facet_cyl = {} # gratings on Cylinder surfaces: per-facet cylinder blocks
         self.stage_facets32 = {}
         self.stage_table = {}
         self.fp32_error = None
@@ -168,6 +169,9 @@ class _Instrument:
                     self.stage_aux[si] = blk
                     self.stage_table[si] = dev_bytes(table.tobytes())
                 elif st.kind in _abi.FACET_STAGES:
+                    if st.facet_cyl is not None:
+                        raise NotImplementedError('gratings on Cylinder surfaces run in the '
+                                                  'float64 mode only')
                     t32 = L.facets32_table(st.facets, detectors=st.kind == _abi.STAGE_DETARRAY)
                     self.stage_facets32[si] = dev_bytes(t32.tobytes())
                     if st.grid is not None:
@@ -181,6 +185,8 @@ class _Instrument:
             fac = torch.from_numpy(st.facets.view(np.uint8).copy()).to(device)
             self.keep.append(fac)
             self.stage_facets[si] = fac
+            if st.facet_cyl is not None:
+                self.stage_facet_cyl[si] = f64(st.facet_cyl)
             sel_structs = (_abi.MgpuSelector * len(st.selectors))()
             for k, s in enumerate(st.selectors):
                 e = torch.from_numpy(np.ascontiguousarray(s.energy)).to(device)
@@ -279,6 +285,8 @@ class _Instrument:
             s.aux_size = len(blk)
         if si in self.stage_sel0:
             s.sel0 = self.stage_sel0[si]
+        if si in self.stage_facet_cyl:
+            s.facet_cyl = self.stage_facet_cyl[si]
         if si in self.stage_facets32:
             s.facets32 = self.stage_facets32[si].data_ptr()
         if si in self.stage_table:

@@ -185,6 +185,7 @@ class StageSpec:
     spline: Optional[tuple] = None   # LENS reflectivity (tx, ty, c[1, ...])
     stack: Optional[dict] = None     # GRATINGS of CATL1L2Stack facets: layer constants
     reads: Optional[str] = None      # SUPPORT: the id column it reads
+    facet_cyl: Optional[np.ndarray] = None   # GRATINGS on Cylinder surfaces: (F, 34)
     host_eval: Optional[dict] = None # GRATINGS: facets with callable d / blaze modifier
 
 
@@ -249,6 +250,40 @@ def host_evaluated(gratings):
     blaze = {i: g for i, g in enumerate(gratings)
              if not default_blaze_modifier(g) and not hasattr(g, 'd_blaze_mm')}
     return d, blaze
+
+
+def cylinder_facets(gratings, facets):
+    """Gratings on Cylinder surfaces (the bent facets of
+    design/bendgratings.py:24-60): per facet the cylinder block of
+    Cylinder.intersect (math/geometry.py:470-564) and sin, cos of the
+    negative groove angle; the facet table's frame is replaced by each
+    patch's tangent plane at the middle of its phi range, half sizes the
+    arc half length plus the sag and the z half length, so the candidate
+    grid bounds the curved patch (the kernel intersects the cylinder)."""
+    out = np.zeros((len(gratings), _abi.FACET_CYL))
+    for i, g in enumerate(gratings):
+        geo = g.geometry
+        blk = cylinder_block(geo)
+        out[i, :32] = blk
+        groove = float(geo._geometry.get('groove_angle', 0.))
+        out[i, 32] = math.sin(-groove)
+        out[i, 33] = math.cos(-groove)
+        pos4d = np.asarray(geo.pos4d, dtype=float)
+        R, zz = blk[25], blk[24]
+        e1 = pos4d[:3, 0] / np.linalg.norm(pos4d[:3, 0])
+        e2 = pos4d[:3, 1] / np.linalg.norm(pos4d[:3, 1])
+        lim = np.asarray(geo.coos_limits[0], dtype=float)
+        half = 0.5 * float(lim[1] - lim[0])
+        if not (0 < half < np.pi / 2):
+            raise NotImplementedError('cylindrical gratings spanning more than 180 degrees')
+        pm = 0.5 * float(lim[0] + lim[1])
+        radial = np.cos(pm) * e1 + np.sin(pm) * e2
+        facets['c'][i] = pos4d[:3, 3] + R * radial
+        facets['ex'][i] = radial
+        facets['ey'][i] = -np.sin(pm) * e1 + np.cos(pm) * e2
+        facets['hy'][i] = R * half + R * (1 - np.cos(half))
+        facets['hz'][i] = zz
+    return out
 
 
 def _grating_facets(gratings, selectors, sel_index):
@@ -516,6 +551,13 @@ def _grating_stage(owner, gratings, id_col):
         [n for n in loc if n is not None]
     if len(gratings) > 1:
         st.grid = grid_params(facets)
+    on_cyl = ['Cylinder' in classnames(g.geometry) for g in gratings]
+    if any(on_cyl):
+        if not all(on_cyl):
+            raise NotImplementedError('a Parallel mixing flat and cylindrical gratings')
+        st.facet_cyl = cylinder_facets(gratings, facets)
+        if st.grid is not None:
+            st.grid = grid_params(facets)
     hd, hb = host_evaluated(gratings)
     if hd or hb:
         # the callables take the photons' local coordinates, which the stage
@@ -581,6 +623,9 @@ def _cat_stack_stage(owner, stacks, id_col):
     (missions/mitsnl/catgrating.py:336-377)."""
     membranes = [st.elements[0] for st in stacks]
     st = _grating_stage(owner, membranes, id_col)
+    if st.facet_cyl is not None or st.host_eval:
+        raise NotImplementedError('CATL1L2Stack facets on Cylinder surfaces or with '
+                                  'position-dependent membranes')
     st.facets['id_num'] = [int(x.id_num) for x in stacks]
     l1s = [x.elements[2] for x in stacks]
     # one L1 order table for all facets (their selectors must agree)

@@ -332,14 +332,33 @@ def _custom_blaze_modifier(g):
     return False
 
 
+def cylinder_groove_coos(geometry, groove, intercoos):
+    """FlatGrating.e_groove_coos (grating.py:186-207) on a Cylinder surface:
+    the local bases of Cylinder.get_local_euklid_bases
+    (math/geometry.py:602-626) at each photon's angle phi."""
+    phi = intercoos[:, 0]
+    zeros = np.zeros_like(phi)
+    e_phi = np.array([-np.sin(phi), np.cos(phi), zeros, zeros]).T
+    e_z = np.tile(_geom_vec(geometry.pos4d, 'e_z'), (intercoos.shape[0], 1))
+    e_n = np.array([np.cos(phi), np.sin(phi), zeros, zeros]).T
+    e_phi = norm_vector(np.einsum('...ij,...j', geometry.pos4d, e_phi))
+    e_n = norm_vector(np.einsum('...ij,...j', geometry.pos4d, e_n))
+    e_groove = math.sin(-groove) * e_phi + math.cos(-groove) * e_z
+    e_perp_groove = math.cos(-groove) * e_phi - math.sin(-groove) * e_z
+    return e_groove, e_perp_groove, e_n
+
+
 def flat_grating_process(g, photons, intersect, intercoos, u):
     """FlatGrating.diffract_photons + specific_process_photons, grating.py:233-277"""
     n_hit = intersect.sum()
     p = norm_vector(photons['dir'][intersect])
-    l1, d1, n1 = e_groove_coos(g.geometry.pos4d, _grating_params(g))
-    l = np.tile(l1, (n_hit, 1))
-    d = np.tile(d1, (n_hit, 1))
-    n = np.tile(n1, (n_hit, 1))
+    if 'Cylinder' in _classnames(g.geometry):
+        l, d, n = cylinder_groove_coos(g.geometry, _grating_params(g), intercoos[intersect])
+    else:
+        l1, d1, n1 = e_groove_coos(g.geometry.pos4d, _grating_params(g))
+        l = np.tile(l1, (n_hit, 1))
+        d = np.tile(d1, (n_hit, 1))
+        n = np.tile(n1, (n_hit, 1))
     d = - d
     wave = ENERGY2WAVE / photons['energy'][intersect]
     p_perp_to_grooves = norm_vector(p - np.einsum('ij,ij->i', p, l)[:, None] * l)
@@ -539,7 +558,8 @@ def cat_stack_process(stack, photons, intersect, interpos, intercoos, d):
 def run_element(elem, photons, draws, stats):
     """One leaf element: OpticalElement.__call__ (optics/base.py:144-147)."""
     names = _classnames(elem)
-    if 'CircularDetector' in names:
+    if 'CircularDetector' in names or 'Cylinder' in _classnames(elem.geometry):
+        # any element on a Cylinder surface (detectors, bent gratings)
         intersect, interpos, intercoos = cylinder_intersect(
             elem.geometry.pos4d, elem.geometry.coos_limits[0], photons['dir'], photons['pos'])
     else:

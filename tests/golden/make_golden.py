@@ -33,7 +33,7 @@ import reference_loader  # noqa: E402
 from marxs_gb300 import configs  # noqa: E402
 
 N_PHOTONS = {'c0': 2000, 'c1': 3000, 'c2': 3000, 'c5': 3000, 'c6': 3000, 'c7': 2000, 'c8': 3000,
-             'c9': 3000}
+             'c9': 3000, 'c10': 3000}
 GLOBAL_SEED = 20261203
 
 
@@ -438,7 +438,7 @@ def generate_poses():
 if __name__ == '__main__':
     check_choice_restatement()
     check_uniform_restatement()
-    names = sys.argv[1:] or ['c0', 'c1', 'c2', 'c5', 'c6', 'c7', 'c8', 'c9', 'source',
+    names = sys.argv[1:] or ['c0', 'c1', 'c2', 'c5', 'c6', 'c7', 'c8', 'c9', 'c10', 'source',
                              'analysis', 'poses']
     for name in names:
         if name == 'source':

@@ -80,7 +80,7 @@ def _column_report(out, ref, ok):
 BLAZE_ABS = 5e-8
 
 
-@pytest.mark.parametrize('name', ['c0', 'c1', 'c2', 'c5', 'c6', 'c7', 'c8', 'c9'])
+@pytest.mark.parametrize('name', ['c0', 'c1', 'c2', 'c5', 'c6', 'c7', 'c8', 'c9', 'c10'])
 def test_golden_parity_fp64(name):
     g, out = _run_gpu(name)
     ref = golden_outputs(g)
@@ -91,7 +91,7 @@ def test_golden_parity_fp64(name):
     assert not bad, 'columns out of tolerance: %s (all: %s)' % (bad, report)
 
 
-@pytest.mark.parametrize('name', ['c1', 'c2', 'c5', 'c6', 'c9'])
+@pytest.mark.parametrize('name', ['c1', 'c2', 'c5', 'c6', 'c9', 'c10'])
 def test_golden_hits_are_counted(name):
     from marxs_gb300 import configs
     g, out = _run_gpu(name)
@@ -256,3 +256,21 @@ def test_chirped_facets_use_their_callables():
     facet = np.asarray(out['facet'])
     mod = np.isin(facet, [e.id_num for k, e in enumerate(inst.gas.elements) if k % 3 == 0])
     assert np.any(np.asarray(out['blaze'])[mod] != np.asarray(flat['blaze'])[mod])
+
+
+def test_bent_gratings_float64_only():
+    """C10 (gratings bent onto cylinders): the float64 mode matches the
+    reference (golden parity above, local coordinates (phi, z)); the
+    FP32-local mode refuses the chain rather than treat the facets as
+    flat."""
+    from marxs_gb300 import configs, PhotonTable
+    from marxs_gb300.gpu import GpuSequence
+    g, out = _run_gpu('c10')
+    ref = golden_outputs(g)
+    hit = np.asarray(out['facet']) >= 0
+    assert hit.mean() > 0.5
+    assert np.nanmax(np.abs(np.asarray(out['grat_y']))) < 0.01        # phi, rad
+    inst = configs.build('c10')
+    with pytest.raises(NotImplementedError):
+        GpuSequence(elements=inst.elements, precision='fp32local', rng='philox')(
+            PhotonTable(golden_inputs(g)))

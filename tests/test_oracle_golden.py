@@ -28,7 +28,7 @@ def _draws(inst, g):
     return draws
 
 
-@pytest.mark.parametrize('name', ['c0', 'c1', 'c2', 'c5', 'c6', 'c7', 'c8', 'c9'])
+@pytest.mark.parametrize('name', ['c0', 'c1', 'c2', 'c5', 'c6', 'c7', 'c8', 'c9', 'c10'])
 def test_oracle_reproduces_reference_bitwise(name):
     g = load_golden(name)
     inst = configs.build(name)

@@ -68,6 +68,7 @@ def lowered(stages):
         rec['spline'] = _arrays(st.spline)
         rec['stack'] = _arrays(st.stack)
         rec['grid'] = _arrays(st.grid)
+        rec['facet_cyl'] = _arrays(st.facet_cyl)
         if st.kind in (_abi.STAGE_LENS, _abi.STAGE_SCATTER, _abi.STAGE_FLATDET):
             rec['fp32'] = L.flat32_block(st)
         elif st.kind == _abi.STAGE_CYLDET:
@@ -75,6 +76,8 @@ def lowered(stages):
             rec['fp32'] = _arrays([blk, table])
         elif st.kind in _abi.FACET_STAGES:
             t32 = L.facets32_table(st.facets, detectors=st.kind == _abi.STAGE_DETARRAY)
+            if st.facet_cyl is not None:
+                t32 = np.zeros(0, dtype=_abi.FACET32_DTYPE)       # float64 mode only
             rec['fp32'] = _arrays(t32.view(np.uint8))
             if st.grid is not None:
                 rec['grid32'] = L.grid32_block(st.grid)
@@ -83,7 +86,7 @@ def lowered(stages):
     return out, (repr(plan.columns), repr(plan.first_writer), repr(plan.order))
 
 
-@pytest.mark.parametrize('name', ['c0', 'c1', 'c2', 'c5', 'c6', 'c7', 'c8', 'c9'])
+@pytest.mark.parametrize('name', ['c0', 'c1', 'c2', 'c5', 'c6', 'c7', 'c8', 'c9', 'c10'])
 def test_reference_objects_lower_like_the_lookalikes(name, reference_marxs):
     import make_golden
     ns = make_golden.reference_namespace(reference_marxs)
