@@ -44,7 +44,7 @@ WORKLOAD = 'cat_rowland_1000facets_circular_detector'
 # captures of a 4e6-photon launch (profiles/chain_fp64_c2.md,
 # profiles/chain_fp32local_c2.md), scaled to the launch by photon count
 NCU_TRAFFIC_BYTES_PER_PHOTON = {'fp64': (358.2e6 + 735.3e6) / 4e6,
-                                'fp32local': (354.1e6 + 725.2e6) / 4e6}
+                                'fp32local': (354.4e6 + 725.4e6) / 4e6}
 
 
 def parse():
