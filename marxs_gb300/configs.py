@@ -33,6 +33,12 @@ travel from large x towards the focus at the origin.
   design/bendgratings.py:24-60 bends a facet (the facet's geometry becomes
   a Cylinder whose axis lies 1500 mm behind the facet centre, phi limits
   +-arctan(half width / radius), keeping the groove angle).
+* ``C11`` C2 with the CAT facets placed by the reference's own
+  RectangularGrid (design/rowland.py:647-700) on its RowlandTorus
+  (R = r = 5900 mm), 26.5 mm pitch over y in [-318, 318], z in [-530, 530]
+  (960 facets): the placement missions use.  The golden records the grid's
+  element positions; this package's build places the facets through a
+  Parallel with those positions (the placement is set-up, not the path).
 * ``C8`` CAT array + CCD strip: C2 with the CircularDetector replaced by
   16 FlatDetectors of 24.576 mm (0.024 mm pixels, 2.4 mm gaps) tangent to
   the Rowland circle, chip 7 on the focus, placed by ParallelCalculated
@@ -425,6 +431,28 @@ def build_c10(ns, seed=10, radius=1500.):
     return inst
 
 
+def build_c11(ns, seed=11, elem_pos=None):
+    """C2 with RectangularGrid facets; ``elem_pos``: the grid's element
+    positions (required unless ``ns`` holds the reference's RowlandTorus
+    and RectangularGrid)."""
+    inst = build_c2(ns, seed=seed)
+    blaze = geomath.axangle2mat(np.array([0, 0, 1.]), np.deg2rad(1.8))
+    args = {'d': 2e-4, 'zoom': [1, 12.5, 12.5], 'orientation': blaze,
+            'order_selector': inst.selector}
+    if elem_pos is None:
+        torus = ns.RowlandTorus(5900., 5900.)
+        gas = ns.RectangularGrid(rowland=torus, d_element=[26.5, 26.5], y_range=[-318., 318.],
+                                 z_range=[-530., 530.], elem_class=ns.CATGrating,
+                                 elem_args=args, id_col='facet')
+    else:
+        gas = ns.Parallel(elem_class=ns.CATGrating, elem_args=args,
+                          elem_pos=[np.asarray(p, dtype=float) for p in elem_pos], id_col='facet')
+    return SimpleNamespace(elements=[inst.lens, inst.scatter, gas, inst.detector], lens=inst.lens,
+                           scatter=inst.scatter, gas=gas, detector=inst.detector,
+                           selector=inst.selector, draw_slots=[(inst.scatter, 'scatter'),
+                                                               (gas, 'order')])
+
+
 def build_c9(ns, seed=9):
     inst = build_c1(ns, seed=seed)
     chirp_facets(inst.gas.elements, seed)
@@ -434,13 +462,13 @@ def build_c9(ns, seed=9):
 def photons_for(config_name, n, seed):
     if config_name == 'c7':
         return ccd_test_photons(n, seed)
-    if config_name in ('c2', 'c5', 'c6', 'c8'):
+    if config_name in ('c2', 'c5', 'c6', 'c8', 'c11'):
         e = piecewise_linear_energies(n, seed)
         return annulus_photons(n, seed, 12000., energies=e)
     return annulus_photons(n, seed, 10000.)
 
 
-def build(config_name, ns=None, seed=None):
+def build(config_name, ns=None, seed=None, **kwargs):
     ns = native_namespace() if ns is None else ns
     if config_name == 'c0':
         return build_c0(ns)
@@ -460,4 +488,6 @@ def build(config_name, ns=None, seed=None):
         return build_c9(ns, seed=9 if seed is None else seed)
     if config_name == 'c10':
         return build_c10(ns, seed=10 if seed is None else seed)
+    if config_name == 'c11':
+        return build_c11(ns, seed=11 if seed is None else seed, **kwargs)
     raise ValueError(config_name)

@@ -21,6 +21,15 @@ def load_golden(name):
         return {k: f[k] for k in f.files}
 
 
+def build_for_golden(name, g):
+    """This package's instrument of a golden workload (C11's facet positions
+    come from the reference's RectangularGrid, recorded in the fixture)."""
+    from marxs_gb300 import configs
+    if name == 'c11':
+        return configs.build(name, elem_pos=g['gas_elem_pos'])
+    return configs.build(name)
+
+
 def golden_inputs(g):
     return {k[3:]: g[k] for k in g if k.startswith('in_')}
 

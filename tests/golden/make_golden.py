@@ -33,7 +33,7 @@ import reference_loader  # noqa: E402
 from marxs_gb300 import configs  # noqa: E402
 
 N_PHOTONS = {'c0': 2000, 'c1': 3000, 'c2': 3000, 'c5': 3000, 'c6': 3000, 'c7': 2000, 'c8': 3000,
-             'c9': 3000, 'c10': 3000}
+             'c9': 3000, 'c10': 3000, 'c11': 3000}
 GLOBAL_SEED = 20261203
 
 
@@ -118,6 +118,7 @@ def reference_namespace(marxs):
                               FlatGrating, CATGrating, OrderSelector, EfficiencyFile)
     from marxs.math.geometry import Cylinder
     from marxs.simulator import Parallel, ParallelCalculated, Sequence
+    from marxs.design.rowland import RowlandTorus, RectangularGrid
 
     def interpolated(wave_nm, blaze_deg, probs, orders):
         # the reference class reads a flattened (wavelength, blaze) table
@@ -159,6 +160,7 @@ def reference_namespace(marxs):
                            OrderSelector=OrderSelector, EfficiencyFile=eff,
                            InterpolateEfficiencyTable=interpolated, Cylinder=Cylinder,
                            Parallel=Parallel, ParallelCalculated=ParallelCalculated,
+                           RowlandTorus=RowlandTorus, RectangularGrid=RectangularGrid,
                            Sequence=Sequence, angle=lambda r: r * u.rad)
 
 
@@ -241,6 +243,8 @@ def generate(name):
         res['out_' + k] = np.asarray(out[k])
     if hasattr(inst, 'gas'):
         res['facet_pos4d'] = np.array([e.geometry.pos4d for e in inst.gas.elements])
+        if name == 'c11':
+            res['gas_elem_pos'] = np.array(inst.gas.elem_pos)
     if hasattr(getattr(inst, 'detector', None), 'elements'):
         res['ccd_pos4d'] = np.array([e.geometry.pos4d for e in inst.detector.elements])
     res['colnames'] = np.array(out.colnames)
@@ -438,8 +442,8 @@ def generate_poses():
 if __name__ == '__main__':
     check_choice_restatement()
     check_uniform_restatement()
-    names = sys.argv[1:] or ['c0', 'c1', 'c2', 'c5', 'c6', 'c7', 'c8', 'c9', 'c10', 'source',
-                             'analysis', 'poses']
+    names = sys.argv[1:] or ['c0', 'c1', 'c2', 'c5', 'c6', 'c7', 'c8', 'c9', 'c10', 'c11',
+                             'source', 'analysis', 'poses']
     for name in names:
         if name == 'source':
             generate_source()

@@ -27,7 +27,7 @@ Tolerances, stated as the acceptance bar of the precision mode:
 import numpy as np
 import pytest
 
-from conftest import load_golden, golden_inputs, golden_outputs
+from conftest import load_golden, golden_inputs, golden_outputs, build_for_golden
 
 pytestmark = pytest.mark.gpu
 
@@ -141,11 +141,11 @@ def test_fp32local_vs_fp64_cat_array(n):
     print('columns:', check_columns(a, b, agree, inst))
 
 
-@pytest.mark.parametrize('name', ['c0', 'c1', 'c2', 'c5', 'c6', 'c7', 'c8', 'c9'])
+@pytest.mark.parametrize('name', ['c0', 'c1', 'c2', 'c5', 'c6', 'c7', 'c8', 'c9', 'c11'])
 def test_fp32local_golden(name):
     from marxs_gb300 import configs
     g = load_golden(name)
-    inst = configs.build(name)
+    inst = build_for_golden(name, g)
     draws = {}
     for elem, kind in inst.draw_slots:
         if kind == 'scatter':

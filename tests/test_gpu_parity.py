@@ -15,7 +15,7 @@ draws, must reproduce them:
 import numpy as np
 import pytest
 
-from conftest import load_golden, golden_inputs, golden_outputs, close_rel
+from conftest import load_golden, golden_inputs, golden_outputs, build_for_golden, close_rel
 
 pytestmark = pytest.mark.gpu
 
@@ -31,7 +31,7 @@ def _run_gpu(name, precision='fp64'):
     from marxs_gb300 import configs, PhotonTable
     from marxs_gb300.gpu import GpuSequence
     g = load_golden(name)
-    inst = configs.build(name)
+    inst = build_for_golden(name, g)
     draws = {}
     for elem, kind in inst.draw_slots:
         if kind == 'scatter':
@@ -80,7 +80,7 @@ def _column_report(out, ref, ok):
 BLAZE_ABS = 5e-8
 
 
-@pytest.mark.parametrize('name', ['c0', 'c1', 'c2', 'c5', 'c6', 'c7', 'c8', 'c9', 'c10'])
+@pytest.mark.parametrize('name', ['c0', 'c1', 'c2', 'c5', 'c6', 'c7', 'c8', 'c9', 'c10', 'c11'])
 def test_golden_parity_fp64(name):
     g, out = _run_gpu(name)
     ref = golden_outputs(g)

@@ -9,7 +9,7 @@ builders are also checked against the reference's own classes.
 import numpy as np
 import pytest
 
-from conftest import load_golden, golden_inputs, golden_outputs
+from conftest import load_golden, golden_inputs, golden_outputs, build_for_golden
 from marxs_gb300 import configs
 from oracle.raytrace import run_sequence
 
@@ -28,10 +28,10 @@ def _draws(inst, g):
     return draws
 
 
-@pytest.mark.parametrize('name', ['c0', 'c1', 'c2', 'c5', 'c6', 'c7', 'c8', 'c9', 'c10'])
+@pytest.mark.parametrize('name', ['c0', 'c1', 'c2', 'c5', 'c6', 'c7', 'c8', 'c9', 'c10', 'c11'])
 def test_oracle_reproduces_reference_bitwise(name):
     g = load_golden(name)
-    inst = configs.build(name)
+    inst = build_for_golden(name, g)
     out, stats = run_sequence(inst.elements, golden_inputs(g), _draws(inst, g))
     ref = golden_outputs(g)
     assert list(out.keys()) == [str(c) for c in g['colnames']]
@@ -42,11 +42,13 @@ def test_oracle_reproduces_reference_bitwise(name):
     assert stats.get('multi_hit', 0) == int(g['multi_hit'].sum())
 
 
-@pytest.mark.parametrize('name', ['c1', 'c2', 'c5', 'c6', 'c8', 'c9'])
+@pytest.mark.parametrize('name', ['c1', 'c2', 'c5', 'c6', 'c8', 'c9', 'c11'])
 def test_native_facet_poses_equal_reference(name):
-    """Parallel.generate_elements restated on the host gives the same poses."""
+    """Parallel.generate_elements restated on the host gives the same poses
+    (C11: from the element positions the reference's RectangularGrid
+    placed on its Rowland torus)."""
     g = load_golden(name)
-    inst = configs.build(name)
+    inst = build_for_golden(name, g)
     mine = np.array([e.geometry.pos4d for e in inst.gas.elements])
     assert np.array_equal(mine, g['facet_pos4d'])
 

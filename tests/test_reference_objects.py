@@ -86,12 +86,18 @@ def lowered(stages):
     return out, (repr(plan.columns), repr(plan.first_writer), repr(plan.order))
 
 
-@pytest.mark.parametrize('name', ['c0', 'c1', 'c2', 'c5', 'c6', 'c7', 'c8', 'c9', 'c10'])
+@pytest.mark.parametrize('name', ['c0', 'c1', 'c2', 'c5', 'c6', 'c7', 'c8', 'c9', 'c10', 'c11'])
 def test_reference_objects_lower_like_the_lookalikes(name, reference_marxs):
     import make_golden
     ns = make_golden.reference_namespace(reference_marxs)
     ref = configs.build(name, ns=ns)
-    nat = configs.build(name)
+    if name == 'c11':
+        # the reference's RectangularGrid (a ParallelCalculated on its Rowland
+        # torus) against a plain Parallel at the positions it chose
+        assert 'RectangularGrid' in {c.__name__ for c in type(ref.gas).__mro__}
+        nat = configs.build(name, elem_pos=np.array(ref.gas.elem_pos))
+    else:
+        nat = configs.build(name)
     # the reference build really holds the reference's classes
     assert type(ref.elements[0]).__module__.startswith('marxs.')
     assert type(nat.elements[0]).__module__.startswith('marxs_gb300.')
