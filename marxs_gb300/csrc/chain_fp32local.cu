@@ -1015,6 +1015,7 @@ __device__ __forceinline__ void count_hits(bool hit, unsigned* s_hits, int s, in
 // generic chain: stage loop over the descriptors
 struct GenericChain {
     static constexpr bool kFixed = false;
+    static constexpr int kSearches = 2;
     template <bool kStack>
     __device__ static void run(const mgpu_chain& chain, PhotonL& ph, int64_t i, bool valid,
                                unsigned* s_hits, int lane) {
@@ -1029,6 +1030,9 @@ struct GenericChain {
 template <int... K>
 struct FixedChain {
     static constexpr bool kFixed = true;
+    // facet-table searches (grating arrays, CCD arrays) in the chain
+    static constexpr int kSearches =
+        (0 + ... + (K == MGPU_STAGE_GRATINGS || K == MGPU_STAGE_DETARRAY ? 1 : 0));
     template <int KIND, int S, bool kStack>
     __device__ static void step(const mgpu_chain& chain, PhotonL& ph, int64_t i, bool valid,
                                 unsigned* s_hits, int lane) {
@@ -1060,13 +1064,15 @@ struct FixedChain {
 };
 
 template <class Chain, bool kStack>
-// fixed plain chains: 4 blocks of 256 per SM (64 registers, no spills; the
+// fixed plain chains with one facet search: 4 blocks of 256 per SM (64
+// registers, no spills; the
 // stage constants come from the parameter bank), measured 6 % faster than
 // 3 blocks (80 registers) on the CAT chain at 1e8 photons; the others keep
 // 3 blocks (at 64 registers they spill), which measured 4 % faster than
 // the unconstrained allocation (100 registers, 2 blocks); 128-thread
 // blocks and a capped (persistent) grid measured no faster
-__global__ void __launch_bounds__(kThreads, (Chain::kFixed && !kStack) ? kMinBlocks : kMinBlocksWide)
+__global__ void __launch_bounds__(kThreads, (Chain::kFixed && !kStack && Chain::kSearches <= 1)
+                                                ? kMinBlocks : kMinBlocksWide)
 chain_fp32local_kernel(const __grid_constant__ mgpu_chain chain, const __grid_constant__ mgpu_photons io) {
     __shared__ unsigned int s_hits[MGPU_MAX_STAGES];
     if (threadIdx.x < MGPU_MAX_STAGES) s_hits[threadIdx.x] = 0;
@@ -1125,6 +1131,9 @@ chain_fp32local_kernel(const __grid_constant__ mgpu_chain chain, const __grid_co
 using ChainCat = FixedChain<MGPU_STAGE_LENS, MGPU_STAGE_SCATTER, MGPU_STAGE_GRATINGS, MGPU_STAGE_CYLDET>;
 using ChainSpec = FixedChain<MGPU_STAGE_LENS, MGPU_STAGE_SCATTER, MGPU_STAGE_GRATINGS, MGPU_STAGE_FLATDET>;
 using ChainTel = FixedChain<MGPU_STAGE_LENS, MGPU_STAGE_SCATTER, MGPU_STAGE_FLATDET>;
+// the grating array followed by a CCD camera (a Parallel of FlatDetectors)
+using ChainCcd = FixedChain<MGPU_STAGE_LENS, MGPU_STAGE_SCATTER, MGPU_STAGE_GRATINGS,
+                            MGPU_STAGE_DETARRAY>;
 // the CAT array followed by its support structure (catsupportbars)
 using ChainCatBars = FixedChain<MGPU_STAGE_LENS, MGPU_STAGE_SCATTER, MGPU_STAGE_GRATINGS,
                                 MGPU_STAGE_SUPPORT, MGPU_STAGE_CYLDET>;
@@ -1165,6 +1174,8 @@ cudaError_t mgpu_launch_chain_fp32local(const mgpu_chain& chain, const mgpu_phot
         chain_fp32local_kernel<ChainCat, false><<<gb, kThreads, 0, stream>>>(chain, io);
     } else if (ChainSpec::matches(chain)) {
         chain_fp32local_kernel<ChainSpec, false><<<gb, kThreads, 0, stream>>>(chain, io);
+    } else if (ChainCcd::matches(chain)) {
+        chain_fp32local_kernel<ChainCcd, false><<<gb, kThreads, 0, stream>>>(chain, io);
     } else if (ChainTel::matches(chain)) {
         chain_fp32local_kernel<ChainTel, false><<<gb, kThreads, 0, stream>>>(chain, io);
     } else if (ChainCatBars::matches(chain)) {
