@@ -48,6 +48,9 @@ extern "C" {
 
 /* mgpu_chain.flags */
 #define MGPU_FLAG_CHECK_W        0x1u  /* read the homogeneous w of pos/dir/pol and check it */
+#define MGPU_FLAG_GENERIC        0x2u  /* FP32-local: run the generic stage loop even where a
+                                          kernel specialised for the chain applies (the same
+                                          results; for checking the specialisations) */
 
 /* precision modes */
 #define MGPU_FP64      0  /* float64 throughout, parity mode */

@@ -27,6 +27,7 @@ STATUS_GRID_FULL = 0x10
 STATUS_BAD_W = 0x20
 STATUS_TABLE_RANGE = 0x80
 FLAG_CHECK_W = 0x1
+FLAG_GENERIC = 0x2
 
 NOALLOC_MAX_CELLS = 65536
 ERR_NOALLOC_LIMIT = -2

@@ -29,9 +29,26 @@
 // with one float64 add per float-float value; in Philox mode no other float64
 // arithmetic runs, except the float64 scan of an energy table whose rows
 // are not increasing.
+//
+// The kernel is issue-bound (one photon per thread), and instruction fetch
+// is a large part of it: each fixed
+// stage sequence gets its own kernel with the stage kinds and constants
+// compiled in, and the plain ones ("lean") compile only the common element
+// configuration (no lens reflectivity table; one sorted, guided efficiency
+// table per grating array; no host-evaluated columns), which took the CAT
+// chain from 90 to 55 KB of code and 6 % of its time; rarely run code
+// (large-angle sines, the reflection form of the polarization transport)
+// stays out of line.  Other configurations run the generic stage loop.
+// Photon i of a column is addressed with 32-bit offsets (launches of at
+// most 2^30 photons).
 #include <cuda_runtime.h>
 #include <utility>
 #include "mgpu_ff.cuh"
+
+// branch hints: cold paths (misses, status flags, the brute-force scan) are
+// laid out away from the hot instruction stream
+#define MGPU_LIKELY(x) __builtin_expect(!!(x), 1)
+#define MGPU_UNLIKELY(x) __builtin_expect(!!(x), 0)
 
 namespace {
 
@@ -63,6 +80,7 @@ struct PhotonL {
     ff energy;
     double energy_d;
     float prob;
+    int row0;      // energy row of the first facet stage's selector (-1: not found yet)
 };
 
 __device__ __forceinline__ ff3 ldff3(const float* hi, const float* lo) {
@@ -76,19 +94,44 @@ __device__ __forceinline__ ff d2ff_hw(double d) {
     return ff{h, __double2float_rn(d - (double)h)};
 }
 
-__device__ __forceinline__ void storef(const mgpu_col& c, int64_t i, float v) {
-    if (c.ptr) c.ptr[i * c.stride] = f2d_bits(v);
-}
-__device__ __forceinline__ void stored(const mgpu_col& c, int64_t i, double v) {
-    if (c.ptr) c.ptr[i * c.stride] = v;
-}
-
-__device__ __forceinline__ void store_id(const mgpu_stage& st, int64_t i, int64_t v) {
-    if ((st.first_writer >> 17) & 1) ((int64_t*)st.id_out)[i * st.id_stride] = v;
-    else ((int32_t*)st.id_out)[i * st.id_stride] = (int32_t)v;
+// element i of a column of stride s (elements).  The launcher keeps
+// i < 2^30 and |s| * sizeof(T) < 2^31, so the address is one 32 x 32 ->
+// 64-bit multiply-add onto the base pointer.
+template <class T>
+__device__ __forceinline__ T* at(T* p, int i, int64_t s) {
+    return (T*)((uintptr_t)p + (uintptr_t)((int64_t)i * (int64_t)(int)(s * (int64_t)sizeof(T))));
 }
 
-__device__ __forceinline__ void write_miss_defaults(const mgpu_stage& st, int64_t i, int nout) {
+__device__ __forceinline__ void storef(const mgpu_col& c, int i, float v) {
+    if (c.ptr) *at(c.ptr, i, c.stride) = f2d_bits(v);
+}
+// the same for values that are finite by construction (hit coordinates,
+// pixels, angles): no infinity / NaN cases in the conversion
+__device__ __forceinline__ void store_hit(const mgpu_col& c, int i, float v) {
+    if (c.ptr) *at(c.ptr, i, c.stride) = f2d_fin_bits(v);
+}
+__device__ __forceinline__ void stored(const mgpu_col& c, int i, double v) {
+    if (c.ptr) *at(c.ptr, i, c.stride) = v;
+}
+
+__device__ __forceinline__ void store_id(const mgpu_stage& st, int i, int64_t v) {
+    if ((st.first_writer >> 17) & 1) *at((int64_t*)st.id_out, i, st.id_stride) = v;
+    else *at((int32_t*)st.id_out, i, st.id_stride) = (int32_t)v;
+}
+
+// 3-vector columns: component c of photon i at ptr + c * cstride, stride s
+__device__ __forceinline__ d3 load3i(const mgpu_vec& v, int i) {
+    return d3{*at(v.ptr, i, v.stride), *at(v.ptr + v.cstride, i, v.stride),
+              *at(v.ptr + 2 * v.cstride, i, v.stride)};
+}
+__device__ __forceinline__ void store3i(const mgpu_vec& v, int i, d3 a) {
+    *at(v.ptr, i, v.stride) = a.x;
+    *at(v.ptr + v.cstride, i, v.stride) = a.y;
+    *at(v.ptr + 2 * v.cstride, i, v.stride) = a.z;
+}
+
+__device__ __forceinline__ void write_miss_defaults(const mgpu_stage& st, int i, int nout) {
+#pragma unroll 1
     for (int k = 0; k < nout; ++k)
         if ((st.first_writer >> k) & 1) stored(st.out[k], i, kNaN);
     if (st.id_out && ((st.first_writer >> 16) & 1)) store_id(st, i, -1);
@@ -120,7 +163,7 @@ __device__ __forceinline__ HitL plane_hit_l(ff3 c, f3 n, f3 ey, f3 ez, float hy,
     float k = -(dotf(s, n) + dotf(e, n)) / kd;
     f3 v{fmaf(k, dir.x, s.x) + e.x, fmaf(k, dir.y, s.y) + e.y, fmaf(k, dir.z, s.z) + e.z};
     const float dk = -dotf(v, n) / kd;
-    if (isfinite(dk)) {
+    if (MGPU_LIKELY(isfinite(dk))) {
         k += dk;
         v = f3{fmaf(dk, dir.x, v.x), fmaf(dk, dir.y, v.y), fmaf(dk, dir.z, v.z)};
     }
@@ -171,48 +214,65 @@ __device__ __forceinline__ HitL facet_hit(const mgpu_facet32* fc, const ff3& pos
     return plane_hit_l(P.c, P.n, P.ey, P.ez, P.hy, P.hz, pos, dir);
 }
 
-// parallel_transport (polarization.py:90-170) in float32
-__device__ __forceinline__ f3 transport_f(f3 d_old, f3 d_new, f3 pol) {
-    f3 a = normf(d_old), b = normf(d_new);
-    f3 s = crossf(a, b);
-    float sn = sqrtf(dotf(s, s));
-    if (sn <= 1e-8f) return pol;
-    s = (1.0f / sn) * s;
-    f3 pin = crossf(a, s), pout = crossf(b, s);
-    float ks = dotf(s, pol), kp = dotf(pin, pol), kd = dotf(a, pol);
-    return f3{s.x * ks + pout.x * kp + b.x * kd, s.y * ks + pout.y * kp + b.y * kd,
-              s.z * ks + pout.z * kp + b.z * kd};
+// parallel_transport (polarization.py:90-170) in float32 for a turn of the
+// direction from a to b (any lengths), given ax = a x b: the rotation about
+// a x b that takes a to b maps the frame (s, a x s, a) of the reference onto
+// (s, b x s, b).  Below 90 degrees in the Rodrigues form
+//   pol cos t + w x pol + w (w . pol) / (1 + cos t),  w = a x b / (|a| |b|),
+// beyond it through the frame, where 1 + cos t loses its precision;
+// |a x b| <= 1e-8 |a| |b| leaves pol unchanged.  The frame form (turns of
+// 90 degrees or more: reflections) is out of line, away from the hot code.
+__device__ __noinline__ f3 transport_frame_f(f3 a, f3 b, f3 ax, f3 pol, float n0, float n1, float ss) {
+    const f3 s = rsqrtf(ss) * ax;
+    const f3 an = rsqrtf(n0) * a, bn = rsqrtf(n1) * b;
+    const f3 pin = crossf(an, s), pout = crossf(bn, s);
+    const float ks = dotf(s, pol), kp = dotf(pin, pol), kd = dotf(an, pol);
+    return f3{s.x * ks + pout.x * kp + bn.x * kd, s.y * ks + pout.y * kp + bn.y * kd,
+              s.z * ks + pout.z * kp + bn.z * kd};
+}
+__device__ __forceinline__ f3 transport_axis_f(f3 a, f3 b, f3 ax, f3 pol) {
+    const float n0 = dotf(a, a), n1 = dotf(b, b);
+    const float ss = dotf(ax, ax);
+    if (MGPU_UNLIKELY(!(ss > 1e-16f * n0 * n1))) return pol;
+    const float r = rsqrtf(n0 * n1);
+    const float c = dotf(a, b) * r;
+    if (MGPU_LIKELY(c > 0.0f)) {
+        const f3 w = r * ax;
+        const f3 wp = crossf(w, pol);
+        const float t = __fdividef(dotf(w, pol), 1.0f + c);
+        return f3{fmaf(c, pol.x, fmaf(w.x, t, wp.x)), fmaf(c, pol.y, fmaf(w.y, t, wp.y)),
+                  fmaf(c, pol.z, fmaf(w.z, t, wp.z))};
+    }
+    return transport_frame_f(a, b, ax, pol, n0, n1, ss);
 }
 
-// parallel transport for d_new = d_old + delta where the change delta is
-// known directly: the axis d_old x delta keeps full relative precision even
-// when the two directions are nearly parallel (a float32 cross product of the
-// two unit vectors would be dominated by rounding there).
+__device__ __forceinline__ f3 transport_f(f3 d_old, f3 d_new, f3 pol) {
+    return transport_axis_f(d_old, d_new, crossf(d_old, d_new), pol);
+}
+
+// the same for d_new = d_old + delta where the change delta is known
+// directly: the axis d_old x delta keeps full relative precision even when
+// the two directions are nearly parallel (a float32 cross product of the
+// two unit vectors would be dominated by rounding there)
 __device__ __forceinline__ f3 transport_delta_f(f3 d_old, f3 delta, f3 pol) {
-    f3 dn = d_old + delta;
-    f3 sx = crossf(d_old, delta);
-    float n0 = dotf(d_old, d_old), n1 = dotf(dn, dn);
-    float ss = dotf(sx, sx);
-    if (!(ss > 1e-16f * n0 * n1)) return pol;       // |a x b| <= 1e-8: identity
-    f3 s = rsqrtf(ss) * sx;
-    f3 a = rsqrtf(n0) * d_old, b = rsqrtf(n1) * dn;
-    f3 pin = crossf(a, s), pout = crossf(b, s);
-    float ks = dotf(s, pol), kp = dotf(pin, pol), kd = dotf(a, pol);
-    return f3{s.x * ks + pout.x * kp + b.x * kd, s.y * ks + pout.y * kp + b.y * kd,
-              s.z * ks + pout.z * kp + b.z * kd};
+    return transport_axis_f(d_old, d_old + delta, crossf(d_old, delta), pol);
 }
 
 // change of v under R^T v for R = axangle2mat(axis, angle):
 // -sin(a) (k x v) + (1 - cos a) k x (k x v), with 1 - cos a = 2 sin^2(a/2)
 // so small angles keep full relative precision
 // sin for the small scatter angles (|a| < 1e-2: odd polynomial, error below
-// a^7/5040 relative), the library sine otherwise
+// a^7/5040 relative), the library sine otherwise, out of line: its
+// argument reduction would add ~1.5 KB of rarely run code to each of the
+// four inlined rotations (instruction-cache pressure measured 1 % of the
+// CAT chain's time)
+__device__ __noinline__ float sin_large(float a) { return sinf(a); }
 __device__ __forceinline__ float sin_small(float a) {
-    if (fabsf(a) < 1e-2f) {
+    if (MGPU_LIKELY(fabsf(a) < 1e-2f)) {
         float a2 = a * a;
         return a * (1.0f - a2 * (1.0f / 6.0f) * (1.0f - a2 * (1.0f / 20.0f)));
     }
-    return sinf(a);
+    return sin_large(a);
 }
 
 __device__ __forceinline__ f3 rot_transpose_delta_f(f3 axis, float a, f3 v) {
@@ -342,18 +402,20 @@ __device__ __forceinline__ int select_order_spline_f(const mgpu_selector& sel, f
 }
 
 // ------------------------------------------------------------------ stages
-__device__ bool stage_lens_l(const mgpu_stage& st, PhotonL& ph, int64_t i, uint32_t* status) {
+// kLean (the plain fixed chains): the lens has no reflectivity table
+template <bool kLean>
+__device__ bool stage_lens_l(const mgpu_stage& st, PhotonL& ph, int i, uint32_t* status) {
     // PerfectLens.specific_process_photons, optics/mirror.py:53-82
     const mgpu_flat32* F = reinterpret_cast<const mgpu_flat32*>(st.aux32);
     HitL h = flat_hit(F, ph.pos, ph.dir);
-    if (!h.hit) {
+    if (MGPU_UNLIKELY(!h.hit)) {
         write_miss_defaults(st, i, 2);
         return false;
     }
     // focus - interpos = (centre - interpos) - d_off e_z + f norm(dir)
     f3 v = (F->p[0] * normf(ph.dir) - F->p[1] * ldf3(F->ez)) - h.v;
     f3 nd = normf(v);
-    if (st.spline.n_surf > 0) {
+    if (!kLean && st.spline.n_surf > 0) {
         // probability *= reflectivity_interpolator(E, angle / 4) ** 2 (mirror.py:73-79);
         // the angle from atan2(|a x b|, a . b), accurate for small deflections
         f3 od = normf(ph.dir);
@@ -362,23 +424,23 @@ __device__ bool stage_lens_l(const mgpu_stage& st, PhotonL& ph, int64_t i, uint3
         const Spline1Wf w = spline1_weights_f(st.spline, ph.energy, ff{0.25f * angle, 0.0f});
         float r = spline1_value_f(st.spline, 0, w);
         r = r * r;
-        if (!(r >= 0.0f && r <= 1.0f)) atomicOr(status, MGPU_STATUS_PROB_RANGE);
+        if (MGPU_UNLIKELY(!(r >= 0.0f && r <= 1.0f))) atomicOr(status, MGPU_STATUS_PROB_RANGE);
         ph.prob = ph.prob * r;
     }
     ph.pol = transport_f(ph.dir, nd, ph.pol);
     ph.dir = nd;
-    storef(st.out[0], i, h.ly);
-    storef(st.out[1], i, h.lz);
+    store_hit(st.out[0], i, h.ly);
+    store_hit(st.out[1], i, h.lz);
     ph.pos = h.ip;
     return true;
 }
 
-__device__ bool stage_scatter_l(const mgpu_stage& st, PhotonL& ph, int64_t i, int rng,
+__device__ bool stage_scatter_l(const mgpu_stage& st, PhotonL& ph, int i, int rng,
                                 uint64_t seed, uint64_t row_base, int sidx, uint32_t* status) {
     // RadialMirrorScatter.specific_process_photons, optics/scatter.py:49-77
     const mgpu_flat32* F = reinterpret_cast<const mgpu_flat32*>(st.aux32);
     HitL h = flat_hit(F, ph.pos, ph.dir);
-    if (!h.hit) {
+    if (MGPU_UNLIKELY(!h.hit)) {
         write_miss_defaults(st, i, 4);
         return false;
     }
@@ -391,8 +453,8 @@ __device__ bool stage_scatter_l(const mgpu_stage& st, PhotonL& ph, int64_t i, in
             atomicOr(status, MGPU_STATUS_BAD_STAGE);
             return false;
         }
-        if (sig_in != 0.0f) a_in_d = st.draw[0][i * st.draw_stride];
-        if (sig_perp != 0.0f) a_perp_d = st.draw[1][i * st.draw_stride];
+        if (sig_in != 0.0f) a_in_d = *at(st.draw[0], i, st.draw_stride);
+        if (sig_perp != 0.0f) a_perp_d = *at(st.draw[1], i, st.draw_stride);
         a_in = d2f_bits(a_in_d);
         a_perp = d2f_bits(a_perp_d);
         have_d = true;
@@ -416,31 +478,31 @@ __device__ bool stage_scatter_l(const mgpu_stage& st, PhotonL& ph, int64_t i, in
     if (sig_perp != 0.0f) delta = delta + rot_transpose_delta_f(radial, a_perp, ph.dir + delta);
     ph.pol = transport_delta_f(ph.dir, delta, ph.pol);
     ph.dir = ph.dir + delta;
-    storef(st.out[0], i, h.ly);
-    storef(st.out[1], i, h.lz);
+    store_hit(st.out[0], i, h.ly);
+    store_hit(st.out[1], i, h.lz);
     if (have_d) {
         stored(st.out[2], i, a_in_d);
         stored(st.out[3], i, a_perp_d);
     } else {
-        storef(st.out[2], i, a_in);
-        storef(st.out[3], i, a_perp);
+        store_hit(st.out[2], i, a_in);
+        store_hit(st.out[3], i, a_perp);
     }
     ph.pos = h.ip;
     return true;
 }
 
-__device__ bool stage_flatdet_l(const mgpu_stage& st, PhotonL& ph, int64_t i) {
+__device__ bool stage_flatdet_l(const mgpu_stage& st, PhotonL& ph, int i) {
     // FlatDetector.specific_process_photons, optics/detector.py:72-75
     const mgpu_flat32* F = reinterpret_cast<const mgpu_flat32*>(st.aux32);
     HitL h = flat_hit(F, ph.pos, ph.dir);
-    if (!h.hit) {
+    if (MGPU_UNLIKELY(!h.hit)) {
         write_miss_defaults(st, i, 4);
         return false;
     }
-    storef(st.out[0], i, h.ly);
-    storef(st.out[1], i, h.lz);
-    storef(st.out[2], i, h.ly * F->p[3] + F->p[1]);
-    storef(st.out[3], i, h.lz * F->p[3] + F->p[2]);
+    store_hit(st.out[0], i, h.ly);
+    store_hit(st.out[1], i, h.lz);
+    store_hit(st.out[2], i, h.ly * F->p[3] + F->p[1]);
+    store_hit(st.out[3], i, h.lz * F->p[3] + F->p[2]);
     if (st.id_out) store_id(st, i, st.id_num);
     ph.pos = h.ip;
     return true;
@@ -457,7 +519,21 @@ __device__ __forceinline__ bool in_arc(const mgpu_cyl32* K, float x, float y) {
     return K->arc == 2 || (K->arc == 0 ? (s1 && s2) : (s1 || s2));
 }
 
-__device__ bool stage_cyldet_l(const mgpu_stage& st, PhotonL& ph, int64_t i) {
+// angle of (x, y) to within 8.3e-5 rad: octant reduction and an odd
+// least-squares polynomial of atan on [0, 1] (fitted here, 4 terms).  It
+// only picks the tabulated reference point of the cylinder solve, where a
+// neighbouring one serves as well
+__device__ __forceinline__ float angle_coarse(float y, float x) {
+    const float ax = fabsf(x), ay = fabsf(y);
+    const float r = __fdividef(fminf(ax, ay), fmaxf(ax, ay));
+    const float r2 = r * r;
+    float a = r * fmaf(fmaf(fmaf(-0.038997583f, r2, 0.14628096f), r2, -0.32118174f), r2, 0.99921447f);
+    if (ay > ax) a = 1.5707964f - a;
+    if (x < 0.0f) a = 3.1415927f - a;
+    return copysignf(a, y);
+}
+
+__device__ bool stage_cyldet_l(const mgpu_stage& st, PhotonL& ph, int i) {
     // Cylinder.intersect (math/geometry.py:470-564) + CircularDetector
     // (optics/detector.py:115-118) for a circular tube
     const mgpu_cyl32* K = reinterpret_cast<const mgpu_cyl32*>(st.aux32);
@@ -477,7 +553,7 @@ __device__ bool stage_cyldet_l(const mgpu_stage& st, PhotonL& ph, int64_t i) {
     const float disc = b * b - a * c;
     bool hit = false;
     float t = 0.0f;
-    if (disc >= 0.0f && a > 0.0f) {
+    if (MGPU_LIKELY(disc >= 0.0f && a > 0.0f)) {
         const float sq = sqrtf(disc);
         const float qq = -(b + copysignf(sq, b));
         const float tA = qq / a, tB = c / qq;
@@ -494,14 +570,14 @@ __device__ bool stage_cyldet_l(const mgpu_stage& st, PhotonL& ph, int64_t i) {
         hit = h1 || h2;
         t = h1 ? a1 : a2;
     }
-    if (!hit) {
+    if (MGPU_UNLIKELY(!hit)) {
         write_miss_defaults(st, i, 4);
         return false;
     }
     // reference point P_k = c + R u_k on the cylinder at the angle k/1024
     // nearest the approximate hit; table row: (P_k hi, u.x), (P_k lo, u.y),
     // (tangent t_k, u.z), P_k global
-    int kk = __float2int_rn(atan2f(q2 + t * d2, q1 + t * d1) * 1024.0f);
+    int kk = __float2int_rn(angle_coarse(q2 + t * d2, q1 + t * d1) * 1024.0f);
     const int idx = min(max(kk - K->k0, 0), K->nk - 1);
     kk = idx + K->k0;
     const float4* tb = reinterpret_cast<const float4*>(st.table) + 3 * idx;
@@ -518,34 +594,37 @@ __device__ bool stage_cyldet_l(const mgpu_stage& st, PhotonL& ph, int64_t i) {
     const float du = dotf(d, u), dtg = dotf(d, tg);
     const float g = fmaf(wu, 2.0f * R + wu, wt * wt);
     const float dt = -g / (2.0f * fmaf(R + wu, du, wt * dtg));
-    if (isfinite(dt)) {
+    if (MGPU_LIKELY(isfinite(dt))) {
         w = f3{fmaf(dt, d.x, w.x), fmaf(dt, d.y, w.y), fmaf(dt, d.z, w.z)};
         wu = fmaf(dt, du, wu);
         wt = fmaf(dt, dtg, wt);
         wa = fmaf(dt, d3, wa);
     }
-    // det_phi = k/1024 + atan(wt / (R + wu)); |ratio| < 6e-4, so two terms
-    // of the series (next term r^5/5 < 2e-17)
+    // det_phi = k/1024 + atan(wt / (R + wu)); |ratio| < 6e-4 (5.8e-4 with
+    // the coarse angle's error), so two terms of the series (next term
+    // r^5/5 < 2e-17)
     const float r = wt / (R + wu);
     const float psi = fmaf(-(1.0f / 3.0f) * r * r, r, r);
     const ff phi = fast_two_sum((float)kk * (1.0f / 1024.0f), psi);
-    stored(st.out[0], i, ff2d(phi));
-    storef(st.out[1], i, wa);                      // P_k - c is perpendicular to the axis
+    stored(st.out[0], i, f2d_fin_bits(phi.hi) + f2d_fin_bits(phi.lo));
+    store_hit(st.out[1], i, wa);                      // P_k - c is perpendicular to the axis
     const ff px = ff_add_f(ff_mul(phi, ff{K->rpix_hi, K->rpix_lo}), K->cp0);
-    stored(st.out[2], i, ff2d(px));
-    storef(st.out[3], i, wa * K->inv_pix + K->cp1);
+    stored(st.out[2], i, f2d_fin_bits(px.hi) + f2d_fin_bits(px.lo));
+    store_hit(st.out[3], i, wa * K->inv_pix + K->cp1);
     if (st.id_out) store_id(st, i, st.id_num);
     ph.pos = ff3{ff_add_f(P.x, w.x), ff_add_f(P.y, w.y), ff_add_f(P.z, w.z)};
     return true;
 }
 
-// exact order selection (see the header comment)
-__device__ __forceinline__ int select_order_l(const mgpu_selector& sel, double e, float ef,
-                                              uint64_t U, float* prob, uint32_t* status) {
+// exact order selection (see the header comment): the energy row of the
+// table for photon energy e (float64; ef its float32 value)
+// kLean: the rows are sorted and carry their midpoints (checked at launch)
+template <bool kLean = false>
+__device__ __forceinline__ int energy_row(const mgpu_selector& sel, double e, float ef) {
     int row = 0;
-    if (sel.by_energy) {
+    if (kLean || sel.by_energy) {
         const int n = sel.n_rows;
-        if (sel.sorted) {
+        if (kLean || sel.sorted) {
             // largest j with E_j <= e (positive doubles order as integers)
             long long key = __double_as_longlong(e);
             const double e0 = sel.energy[0], e1 = sel.energy[n - 1];
@@ -553,7 +632,7 @@ __device__ __forceinline__ int select_order_l(const mgpu_selector& sel, double e
                 row = 0;
             } else {
                 // guess from a uniform grid, then step to the largest j with E_j <= e
-                const float g = sel.e_mid ? (ef - sel.e0_f) * sel.e_scale_f
+                const float g = (kLean || sel.e_mid) ? (ef - sel.e0_f) * sel.e_scale_f
                                           : __fdividef((float)(e - e0), (float)(e1 - e0)) *
                                                 (float)(n - 1);
                 int lo = min(max((int)g, 0), n - 1);
@@ -562,7 +641,7 @@ __device__ __forceinline__ int select_order_l(const mgpu_selector& sel, double e
                 row = lo;
                 if (row + 1 < n) {
                     // the nearer row: past the midpoint (integer keys), or |E - e| in float64
-                    if (sel.e_mid) {
+                    if (kLean || sel.e_mid) {
                         if (key > __double_as_longlong(sel.e_mid[row])) row = row + 1;
                     } else {
                         double d0 = fabs(sel.energy[row] - e), d1 = fabs(sel.energy[row + 1] - e);
@@ -581,9 +660,17 @@ __device__ __forceinline__ int select_order_l(const mgpu_selector& sel, double e
             }
         }
     }
+    return row;
+}
+
+// the order for the draw U (53 bits) in table row `row`; *prob the row's
+// total.  kLean: the selector has its guide table (checked at launch)
+template <bool kLean = false>
+__device__ __forceinline__ int select_order_row(const mgpu_selector& sel, int row, uint64_t U,
+                                                float* prob, uint32_t* status) {
     const uint64_t* th = sel.thresholds + (int64_t)row * sel.n_orders;
     int k = 0;
-    if (sel.guide) {
+    if (kLean || sel.guide) {
         // start at the first order of the draw's 1/64 bin, then step
         k = __ldg(sel.guide + row * 64 + (int)(U >> 47));
         while (k < sel.n_orders && !(U < th[k])) ++k;
@@ -597,68 +684,25 @@ __device__ __forceinline__ int select_order_l(const mgpu_selector& sel, double e
     } else {
         while (k < sel.n_orders && !(U < th[k])) ++k;
     }
-    if (k == sel.n_orders) {
+    if (MGPU_UNLIKELY(k == sel.n_orders)) {
         atomicOr(status, MGPU_STATUS_ORDER_EMPTY);
         k = sel.n_orders - 1;
     }
     double tot = sel.total[row];
     *prob = d2f_bits(tot);
-    if (tot < 0.0 || tot > 1.0) atomicOr(status, MGPU_STATUS_PROB_RANGE);
+    if (MGPU_UNLIKELY(tot < 0.0 || tot > 1.0)) atomicOr(status, MGPU_STATUS_PROB_RANGE);
     return sel.orders[k];
 }
 
-// nearest facet through the candidate grid: every candidate gets the full
-// FP32-local plane test (re-centring, float32 solve, one refinement), the
-// nearest hit (smallest k, then lowest index) keeps its local offset, so the
-// winner needs no second test; its global point is c + v.
-__device__ __forceinline__ int nearest_facet_grid_l(const mgpu_stage& st, const PhotonL& ph,
-                                                    bool valid, HitL* best_hit, bool* need_brute) {
-    const mgpu_grid32* G = reinterpret_cast<const mgpu_grid32*>(st.aux32);
-    *need_brute = false;
-    int best = -1;
-    best_hit->k = 0.0f;
-    if (!valid) return -1;
-    if (G == nullptr || st.grid.cell_start == nullptr) {
-        *need_brute = true;
-        return -1;
-    }
-    f3 rs, re;
-    ff3_rel(ph.pos, ldff3(G->o_hi, G->o_lo), rs, re);
-    const f3 rel = rs + re;
-    f3 n = ldf3(G->n), a = ldf3(G->a), b = ldf3(G->b);
-    float dn = dotf(ph.dir, n), da = dotf(ph.dir, a), db = dotf(ph.dir, b);
-    if (!(fabsf(da) <= G->slope_max * fabsf(dn)) || !(fabsf(db) <= G->slope_max * fabsf(dn)) ||
-        dn == 0.0f) {
-        *need_brute = true;
-        return -1;
-    }
-    float t0 = -dotf(rel, n) / dn;
-    float u = dotf(rel, a) + t0 * da;
-    float v = dotf(rel, b) + t0 * db;
-    float fu = floorf((u - G->u0) * G->inv_cell);
-    float fv = floorf((v - G->v0) * G->inv_cell);
-    if (!(fu >= 0.0f && fu < (float)G->nu && fv >= 0.0f && fv < (float)G->nv)) return -1;
-    int cell = (int)fu * G->nv + (int)fv;
-    const mgpu_grid& g = st.grid;
-    int s0 = __ldg(g.cell_start + cell), s1 = min(__ldg(g.cell_start + cell + 1), g.capacity);
-    for (int q = s0; q < s1; ++q) {
-        const int f = __ldg(g.cell_items + q);
-        const HitL h = facet_hit(st.facets32 + f, ph.pos, ph.dir);
-        if (h.hit && (best < 0 || h.k < best_hit->k || (h.k == best_hit->k && f < best))) {
-            best = f;
-            best_hit->k = h.k;
-            best_hit->v = h.v;
-            best_hit->ly = h.ly;
-            best_hit->lz = h.lz;
-        }
-    }
-    return best;
+__device__ __forceinline__ int select_order_l(const mgpu_selector& sel, double e, float ef,
+                                              uint64_t U, float* prob, uint32_t* status) {
+    return select_order_row(sel, energy_row(sel, e, ef), U, prob, status);
 }
 
 // photons the grid cannot bound (slope beyond the grid's limit): the whole
 // warp scans all facets for each of them, one photon at a time, with a warp
-// min-reduction on (k, facet).  (Inlined: an out-of-line call measured 1.3 %
-// slower through the extra registers it forces.)
+// min-reduction on (k, facet).  (Inlined: an out-of-line call spills at 64
+// registers and measured slower.)
 __device__ __forceinline__ int brute_force_nearest(const mgpu_stage& st, ff3 pos, f3 dir, unsigned bm) {
     const int lane = threadIdx.x & 31;
     int mine = -1;
@@ -693,6 +737,76 @@ __device__ __forceinline__ int brute_force_nearest(const mgpu_stage& st, ff3 pos
         if (lane == src) mine = bf;
     }
     return mine;
+}
+
+// the candidate range [*s0, *s1) of the photon's grid cell in cell_items;
+// *brute: the grid cannot bound the ray (slope beyond its limit, or no grid)
+__device__ __forceinline__ void grid_cell_range(const mgpu_stage& st, const PhotonL& ph, bool valid,
+                                                int* s0, int* s1, bool* brute) {
+    const mgpu_grid32* G = reinterpret_cast<const mgpu_grid32*>(st.aux32);
+    *s0 = *s1 = 0;
+    *brute = false;
+    if (!valid) return;
+    if (MGPU_UNLIKELY(G == nullptr || st.grid.cell_start == nullptr)) {
+        *brute = true;
+        return;
+    }
+    f3 rs, re;
+    ff3_rel(ph.pos, ldff3(G->o_hi, G->o_lo), rs, re);
+    const f3 rel = rs + re;
+    f3 n = ldf3(G->n), a = ldf3(G->a), b = ldf3(G->b);
+    float dn = dotf(ph.dir, n), da = dotf(ph.dir, a), db = dotf(ph.dir, b);
+    if (MGPU_UNLIKELY(!(fabsf(da) <= G->slope_max * fabsf(dn)) || !(fabsf(db) <= G->slope_max * fabsf(dn)) ||
+                      dn == 0.0f)) {
+        *brute = true;
+        return;
+    }
+    float t0 = -dotf(rel, n) / dn;
+    float u = dotf(rel, a) + t0 * da;
+    float v = dotf(rel, b) + t0 * db;
+    float fu = floorf((u - G->u0) * G->inv_cell);
+    float fv = floorf((v - G->v0) * G->inv_cell);
+    if (MGPU_UNLIKELY(!(fu >= 0.0f && fu < (float)G->nu && fv >= 0.0f && fv < (float)G->nv))) return;
+    int cell = (int)fu * G->nv + (int)fv;
+    const mgpu_grid& g = st.grid;
+    *s0 = __ldg(g.cell_start + cell);
+    *s1 = min(__ldg(g.cell_start + cell + 1), g.capacity);
+}
+
+// nearest facet: every candidate of the photon's grid cell gets the full
+// FP32-local plane test (re-centring, float32 solve, one refinement), the
+// nearest hit (smallest k, then lowest index) keeps its local offset, so the
+// winner needs no second test; its global point is c + v.  Photons the grid
+// cannot bound take the warp's brute-force scan, whose winner then runs
+// through the same candidate test (one code path for the hit record).
+__device__ __forceinline__ int nearest_facet_l(const mgpu_stage& st, const PhotonL& ph, bool valid,
+                                               HitL* best_hit) {
+    int s0, s1;
+    bool brute;
+    grid_cell_range(st, ph, valid, &s0, &s1, &brute);
+    const unsigned bm = __ballot_sync(MGPU_FULL_MASK, brute);
+    int bf = -1;
+    if (MGPU_UNLIKELY(bm != 0)) {
+        bf = brute_force_nearest(st, ph.pos, ph.dir, bm);
+        if (brute) {
+            s0 = 0;
+            s1 = bf >= 0 ? 1 : 0;
+        }
+    }
+    int best = -1;
+    best_hit->k = 0.0f;
+    for (int q = s0; q < s1; ++q) {
+        const int f = brute ? bf : __ldg(st.grid.cell_items + q);
+        const HitL h = facet_hit(st.facets32 + f, ph.pos, ph.dir);
+        if (h.hit && (best < 0 || h.k < best_hit->k || (h.k == best_hit->k && f < best))) {
+            best = f;
+            best_hit->k = h.k;
+            best_hit->v = h.v;
+            best_hit->ly = h.ly;
+            best_hit->lz = h.lz;
+        }
+    }
+    return best;
 }
 
 // order-preserving integer key of a float64 (all finite values and
@@ -737,12 +851,12 @@ __device__ __forceinline__ float np_interp_f(const double* x, const float* x32, 
 __device__ __forceinline__ void cat_stack_layers_l(const mgpu_stage& st, const mgpu_catstack& K,
                                                 int f, int m, float ly, float lz, uint64_t U1,
                                                 bool support, float z_l2, float u_phi,
-                                                PhotonL& ph, int64_t i, uint32_t* status) {
+                                                PhotonL& ph, int i, uint32_t* status) {
     const mgpu_facet32* fc = st.facets32 + f;
     const f3 n = ldf3(fc->ex);
     // QualityFactor: factor ** (order ** 2)
     const float q = powf(K.qf32, (float)(m * m));
-    if (!(q >= 0.0f && q <= 1.0f)) atomicOr(status, MGPU_STATUS_PROB_RANGE);
+    if (MGPU_UNLIKELY(!(q >= 0.0f && q <= 1.0f))) atomicOr(status, MGPU_STATUS_PROB_RANGE);
     ph.prob *= q;
     // L1: a CAT grating with grooves at pi/2, or the support bars
     const float* lv = K.l1_vec32 + 6 * (int64_t)f;
@@ -772,7 +886,7 @@ __device__ __forceinline__ void cat_stack_layers_l(const mgpu_stage& st, const m
         ph.pol = transport_delta_f(p, delta, ph.pol);
         ph.dir = p + delta;
     }
-    if (!(prob1 >= 0.0f && prob1 <= 1.0f)) atomicOr(status, MGPU_STATUS_PROB_RANGE);
+    if (MGPU_UNLIKELY(!(prob1 >= 0.0f && prob1 <= 1.0f))) atomicOr(status, MGPU_STATUS_PROB_RANGE);
     ph.prob *= prob1;
     stored(st.out[6], i, f2d_bits((float)m1));
     storef(st.out[7], i, blaze1);
@@ -782,7 +896,7 @@ __device__ __forceinline__ void cat_stack_layers_l(const mgpu_stage& st, const m
     const f3 pxn = crossf(p3, n);
     const float sin3 = fminf(sqrtf(dotf(pxn, pxn)), 1.0f);
     const float a2 = K.l2_open32 - K.l2_absorb32 * sin3;
-    if (!(a2 >= 0.0f && a2 <= 1.0f)) atomicOr(status, MGPU_STATUS_PROB_RANGE);
+    if (MGPU_UNLIKELY(!(a2 >= 0.0f && a2 <= 1.0f))) atomicOr(status, MGPU_STATUS_PROB_RANGE);
     ph.prob *= a2;
     // L2Diffraction: N(0,1) * sigma about dir x guess, then a uniform turn
     // about the direction, both as direction changes
@@ -804,24 +918,17 @@ __device__ __forceinline__ void cat_stack_layers_l(const mgpu_stage& st, const m
 // kStack: compiled with the CATL1L2Stack layers (launches whose chain has a
 // stacked facet stage); plain facet chains leave them out entirely.
 // kSel0: every facet uses the stage's first selector, read from the inline
-// copy in the parameter bank
-template <bool kStack, bool kSel0>
-__device__ bool stage_gratings_l(const mgpu_stage& st, PhotonL& ph, int64_t i, bool valid,
+// copy in the parameter bank.  kLean (the plain fixed chains): that
+// selector is a sorted, guided efficiency table and no column is evaluated
+// on the host
+template <bool kStack, bool kSel0, bool kLean>
+__device__ bool stage_gratings_l(const mgpu_stage& st, PhotonL& ph, int i, bool valid,
                                  int rng, uint64_t seed, uint64_t row_base, int sidx,
                                  uint32_t* status) {
     HitL h;
-    bool brute;
-    int f = nearest_facet_grid_l(st, ph, valid, &h, &brute);
-    unsigned bm = __ballot_sync(MGPU_FULL_MASK, brute);
-    if (bm) {
-        int bf = brute_force_nearest(st, ph.pos, ph.dir, bm);
-        if (brute) {
-            f = bf;
-            if (f >= 0) h = facet_hit(st.facets32 + f, ph.pos, ph.dir);
-        }
-    }
+    int f = nearest_facet_l(st, ph, valid, &h);
     if (!valid) return false;
-    if (f < 0) {
+    if (MGPU_UNLIKELY(f < 0)) {
         write_miss_defaults(st, i, kStack ? MGPU_MAX_OUT : 4);
         return false;
     }
@@ -843,8 +950,8 @@ __device__ bool stage_gratings_l(const mgpu_stage& st, PhotonL& ph, int64_t i, b
                         ? blaze + (st.stack->blaze_center32 + h.ly * st.stack->d_blaze32)
                         : blaze;
     // a custom blaze_angle_modifier, evaluated on the host (grating.py:255)
-    if (st.blaze_add.ptr) {
-        blaze_s += d2f_bits(st.blaze_add.ptr[i * st.blaze_add.stride]);
+    if (!kLean && st.blaze_add.ptr) {
+        blaze_s += d2f_bits(*at(st.blaze_add.ptr, i, st.blaze_add.stride));
         blaze = blaze_s;
     }
     uint64_t U, U1 = 0;
@@ -854,9 +961,9 @@ __device__ bool stage_gratings_l(const mgpu_stage& st, PhotonL& ph, int64_t i, b
             atomicOr(status, MGPU_STATUS_BAD_STAGE);
             return false;
         }
-        u_pre = st.draw[0][i * st.draw_stride];
+        u_pre = *at(st.draw[0], i, st.draw_stride);
         U = (uint64_t)(u_pre * 9007199254740992.0);
-        if (kStack && st.draw[1]) U1 = (uint64_t)(st.draw[1][i * st.draw_stride] * 9007199254740992.0);
+        if (kStack && st.draw[1]) U1 = (uint64_t)(*at(st.draw[1], i, st.draw_stride) * 9007199254740992.0);
     } else {
         philox_u53(seed, row_base + (uint64_t)i, (uint32_t)sidx, &U, &U1);
     }
@@ -864,21 +971,23 @@ __device__ bool stage_gratings_l(const mgpu_stage& st, PhotonL& ph, int64_t i, b
     const int flags = __float_as_int(R6.w);
     const mgpu_selector& sel = kSel0 ? st.sel0 : st.selectors[__float_as_int(R6.z)];
     int m;
-    if (sel.kind == MGPU_SEL_SPLINE) {
+    if (!kLean && sel.kind == MGPU_SEL_SPLINE) {
         // float32 evaluation of the interpolated table
         m = select_order_spline_f(sel, ph.energy, blaze_s, u53_to_f(U), &selprob);
-        if (!(selprob >= 0.0f && selprob <= 1.0f)) atomicOr(status, MGPU_STATUS_PROB_RANGE);
+        if (MGPU_UNLIKELY(!(selprob >= 0.0f && selprob <= 1.0f))) atomicOr(status, MGPU_STATUS_PROB_RANGE);
     } else {
-        m = select_order_l(sel, ph.energy_d, ph.energy.hi, U, &selprob, status);
+        // fixed chains found the energy row at the start of the photon
+        const int row = kSel0 ? ph.row0 : energy_row(sel, ph.energy_d, ph.energy.hi);
+        m = select_order_row<kLean>(sel, row, U, &selprob, status);
     }
     float sign;
     if (flags & 1) sign = (p_d > 0.0f) ? 1.0f : ((p_d < 0.0f) ? -1.0f : 1.0f);
     else sign = -1.0f;
     // sign * m * lambda / d in float-float
     ff wd{R5.w, R6.x};
-    if (st.grating_d.ptr) {
+    if (!kLean && st.grating_d.ptr) {
         // a position-dependent grating constant: energy2wave / d per photon
-        const double v = st.grating_d.ptr[i * st.grating_d.stride];
+        const double v = *at(st.grating_d.ptr, i, st.grating_d.stride);
         if (!isnan(v)) wd = ff_div(ff{kE2wHi, kE2wLo}, d2ff_hw(v));
     }
     ff term = ff_div(wd, ph.energy);
@@ -897,10 +1006,11 @@ __device__ bool stage_gratings_l(const mgpu_stage& st, PhotonL& ph, int64_t i, b
     ph.pol = transport_delta_f(p, delta, ph.pol);
     ph.dir = p + delta;
     ph.prob *= selprob;
-    storef(st.out[0], i, h.ly);
-    storef(st.out[1], i, h.lz);
-    stored(st.out[2], i, f2d_bits((float)m));
+    store_hit(st.out[0], i, h.ly);
+    store_hit(st.out[1], i, h.lz);
+    stored(st.out[2], i, f2d_fin_bits((float)m));
     if (kStack && st.stack) storef(st.out[3], i, blaze_s);
+    else if (kLean) store_hit(st.out[3], i, blaze);
     else storef(st.out[3], i, blaze);
     if (st.id_out) store_id(st, i, __float_as_int(R6.y));
     if (kStack && st.stack) {
@@ -911,9 +1021,9 @@ __device__ bool stage_gratings_l(const mgpu_stage& st, PhotonL& ph, int64_t i, b
                 atomicOr(status, MGPU_STATUS_BAD_STAGE);
                 return false;
             }
-            support = st.draw[2][i * st.draw_stride] > st.stack->l1_open;
-            z = __double2float_rn(st.draw[3][i * st.draw_stride]);
-            u_phi = __double2float_rn(st.draw[4][i * st.draw_stride]);
+            support = *at(st.draw[2], i, st.draw_stride) > st.stack->l1_open;
+            z = __double2float_rn(*at(st.draw[3], i, st.draw_stride));
+            u_phi = __double2float_rn(*at(st.draw[4], i, st.draw_stride));
         } else {
             // the float64 kernel's counters: draw 1 (u_sup, u_phi), draw 2
             // (the normal, by Box-Muller in float32 from the same uniforms);
@@ -938,30 +1048,21 @@ __device__ bool stage_gratings_l(const mgpu_stage& st, PhotonL& ph, int64_t i, b
 // Parallel of FlatDetectors (a CCD array): FlatDetector.specific_process_photons
 // (optics/detector.py:72-75) on the nearest element the ray crosses; record
 // row (ez.z, l) holds 1 / pixel size and the centre pixel
-__device__ bool stage_detarray_l(const mgpu_stage& st, PhotonL& ph, int64_t i, bool valid) {
+__device__ bool stage_detarray_l(const mgpu_stage& st, PhotonL& ph, int i, bool valid) {
     HitL h;
-    bool brute;
-    int f = nearest_facet_grid_l(st, ph, valid, &h, &brute);
-    const unsigned bm = __ballot_sync(MGPU_FULL_MASK, brute);
-    if (bm) {
-        const int bf = brute_force_nearest(st, ph.pos, ph.dir, bm);
-        if (brute) {
-            f = bf;
-            if (f >= 0) h = facet_hit(st.facets32 + f, ph.pos, ph.dir);
-        }
-    }
+    int f = nearest_facet_l(st, ph, valid, &h);
     if (!valid) return false;
-    if (f < 0) {
+    if (MGPU_UNLIKELY(f < 0)) {
         write_miss_defaults(st, i, 4);
         return false;
     }
     const mgpu_facet32* fc = st.facets32 + f;
     const ff3 c = facet_centre(fc);
     const float4 R4 = __ldg(facet_rows(fc) + 4), R6 = __ldg(facet_rows(fc) + 6);
-    storef(st.out[0], i, h.ly);
-    storef(st.out[1], i, h.lz);
-    storef(st.out[2], i, fmaf(h.ly, R4.y, R4.z));
-    storef(st.out[3], i, fmaf(h.lz, R4.y, R4.w));
+    store_hit(st.out[0], i, h.ly);
+    store_hit(st.out[1], i, h.lz);
+    store_hit(st.out[2], i, fmaf(h.ly, R4.y, R4.z));
+    store_hit(st.out[3], i, fmaf(h.lz, R4.y, R4.w));
     if (st.id_out) store_id(st, i, __float_as_int(R6.y));
     ph.pos = ff3{ff_add_f(c.x, h.v.x), ff_add_f(c.y, h.v.y), ff_add_f(c.z, h.v.z)};
     return true;
@@ -970,19 +1071,21 @@ __device__ bool stage_detarray_l(const mgpu_stage& st, PhotonL& ph, int64_t i, b
 // one stage, kind known at compile time (KIND > 0) or read from the
 // descriptor (KIND == 0, generic chains)
 template <int KIND, bool kStack, bool kSel0, bool kPhilox>
-__device__ __forceinline__ bool run_stage_l(const mgpu_stage& st, PhotonL& ph, int64_t i,
+__device__ __forceinline__ bool run_stage_l(const mgpu_stage& st, PhotonL& ph, int i,
                                             bool valid, const mgpu_chain& chain, int s) {
     // fixed chains run Philox only: the pre-drawn branches fold away
     const int rng = kPhilox ? MGPU_RNG_PHILOX : chain.rng;
+    // the plain fixed chains run the common configuration only
+    constexpr bool kLean = kSel0 && !kStack;
     const int kind = KIND ? KIND : st.kind;
     switch (kind) {
     case MGPU_STAGE_GRATINGS:
-        return stage_gratings_l<kStack, kSel0>(st, ph, i, valid, rng, chain.seed, chain.row_base,
+        return stage_gratings_l<kStack, kSel0, kLean>(st, ph, i, valid, rng, chain.seed, chain.row_base,
                                         s, chain.status);
     case MGPU_STAGE_DETARRAY:
         return stage_detarray_l(st, ph, i, valid);
     case MGPU_STAGE_LENS:
-        return valid && stage_lens_l(st, ph, i, chain.status);
+        return valid && stage_lens_l<kLean>(st, ph, i, chain.status);
     case MGPU_STAGE_SCATTER:
         return valid && stage_scatter_l(st, ph, i, rng, chain.seed, chain.row_base, s,
                                         chain.status);
@@ -996,8 +1099,8 @@ __device__ __forceinline__ bool run_stage_l(const mgpu_stage& st, PhotonL& ph, i
             bool absorb = true;
             if (st.id_out)
                 absorb = (((st.first_writer >> 17) & 1)
-                              ? ((const int64_t*)st.id_out)[i * st.id_stride]
-                              : (int64_t)((const int32_t*)st.id_out)[i * st.id_stride]) < 0;
+                              ? *at((const int64_t*)st.id_out, i, st.id_stride)
+                              : (int64_t)*at((const int32_t*)st.id_out, i, st.id_stride)) < 0;
             if (absorb) ph.prob = 0.0f;
         }
         return false;
@@ -1007,9 +1110,15 @@ __device__ __forceinline__ bool run_stage_l(const mgpu_stage& st, PhotonL& ph, i
     }
 }
 
-__device__ __forceinline__ void count_hits(bool hit, unsigned* s_hits, int s, int lane) {
-    unsigned m = __ballot_sync(MGPU_FULL_MASK, hit);
-    if (lane == 0 && m) atomicAdd(&s_hits[s], (unsigned)__popc(m));
+// per-warp hit counts of a photon's stages (bit s of mask: stage s hit),
+// added once at the end of the chain: one short loop instead of a vote and
+// an atomic between every two stages (4 KB less code in the CAT chain)
+__device__ __forceinline__ void count_hits(uint32_t mask, unsigned* s_hits, int n_stages, int lane) {
+#pragma unroll 1
+    for (int s = 0; s < n_stages; ++s) {
+        const unsigned m = __ballot_sync(MGPU_FULL_MASK, (mask >> s) & 1u);
+        if (lane == 0 && m) atomicAdd(&s_hits[s], (unsigned)__popc(m));
+    }
 }
 
 // generic chain: stage loop over the descriptors
@@ -1017,11 +1126,12 @@ struct GenericChain {
     static constexpr bool kFixed = false;
     static constexpr int kSearches = 2;
     template <bool kStack>
-    __device__ static void run(const mgpu_chain& chain, PhotonL& ph, int64_t i, bool valid,
-                               unsigned* s_hits, int lane) {
+    __device__ static uint32_t run(const mgpu_chain& chain, PhotonL& ph, int i, bool valid) {
+        uint32_t mask = 0;
         for (int s = 0; s < chain.n_stages; ++s)
-            count_hits(run_stage_l<0, kStack, false, false>(chain.stages[s], ph, i, valid, chain, s), s_hits, s,
-                       lane);
+            mask |= (uint32_t)run_stage_l<0, kStack, false, false>(chain.stages[s], ph, i, valid, chain, s)
+                    << s;
+        return mask;
     }
 };
 
@@ -1034,21 +1144,35 @@ struct FixedChain {
     static constexpr int kSearches =
         (0 + ... + (K == MGPU_STAGE_GRATINGS || K == MGPU_STAGE_DETARRAY ? 1 : 0));
     template <int KIND, int S, bool kStack>
-    __device__ static void step(const mgpu_chain& chain, PhotonL& ph, int64_t i, bool valid,
-                                unsigned* s_hits, int lane) {
-        count_hits(run_stage_l<KIND, kStack, true, true>(chain.stages[S], ph, i, valid, chain, S), s_hits, S,
-                   lane);
+    __device__ static uint32_t step(const mgpu_chain& chain, PhotonL& ph, int i, bool valid) {
+        return (uint32_t)run_stage_l<KIND, kStack, true, true>(chain.stages[S], ph, i, valid, chain, S)
+               << S;
     }
     template <bool kStack, int... S>
-    __device__ static void run_seq(const mgpu_chain& chain, PhotonL& ph, int64_t i, bool valid,
-                                   unsigned* s_hits, int lane, std::integer_sequence<int, S...>) {
-        (step<K, S, kStack>(chain, ph, i, valid, s_hits, lane), ...);
+    __device__ static uint32_t run_seq(const mgpu_chain& chain, PhotonL& ph, int i, bool valid,
+                                       std::integer_sequence<int, S...>) {
+        uint32_t mask = 0;
+        ((mask |= step<K, S, kStack>(chain, ph, i, valid)), ...);
+        return mask;
     }
+    // the facet stage (at most one) whose selector's energy row is found
+    // at the start, so its table loads overlap the stages before it
+    static constexpr int kGratings = []() {
+        const int kinds[] = {K...};
+        for (int s = 0; s < (int)sizeof...(K); ++s)
+            if (kinds[s] == MGPU_STAGE_GRATINGS) return s;
+        return -1;
+    }();
+    static_assert((0 + ... + (K == MGPU_STAGE_GRATINGS ? 1 : 0)) <= 1,
+                  "fixed chains hold at most one grating array");
     template <bool kStack>
-    __device__ static void run(const mgpu_chain& chain, PhotonL& ph, int64_t i, bool valid,
-                               unsigned* s_hits, int lane) {
-        run_seq<kStack>(chain, ph, i, valid, s_hits, lane,
-                        std::make_integer_sequence<int, sizeof...(K)>{});
+    __device__ static uint32_t run(const mgpu_chain& chain, PhotonL& ph, int i, bool valid) {
+        if constexpr (kGratings >= 0) {
+            const mgpu_selector& sel = chain.stages[kGratings].sel0;
+            if (!kStack) ph.row0 = energy_row<true>(sel, ph.energy_d, ph.energy.hi);
+            else if (sel.kind != MGPU_SEL_SPLINE) ph.row0 = energy_row(sel, ph.energy_d, ph.energy.hi);
+        }
+        return run_seq<kStack>(chain, ph, i, valid, std::make_integer_sequence<int, sizeof...(K)>{});
     }
     // the stage kinds match, every facet stage reads its first selector, and
     // the draws come from Philox (the pre-drawn code is compiled out)
@@ -1063,14 +1187,34 @@ struct FixedChain {
     }
 };
 
+// the configuration the plain fixed chains are compiled for (kLean): lenses
+// without a reflectivity table; grating arrays whose facets all use one
+// efficiency table with increasing energy rows, row midpoints and a guide
+// table, with no column evaluated on the host
+bool lean_ok(const mgpu_chain& chain) {
+    for (int s = 0; s < chain.n_stages; ++s) {
+        const mgpu_stage& st = chain.stages[s];
+        if (st.kind == MGPU_STAGE_LENS && st.spline.n_surf > 0) return false;
+        if (st.kind == MGPU_STAGE_GRATINGS) {
+            const mgpu_selector& q = st.sel0;
+            if (!st.facet_sel0 || st.stack || st.grating_d.ptr || st.blaze_add.ptr ||
+                q.kind != MGPU_SEL_CDF || !q.by_energy || !q.sorted || !q.guide || !q.e_mid ||
+                q.n_rows < 1)
+                return false;
+        }
+    }
+    return true;
+}
+
 template <class Chain, bool kStack>
 // fixed plain chains with one facet search: 4 blocks of 256 per SM (64
-// registers, no spills; the
-// stage constants come from the parameter bank), measured 6 % faster than
-// 3 blocks (80 registers) on the CAT chain at 1e8 photons; the others keep
-// 3 blocks (at 64 registers they spill), which measured 4 % faster than
-// the unconstrained allocation (100 registers, 2 blocks); 128-thread
-// blocks and a capped (persistent) grid measured no faster
+// registers, no spills; the stage constants come from the parameter bank),
+// measured 6 % faster than 3 blocks (80 registers) on the CAT chain at 1e8
+// photons; 5 blocks (48 registers) spill and measured 4 % slower, 128-thread
+// blocks at 56 registers (36 warps, small spills) 5 % slower.  The others
+// keep 3 blocks (at 64 registers they spill), which measured 4 % faster
+// than the unconstrained allocation (100 registers, 2 blocks); a capped
+// (persistent) grid measured no faster.  One photon per thread.
 __global__ void __launch_bounds__(kThreads, (Chain::kFixed && !kStack && Chain::kSearches <= 1)
                                                 ? kMinBlocks : kMinBlocksWide)
 chain_fp32local_kernel(const __grid_constant__ mgpu_chain chain, const __grid_constant__ mgpu_photons io) {
@@ -1078,48 +1222,49 @@ chain_fp32local_kernel(const __grid_constant__ mgpu_chain chain, const __grid_co
     if (threadIdx.x < MGPU_MAX_STAGES) s_hits[threadIdx.x] = 0;
     __syncthreads();
     const int lane = threadIdx.x & 31;
-    const int64_t n = io.n;
-    const int64_t warp_id = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t base = warp_id * 32; base < n; base += n_warps * 32) {
-        const int64_t i = base + lane;
+    const int n = (int)io.n;                      // < 2^30 per launch
+    const int warp_id = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int n_warps = (int)((gridDim.x * blockDim.x) >> 5);
+    for (int base = warp_id * 32; base < n; base += n_warps * 32) {
+        const int i = base + lane;
         const bool valid = i < n;
         PhotonL ph;
         if (valid) {
-            // input conversions on the (otherwise idle) FP64 pipe: measured
-            // 4 % faster than the integer-pipe routines used for the outputs
-            d3 p = load3(io.pos, i), d = load3(io.dir, i), q = load3(io.pol, i);
+            d3 p = load3i(io.pos, i), d = load3i(io.dir, i), q = load3i(io.pol, i);
             // positions on the integer pipe, the rest on the FP64 pipe's
             // conversions: measured 1.2 % faster than all of them on either
             ph.pos = ff3{d2ff_bits(p.x), d2ff_bits(p.y), d2ff_bits(p.z)};
             ph.dir = f3{__double2float_rn(d.x), __double2float_rn(d.y), __double2float_rn(d.z)};
             ph.pol = f3{__double2float_rn(q.x), __double2float_rn(q.y), __double2float_rn(q.z)};
-            ph.energy_d = io.energy.ptr[i * io.energy.stride];
+            ph.energy_d = *at(io.energy.ptr, i, io.energy.stride);
             ph.energy = d2ff_hw(ph.energy_d);
-            ph.prob = __double2float_rn(io.prob.ptr[i * io.prob.stride]);
+            ph.prob = __double2float_rn(*at(io.prob.ptr, i, io.prob.stride));
+            ph.row0 = -1;
         } else {
             ph.pos = ff3{ff{0.f, 0.f}, ff{0.f, 0.f}, ff{0.f, 0.f}};
             ph.dir = ph.pol = f3{0.f, 0.f, 0.f};
             ph.energy = ff{1.f, 0.f};
             ph.energy_d = 1.0;
             ph.prob = 0.f;
+            ph.row0 = -1;
         }
         if (valid && (chain.flags & MGPU_FLAG_CHECK_W)) {
-            if (io.pos.ptr[i * io.pos.stride + 3 * io.pos.cstride] != 1.0 ||
-                io.dir.ptr[i * io.dir.stride + 3 * io.dir.cstride] != 0.0 ||
-                io.pol.ptr[i * io.pol.stride + 3 * io.pol.cstride] != 0.0)
+            if (*at(io.pos.ptr + 3 * io.pos.cstride, i, io.pos.stride) != 1.0 ||
+                *at(io.dir.ptr + 3 * io.dir.cstride, i, io.dir.stride) != 0.0 ||
+                *at(io.pol.ptr + 3 * io.pol.cstride, i, io.pol.stride) != 0.0)
                 atomicOr(chain.status, MGPU_STATUS_BAD_W);
         }
-        Chain::template run<kStack>(chain, ph, i, valid, s_hits, lane);
+        const uint32_t hits = Chain::template run<kStack>(chain, ph, i, valid);
         if (valid) {
-            store3(io.pos_out, i, d3{ff2d(ph.pos.x), ff2d(ph.pos.y), ff2d(ph.pos.z)});
+            store3i(io.pos_out, i, d3{ff2d(ph.pos.x), ff2d(ph.pos.y), ff2d(ph.pos.z)});
             // state outputs on the FP64 pipe's conversions, stage columns on
             // the integer pipe: the split measured fastest (0.6 % against
             // all on the integer pipe, which the columns keep)
-            store3(io.dir_out, i, d3{(double)ph.dir.x, (double)ph.dir.y, (double)ph.dir.z});
-            store3(io.pol_out, i, d3{(double)ph.pol.x, (double)ph.pol.y, (double)ph.pol.z});
-            io.prob_out.ptr[i * io.prob_out.stride] = (double)ph.prob;
+            store3i(io.dir_out, i, d3{(double)ph.dir.x, (double)ph.dir.y, (double)ph.dir.z});
+            store3i(io.pol_out, i, d3{(double)ph.pol.x, (double)ph.pol.y, (double)ph.pol.z});
+            *at(io.prob_out.ptr, i, io.prob_out.stride) = (double)ph.prob;
         }
+        count_hits(hits, s_hits, chain.n_stages, lane);
     }
     __syncthreads();
     if (threadIdx.x < chain.n_stages && s_hits[threadIdx.x])
@@ -1140,36 +1285,61 @@ using ChainCatBars = FixedChain<MGPU_STAGE_LENS, MGPU_STAGE_SCATTER, MGPU_STAGE_
 
 }  // namespace
 
-cudaError_t mgpu_launch_chain_fp32local(const mgpu_chain& chain, const mgpu_photons& io,
-                                        cudaStream_t stream, int sm_count) {
-    if (io.n <= 0) return cudaSuccess;
-    for (int s = 0; s < chain.n_stages; ++s) {
-        const mgpu_stage& st = chain.stages[s];
-        if (st.aux_size <= 0 && st.kind != MGPU_STAGE_SUPPORT) return cudaErrorInvalidValue;
-        if ((st.kind == MGPU_STAGE_GRATINGS || st.kind == MGPU_STAGE_DETARRAY) &&
-            (st.facets32 == nullptr || ((uintptr_t)st.facets32 & 15u) != 0))
-            return cudaErrorInvalidValue;
-        if (st.kind == MGPU_STAGE_CYLDET && (st.table == nullptr || ((uintptr_t)st.table & 15u) != 0))
-            return cudaErrorInvalidValue;
-        if (st.kind == MGPU_STAGE_LENS && st.spline.n_surf > 0 &&
-            (st.spline.tx_ff == nullptr || st.spline.ty_ff == nullptr || st.spline.c32 == nullptr))
-            return cudaErrorInvalidValue;
+namespace {
+
+// the kernel addresses photon i of a column with a 32-bit byte offset
+// (i * stride * 8), so launches cover at most 2^30 photons and strides stay
+// below 2^28 elements
+constexpr int64_t kMaxLaunch = 1ll << 30;
+bool stride_ok(int64_t s) { return s > -(1ll << 28) && s < (1ll << 28); }
+bool col_ok(const mgpu_col& c) { return c.ptr == nullptr || stride_ok(c.stride); }
+bool vec_ok(const mgpu_vec& v) { return stride_ok(v.stride); }
+
+template <class T>
+T* advanced(T* p, int64_t off, int64_t stride, int64_t size) {
+    return p ? (T*)((char*)p + off * stride * size) : p;
+}
+
+// the descriptors of photon rows [off, ...): every column pointer moved
+// to row off, the Philox row counter with them
+void advance_rows(mgpu_chain& c, mgpu_photons& io, int64_t off) {
+    for (mgpu_vec* v : {&io.pos, &io.dir, &io.pol, &io.pos_out, &io.dir_out, &io.pol_out})
+        v->ptr = advanced(v->ptr, off, v->stride, 8);
+    for (mgpu_col* k : {&io.energy, &io.prob, &io.prob_out}) k->ptr = advanced(k->ptr, off, k->stride, 8);
+    c.row_base += (uint64_t)off;
+    for (int s = 0; s < c.n_stages; ++s) {
+        mgpu_stage& st = c.stages[s];
+        for (int k = 0; k < MGPU_MAX_OUT; ++k) st.out[k].ptr = advanced(st.out[k].ptr, off, st.out[k].stride, 8);
+        st.id_out = advanced((char*)st.id_out, off, st.id_stride, ((st.first_writer >> 17) & 1) ? 8 : 4);
+        for (int k = 0; k < MGPU_MAX_DRAWS; ++k) st.draw[k] = advanced(st.draw[k], off, st.draw_stride, 8);
+        st.grating_d.ptr = advanced(st.grating_d.ptr, off, st.grating_d.stride, 8);
+        st.blaze_add.ptr = advanced(st.blaze_add.ptr, off, st.blaze_add.stride, 8);
     }
+}
+
+cudaError_t launch_rows(const mgpu_chain& chain, const mgpu_photons& io, cudaStream_t stream,
+                        int sm_count) {
     int64_t warps = (io.n + 31) / 32;
     int64_t blocks = (warps * 32 + kThreads - 1) / kThreads;
     if (kGridPerSm > 0) {
         const int64_t cap = (int64_t)sm_count * kGridPerSm * 256 / kThreads;
         if (blocks > cap) blocks = cap;
     }
-    if (blocks > (1 << 30)) blocks = 1 << 30;   // grid-stride beyond
     bool stacked = false;
     for (int s = 0; s < chain.n_stages; ++s) stacked = stacked || chain.stages[s].stack != nullptr;
     const unsigned gb = (unsigned)blocks;
-    if (stacked) {
+    if (chain.flags & MGPU_FLAG_GENERIC) {
+        if (stacked)
+            chain_fp32local_kernel<GenericChain, true><<<gb, kThreads, 0, stream>>>(chain, io);
+        else
+            chain_fp32local_kernel<GenericChain, false><<<gb, kThreads, 0, stream>>>(chain, io);
+    } else if (stacked) {
         if (ChainCatBars::matches(chain))
             chain_fp32local_kernel<ChainCatBars, true><<<gb, kThreads, 0, stream>>>(chain, io);
         else
             chain_fp32local_kernel<GenericChain, true><<<gb, kThreads, 0, stream>>>(chain, io);
+    } else if (!lean_ok(chain)) {
+        chain_fp32local_kernel<GenericChain, false><<<gb, kThreads, 0, stream>>>(chain, io);
     } else if (ChainCat::matches(chain)) {
         chain_fp32local_kernel<ChainCat, false><<<gb, kThreads, 0, stream>>>(chain, io);
     } else if (ChainSpec::matches(chain)) {
@@ -1184,4 +1354,42 @@ cudaError_t mgpu_launch_chain_fp32local(const mgpu_chain& chain, const mgpu_phot
         chain_fp32local_kernel<GenericChain, false><<<gb, kThreads, 0, stream>>>(chain, io);
     }
     return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t mgpu_launch_chain_fp32local(const mgpu_chain& chain, const mgpu_photons& io,
+                                        cudaStream_t stream, int sm_count) {
+    if (io.n <= 0) return cudaSuccess;
+    if (!vec_ok(io.pos) || !vec_ok(io.dir) || !vec_ok(io.pol) || !vec_ok(io.pos_out) ||
+        !vec_ok(io.dir_out) || !vec_ok(io.pol_out) || !col_ok(io.energy) || !col_ok(io.prob) ||
+        !col_ok(io.prob_out))
+        return cudaErrorInvalidValue;
+    for (int s = 0; s < chain.n_stages; ++s) {
+        const mgpu_stage& st = chain.stages[s];
+        if (st.aux_size <= 0 && st.kind != MGPU_STAGE_SUPPORT) return cudaErrorInvalidValue;
+        if ((st.kind == MGPU_STAGE_GRATINGS || st.kind == MGPU_STAGE_DETARRAY) &&
+            (st.facets32 == nullptr || ((uintptr_t)st.facets32 & 15u) != 0))
+            return cudaErrorInvalidValue;
+        if (st.kind == MGPU_STAGE_CYLDET && (st.table == nullptr || ((uintptr_t)st.table & 15u) != 0))
+            return cudaErrorInvalidValue;
+        if (st.kind == MGPU_STAGE_LENS && st.spline.n_surf > 0 &&
+            (st.spline.tx_ff == nullptr || st.spline.ty_ff == nullptr || st.spline.c32 == nullptr))
+            return cudaErrorInvalidValue;
+        for (int k = 0; k < MGPU_MAX_OUT; ++k)
+            if (!col_ok(st.out[k])) return cudaErrorInvalidValue;
+        if ((st.id_out && !stride_ok(st.id_stride)) || !stride_ok(st.draw_stride) ||
+            !col_ok(st.grating_d) || !col_ok(st.blaze_add))
+            return cudaErrorInvalidValue;
+    }
+    if (io.n <= kMaxLaunch) return launch_rows(chain, io, stream, sm_count);
+    for (int64_t off = 0; off < io.n; off += kMaxLaunch) {
+        mgpu_chain c = chain;
+        mgpu_photons part = io;
+        advance_rows(c, part, off);
+        part.n = (io.n - off < kMaxLaunch) ? io.n - off : kMaxLaunch;
+        const cudaError_t e = launch_rows(c, part, stream, sm_count);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }

@@ -96,6 +96,17 @@ MGPU_HD double f2d_bits(float f) {
     return mgpu_mkd(hi | sign, lo);
 }
 
+// float32 -> float64 for finite values, exact (denormal floats -> signed
+// zero); infinities and NaN are not handled (callers pass hit coordinates
+// and angles only)
+MGPU_HD double f2d_fin_bits(float f) {
+    uint32_t b = mgpu_f2u(f);
+    uint32_t mag = b & 0x7fffffffu;
+    uint32_t hi = (mag >> 3) + 0x38000000u, lo = b << 29;
+    if (mag < 0x00800000u) hi = lo = 0u;
+    return mgpu_mkd(hi | (b & 0x80000000u), lo);
+}
+
 // float64 -> (hi, lo) float32 pair: hi = d2f_bits(d), lo = d - hi rounded
 // to float32 (exact residual of the 53-bit mantissa, scaled).  Values below
 // 2^-74 or outside the float range get lo = 0.

@@ -78,11 +78,15 @@ __device__ __forceinline__ ff ff_mul(ff a, ff b) {
     p.lo = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, p.lo));
     return fast_two_sum(p.hi, p.lo);
 }
+// a / b: q1 = a.hi / b.hi, then the remainder a - q1 b formed with FMAs,
+// (a.hi - q1 b.hi) rounded once (|.| a few ulp of a.hi, so its rounding is
+// ~2^-47 |a|) plus (a.lo - q1 b.lo), and q2 = remainder / b.hi: ~2^-44
+// relative, in 8 operations instead of the 30 of a float-float subtraction
 __device__ __forceinline__ ff ff_div(ff a, ff b) {
-    float q1 = __fdividef(a.hi, b.hi);
-    ff r = ff_sub(a, ff_mul_f(b, q1));
-    float q2 = __fdividef(r.hi, b.hi);
-    return fast_two_sum(q1, q2);
+    const float rb = __fdividef(1.0f, b.hi);
+    const float q1 = a.hi * rb;
+    const float r = fmaf(-q1, b.hi, a.hi) + fmaf(-q1, b.lo, a.lo);
+    return fast_two_sum(q1, r * rb);
 }
 __device__ __forceinline__ float ff_f(ff a) { return a.hi + a.lo; }
 

@@ -352,6 +352,9 @@ class GpuSequence:
         self._watch = None
         self.last_hits = None
         self.last_status = 0
+        # False: FP32-local chains run the generic stage loop instead of the
+        # kernel specialised for their stage sequence (same results)
+        self.specialised = True
 
     # ------------------------------------------------------------ lowering
     def lower(self, stream=None):
@@ -380,6 +383,7 @@ class GpuSequence:
         chain.seed = self.seed
         chain.status = status.data_ptr()
         chain.hits = hits.data_ptr()
+        chain.flags = 0 if self.specialised else _abi.FLAG_GENERIC
         for si, st in enumerate(inst.stages):
             s = chain.stages[si]
             inst.fill_stage(si, s)
@@ -698,7 +702,7 @@ class GpuSequence:
                              for si, ts in draws_dev.items()}
                 chain = self._chain(inst, plan, sub_bufs, sub_draws, b - a, status, hits,
                                     row_base + a)
-                chain.flags = _abi.FLAG_CHECK_W
+                chain.flags |= _abi.FLAG_CHECK_W
                 ph = _abi.MgpuPhotons()
                 ph.n = b - a
                 ph.pos = ph.pos_out = _abi.vec_aos(dstate['pos'][a:b])

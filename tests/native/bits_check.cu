@@ -63,12 +63,16 @@ int main() {
         uint32_t u = (uint32_t)rng();
         float f; memcpy(&f, &u, 4);
         if (!(std::fabs(f) >= 1.17549435e-38f) || std::isinf(f) || std::isnan(f)) continue;
-        if (dbits((double)f) != dbits(f2d_bits(f))) {
+        if (dbits((double)f) != dbits(f2d_bits(f)) || dbits((double)f) != dbits(f2d_fin_bits(f))) {
             if (fail_f2d < 5) printf("f2d %.9g\n", f);
             ++fail_f2d;
         }
     }
     if (f2d_bits(0.0f) != 0.0 || !std::isinf(f2d_bits(INFINITY)) || !std::isnan(f2d_bits(NAN)))
+        ++fail_f2d;
+    // the finite-only conversion: signed zeros and denormals -> signed zero
+    if (dbits(f2d_fin_bits(0.0f)) != dbits(0.0) || dbits(f2d_fin_bits(-0.0f)) != dbits(-0.0) ||
+        dbits(f2d_fin_bits(1e-40f)) != dbits(0.0) || dbits(f2d_fin_bits(-1e-40f)) != dbits(-0.0))
         ++fail_f2d;
     printf("checked %ld doubles: d2f failures %ld, ff failures %ld, f2d failures %ld\n", n,
            fail_d2f, fail_ff, fail_f2d);

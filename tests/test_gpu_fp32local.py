@@ -224,3 +224,27 @@ def test_fp32local_vs_fp64_ccd_strip():
     d = _pos_err(a, b, agree)
     assert np.sqrt(np.mean(d ** 2)) <= 0.5 * UM and d.max() <= 5 * UM
     check_columns(a, b, agree, inst)
+
+
+@pytest.mark.parametrize('name', ['c0', 'c1', 'c2', 'c6', 'c8'])
+def test_specialised_kernels_match_generic(name):
+    """The kernels specialised for a stage sequence (stage kinds and
+    constants fixed at compile time, the common lens and efficiency-table
+    configuration compiled in alone, the order's energy row found at the
+    start of the photon) give the same result bits as the generic stage
+    loop on the same chain (``GpuSequence.specialised = False``)."""
+    from marxs_gb300 import configs, PhotonTable
+    from marxs_gb300.gpu import GpuSequence
+    n = 100000
+    inst = configs.build(name)
+    host = configs.photons_for(name, n, seed=27)
+    outs = []
+    for specialised in (True, False):
+        seq = GpuSequence(elements=inst.elements, precision='fp32local', rng='philox', seed=99)
+        seq.specialised = specialised
+        outs.append(seq(PhotonTable({k: np.array(v, copy=True) for k, v in host.items()})))
+    a, b = outs
+    assert list(a.colnames) == list(b.colnames)
+    for col in a.colnames:
+        x, y = np.asarray(a[col]), np.asarray(b[col])
+        assert np.array_equal(x, y, equal_nan=x.dtype.kind == 'f'), col
