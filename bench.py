@@ -40,11 +40,11 @@ METRIC = 'photons/s at 1e8 (FP32-local vs FP64); adjoint grads/s vs finite-diff;
 UNIT = 'photons/s'
 WORKLOAD = 'cat_rowland_1000facets_circular_detector'
 
-# DRAM bytes (read + write) per photon of the chain kernel, from the ncu
-# captures of a 4e6-photon launch (profiles/chain_fp64_c2.md,
-# profiles/chain_fp32local_c2.md), scaled to the launch by photon count
+# DRAM bytes (read + write) per photon of each chain kernel, from one ncu
+# capture (dram__bytes_read.sum + dram__bytes_write.sum) of a 4e6-photon
+# launch, scaled to the launch by photon count
 NCU_TRAFFIC_BYTES_PER_PHOTON = {'fp64': (358.2e6 + 735.3e6) / 4e6,
-                                'fp32local': (354.4e6 + 725.4e6) / 4e6}
+                                'fp32local': (354.2e6 + 725.0e6) / 4e6}
 
 
 def parse():

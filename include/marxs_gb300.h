@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define MGPU_ABI_VERSION 2
+#define MGPU_ABI_VERSION 3
 #define MGPU_MAX_STAGES 16
 #define MGPU_MAX_OUT 10
 #define MGPU_MAX_DRAWS 6
@@ -48,6 +48,8 @@ extern "C" {
 
 /* mgpu_chain.flags */
 #define MGPU_FLAG_CHECK_W        0x1u  /* read the homogeneous w of pos/dir/pol and check it */
+#define MGPU_FLAG_NO_GRID        0x4u  /* every facet stage scans all its facets (no candidate
+                                          grid; for checking the grids' candidate lists) */
 #define MGPU_FLAG_GENERIC        0x2u  /* FP32-local: run the generic stage loop even where a
                                           kernel specialised for the chain applies (the same
                                           results; for checking the specialisations) */
@@ -195,6 +197,7 @@ typedef struct {
     float n[3], a[3], b[3];
     float u0, v0, inv_cell, slope_max;
     int32_t nu, nv;
+    float depth[6];        /* mgpu_grid.depth */
 } mgpu_grid32;
 
 /* FP32-local constants of a circular cylinder detector.  e1, e2, a are the
@@ -217,13 +220,20 @@ typedef struct {
     int32_t k0, nk;
 } mgpu_cyl32;
 
-/* uniform candidate grid in a plane (origin o, normal n, in-plane axes a,b) */
+/* uniform candidate grid in a plane (origin o, normal n, in-plane axes a,b).
+ * A ray crossing the plane at (u0, v0) with slopes su = d.a/d.n, sv = d.b/d.n
+ * is looked up at (u0 + su D, v0 + sv D), D = depth model at (u0, v0): where
+ * it meets the facets' surface, up to their deviation from the model (all
+ * depth coefficients zero: the plane itself) */
 typedef struct {
     double o[3], n[3], a[3], b[3];
     double u0, v0, cell;   /* grid origin (u,v) and cell size, mm */
     int32_t nu, nv;
     double slope_max;      /* |d.a/d.n|, |d.b/d.n| bound for grid lookup */
     double margin;         /* extra footprint margin, mm */
+    double depth[6];       /* depth of the facet surface along n over the plane:
+                              D(u,v) = d0 + d1 u + d2 v + d3 u^2 + d4 u v + d5 v^2 */
+    double depth_lip;      /* bound on |dD/du| + |dD/dv| over the grid's area */
     int32_t* cell_start;   /* nu*nv+1, device */
     int32_t* cell_items;   /* capacity entries, device */
     int32_t capacity;

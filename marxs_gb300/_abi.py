@@ -13,7 +13,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, 'libmarxs_gb300.so')
 
-MGPU_ABI_VERSION = 2
+MGPU_ABI_VERSION = 3
 MAX_STAGES = 16
 MAX_OUT = 10
 FACET_CYL = 34
@@ -28,6 +28,7 @@ STATUS_BAD_W = 0x20
 STATUS_TABLE_RANGE = 0x80
 FLAG_CHECK_W = 0x1
 FLAG_GENERIC = 0x2
+FLAG_NO_GRID = 0x4
 
 NOALLOC_MAX_CELLS = 65536
 ERR_NOALLOC_LIMIT = -2
@@ -99,7 +100,7 @@ class MgpuGrid32(C.Structure):
     _fields_ = [('o_hi', C.c_float * 3), ('o_lo', C.c_float * 3), ('n', C.c_float * 3),
                 ('a', C.c_float * 3), ('b', C.c_float * 3), ('u0', C.c_float),
                 ('v0', C.c_float), ('inv_cell', C.c_float), ('slope_max', C.c_float),
-                ('nu', C.c_int32), ('nv', C.c_int32)]
+                ('nu', C.c_int32), ('nv', C.c_int32), ('depth', C.c_float * 6)]
 
 
 class MgpuCyl32(C.Structure):
@@ -116,6 +117,7 @@ class MgpuGrid(C.Structure):
                 ('b', C.c_double * 3), ('u0', C.c_double), ('v0', C.c_double),
                 ('cell', C.c_double), ('nu', C.c_int32), ('nv', C.c_int32),
                 ('slope_max', C.c_double), ('margin', C.c_double),
+                ('depth', C.c_double * 6), ('depth_lip', C.c_double),
                 ('cell_start', C.c_void_p), ('cell_items', C.c_void_p),
                 ('capacity', C.c_int32), ('pad', C.c_int32)]
 

@@ -96,11 +96,19 @@ int mgpu_trace(const mgpu_chain* chain, const mgpu_photons* photons, void* strea
         return (int)cudaErrorInvalidValue;
     if (photons->n < 0) return (int)cudaErrorInvalidValue;
     cudaStream_t s = (cudaStream_t)stream;
+    const mgpu_chain* c = chain;
+    mgpu_chain scan;
+    if (chain->flags & MGPU_FLAG_NO_GRID) {
+        // no candidate grids: every facet stage scans all its facets
+        scan = *chain;
+        for (int k = 0; k < scan.n_stages; ++k) scan.stages[k].grid.cell_start = nullptr;
+        c = &scan;
+    }
     cudaError_t e;
-    if (chain->precision == MGPU_FP32LOCAL)
-        e = mgpu_launch_chain_fp32local(*chain, *photons, s, sm_count_cached());
+    if (c->precision == MGPU_FP32LOCAL)
+        e = mgpu_launch_chain_fp32local(*c, *photons, s, sm_count_cached());
     else
-        e = mgpu_launch_chain_fp64(*chain, *photons, s, sm_count_cached());
+        e = mgpu_launch_chain_fp64(*c, *photons, s, sm_count_cached());
     return (int)e;
 }
 

@@ -761,9 +761,15 @@ __device__ __forceinline__ void grid_cell_range(const mgpu_stage& st, const Phot
         *brute = true;
         return;
     }
-    float t0 = -dotf(rel, n) / dn;
+    const float rdn = 1.0f / dn;
+    const float t0 = -dotf(rel, n) * rdn;
     float u = dotf(rel, a) + t0 * da;
     float v = dotf(rel, b) + t0 * db;
+    // looked up where the ray meets the depth model of the facet surface
+    const float* dq = G->depth;
+    const float D = dq[0] + u * (dq[1] + dq[3] * u + dq[4] * v) + v * (dq[2] + dq[5] * v);
+    u = fmaf(da * rdn, D, u);
+    v = fmaf(db * rdn, D, v);
     float fu = floorf((u - G->u0) * G->inv_cell);
     float fv = floorf((v - G->v0) * G->inv_cell);
     if (MGPU_UNLIKELY(!(fu >= 0.0f && fu < (float)G->nu && fv >= 0.0f && fv < (float)G->nv))) return;

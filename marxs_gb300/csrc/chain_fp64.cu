@@ -238,6 +238,11 @@ __device__ __forceinline__ int nearest_facet_grid(const mgpu_stage& st, const Ph
     double t0 = -dot3(rel, arr3(g.n)) / dn;
     double u = dot3(rel, arr3(g.a)) + t0 * da;
     double v = dot3(rel, arr3(g.b)) + t0 * db;
+    // looked up where the ray meets the depth model of the facet surface
+    const double* dq = g.depth;
+    const double D = dq[0] + u * (dq[1] + dq[3] * u + dq[4] * v) + v * (dq[2] + dq[5] * v);
+    u += (da / dn) * D;
+    v += (db / dn) * D;
     double fu = floor((u - g.u0) / g.cell);
     double fv = floor((v - g.v0) / g.cell);
     if (!(fu >= 0.0 && fu < (double)g.nu && fv >= 0.0 && fv < (double)g.nv)) return -1;

@@ -3,13 +3,20 @@
 // MARXS has no acceleration structure: Parallel.__call__ intersects every
 // facet with every photon (simulator.py:42-49).  Here each facet's
 // rectangle is projected onto the array's mean plane (origin o, normal n,
-// axes a, b).  A ray that hits the facet at depth delta = (P - o).n crosses
-// the mean plane within |delta| * slope_max of the hit point (u, v), as
-// long as its slopes |d.a / d.n|, |d.b / d.n| stay below slope_max; the
-// kernels send steeper rays to an all-facet scan.  So registering the facet
-// in every cell its footprint box, grown by max|delta| * slope_max + margin,
-// overlaps gives each cell a superset of the facets a ray through that cell
-// can hit.  Lists are built as counts -> exclusive scan -> fill (CSR).
+// axes a, b).  A ray with slopes su = d.a / d.n, sv = d.b / d.n below
+// slope_max crosses the plane at (u0, v0) and is looked up at
+// (u1, v1) = (u0, v0) + (su, sv) D(u0, v0), D the depth model of the facet
+// surface (a quadric in (u, v), or zero: the plane itself); steeper rays go
+// to an all-facet scan.  A ray that hits a facet at X (coordinates uX, vX,
+// depth hX) has u1 - uX = -su (hX - D(u0, v0)), and
+//   |hX - D(u0, v0)| <= |hX - D(uX, vX)| + L slope_max |hX|
+// with L >= |dD/du| + |dD/dv| over the grid (the drift (u0 - uX, v0 - vX)
+// is at most slope_max |hX| per axis).  So registering the facet in every
+// cell its footprint box, grown by
+//   slope_max (max |h - D| over the facet + L slope_max max |h|) + margin,
+// overlaps gives each cell a superset of the facets a ray looked up there
+// can hit.  (With D = 0 the growth is max|h| slope_max + margin.)  Lists
+// are built as counts -> exclusive scan -> fill (CSR).
 #include <atomic>
 #include <cuda_runtime.h>
 #include "mgpu_device.cuh"
@@ -20,6 +27,44 @@ struct CellRange {
     int iu0, iu1, iv0, iv1;
     bool inside;
 };
+
+__device__ __forceinline__ double depth_at(const mgpu_grid& g, double u, double v) {
+    const double* d = g.depth;
+    return d[0] + u * (d[1] + d[3] * u + d[4] * v) + v * (d[2] + d[5] * v);
+}
+
+// max over the facet rectangle of |depth - D(u, v)|: a quadratic in the
+// rectangle's coordinates (s, t) in [-1, 1]^2, largest in magnitude at a
+// corner, at an edge's stationary point or at the interior one
+__device__ double facet_depth_deviation(d3 c, d3 ey, d3 ez, double hy, double hz,
+                                        const mgpu_grid& g) {
+    const d3 o = arr3(g.o), n = arr3(g.n), a = arr3(g.a), b = arr3(g.b);
+    auto q = [&](double s, double t) {
+        const d3 p = c + (s * hy) * ey + (t * hz) * ez - o;
+        return dot3(p, n) - depth_at(g, dot3(p, a), dot3(p, b));
+    };
+    const double q0 = q(0.0, 0.0), qp0 = q(1.0, 0.0), qm0 = q(-1.0, 0.0);
+    const double q0p = q(0.0, 1.0), q0m = q(0.0, -1.0);
+    const double qs = 0.5 * (qp0 - qm0), qt = 0.5 * (q0p - q0m);
+    const double qss = 0.5 * (qp0 + qm0) - q0, qtt = 0.5 * (q0p + q0m) - q0;
+    const double qst = 0.25 * (q(1.0, 1.0) - q(1.0, -1.0) - q(-1.0, 1.0) + q(-1.0, -1.0));
+    auto Q = [&](double s, double t) {
+        return fabs(q0 + qs * s + qt * t + qss * s * s + qst * s * t + qtt * t * t);
+    };
+    double best = 0.0;
+    for (int k = 0; k < 4; ++k) best = fmax(best, Q((k & 1) ? 1.0 : -1.0, (k & 2) ? 1.0 : -1.0));
+    for (int k = 0; k < 2; ++k) {
+        const double e = k ? 1.0 : -1.0;
+        const double ts = -(qt + e * qst) / (2.0 * qtt);       // edge s = e
+        if (isfinite(ts) && fabs(ts) < 1.0) best = fmax(best, Q(e, ts));
+        const double ss = -(qs + e * qst) / (2.0 * qss);       // edge t = e
+        if (isfinite(ss) && fabs(ss) < 1.0) best = fmax(best, Q(ss, e));
+    }
+    const double det = 4.0 * qss * qtt - qst * qst;
+    const double si = (-2.0 * qtt * qs + qst * qt) / det, ti = (-2.0 * qss * qt + qst * qs) / det;
+    if (isfinite(si) && isfinite(ti) && fabs(si) < 1.0 && fabs(ti) < 1.0) best = fmax(best, Q(si, ti));
+    return best;
+}
 
 __device__ CellRange facet_cells(const mgpu_facet& f, const mgpu_grid& g) {
     d3 c = arr3(f.c), ey = arr3(f.ey), ez = arr3(f.ez);
@@ -36,7 +81,8 @@ __device__ CellRange facet_cells(const mgpu_facet& f, const mgpu_grid& g) {
         vmax = fmax(vmax, v);
         dmax = fmax(dmax, dep);
     }
-    double grow = dmax * g.slope_max + g.margin;
+    const double dev = facet_depth_deviation(c, ey, ez, f.hy, f.hz, g);
+    double grow = g.slope_max * (dev + g.depth_lip * g.slope_max * dmax) + g.margin;
     double fu0 = floor((umin - grow - g.u0) / g.cell), fu1 = floor((umax + grow - g.u0) / g.cell);
     double fv0 = floor((vmin - grow - g.v0) / g.cell), fv1 = floor((vmax + grow - g.v0) / g.cell);
     CellRange r;

@@ -246,6 +246,8 @@ class _Instrument:
         grid.u0, grid.v0, grid.cell = g['u0'], g['v0'], g['cell']
         grid.nu, grid.nv = g['nu'], g['nv']
         grid.slope_max, grid.margin = g['slope_max'], g['margin']
+        grid.depth[:] = [float(x) for x in g.get('depth', np.zeros(6))]
+        grid.depth_lip = float(g.get('depth_lip', 0.0))
         grid.cell_start, grid.cell_items = start.data_ptr(), items.data_ptr()
         grid.capacity = g['capacity']
         self.stage_grid[si] = grid
@@ -355,6 +357,9 @@ class GpuSequence:
         # False: FP32-local chains run the generic stage loop instead of the
         # kernel specialised for their stage sequence (same results)
         self.specialised = True
+        # False: facet stages scan all their facets instead of the candidate
+        # grid's lists (same results)
+        self.use_grid = True
 
     # ------------------------------------------------------------ lowering
     def lower(self, stream=None):
@@ -383,7 +388,8 @@ class GpuSequence:
         chain.seed = self.seed
         chain.status = status.data_ptr()
         chain.hits = hits.data_ptr()
-        chain.flags = 0 if self.specialised else _abi.FLAG_GENERIC
+        chain.flags = ((0 if self.specialised else _abi.FLAG_GENERIC) |
+                       (0 if self.use_grid else _abi.FLAG_NO_GRID))
         for si, st in enumerate(inst.stages):
             s = chain.stages[si]
             inst.fill_stage(si, s)

@@ -168,7 +168,9 @@ def test_run_tolerances_matches_host_loop():
     inst = configs.build('c2')
     F = len(inst.gas.elements)
     seq = GpuSequence(elements=inst.elements, precision='fp64', rng='philox', seed=11)
-    poses = DeviceFacetPoses(seq, inst.gas)
+    # rz = 1e-3 about the global origin moves the array (~11 m out) by ~11
+    # mm, dy another 1 mm: beyond the default 10 mm of room
+    poses = DeviceFacetPoses(seq, inst.gas, max_shift=20.0)
     poses.set_perturbation(np.zeros((F, 6)))
     ap = CircleAperture(position=[12000., 0, 0], zoom=[1, 500, 500], r_inner=300.)
     src = DeviceSource(ap, energy=0.5)

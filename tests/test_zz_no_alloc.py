@@ -51,6 +51,8 @@ def _build(facets, g, noalloc):
     grid.u0, grid.v0, grid.cell = g['u0'], g['v0'], g['cell']
     grid.nu, grid.nv = g['nu'], g['nv']
     grid.slope_max, grid.margin = g['slope_max'], g['margin']
+    grid.depth[:] = [float(x) for x in g['depth']]
+    grid.depth_lip = g['depth_lip']
     grid.cell_start, grid.cell_items = start.data_ptr(), items.data_ptr()
     grid.capacity = g['capacity']
     stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
