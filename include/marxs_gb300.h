@@ -50,6 +50,9 @@ extern "C" {
 #define MGPU_FLAG_CHECK_W        0x1u  /* read the homogeneous w of pos/dir/pol and check it */
 #define MGPU_FLAG_NO_GRID        0x4u  /* every facet stage scans all its facets (no candidate
                                           grid; for checking the grids' candidate lists) */
+#define MGPU_FLAG_SPLIT_4K       0x8u  /* FP32-local: split the launch every 4096 photons, as
+                                          launches beyond 2^30 photons are split (checks the
+                                          split: the same results) */
 #define MGPU_FLAG_GENERIC        0x2u  /* FP32-local: run the generic stage loop even where a
                                           kernel specialised for the chain applies (the same
                                           results; for checking the specialisations) */
@@ -511,7 +514,9 @@ typedef struct {
     int32_t n_facets;
     int32_t n_groups;
     int32_t det_kind;           /* MGPU_ADJ_DET_* */
-    int32_t reserved;
+    int32_t precision;          /* MGPU_FP64, or MGPU_FP32LOCAL for FORWARD / BACKWARD with a
+                                 * flat detector (FREEZE runs in float64 either way); FP32LOCAL
+                                 * needs rot of (n_facets + 3) * 192 bytes */
     const double* pos;          /* 3 x n (SoA), position before the lens */
     const double* dir;          /* 3 x n, direction before the lens */
     const double* alpha;        /* in-plane scatter angle (rad; 0 = no rotation) */
@@ -533,7 +538,8 @@ typedef struct {
     const double* ref;          /* device, n_groups x 2 moment centres */
     double* x_out;              /* optional, FORWARD: per-photon x */
     double* y_out;              /* optional, FORWARD: per-photon y */
-    double* rot;                /* device scratch, 36 (F + 1) doubles */
+    double* rot;                /* device scratch, 36 (F + 1) doubles (FP32LOCAL: at least
+                                 * 24 (F + 3)) */
     uint32_t* status;           /* device status word */
 } mgpu_adjoint_problem;
 

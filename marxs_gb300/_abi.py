@@ -29,6 +29,7 @@ STATUS_TABLE_RANGE = 0x80
 FLAG_CHECK_W = 0x1
 FLAG_GENERIC = 0x2
 FLAG_NO_GRID = 0x4
+FLAG_SPLIT_4K = 0x8
 
 NOALLOC_MAX_CELLS = 65536
 ERR_NOALLOC_LIMIT = -2
@@ -184,7 +185,7 @@ class MgpuSource(C.Structure):
 
 class MgpuAdjointProblem(C.Structure):
     _fields_ = [('n', C.c_int64), ('n_facets', C.c_int32), ('n_groups', C.c_int32),
-                ('det_kind', C.c_int32), ('reserved', C.c_int32),
+                ('det_kind', C.c_int32), ('precision', C.c_int32),
                 ('pos', C.c_void_p), ('dir', C.c_void_p), ('alpha', C.c_void_p),
                 ('beta', C.c_void_p), ('energy', C.c_void_p), ('weight', C.c_void_p),
                 ('facet', C.c_void_p), ('order', C.c_void_p), ('group', C.c_void_p),

@@ -1388,12 +1388,13 @@ cudaError_t mgpu_launch_chain_fp32local(const mgpu_chain& chain, const mgpu_phot
             !col_ok(st.grating_d) || !col_ok(st.blaze_add))
             return cudaErrorInvalidValue;
     }
-    if (io.n <= kMaxLaunch) return launch_rows(chain, io, stream, sm_count);
-    for (int64_t off = 0; off < io.n; off += kMaxLaunch) {
+    const int64_t max_launch = (chain.flags & MGPU_FLAG_SPLIT_4K) ? 4096 : kMaxLaunch;
+    if (io.n <= max_launch) return launch_rows(chain, io, stream, sm_count);
+    for (int64_t off = 0; off < io.n; off += max_launch) {
         mgpu_chain c = chain;
         mgpu_photons part = io;
         advance_rows(c, part, off);
-        part.n = (io.n - off < kMaxLaunch) ? io.n - off : kMaxLaunch;
+        part.n = (io.n - off < max_launch) ? io.n - off : max_launch;
         const cudaError_t e = launch_rows(c, part, stream, sm_count);
         if (e != cudaSuccess) return e;
     }

@@ -360,6 +360,9 @@ class GpuSequence:
         # False: facet stages scan all their facets instead of the candidate
         # grid's lists (same results)
         self.use_grid = True
+        # True: FP32-local launches are split every 4096 photons the way
+        # launches beyond 2^30 photons are (same results)
+        self.split_launches = False
 
     # ------------------------------------------------------------ lowering
     def lower(self, stream=None):
@@ -389,7 +392,8 @@ class GpuSequence:
         chain.status = status.data_ptr()
         chain.hits = hits.data_ptr()
         chain.flags = ((0 if self.specialised else _abi.FLAG_GENERIC) |
-                       (0 if self.use_grid else _abi.FLAG_NO_GRID))
+                       (0 if self.use_grid else _abi.FLAG_NO_GRID) |
+                       (_abi.FLAG_SPLIT_4K if self.split_launches else 0))
         for si, st in enumerate(inst.stages):
             s = chain.stages[si]
             inst.fill_stage(si, s)

@@ -66,7 +66,7 @@ def test_header_constants_match():
     assert int(consts['MGPU_ABI_VERSION']) == _abi.MGPU_ABI_VERSION
     assert int(consts['MGPU_MAX_STAGES']) == _abi.MAX_STAGES
     assert int(consts['MGPU_MAX_OUT']) == _abi.MAX_OUT
-    for name in ('CHECK_W', 'GENERIC', 'NO_GRID'):
+    for name in ('CHECK_W', 'GENERIC', 'NO_GRID', 'SPLIT_4K'):
         assert int(consts['MGPU_FLAG_' + name], 16) == getattr(_abi, 'FLAG_' + name), name
     for name in ('PROB_RANGE', 'ORDER_EMPTY', 'BAD_STAGE', 'GRID_RANGE', 'GRID_FULL'):
         assert int(consts['MGPU_STATUS_' + name].rstrip('u'), 16) == getattr(_abi, 'STATUS_' + name)

@@ -248,3 +248,37 @@ def test_specialised_kernels_match_generic(name):
     for col in a.colnames:
         x, y = np.asarray(a[col]), np.asarray(b[col])
         assert np.array_equal(x, y, equal_nan=x.dtype.kind == 'f'), col
+
+
+def test_split_launches_match_one_launch():
+    """Launches beyond 2^30 photons are split, every column pointer and the
+    Philox row moved to each part's first photon; splitting every 4096
+    photons (``GpuSequence.split_launches``) runs that path at a testable
+    size and must give the same result bits, through the table path
+    ((N, 4) host columns) and on device planes."""
+    from marxs_gb300 import configs, PhotonTable
+    from marxs_gb300.gpu import GpuSequence, DevicePhotons
+    n = 100003
+    inst = configs.build('c2')
+    host = configs.photons_for('c2', n, seed=37)
+    tables, planes = [], []
+    for split in (False, True):
+        seq = GpuSequence(elements=inst.elements, precision='fp32local', rng='philox', seed=5)
+        seq.split_launches = split
+        tables.append(seq(PhotonTable({k: np.array(v, copy=True) for k, v in host.items()}),
+                          row_base=1000))
+        hits_table = seq.last_hits
+        din, dout = DevicePhotons.from_columns(host), DevicePhotons(n)
+        plan, bufs = seq.allocate_columns(n)
+        seq.trace_device(din, dout, plan, bufs)
+        planes.append({'pos': dout.pos.cpu().numpy(), 'dir': dout.dir.cpu().numpy(),
+                       'pol': dout.pol.cpu().numpy(), 'prob': dout.prob.cpu().numpy(),
+                       **{k: v.cpu().numpy() for k, v in bufs.items()}, 'hits': hits_table})
+    a, b = tables
+    assert list(a.colnames) == list(b.colnames)
+    for col in a.colnames:
+        x, y = np.asarray(a[col]), np.asarray(b[col])
+        assert np.array_equal(x, y, equal_nan=x.dtype.kind == 'f'), col
+    for key in planes[0]:
+        x, y = planes[0][key], planes[1][key]
+        assert np.array_equal(x, y, equal_nan=x.dtype.kind == 'f'), key
