@@ -607,11 +607,45 @@ def adjoint_bench(args, torch):
     torch.cuda.synchronize()
     fd_ms = ev[0].elapsed_time(ev[1])
     g_np, fd_np = g.cpu().numpy(), fd.cpu().numpy()
-    blk = 0.0
-    for idx in model.param_slices().values():
-        sc = np.max(np.abs(fd_np[idx]))
-        if sc > 0:
-            blk = max(blk, float(np.max(np.abs(g_np[idx] - fd_np[idx])) / sc))
+
+    def blockwise(a):
+        worst = 0.0
+        for idx in model.param_slices().values():
+            sc = np.max(np.abs(fd_np[idx]))
+            if sc > 0:
+                worst = max(worst, float(np.max(np.abs(a[idx] - fd_np[idx])) / sc))
+        return worst
+    blk = blockwise(g_np)
+    # the same gradient with FP32-local moments and reverse sweep
+    fr.precision = 'fp32local'
+    for _ in range(5):
+        fr.loss_and_grad(theta, loss)
+    torch.cuda.synchronize()
+    ev[0].record(stream)
+    for _ in range(K):
+        _, g32 = fr.loss_and_grad(theta, loss)
+    ev[1].record(stream)
+    torch.cuda.synchronize()
+    grad32_ms = ev[0].elapsed_time(ev[1]) / K
+    gg32 = GraphedGradient(fr, loss)
+    for _ in range(5):
+        gg32(theta)
+    torch.cuda.synchronize()
+    ev[0].record(stream)
+    for _ in range(K):
+        gg32(theta)
+    ev[1].record(stream)
+    torch.cuda.synchronize()
+    graph32_ms = ev[0].elapsed_time(ev[1]) / K
+    fr.precision = 'fp64'
+    g32_np = g32.cpu().numpy()
+    fp32local = {'grad_ms': graph32_ms, 'grads_per_s': 1e3 / graph32_ms,
+                 'grad_eager_ms': grad32_ms, 'speedup_vs_fd': fd_ms / graph32_ms,
+                 'rel_err_vs_fd': float(np.linalg.norm(g32_np - fd_np) / np.linalg.norm(fd_np)),
+                 'blockwise_rel_err_vs_fd': blockwise(g32_np),
+                 'note': 'moments and reverse sweep in FP32-local precision (float-float '
+                         'positions re-centred on every element, float32 reverse sweep, '
+                         'float64 sums), against the same float64 central differences'}
     # one forward pass of the plain FP64 raytrace over the same photons, with
     # the orders and scatter angles fixed (pre-drawn): the forward a
     # raytrace-based finite difference repeats 2 x 1,207 times
@@ -642,7 +676,7 @@ def adjoint_bench(args, torch):
         'fd_raytrace_ms': fd_trace_ms, 'raytrace_fp64_ms_per_pass': trace_ms,
         'speedup_vs_fd_raytrace': fd_trace_ms / graph_ms,
         'rel_err_vs_fd': float(np.linalg.norm(g_np - fd_np) / np.linalg.norm(fd_np)),
-        'blockwise_rel_err_vs_fd': blk, 'loss': float(L),
+        'blockwise_rel_err_vs_fd': blk, 'loss': float(L), 'fp32local': fp32local,
         'grad_note': 'grad_ms: forward + torch loss + reverse captured in one CUDA graph '
                      '(GraphedGradient); grad_eager_ms: the same launched op by op',
         'fd_note': 'fd_ms: central differences on the frozen float64 forward kernel '

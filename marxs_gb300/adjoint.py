@@ -217,9 +217,11 @@ class PoseModel:
     # --------------------------------------------------------- frozen photons
     def trace(self, photons, orders, draws=None, precision='fp64', rng=None, seed=0,
               theta=None, energy_range=None, device=None, freeze=True, process_group=None,
-              row_base=0):
+              row_base=0, adjoint_precision='fp64'):
         """Trace ``photons`` (host columns or DevicePhotons) through the
-        elements as they are posed now and freeze the result.
+        elements as they are posed now and freeze the result.  ``precision``
+        is the raytrace's, ``adjoint_precision`` the frozen photons' moments
+        and gradients' (``FrozenPhotons.precision``).
 
         Returns (FrozenPhotons or None if not ``freeze``, trace) with trace =
         (sequence, input, output, column buffers) of the device run.  For
@@ -239,11 +241,11 @@ class PoseModel:
         if not freeze:
             return None, (seq, inp, out, bufs)
         frozen = self.freeze_trace(seq, inp, out, bufs, orders, energy_range, theta,
-                                   process_group)
+                                   process_group, adjoint_precision)
         return frozen, (seq, inp, out, bufs)
 
     def freeze_trace(self, seq, inp, out, bufs, orders, energy_range=None, theta=None,
-                     process_group=None):
+                     process_group=None, adjoint_precision='fp64'):
         """Frozen photons of a device trace ``seq.trace_device(inp, out, ...)``.
 
         Photons count when they met a facet and the detector; group g holds
@@ -280,16 +282,34 @@ class PoseModel:
             self, pos=inp.pos[:, sel], dir=inp.dir[:, sel], energy=inp.energy[sel],
             weight=out.prob[sel], alpha=alpha[sel], beta=beta[sel], facet=lut[fid],
             order=order[sel].to(torch.int32), group=group[sel].to(torch.int32),
-            n_groups=len(orders), theta=theta, rows=sel, process_group=process_group)
+            n_groups=len(orders), theta=theta, rows=sel, process_group=process_group,
+            precision=adjoint_precision)
+
+
+_ADJ_PRECISIONS = {'fp64': 0, 'fp32local': 1}
 
 
 class FrozenPhotons:
-    """Device arrays of the frozen photons and the C-ABI problem over them."""
+    """Device arrays of the frozen photons and the C-ABI problem over them.
+
+    ``precision``: 'fp64', or 'fp32local' for the moments and gradients of
+    a flat-detector chain (float-float positions re-centred on every
+    element, float32 reverse sweep, float64 sums; csrc/adjoint32.cu).  The
+    freeze (the photons' discrete choices) and ``finite_differences`` run
+    in float64 either way.
+    """
 
     def __init__(self, model, pos, dir, energy, weight, alpha, beta, facet, order, group,
-                 n_groups, theta=None, stream=None, rows=None, process_group=None):
+                 n_groups, theta=None, stream=None, rows=None, process_group=None,
+                 precision='fp64'):
         if n_groups < 1 or n_groups > _abi.ADJ_MAX_GROUPS:
             raise ValueError('pose adjoint: 1..%d groups' % _abi.ADJ_MAX_GROUPS)
+        if precision not in _ADJ_PRECISIONS:
+            raise ValueError('precision must be one of %s' % list(_ADJ_PRECISIONS))
+        if precision == 'fp32local' and model.det_kind != _abi.ADJ_DET_FLAT:
+            raise NotImplementedError('FP32-local pose adjoint: flat detectors only '
+                                      '(use precision="fp64" for a CircularDetector)')
+        self.precision = precision
         self.model = model
         self.rows = rows            # indices of the frozen photons in the traced table
         # photons sharded over the ranks of this torch.distributed group: the
@@ -315,7 +335,8 @@ class FrozenPhotons:
         self.facets = torch.from_numpy(model.facet_base).to(**f64).contiguous()
         self.flags = torch.from_numpy(model.facet_flags).to(dev).contiguous()
         self.ref = torch.zeros((self.n_groups, 2), **f64)
-        self.rot = torch.empty(36 * (model.n_facets + 1), **f64)
+        # float64 rotations (36 per pose) or FP32-local posed records (24 per element)
+        self.rot = torch.empty(max(36 * (model.n_facets + 1), 24 * (model.n_facets + 3)), **f64)
         self.status = torch.zeros(1, dtype=torch.int32, device=dev)
         self.stream = stream
         self._P = None
@@ -330,12 +351,13 @@ class FrozenPhotons:
         self._P = None
 
     # ------------------------------------------------------------- launches
-    def _problem(self, x_out=None, y_out=None):
+    def _problem(self, x_out=None, y_out=None, precision=None):
         P = _abi.MgpuAdjointProblem()
         P.n = self.n
         P.n_facets = self.model.n_facets
         P.n_groups = self.n_groups
         P.det_kind = self.model.det_kind
+        P.precision = _ADJ_PRECISIONS[precision or self.precision]
         P.pos, P.dir = self.pos.data_ptr(), self.dir.data_ptr()
         P.alpha, P.beta = self.alpha.data_ptr(), self.beta.data_ptr()
         P.energy, P.weight = self.energy.data_ptr(), self.weight.data_ptr()
@@ -356,14 +378,15 @@ class FrozenPhotons:
         P.status = self.status.data_ptr()
         return P
 
-    def _run(self, theta, mode, seeds=None, moments=None, grad=None, x_out=None, y_out=None):
+    def _run(self, theta, mode, seeds=None, moments=None, grad=None, x_out=None, y_out=None,
+             precision=None):
         theta = self._theta(theta)
-        if x_out is None and y_out is None:
-            if self._P is None:
+        if x_out is None and y_out is None and precision in (None, self.precision):
+            if self._P is None or self._P.precision != _ADJ_PRECISIONS[self.precision]:
                 self._P = self._problem()
             P = self._P
         else:
-            P = self._problem(x_out, y_out)
+            P = self._problem(x_out, y_out, precision)
         lib = _abi.load()
         _abi.check(lib.mgpu_pose_adjoint(C.byref(P), _ptr(theta), mode, _ptr(seeds),
                                          _ptr(moments), _ptr(grad), _stream_handle(self.stream)),
@@ -434,7 +457,7 @@ class FrozenPhotons:
         mom = torch.zeros((2 * P, self.n_groups, _abi.ADJ_NMOM), dtype=torch.float64,
                           device=self.device)
         for k in range(2 * P):
-            self._run(thetas[k], _abi.ADJ_FORWARD, moments=mom[k])
+            self._run(thetas[k], _abi.ADJ_FORWARD, moments=mom[k], precision='fp64')
         L = loss_fn(moment_stats(mom, self.ref))
         return (L[:P] - L[P:]) / (2 * hk)
 

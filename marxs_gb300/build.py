@@ -14,14 +14,15 @@ CSRC = os.path.join(HERE, 'csrc')
 BUILD = os.path.join(HERE, '_build')
 LIB = os.path.join(HERE, 'libmarxs_gb300.so')
 SOURCES = ['chain_fp64.cu', 'chain_fp32local.cu', 'grid_build.cu', 'capi.cu', 'adjoint.cu',
-           'source.cu', 'analysis.cu', 'poses.cu', 'peaks.cu']
+           'adjoint32.cu', 'source.cu', 'analysis.cu', 'poses.cu', 'peaks.cu']
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 FLAGS = ['-O3', '-lineinfo', '-std=c++17', '-Xcompiler', '-fPIC', '--expt-relaxed-constexpr']
 # per-file flags: the FP32-local chain divides and takes square roots with
 # the approximate float32 instructions (a few ulp; measured 5.8 % faster at
 # 1e8 photons, within the FP32-local precision bars); logf, sincospif and
 # the other math functions keep their accurate versions
-FILE_FLAGS = {'chain_fp32local.cu': ['-prec-div=false', '-prec-sqrt=false']}
+FILE_FLAGS = {'chain_fp32local.cu': ['-prec-div=false', '-prec-sqrt=false'],
+              'adjoint32.cu': ['-prec-div=false', '-prec-sqrt=false']}
 
 
 def nvcc():

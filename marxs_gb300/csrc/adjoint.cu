@@ -511,6 +511,10 @@ int launch_mode(const mgpu_adjoint_problem& P, const double* theta, const double
 
 }  // namespace
 
+cudaError_t mgpu_pose_adjoint_fp32local(const mgpu_adjoint_problem& P, const double* theta,
+                                        int mode, const double* seeds, double* moments,
+                                        double* grad, cudaStream_t s);
+
 extern "C" int mgpu_pose_adjoint(const mgpu_adjoint_problem* prob, const double* theta,
                                  int32_t mode, const double* seeds, double* moments, double* grad,
                                  void* stream) {
@@ -521,6 +525,9 @@ extern "C" int mgpu_pose_adjoint(const mgpu_adjoint_problem* prob, const double*
         P.n_groups > MGPU_ADJ_MAX_GROUPS || P.n < 0)
         return (int)cudaErrorInvalidValue;
     if (P.det_kind != MGPU_ADJ_DET_FLAT && P.det_kind != MGPU_ADJ_DET_CYL)
+        return (int)cudaErrorInvalidValue;
+    if (P.precision != MGPU_FP64 && P.precision != MGPU_FP32LOCAL) return (int)cudaErrorInvalidValue;
+    if (P.precision == MGPU_FP32LOCAL && P.det_kind != MGPU_ADJ_DET_FLAT && mode != MGPU_ADJ_FREEZE)
         return (int)cudaErrorInvalidValue;
     if (P.n > 0 && (!P.pos || !P.dir || !P.alpha || !P.beta || !P.energy || !P.weight ||
                     !P.facet || !P.order || !P.group || !P.facets || !P.facet_flags ||
@@ -536,6 +543,8 @@ extern "C" int mgpu_pose_adjoint(const mgpu_adjoint_problem* prob, const double*
     }
     cudaStream_t s = (cudaStream_t)stream;
     const int F = P.n_facets;
+    if (P.precision == MGPU_FP32LOCAL && mode != MGPU_ADJ_FREEZE)
+        return (int)mgpu_pose_adjoint_fp32local(P, theta, mode, seeds, moments, grad, s);
     pose_prep_kernel<<<(F + 1 + 127) / 128, 128, 0, s>>>(theta, F, P.rot);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess || P.n == 0) return (int)e;

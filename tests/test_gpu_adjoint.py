@@ -278,3 +278,60 @@ def test_graphed_gradient_equals_direct_gradient(c1):
         L0, g0 = fr.loss_and_grad(theta, c1['loss'])
         assert abs(float(L) - float(L0)) <= 1e-12 * abs(float(L0))
         assert torch.allclose(g, g0, rtol=1e-10, atol=1e-12 * float(g0.abs().max()))
+
+
+class _Precision:
+    """The fixture's frozen photons with another moments/gradient precision."""
+
+    def __init__(self, fr, precision):
+        self.fr, self.precision = fr, precision
+
+    def __enter__(self):
+        self.old = self.fr.precision
+        self.fr.precision = self.precision
+        return self.fr
+
+    def __exit__(self, *exc):
+        self.fr.precision = self.old
+
+
+def test_fp32local_coordinates_match_float64(c1):
+    """FP32-local forward (float-float positions re-centred on every
+    element): detector coordinates within 0.1 um RMS / 1 um of float64,
+    nominal and perturbed."""
+    fr, model = c1['fr'], c1['model']
+    for theta in (model.theta0('cuda'), _random_theta(model, 5)):
+        x64, y64 = fr.xy(theta)
+        with _Precision(fr, 'fp32local'):
+            x32, y32 = fr.xy(theta)
+        d = torch.cat([x32 - x64, y32 - y64]).cpu().numpy()
+        assert np.sqrt(np.mean(d ** 2)) <= 1e-4 and np.max(np.abs(d)) <= 1e-3, \
+            (np.sqrt(np.mean(d ** 2)), np.max(np.abs(d)))
+
+
+def test_fp32local_gradient_equals_central_differences(c1):
+    """The FP32-local gradient (float32 reverse sweep, float64 sums) against
+    central differences of the float64 forward and against the float64
+    adjoint, all 1,207 parameters: 1e-4 relative per parameter block."""
+    fr, model = c1['fr'], c1['model']
+    theta = model.theta0('cuda')
+    _, g64 = fr.loss_and_grad(theta, c1['loss'])
+    fd = fr.finite_differences(theta, c1['loss'])
+    with _Precision(fr, 'fp32local'):
+        _, g32 = fr.loss_and_grad(theta, c1['loss'])
+        fd32 = fr.finite_differences(theta, c1['loss'])     # float64 forward either way
+    g32, g64, fd, fd32 = (t.cpu().numpy() for t in (g32, g64, fd, fd32))
+    # the same float64 forward, up to the atomics' summation order (which the
+    # differences amplify to ~1e-8 on the rotations; a float32 forward would
+    # be off by ~1e-4)
+    assert np.linalg.norm(fd - fd32) <= 1e-6 * np.linalg.norm(fd)
+    assert np.linalg.norm(g32 - fd) <= 1e-4 * np.linalg.norm(fd)
+    assert _blockwise_rel(g32, fd, model) <= 1e-4
+    assert _blockwise_rel(g32, g64, model) <= 1e-4
+
+
+def test_fp32local_adjoint_needs_a_flat_detector(c2):
+    from marxs_gb300.adjoint import PoseModel
+    model = PoseModel(c2['inst'].elements)
+    with pytest.raises(NotImplementedError):
+        model.trace(c2['host'], orders=[-5], draws=c2['draws'], adjoint_precision='fp32local')
