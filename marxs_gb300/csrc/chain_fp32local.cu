@@ -11,7 +11,10 @@
 //     is refined once against the element so the stored position lies on it
 //     (the float32 solve alone leaves it ~1e-7 k off along the ray);
 //   * directions, polarization, probability and local coordinates are
-//     float32; the grating term m * lambda / d is formed in float-float;
+//     float32 (the lean fixed chains keep the probability in float64: it
+//     only meets the efficiency table's total there, one float64 multiply
+//     instead of two conversions); the grating term m * lambda / d is
+//     formed in float-float;
 //   * the cylinder hit is solved in float32 around the tabulated reference
 //     point at the nearest angle k/1024 (global float-float point, radial
 //     and tangential unit vectors): one Newton step on the small offset from
@@ -80,6 +83,7 @@ struct PhotonL {
     ff energy;
     double energy_d;
     float prob;
+    double prob_d;   // lean fixed chains: the probability in float64
     int row0;      // energy row of the first facet stage's selector (-1: not found yet)
 };
 
@@ -664,10 +668,11 @@ __device__ __forceinline__ int energy_row(const mgpu_selector& sel, double e, fl
 }
 
 // the order for the draw U (53 bits) in table row `row`; *prob the row's
-// total.  kLean: the selector has its guide table (checked at launch)
+// total (in float64 into *prob_d instead, when given).  kLean: the selector
+// has its guide table (checked at launch)
 template <bool kLean = false>
 __device__ __forceinline__ int select_order_row(const mgpu_selector& sel, int row, uint64_t U,
-                                                float* prob, uint32_t* status) {
+                                                float* prob, uint32_t* status, double* prob_d = nullptr) {
     const uint64_t* th = sel.thresholds + (int64_t)row * sel.n_orders;
     int k = 0;
     if (kLean || sel.guide) {
@@ -689,7 +694,8 @@ __device__ __forceinline__ int select_order_row(const mgpu_selector& sel, int ro
         k = sel.n_orders - 1;
     }
     double tot = sel.total[row];
-    *prob = d2f_bits(tot);
+    if (prob_d) *prob_d = tot;
+    else *prob = d2f_bits(tot);
     if (MGPU_UNLIKELY(tot < 0.0 || tot > 1.0)) atomicOr(status, MGPU_STATUS_PROB_RANGE);
     return sel.orders[k];
 }
@@ -973,7 +979,8 @@ __device__ bool stage_gratings_l(const mgpu_stage& st, PhotonL& ph, int i, bool 
     } else {
         philox_u53(seed, row_base + (uint64_t)i, (uint32_t)sidx, &U, &U1);
     }
-    float selprob;
+    float selprob = 1.0f;
+    double selprob_d = 1.0;
     const int flags = __float_as_int(R6.w);
     const mgpu_selector& sel = kSel0 ? st.sel0 : st.selectors[__float_as_int(R6.z)];
     int m;
@@ -984,7 +991,8 @@ __device__ bool stage_gratings_l(const mgpu_stage& st, PhotonL& ph, int i, bool 
     } else {
         // fixed chains found the energy row at the start of the photon
         const int row = kSel0 ? ph.row0 : energy_row(sel, ph.energy_d, ph.energy.hi);
-        m = select_order_row<kLean>(sel, row, U, &selprob, status);
+        if (kLean) m = select_order_row<kLean>(sel, row, U, &selprob, status, &selprob_d);
+        else m = select_order_row<kLean>(sel, row, U, &selprob, status);
     }
     float sign;
     if (flags & 1) sign = (p_d > 0.0f) ? 1.0f : ((p_d < 0.0f) ? -1.0f : 1.0f);
@@ -1011,7 +1019,8 @@ __device__ bool stage_gratings_l(const mgpu_stage& st, PhotonL& ph, int i, bool 
     f3 delta = tf * dn + dn_comp * n;
     ph.pol = transport_delta_f(p, delta, ph.pol);
     ph.dir = p + delta;
-    ph.prob *= selprob;
+    if (kLean) ph.prob_d *= selprob_d;
+    else ph.prob *= selprob;
     store_hit(st.out[0], i, h.ly);
     store_hit(st.out[1], i, h.lz);
     stored(st.out[2], i, f2d_fin_bits((float)m));
@@ -1224,6 +1233,7 @@ template <class Chain, bool kStack>
 __global__ void __launch_bounds__(kThreads, (Chain::kFixed && !kStack && Chain::kSearches <= 1)
                                                 ? kMinBlocks : kMinBlocksWide)
 chain_fp32local_kernel(const __grid_constant__ mgpu_chain chain, const __grid_constant__ mgpu_photons io) {
+    constexpr bool kLeanChain = Chain::kFixed && !kStack;
     __shared__ unsigned int s_hits[MGPU_MAX_STAGES];
     if (threadIdx.x < MGPU_MAX_STAGES) s_hits[threadIdx.x] = 0;
     __syncthreads();
@@ -1244,7 +1254,8 @@ chain_fp32local_kernel(const __grid_constant__ mgpu_chain chain, const __grid_co
             ph.pol = f3{__double2float_rn(q.x), __double2float_rn(q.y), __double2float_rn(q.z)};
             ph.energy_d = *at(io.energy.ptr, i, io.energy.stride);
             ph.energy = d2ff_hw(ph.energy_d);
-            ph.prob = __double2float_rn(*at(io.prob.ptr, i, io.prob.stride));
+            if (kLeanChain) ph.prob_d = *at(io.prob.ptr, i, io.prob.stride);
+            else ph.prob = __double2float_rn(*at(io.prob.ptr, i, io.prob.stride));
             ph.row0 = -1;
         } else {
             ph.pos = ff3{ff{0.f, 0.f}, ff{0.f, 0.f}, ff{0.f, 0.f}};
@@ -1252,6 +1263,7 @@ chain_fp32local_kernel(const __grid_constant__ mgpu_chain chain, const __grid_co
             ph.energy = ff{1.f, 0.f};
             ph.energy_d = 1.0;
             ph.prob = 0.f;
+            ph.prob_d = 0.0;
             ph.row0 = -1;
         }
         if (valid && (chain.flags & MGPU_FLAG_CHECK_W)) {
@@ -1268,7 +1280,7 @@ chain_fp32local_kernel(const __grid_constant__ mgpu_chain chain, const __grid_co
             // all on the integer pipe, which the columns keep)
             store3i(io.dir_out, i, d3{(double)ph.dir.x, (double)ph.dir.y, (double)ph.dir.z});
             store3i(io.pol_out, i, d3{(double)ph.pol.x, (double)ph.pol.y, (double)ph.pol.z});
-            *at(io.prob_out.ptr, i, io.prob_out.stride) = (double)ph.prob;
+            *at(io.prob_out.ptr, i, io.prob_out.stride) = kLeanChain ? ph.prob_d : (double)ph.prob;
         }
         count_hits(hits, s_hits, chain.n_stages, lane);
     }

@@ -138,6 +138,9 @@ def test_fp32local_vs_fp64_cat_array(n):
     assert rms <= 0.5 * UM and mx <= 5 * UM, report
     assert np.sqrt(np.mean(dphi ** 2)) <= 0.5 * UM and dphi.max() <= 5 * UM, report
     assert dy.max() <= 5 * UM, report
+    # the lean chain keeps the probability in float64: the float64 product
+    pa, pb = np.asarray(a['probability'])[agree], np.asarray(b['probability'])[agree]
+    assert np.array_equal(pa, pb)
     print('columns:', check_columns(a, b, agree, inst))
 
 
