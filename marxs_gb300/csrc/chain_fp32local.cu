@@ -1116,7 +1116,10 @@ __device__ __forceinline__ bool run_stage_l(const mgpu_stage& st, PhotonL& ph, i
                 absorb = (((st.first_writer >> 17) & 1)
                               ? *at((const int64_t*)st.id_out, i, st.id_stride)
                               : (int64_t)*at((const int32_t*)st.id_out, i, st.id_stride)) < 0;
-            if (absorb) ph.prob = 0.0f;
+            if (absorb) {
+                ph.prob = 0.0f;
+                ph.prob_d = 0.0;     // the lean chains' float64 probability
+            }
         }
         return false;
     default:
