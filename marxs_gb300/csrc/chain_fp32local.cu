@@ -41,7 +41,9 @@
 // table per grating array; no host-evaluated columns), which took the CAT
 // chain from 90 to 55 KB of code and 6 % of its time; rarely run code
 // (large-angle sines, the reflection form of the polarization transport)
-// stays out of line.  Other configurations run the generic stage loop.
+// stays out of line.  Other configurations of the same stage sequences run
+// the fixed chains compiled with every path; other sequences the generic
+// stage loop.
 // Photon i of a column is addressed with 32-bit offsets (launches of at
 // most 2^30 photons).
 #include <cuda_runtime.h>
@@ -1085,13 +1087,11 @@ __device__ bool stage_detarray_l(const mgpu_stage& st, PhotonL& ph, int i, bool 
 
 // one stage, kind known at compile time (KIND > 0) or read from the
 // descriptor (KIND == 0, generic chains)
-template <int KIND, bool kStack, bool kSel0, bool kPhilox>
+template <int KIND, bool kStack, bool kSel0, bool kPhilox, bool kLean>
 __device__ __forceinline__ bool run_stage_l(const mgpu_stage& st, PhotonL& ph, int i,
                                             bool valid, const mgpu_chain& chain, int s) {
     // fixed chains run Philox only: the pre-drawn branches fold away
     const int rng = kPhilox ? MGPU_RNG_PHILOX : chain.rng;
-    // the plain fixed chains run the common configuration only
-    constexpr bool kLean = kSel0 && !kStack;
     const int kind = KIND ? KIND : st.kind;
     switch (kind) {
     case MGPU_STAGE_GRATINGS:
@@ -1143,11 +1143,13 @@ __device__ __forceinline__ void count_hits(uint32_t mask, unsigned* s_hits, int 
 struct GenericChain {
     static constexpr bool kFixed = false;
     static constexpr int kSearches = 2;
-    template <bool kStack>
+    template <bool kStack, bool kLean>
     __device__ static uint32_t run(const mgpu_chain& chain, PhotonL& ph, int i, bool valid) {
+        static_assert(!kLean, "the generic loop serves every configuration");
         uint32_t mask = 0;
         for (int s = 0; s < chain.n_stages; ++s)
-            mask |= (uint32_t)run_stage_l<0, kStack, false, false>(chain.stages[s], ph, i, valid, chain, s)
+            mask |= (uint32_t)run_stage_l<0, kStack, false, false, false>(chain.stages[s], ph, i, valid,
+                                                                       chain, s)
                     << s;
         return mask;
     }
@@ -1161,16 +1163,17 @@ struct FixedChain {
     // facet-table searches (grating arrays, CCD arrays) in the chain
     static constexpr int kSearches =
         (0 + ... + (K == MGPU_STAGE_GRATINGS || K == MGPU_STAGE_DETARRAY ? 1 : 0));
-    template <int KIND, int S, bool kStack>
+    template <int KIND, int S, bool kStack, bool kLean>
     __device__ static uint32_t step(const mgpu_chain& chain, PhotonL& ph, int i, bool valid) {
-        return (uint32_t)run_stage_l<KIND, kStack, true, true>(chain.stages[S], ph, i, valid, chain, S)
+        return (uint32_t)run_stage_l<KIND, kStack, true, true, kLean>(chain.stages[S], ph, i, valid,
+                                                                     chain, S)
                << S;
     }
-    template <bool kStack, int... S>
+    template <bool kStack, bool kLean, int... S>
     __device__ static uint32_t run_seq(const mgpu_chain& chain, PhotonL& ph, int i, bool valid,
                                        std::integer_sequence<int, S...>) {
         uint32_t mask = 0;
-        ((mask |= step<K, S, kStack>(chain, ph, i, valid)), ...);
+        ((mask |= step<K, S, kStack, kLean>(chain, ph, i, valid)), ...);
         return mask;
     }
     // the facet stage (at most one) whose selector's energy row is found
@@ -1183,14 +1186,17 @@ struct FixedChain {
     }();
     static_assert((0 + ... + (K == MGPU_STAGE_GRATINGS ? 1 : 0)) <= 1,
                   "fixed chains hold at most one grating array");
-    template <bool kStack>
+    // kLean: compiled for the common element configuration only (lean_ok)
+    template <bool kStack, bool kLean>
     __device__ static uint32_t run(const mgpu_chain& chain, PhotonL& ph, int i, bool valid) {
+        static_assert(!(kLean && kStack), "the stacked chains are not lean");
         if constexpr (kGratings >= 0) {
             const mgpu_selector& sel = chain.stages[kGratings].sel0;
-            if (!kStack) ph.row0 = energy_row<true>(sel, ph.energy_d, ph.energy.hi);
+            if (kLean) ph.row0 = energy_row<true>(sel, ph.energy_d, ph.energy.hi);
             else if (sel.kind != MGPU_SEL_SPLINE) ph.row0 = energy_row(sel, ph.energy_d, ph.energy.hi);
         }
-        return run_seq<kStack>(chain, ph, i, valid, std::make_integer_sequence<int, sizeof...(K)>{});
+        return run_seq<kStack, kLean>(chain, ph, i, valid,
+                                      std::make_integer_sequence<int, sizeof...(K)>{});
     }
     // the stage kinds match, every facet stage reads its first selector, and
     // the draws come from Philox (the pre-drawn code is compiled out)
@@ -1224,7 +1230,7 @@ bool lean_ok(const mgpu_chain& chain) {
     return true;
 }
 
-template <class Chain, bool kStack>
+template <class Chain, bool kStack, bool kLean>
 // fixed plain chains with one facet search: 4 blocks of 256 per SM (64
 // registers, no spills; the stage constants come from the parameter bank),
 // measured 6 % faster than 3 blocks (80 registers) on the CAT chain at 1e8
@@ -1236,7 +1242,7 @@ template <class Chain, bool kStack>
 __global__ void __launch_bounds__(kThreads, (Chain::kFixed && !kStack && Chain::kSearches <= 1)
                                                 ? kMinBlocks : kMinBlocksWide)
 chain_fp32local_kernel(const __grid_constant__ mgpu_chain chain, const __grid_constant__ mgpu_photons io) {
-    constexpr bool kLeanChain = Chain::kFixed && !kStack;
+    constexpr bool kLeanChain = kLean;
     __shared__ unsigned int s_hits[MGPU_MAX_STAGES];
     if (threadIdx.x < MGPU_MAX_STAGES) s_hits[threadIdx.x] = 0;
     __syncthreads();
@@ -1275,7 +1281,7 @@ chain_fp32local_kernel(const __grid_constant__ mgpu_chain chain, const __grid_co
                 *at(io.pol.ptr + 3 * io.pol.cstride, i, io.pol.stride) != 0.0)
                 atomicOr(chain.status, MGPU_STATUS_BAD_W);
         }
-        const uint32_t hits = Chain::template run<kStack>(chain, ph, i, valid);
+        const uint32_t hits = Chain::template run<kStack, kLean>(chain, ph, i, valid);
         if (valid) {
             store3i(io.pos_out, i, d3{ff2d(ph.pos.x), ff2d(ph.pos.y), ff2d(ph.pos.z)});
             // state outputs on the FP64 pipe's conversions, stage columns on
@@ -1338,6 +1344,25 @@ void advance_rows(mgpu_chain& c, mgpu_photons& io, int64_t off) {
     }
 }
 
+// the fixed (plain) chain kernel of the chain's stage sequence, lean or
+// not; false when no fixed chain matches
+template <bool kLean>
+bool launch_fixed(const mgpu_chain& chain, const mgpu_photons& io, unsigned gb, cudaStream_t stream) {
+    if (ChainCat::matches(chain))
+        chain_fp32local_kernel<ChainCat, false, kLean><<<gb, kThreads, 0, stream>>>(chain, io);
+    else if (ChainSpec::matches(chain))
+        chain_fp32local_kernel<ChainSpec, false, kLean><<<gb, kThreads, 0, stream>>>(chain, io);
+    else if (ChainCcd::matches(chain))
+        chain_fp32local_kernel<ChainCcd, false, kLean><<<gb, kThreads, 0, stream>>>(chain, io);
+    else if (ChainTel::matches(chain))
+        chain_fp32local_kernel<ChainTel, false, kLean><<<gb, kThreads, 0, stream>>>(chain, io);
+    else if (ChainCatBars::matches(chain))
+        chain_fp32local_kernel<ChainCatBars, false, kLean><<<gb, kThreads, 0, stream>>>(chain, io);
+    else
+        return false;
+    return true;
+}
+
 cudaError_t launch_rows(const mgpu_chain& chain, const mgpu_photons& io, cudaStream_t stream,
                         int sm_count) {
     int64_t warps = (io.n + 31) / 32;
@@ -1351,28 +1376,19 @@ cudaError_t launch_rows(const mgpu_chain& chain, const mgpu_photons& io, cudaStr
     const unsigned gb = (unsigned)blocks;
     if (chain.flags & MGPU_FLAG_GENERIC) {
         if (stacked)
-            chain_fp32local_kernel<GenericChain, true><<<gb, kThreads, 0, stream>>>(chain, io);
+            chain_fp32local_kernel<GenericChain, true, false><<<gb, kThreads, 0, stream>>>(chain, io);
         else
-            chain_fp32local_kernel<GenericChain, false><<<gb, kThreads, 0, stream>>>(chain, io);
+            chain_fp32local_kernel<GenericChain, false, false><<<gb, kThreads, 0, stream>>>(chain, io);
     } else if (stacked) {
         if (ChainCatBars::matches(chain))
-            chain_fp32local_kernel<ChainCatBars, true><<<gb, kThreads, 0, stream>>>(chain, io);
+            chain_fp32local_kernel<ChainCatBars, true, false><<<gb, kThreads, 0, stream>>>(chain, io);
         else
-            chain_fp32local_kernel<GenericChain, true><<<gb, kThreads, 0, stream>>>(chain, io);
-    } else if (!lean_ok(chain)) {
-        chain_fp32local_kernel<GenericChain, false><<<gb, kThreads, 0, stream>>>(chain, io);
-    } else if (ChainCat::matches(chain)) {
-        chain_fp32local_kernel<ChainCat, false><<<gb, kThreads, 0, stream>>>(chain, io);
-    } else if (ChainSpec::matches(chain)) {
-        chain_fp32local_kernel<ChainSpec, false><<<gb, kThreads, 0, stream>>>(chain, io);
-    } else if (ChainCcd::matches(chain)) {
-        chain_fp32local_kernel<ChainCcd, false><<<gb, kThreads, 0, stream>>>(chain, io);
-    } else if (ChainTel::matches(chain)) {
-        chain_fp32local_kernel<ChainTel, false><<<gb, kThreads, 0, stream>>>(chain, io);
-    } else if (ChainCatBars::matches(chain)) {
-        chain_fp32local_kernel<ChainCatBars, false><<<gb, kThreads, 0, stream>>>(chain, io);
-    } else {
-        chain_fp32local_kernel<GenericChain, false><<<gb, kThreads, 0, stream>>>(chain, io);
+            chain_fp32local_kernel<GenericChain, true, false><<<gb, kThreads, 0, stream>>>(chain, io);
+    } else if (lean_ok(chain)) {
+        if (!launch_fixed<true>(chain, io, gb, stream))
+            chain_fp32local_kernel<GenericChain, false, false><<<gb, kThreads, 0, stream>>>(chain, io);
+    } else if (!launch_fixed<false>(chain, io, gb, stream)) {
+        chain_fp32local_kernel<GenericChain, false, false><<<gb, kThreads, 0, stream>>>(chain, io);
     }
     return cudaGetLastError();
 }

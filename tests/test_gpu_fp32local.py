@@ -229,12 +229,13 @@ def test_fp32local_vs_fp64_ccd_strip():
     check_columns(a, b, agree, inst)
 
 
-@pytest.mark.parametrize('name', ['c0', 'c1', 'c2', 'c6', 'c8'])
+@pytest.mark.parametrize('name', ['c0', 'c1', 'c2', 'c5', 'c6', 'c8'])
 def test_specialised_kernels_match_generic(name):
     """The kernels specialised for a stage sequence (stage kinds and
-    constants fixed at compile time, the common lens and efficiency-table
-    configuration compiled in alone, the order's energy row found at the
-    start of the photon) give the same result bits as the generic stage
+    constants fixed at compile time, the order's energy row found at the
+    start of the photon; for the common lens and efficiency-table
+    configuration that configuration compiled in alone, c5's spline
+    selector and lens reflectivity the full one) give the same result bits as the generic stage
     loop on the same chain (``GpuSequence.specialised = False``); the
     probability, which the lean chains keep in float64 and the generic loop
     in float32, to float32 rounding."""
