@@ -113,11 +113,16 @@ __device__ __forceinline__ void storef(const mgpu_col& c, int i, float v) {
 }
 // the same for values that are finite by construction (hit coordinates,
 // pixels, angles): no infinity / NaN cases in the conversion
+// kAll (the lean chains): the launcher checked that the column exists, so
+// the store needs no test (the tests' uniform branches measured 2.8 % of
+// the CAT chain: they split the stages' straight-line code)
+template <bool kAll = false>
 __device__ __forceinline__ void store_hit(const mgpu_col& c, int i, float v) {
-    if (c.ptr) *at(c.ptr, i, c.stride) = f2d_fin_bits(v);
+    if (kAll || c.ptr) *at(c.ptr, i, c.stride) = f2d_fin_bits(v);
 }
+template <bool kAll = false>
 __device__ __forceinline__ void stored(const mgpu_col& c, int i, double v) {
-    if (c.ptr) *at(c.ptr, i, c.stride) = v;
+    if (kAll || c.ptr) *at(c.ptr, i, c.stride) = v;
 }
 
 __device__ __forceinline__ void store_id(const mgpu_stage& st, int i, int64_t v) {
@@ -435,12 +440,13 @@ __device__ bool stage_lens_l(const mgpu_stage& st, PhotonL& ph, int i, uint32_t*
     }
     ph.pol = transport_f(ph.dir, nd, ph.pol);
     ph.dir = nd;
-    store_hit(st.out[0], i, h.ly);
-    store_hit(st.out[1], i, h.lz);
+    store_hit<kLean>(st.out[0], i, h.ly);
+    store_hit<kLean>(st.out[1], i, h.lz);
     ph.pos = h.ip;
     return true;
 }
 
+template <bool kLean>
 __device__ bool stage_scatter_l(const mgpu_stage& st, PhotonL& ph, int i, int rng,
                                 uint64_t seed, uint64_t row_base, int sidx, uint32_t* status) {
     // RadialMirrorScatter.specific_process_photons, optics/scatter.py:49-77
@@ -484,19 +490,20 @@ __device__ bool stage_scatter_l(const mgpu_stage& st, PhotonL& ph, int i, int rn
     if (sig_perp != 0.0f) delta = delta + rot_transpose_delta_f(radial, a_perp, ph.dir + delta);
     ph.pol = transport_delta_f(ph.dir, delta, ph.pol);
     ph.dir = ph.dir + delta;
-    store_hit(st.out[0], i, h.ly);
-    store_hit(st.out[1], i, h.lz);
+    store_hit<kLean>(st.out[0], i, h.ly);
+    store_hit<kLean>(st.out[1], i, h.lz);
     if (have_d) {
-        stored(st.out[2], i, a_in_d);
-        stored(st.out[3], i, a_perp_d);
+        stored<kLean>(st.out[2], i, a_in_d);
+        stored<kLean>(st.out[3], i, a_perp_d);
     } else {
-        store_hit(st.out[2], i, a_in);
-        store_hit(st.out[3], i, a_perp);
+        store_hit<kLean>(st.out[2], i, a_in);
+        store_hit<kLean>(st.out[3], i, a_perp);
     }
     ph.pos = h.ip;
     return true;
 }
 
+template <bool kLean>
 __device__ bool stage_flatdet_l(const mgpu_stage& st, PhotonL& ph, int i) {
     // FlatDetector.specific_process_photons, optics/detector.py:72-75
     const mgpu_flat32* F = reinterpret_cast<const mgpu_flat32*>(st.aux32);
@@ -505,10 +512,10 @@ __device__ bool stage_flatdet_l(const mgpu_stage& st, PhotonL& ph, int i) {
         write_miss_defaults(st, i, 4);
         return false;
     }
-    store_hit(st.out[0], i, h.ly);
-    store_hit(st.out[1], i, h.lz);
-    store_hit(st.out[2], i, h.ly * F->p[3] + F->p[1]);
-    store_hit(st.out[3], i, h.lz * F->p[3] + F->p[2]);
+    store_hit<kLean>(st.out[0], i, h.ly);
+    store_hit<kLean>(st.out[1], i, h.lz);
+    store_hit<kLean>(st.out[2], i, h.ly * F->p[3] + F->p[1]);
+    store_hit<kLean>(st.out[3], i, h.lz * F->p[3] + F->p[2]);
     if (st.id_out) store_id(st, i, st.id_num);
     ph.pos = h.ip;
     return true;
@@ -539,6 +546,7 @@ __device__ __forceinline__ float angle_coarse(float y, float x) {
     return copysignf(a, y);
 }
 
+template <bool kLean>
 __device__ bool stage_cyldet_l(const mgpu_stage& st, PhotonL& ph, int i) {
     // Cylinder.intersect (math/geometry.py:470-564) + CircularDetector
     // (optics/detector.py:115-118) for a circular tube
@@ -612,11 +620,11 @@ __device__ bool stage_cyldet_l(const mgpu_stage& st, PhotonL& ph, int i) {
     const float r = wt / (R + wu);
     const float psi = fmaf(-(1.0f / 3.0f) * r * r, r, r);
     const ff phi = fast_two_sum((float)kk * (1.0f / 1024.0f), psi);
-    stored(st.out[0], i, f2d_fin_bits(phi.hi) + f2d_fin_bits(phi.lo));
-    store_hit(st.out[1], i, wa);                      // P_k - c is perpendicular to the axis
+    stored<kLean>(st.out[0], i, f2d_fin_bits(phi.hi) + f2d_fin_bits(phi.lo));
+    store_hit<kLean>(st.out[1], i, wa);               // P_k - c is perpendicular to the axis
     const ff px = ff_add_f(ff_mul(phi, ff{K->rpix_hi, K->rpix_lo}), K->cp0);
-    stored(st.out[2], i, f2d_fin_bits(px.hi) + f2d_fin_bits(px.lo));
-    store_hit(st.out[3], i, wa * K->inv_pix + K->cp1);
+    stored<kLean>(st.out[2], i, f2d_fin_bits(px.hi) + f2d_fin_bits(px.lo));
+    store_hit<kLean>(st.out[3], i, wa * K->inv_pix + K->cp1);
     if (st.id_out) store_id(st, i, st.id_num);
     ph.pos = ff3{ff_add_f(P.x, w.x), ff_add_f(P.y, w.y), ff_add_f(P.z, w.z)};
     return true;
@@ -1023,11 +1031,11 @@ __device__ bool stage_gratings_l(const mgpu_stage& st, PhotonL& ph, int i, bool 
     ph.dir = p + delta;
     if (kLean) ph.prob_d *= selprob_d;
     else ph.prob *= selprob;
-    store_hit(st.out[0], i, h.ly);
-    store_hit(st.out[1], i, h.lz);
-    stored(st.out[2], i, f2d_fin_bits((float)m));
+    store_hit<kLean>(st.out[0], i, h.ly);
+    store_hit<kLean>(st.out[1], i, h.lz);
+    stored<kLean>(st.out[2], i, f2d_fin_bits((float)m));
     if (kStack && st.stack) storef(st.out[3], i, blaze_s);
-    else if (kLean) store_hit(st.out[3], i, blaze);
+    else if (kLean) store_hit<kLean>(st.out[3], i, blaze);
     else storef(st.out[3], i, blaze);
     if (st.id_out) store_id(st, i, __float_as_int(R6.y));
     if (kStack && st.stack) {
@@ -1065,6 +1073,7 @@ __device__ bool stage_gratings_l(const mgpu_stage& st, PhotonL& ph, int i, bool 
 // Parallel of FlatDetectors (a CCD array): FlatDetector.specific_process_photons
 // (optics/detector.py:72-75) on the nearest element the ray crosses; record
 // row (ez.z, l) holds 1 / pixel size and the centre pixel
+template <bool kLean>
 __device__ bool stage_detarray_l(const mgpu_stage& st, PhotonL& ph, int i, bool valid) {
     HitL h;
     int f = nearest_facet_l(st, ph, valid, &h);
@@ -1076,10 +1085,10 @@ __device__ bool stage_detarray_l(const mgpu_stage& st, PhotonL& ph, int i, bool 
     const mgpu_facet32* fc = st.facets32 + f;
     const ff3 c = facet_centre(fc);
     const float4 R4 = __ldg(facet_rows(fc) + 4), R6 = __ldg(facet_rows(fc) + 6);
-    store_hit(st.out[0], i, h.ly);
-    store_hit(st.out[1], i, h.lz);
-    store_hit(st.out[2], i, fmaf(h.ly, R4.y, R4.z));
-    store_hit(st.out[3], i, fmaf(h.lz, R4.y, R4.w));
+    store_hit<kLean>(st.out[0], i, h.ly);
+    store_hit<kLean>(st.out[1], i, h.lz);
+    store_hit<kLean>(st.out[2], i, fmaf(h.ly, R4.y, R4.z));
+    store_hit<kLean>(st.out[3], i, fmaf(h.lz, R4.y, R4.w));
     if (st.id_out) store_id(st, i, __float_as_int(R6.y));
     ph.pos = ff3{ff_add_f(c.x, h.v.x), ff_add_f(c.y, h.v.y), ff_add_f(c.z, h.v.z)};
     return true;
@@ -1098,16 +1107,16 @@ __device__ __forceinline__ bool run_stage_l(const mgpu_stage& st, PhotonL& ph, i
         return stage_gratings_l<kStack, kSel0, kLean>(st, ph, i, valid, rng, chain.seed, chain.row_base,
                                         s, chain.status);
     case MGPU_STAGE_DETARRAY:
-        return stage_detarray_l(st, ph, i, valid);
+        return stage_detarray_l<kLean>(st, ph, i, valid);
     case MGPU_STAGE_LENS:
         return valid && stage_lens_l<kLean>(st, ph, i, chain.status);
     case MGPU_STAGE_SCATTER:
-        return valid && stage_scatter_l(st, ph, i, rng, chain.seed, chain.row_base, s,
+        return valid && stage_scatter_l<kLean>(st, ph, i, rng, chain.seed, chain.row_base, s,
                                         chain.status);
     case MGPU_STAGE_FLATDET:
-        return valid && stage_flatdet_l(st, ph, i);
+        return valid && stage_flatdet_l<kLean>(st, ph, i);
     case MGPU_STAGE_CYLDET:
-        return valid && stage_cyldet_l(st, ph, i);
+        return valid && stage_cyldet_l<kLean>(st, ph, i);
     case MGPU_STAGE_SUPPORT:
         // catsupportbars (missions/mitsnl/catgrating.py:314-324)
         if (valid) {
@@ -1211,13 +1220,18 @@ struct FixedChain {
     }
 };
 
-// the configuration the plain fixed chains are compiled for (kLean): lenses
-// without a reflectivity table; grating arrays whose facets all use one
-// efficiency table with increasing energy rows, row midpoints and a guide
-// table, with no column evaluated on the host
+// the configuration the plain fixed chains are compiled for (kLean): every
+// column the stages write present; lenses without a reflectivity table;
+// grating arrays whose facets all use one efficiency table with increasing
+// energy rows, row midpoints and a guide table, with no column evaluated on
+// the host
 bool lean_ok(const mgpu_chain& chain) {
     for (int s = 0; s < chain.n_stages; ++s) {
         const mgpu_stage& st = chain.stages[s];
+        // every column the stage kind writes exists
+        const int nout = (st.kind == MGPU_STAGE_LENS) ? 2 : (st.kind == MGPU_STAGE_SUPPORT ? 0 : 4);
+        for (int k = 0; k < nout; ++k)
+            if (st.out[k].ptr == nullptr) return false;
         if (st.kind == MGPU_STAGE_LENS && st.spline.n_surf > 0) return false;
         if (st.kind == MGPU_STAGE_GRATINGS) {
             const mgpu_selector& q = st.sel0;
