@@ -365,7 +365,10 @@ int mgpu_abi_version(void);
 /* Trace photons through the chain.  Photon state is read from the input
  * columns and the final state written to the output columns for every
  * photon; stage columns are written for hits (and defaults for misses
- * where first_writer says so). */
+ * where first_writer says so).  FP32-local addresses photon rows with
+ * 32-bit offsets: every column stride must stay below 2^28 elements
+ * (cudaErrorInvalidValue otherwise), and launches beyond 2^30 photons are
+ * split internally. */
 int mgpu_trace(const mgpu_chain* chain, const mgpu_photons* photons, void* stream);
 
 /* Build the candidate lists of a grating stage's grid on the device:
