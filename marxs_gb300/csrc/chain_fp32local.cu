@@ -108,13 +108,14 @@ __device__ __forceinline__ T* at(T* p, int i, int64_t s) {
     return (T*)((uintptr_t)p + (uintptr_t)((int64_t)i * (int64_t)(int)(s * (int64_t)sizeof(T))));
 }
 
+template <bool kAll = false>
 __device__ __forceinline__ void storef(const mgpu_col& c, int i, float v) {
-    if (c.ptr) *at(c.ptr, i, c.stride) = f2d_bits(v);
+    if (kAll || c.ptr) *at(c.ptr, i, c.stride) = f2d_bits(v);
 }
 // the same for values that are finite by construction (hit coordinates,
 // pixels, angles): no infinity / NaN cases in the conversion
-// kAll (the lean chains): the launcher checked that the column exists, so
-// the store needs no test (the tests' uniform branches measured 2.8 % of
+// kAll (the fixed chains): the launcher checked that the column exists,
+// so the store needs no test (the tests' uniform branches measured 2.8 % of
 // the CAT chain: they split the stages' straight-line code)
 template <bool kAll = false>
 __device__ __forceinline__ void store_hit(const mgpu_col& c, int i, float v) {
@@ -414,7 +415,7 @@ __device__ __forceinline__ int select_order_spline_f(const mgpu_selector& sel, f
 
 // ------------------------------------------------------------------ stages
 // kLean (the plain fixed chains): the lens has no reflectivity table
-template <bool kLean>
+template <bool kLean, bool kAll>
 __device__ bool stage_lens_l(const mgpu_stage& st, PhotonL& ph, int i, uint32_t* status) {
     // PerfectLens.specific_process_photons, optics/mirror.py:53-82
     const mgpu_flat32* F = reinterpret_cast<const mgpu_flat32*>(st.aux32);
@@ -440,13 +441,14 @@ __device__ bool stage_lens_l(const mgpu_stage& st, PhotonL& ph, int i, uint32_t*
     }
     ph.pol = transport_f(ph.dir, nd, ph.pol);
     ph.dir = nd;
-    store_hit<kLean>(st.out[0], i, h.ly);
-    store_hit<kLean>(st.out[1], i, h.lz);
+    store_hit<kAll>(st.out[0], i, h.ly);
+    store_hit<kAll>(st.out[1], i, h.lz);
     ph.pos = h.ip;
     return true;
 }
 
-template <bool kLean>
+// kAll: every column of the stage exists (fixed chains; checked at launch)
+template <bool kAll>
 __device__ bool stage_scatter_l(const mgpu_stage& st, PhotonL& ph, int i, int rng,
                                 uint64_t seed, uint64_t row_base, int sidx, uint32_t* status) {
     // RadialMirrorScatter.specific_process_photons, optics/scatter.py:49-77
@@ -490,20 +492,20 @@ __device__ bool stage_scatter_l(const mgpu_stage& st, PhotonL& ph, int i, int rn
     if (sig_perp != 0.0f) delta = delta + rot_transpose_delta_f(radial, a_perp, ph.dir + delta);
     ph.pol = transport_delta_f(ph.dir, delta, ph.pol);
     ph.dir = ph.dir + delta;
-    store_hit<kLean>(st.out[0], i, h.ly);
-    store_hit<kLean>(st.out[1], i, h.lz);
+    store_hit<kAll>(st.out[0], i, h.ly);
+    store_hit<kAll>(st.out[1], i, h.lz);
     if (have_d) {
-        stored<kLean>(st.out[2], i, a_in_d);
-        stored<kLean>(st.out[3], i, a_perp_d);
+        stored<kAll>(st.out[2], i, a_in_d);
+        stored<kAll>(st.out[3], i, a_perp_d);
     } else {
-        store_hit<kLean>(st.out[2], i, a_in);
-        store_hit<kLean>(st.out[3], i, a_perp);
+        store_hit<kAll>(st.out[2], i, a_in);
+        store_hit<kAll>(st.out[3], i, a_perp);
     }
     ph.pos = h.ip;
     return true;
 }
 
-template <bool kLean>
+template <bool kAll>
 __device__ bool stage_flatdet_l(const mgpu_stage& st, PhotonL& ph, int i) {
     // FlatDetector.specific_process_photons, optics/detector.py:72-75
     const mgpu_flat32* F = reinterpret_cast<const mgpu_flat32*>(st.aux32);
@@ -512,10 +514,10 @@ __device__ bool stage_flatdet_l(const mgpu_stage& st, PhotonL& ph, int i) {
         write_miss_defaults(st, i, 4);
         return false;
     }
-    store_hit<kLean>(st.out[0], i, h.ly);
-    store_hit<kLean>(st.out[1], i, h.lz);
-    store_hit<kLean>(st.out[2], i, h.ly * F->p[3] + F->p[1]);
-    store_hit<kLean>(st.out[3], i, h.lz * F->p[3] + F->p[2]);
+    store_hit<kAll>(st.out[0], i, h.ly);
+    store_hit<kAll>(st.out[1], i, h.lz);
+    store_hit<kAll>(st.out[2], i, h.ly * F->p[3] + F->p[1]);
+    store_hit<kAll>(st.out[3], i, h.lz * F->p[3] + F->p[2]);
     if (st.id_out) store_id(st, i, st.id_num);
     ph.pos = h.ip;
     return true;
@@ -546,7 +548,7 @@ __device__ __forceinline__ float angle_coarse(float y, float x) {
     return copysignf(a, y);
 }
 
-template <bool kLean>
+template <bool kAll>
 __device__ bool stage_cyldet_l(const mgpu_stage& st, PhotonL& ph, int i) {
     // Cylinder.intersect (math/geometry.py:470-564) + CircularDetector
     // (optics/detector.py:115-118) for a circular tube
@@ -620,11 +622,11 @@ __device__ bool stage_cyldet_l(const mgpu_stage& st, PhotonL& ph, int i) {
     const float r = wt / (R + wu);
     const float psi = fmaf(-(1.0f / 3.0f) * r * r, r, r);
     const ff phi = fast_two_sum((float)kk * (1.0f / 1024.0f), psi);
-    stored<kLean>(st.out[0], i, f2d_fin_bits(phi.hi) + f2d_fin_bits(phi.lo));
-    store_hit<kLean>(st.out[1], i, wa);               // P_k - c is perpendicular to the axis
+    stored<kAll>(st.out[0], i, f2d_fin_bits(phi.hi) + f2d_fin_bits(phi.lo));
+    store_hit<kAll>(st.out[1], i, wa);                // P_k - c is perpendicular to the axis
     const ff px = ff_add_f(ff_mul(phi, ff{K->rpix_hi, K->rpix_lo}), K->cp0);
-    stored<kLean>(st.out[2], i, f2d_fin_bits(px.hi) + f2d_fin_bits(px.lo));
-    store_hit<kLean>(st.out[3], i, wa * K->inv_pix + K->cp1);
+    stored<kAll>(st.out[2], i, f2d_fin_bits(px.hi) + f2d_fin_bits(px.lo));
+    store_hit<kAll>(st.out[3], i, wa * K->inv_pix + K->cp1);
     if (st.id_out) store_id(st, i, st.id_num);
     ph.pos = ff3{ff_add_f(P.x, w.x), ff_add_f(P.y, w.y), ff_add_f(P.z, w.z)};
     return true;
@@ -870,6 +872,7 @@ __device__ __forceinline__ float np_interp_f(const double* x, const float* x32, 
 // float64 arithmetic.  ``support``: the support draw exceeded the open
 // fraction.  Inlined into the stacked-chain kernels only (kStack), which
 // then fit 80 registers without spills.
+template <bool kAll>
 __device__ __forceinline__ void cat_stack_layers_l(const mgpu_stage& st, const mgpu_catstack& K,
                                                 int f, int m, float ly, float lz, uint64_t U1,
                                                 bool support, float z_l2, float u_phi,
@@ -910,8 +913,8 @@ __device__ __forceinline__ void cat_stack_layers_l(const mgpu_stage& st, const m
     }
     if (MGPU_UNLIKELY(!(prob1 >= 0.0f && prob1 <= 1.0f))) atomicOr(status, MGPU_STATUS_PROB_RANGE);
     ph.prob *= prob1;
-    stored(st.out[6], i, f2d_bits((float)m1));
-    storef(st.out[7], i, blaze1);
+    stored<kAll>(st.out[6], i, f2d_bits((float)m1));
+    storef<kAll>(st.out[7], i, blaze1);
     // L2Abs: open fraction minus the shadow of the inclined hexagon walls;
     // sin(arccos |p . n|) = |p x n| (no cancellation near normal incidence)
     const f3 p3 = normf(ph.dir);
@@ -932,9 +935,9 @@ __device__ __forceinline__ void cat_stack_layers_l(const mgpu_stage& st, const m
     const f3 delta2 = dl1 + dl2;
     ph.pol = transport_delta_f(p3, delta2, ph.pol);
     ph.dir = p3 + delta2;
-    storef(st.out[8], i, ang);
-    storef(st.out[4], i, ly);
-    storef(st.out[5], i, lz);
+    storef<kAll>(st.out[8], i, ang);
+    storef<kAll>(st.out[4], i, ly);
+    storef<kAll>(st.out[5], i, lz);
 }
 
 // kStack: compiled with the CATL1L2Stack layers (launches whose chain has a
@@ -1031,12 +1034,12 @@ __device__ bool stage_gratings_l(const mgpu_stage& st, PhotonL& ph, int i, bool 
     ph.dir = p + delta;
     if (kLean) ph.prob_d *= selprob_d;
     else ph.prob *= selprob;
-    store_hit<kLean>(st.out[0], i, h.ly);
-    store_hit<kLean>(st.out[1], i, h.lz);
-    stored<kLean>(st.out[2], i, f2d_fin_bits((float)m));
-    if (kStack && st.stack) storef(st.out[3], i, blaze_s);
-    else if (kLean) store_hit<kLean>(st.out[3], i, blaze);
-    else storef(st.out[3], i, blaze);
+    store_hit<kSel0>(st.out[0], i, h.ly);
+    store_hit<kSel0>(st.out[1], i, h.lz);
+    stored<kSel0>(st.out[2], i, f2d_fin_bits((float)m));
+    if (kStack && st.stack) storef<kSel0>(st.out[3], i, blaze_s);
+    else if (kLean) store_hit<kSel0>(st.out[3], i, blaze);
+    else storef<kSel0>(st.out[3], i, blaze);
     if (st.id_out) store_id(st, i, __float_as_int(R6.y));
     if (kStack && st.stack) {
         bool support;
@@ -1064,7 +1067,8 @@ __device__ bool stage_gratings_l(const mgpu_stage& st, PhotonL& ph, int i, bool 
             sincospif(2.0f * u53_to_f(B), &sn, &cs);
             z = sqrtf(-2.0f * logf(one_minus_u0)) * cs;   // accurate log: small u
         }
-        cat_stack_layers_l(st, *st.stack, f, m, h.ly, h.lz, U1, support, z, u_phi, ph, i, status);
+        cat_stack_layers_l<kSel0>(st, *st.stack, f, m, h.ly, h.lz, U1, support, z, u_phi, ph, i,
+                                  status);
     }
     ph.pos = h.ip;
     return true;
@@ -1073,7 +1077,7 @@ __device__ bool stage_gratings_l(const mgpu_stage& st, PhotonL& ph, int i, bool 
 // Parallel of FlatDetectors (a CCD array): FlatDetector.specific_process_photons
 // (optics/detector.py:72-75) on the nearest element the ray crosses; record
 // row (ez.z, l) holds 1 / pixel size and the centre pixel
-template <bool kLean>
+template <bool kAll>
 __device__ bool stage_detarray_l(const mgpu_stage& st, PhotonL& ph, int i, bool valid) {
     HitL h;
     int f = nearest_facet_l(st, ph, valid, &h);
@@ -1085,10 +1089,10 @@ __device__ bool stage_detarray_l(const mgpu_stage& st, PhotonL& ph, int i, bool 
     const mgpu_facet32* fc = st.facets32 + f;
     const ff3 c = facet_centre(fc);
     const float4 R4 = __ldg(facet_rows(fc) + 4), R6 = __ldg(facet_rows(fc) + 6);
-    store_hit<kLean>(st.out[0], i, h.ly);
-    store_hit<kLean>(st.out[1], i, h.lz);
-    store_hit<kLean>(st.out[2], i, fmaf(h.ly, R4.y, R4.z));
-    store_hit<kLean>(st.out[3], i, fmaf(h.lz, R4.y, R4.w));
+    store_hit<kAll>(st.out[0], i, h.ly);
+    store_hit<kAll>(st.out[1], i, h.lz);
+    store_hit<kAll>(st.out[2], i, fmaf(h.ly, R4.y, R4.z));
+    store_hit<kAll>(st.out[3], i, fmaf(h.lz, R4.y, R4.w));
     if (st.id_out) store_id(st, i, __float_as_int(R6.y));
     ph.pos = ff3{ff_add_f(c.x, h.v.x), ff_add_f(c.y, h.v.y), ff_add_f(c.z, h.v.z)};
     return true;
@@ -1107,16 +1111,16 @@ __device__ __forceinline__ bool run_stage_l(const mgpu_stage& st, PhotonL& ph, i
         return stage_gratings_l<kStack, kSel0, kLean>(st, ph, i, valid, rng, chain.seed, chain.row_base,
                                         s, chain.status);
     case MGPU_STAGE_DETARRAY:
-        return stage_detarray_l<kLean>(st, ph, i, valid);
+        return stage_detarray_l<kSel0>(st, ph, i, valid);
     case MGPU_STAGE_LENS:
-        return valid && stage_lens_l<kLean>(st, ph, i, chain.status);
+        return valid && stage_lens_l<kLean, kSel0>(st, ph, i, chain.status);
     case MGPU_STAGE_SCATTER:
-        return valid && stage_scatter_l<kLean>(st, ph, i, rng, chain.seed, chain.row_base, s,
+        return valid && stage_scatter_l<kSel0>(st, ph, i, rng, chain.seed, chain.row_base, s,
                                         chain.status);
     case MGPU_STAGE_FLATDET:
-        return valid && stage_flatdet_l<kLean>(st, ph, i);
+        return valid && stage_flatdet_l<kSel0>(st, ph, i);
     case MGPU_STAGE_CYLDET:
-        return valid && stage_cyldet_l<kLean>(st, ph, i);
+        return valid && stage_cyldet_l<kSel0>(st, ph, i);
     case MGPU_STAGE_SUPPORT:
         // catsupportbars (missions/mitsnl/catgrating.py:314-324)
         if (valid) {
@@ -1220,18 +1224,29 @@ struct FixedChain {
     }
 };
 
-// the configuration the plain fixed chains are compiled for (kLean): every
-// column the stages write present; lenses without a reflectivity table;
+// the configuration the plain fixed chains are compiled for (kLean): lenses
+// without a reflectivity table;
 // grating arrays whose facets all use one efficiency table with increasing
 // energy rows, row midpoints and a guide table, with no column evaluated on
 // the host
+// every column the stages write exists (what the fixed chains store to
+// without a pointer test): 2 for a lens, 9 for a stacked facet array, none
+// for the support bars, 4 otherwise
+bool cols_ok(const mgpu_chain& chain) {
+    for (int s = 0; s < chain.n_stages; ++s) {
+        const mgpu_stage& st = chain.stages[s];
+        const int nout = (st.kind == MGPU_STAGE_LENS) ? 2
+                         : (st.kind == MGPU_STAGE_SUPPORT) ? 0
+                         : (st.kind == MGPU_STAGE_GRATINGS && st.stack) ? 9 : 4;
+        for (int k = 0; k < nout; ++k)
+            if (st.out[k].ptr == nullptr) return false;
+    }
+    return true;
+}
+
 bool lean_ok(const mgpu_chain& chain) {
     for (int s = 0; s < chain.n_stages; ++s) {
         const mgpu_stage& st = chain.stages[s];
-        // every column the stage kind writes exists
-        const int nout = (st.kind == MGPU_STAGE_LENS) ? 2 : (st.kind == MGPU_STAGE_SUPPORT ? 0 : 4);
-        for (int k = 0; k < nout; ++k)
-            if (st.out[k].ptr == nullptr) return false;
         if (st.kind == MGPU_STAGE_LENS && st.spline.n_surf > 0) return false;
         if (st.kind == MGPU_STAGE_GRATINGS) {
             const mgpu_selector& q = st.sel0;
@@ -1389,6 +1404,12 @@ cudaError_t launch_rows(const mgpu_chain& chain, const mgpu_photons& io, cudaStr
     for (int s = 0; s < chain.n_stages; ++s) stacked = stacked || chain.stages[s].stack != nullptr;
     const unsigned gb = (unsigned)blocks;
     if (chain.flags & MGPU_FLAG_GENERIC) {
+        if (stacked)
+            chain_fp32local_kernel<GenericChain, true, false><<<gb, kThreads, 0, stream>>>(chain, io);
+        else
+            chain_fp32local_kernel<GenericChain, false, false><<<gb, kThreads, 0, stream>>>(chain, io);
+    } else if (!cols_ok(chain)) {
+        // a column the stages write is missing: the generic loop tests each
         if (stacked)
             chain_fp32local_kernel<GenericChain, true, false><<<gb, kThreads, 0, stream>>>(chain, io);
         else
