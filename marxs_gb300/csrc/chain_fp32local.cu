@@ -447,8 +447,9 @@ __device__ bool stage_lens_l(const mgpu_stage& st, PhotonL& ph, int i, uint32_t*
     return true;
 }
 
-// kAll: every column of the stage exists (fixed chains; checked at launch)
-template <bool kAll>
+// kAll: every column of the stage exists (fixed chains; checked at launch);
+// kLean: both widths are nonzero (checked at launch)
+template <bool kAll, bool kLean>
 __device__ bool stage_scatter_l(const mgpu_stage& st, PhotonL& ph, int i, int rng,
                                 uint64_t seed, uint64_t row_base, int sidx, uint32_t* status) {
     // RadialMirrorScatter.specific_process_photons, optics/scatter.py:49-77
@@ -488,8 +489,8 @@ __device__ bool stage_scatter_l(const mgpu_stage& st, PhotonL& ph, int i, int rn
     const f3 radial = h.r0;   // previous position - centre
     f3 perpplane = crossf(ph.dir, radial);
     f3 delta{0.0f, 0.0f, 0.0f};
-    if (sig_in != 0.0f) delta = rot_transpose_delta_f(perpplane, a_in, ph.dir);
-    if (sig_perp != 0.0f) delta = delta + rot_transpose_delta_f(radial, a_perp, ph.dir + delta);
+    if (kLean || sig_in != 0.0f) delta = rot_transpose_delta_f(perpplane, a_in, ph.dir);
+    if (kLean || sig_perp != 0.0f) delta = delta + rot_transpose_delta_f(radial, a_perp, ph.dir + delta);
     ph.pol = transport_delta_f(ph.dir, delta, ph.pol);
     ph.dir = ph.dir + delta;
     store_hit<kAll>(st.out[0], i, h.ly);
@@ -1040,7 +1041,7 @@ __device__ bool stage_gratings_l(const mgpu_stage& st, PhotonL& ph, int i, bool 
     if (kStack && st.stack) storef<kSel0>(st.out[3], i, blaze_s);
     else if (kLean) store_hit<kSel0>(st.out[3], i, blaze);
     else storef<kSel0>(st.out[3], i, blaze);
-    if (st.id_out) store_id(st, i, __float_as_int(R6.y));
+    if (kLean || st.id_out) store_id(st, i, __float_as_int(R6.y));
     if (kStack && st.stack) {
         bool support;
         float u_phi, z;
@@ -1077,7 +1078,7 @@ __device__ bool stage_gratings_l(const mgpu_stage& st, PhotonL& ph, int i, bool 
 // Parallel of FlatDetectors (a CCD array): FlatDetector.specific_process_photons
 // (optics/detector.py:72-75) on the nearest element the ray crosses; record
 // row (ez.z, l) holds 1 / pixel size and the centre pixel
-template <bool kAll>
+template <bool kAll, bool kLean>
 __device__ bool stage_detarray_l(const mgpu_stage& st, PhotonL& ph, int i, bool valid) {
     HitL h;
     int f = nearest_facet_l(st, ph, valid, &h);
@@ -1093,7 +1094,7 @@ __device__ bool stage_detarray_l(const mgpu_stage& st, PhotonL& ph, int i, bool 
     store_hit<kAll>(st.out[1], i, h.lz);
     store_hit<kAll>(st.out[2], i, fmaf(h.ly, R4.y, R4.z));
     store_hit<kAll>(st.out[3], i, fmaf(h.lz, R4.y, R4.w));
-    if (st.id_out) store_id(st, i, __float_as_int(R6.y));
+    if (kLean || st.id_out) store_id(st, i, __float_as_int(R6.y));
     ph.pos = ff3{ff_add_f(c.x, h.v.x), ff_add_f(c.y, h.v.y), ff_add_f(c.z, h.v.z)};
     return true;
 }
@@ -1111,11 +1112,11 @@ __device__ __forceinline__ bool run_stage_l(const mgpu_stage& st, PhotonL& ph, i
         return stage_gratings_l<kStack, kSel0, kLean>(st, ph, i, valid, rng, chain.seed, chain.row_base,
                                         s, chain.status);
     case MGPU_STAGE_DETARRAY:
-        return stage_detarray_l<kSel0>(st, ph, i, valid);
+        return stage_detarray_l<kSel0, kLean>(st, ph, i, valid);
     case MGPU_STAGE_LENS:
         return valid && stage_lens_l<kLean, kSel0>(st, ph, i, chain.status);
     case MGPU_STAGE_SCATTER:
-        return valid && stage_scatter_l<kSel0>(st, ph, i, rng, chain.seed, chain.row_base, s,
+        return valid && stage_scatter_l<kSel0, kLean>(st, ph, i, rng, chain.seed, chain.row_base, s,
                                         chain.status);
     case MGPU_STAGE_FLATDET:
         return valid && stage_flatdet_l<kSel0>(st, ph, i);
@@ -1144,6 +1145,20 @@ __device__ __forceinline__ bool run_stage_l(const mgpu_stage& st, PhotonL& ph, i
 // per-warp hit counts of a photon's stages (bit s of mask: stage s hit),
 // added once at the end of the chain: one short loop instead of a vote and
 // an atomic between every two stages (4 KB less code in the CAT chain)
+// the same for a stage count known at compile time: the votes unrolled, one
+// lane-0 block for the atomics
+template <int N>
+__device__ __forceinline__ void count_hits_fixed(uint32_t mask, unsigned* s_hits, int lane) {
+    unsigned m[N];
+#pragma unroll
+    for (int s = 0; s < N; ++s) m[s] = __ballot_sync(MGPU_FULL_MASK, (mask >> s) & 1u);
+    if (lane == 0) {
+#pragma unroll
+        for (int s = 0; s < N; ++s)
+            if (m[s]) atomicAdd(&s_hits[s], (unsigned)__popc(m[s]));
+    }
+}
+
 __device__ __forceinline__ void count_hits(uint32_t mask, unsigned* s_hits, int n_stages, int lane) {
 #pragma unroll 1
     for (int s = 0; s < n_stages; ++s) {
@@ -1155,6 +1170,7 @@ __device__ __forceinline__ void count_hits(uint32_t mask, unsigned* s_hits, int 
 // generic chain: stage loop over the descriptors
 struct GenericChain {
     static constexpr bool kFixed = false;
+    static constexpr int kStages = 0;
     static constexpr int kSearches = 2;
     template <bool kStack, bool kLean>
     __device__ static uint32_t run(const mgpu_chain& chain, PhotonL& ph, int i, bool valid) {
@@ -1176,6 +1192,7 @@ struct FixedChain {
     // facet-table searches (grating arrays, CCD arrays) in the chain
     static constexpr int kSearches =
         (0 + ... + (K == MGPU_STAGE_GRATINGS || K == MGPU_STAGE_DETARRAY ? 1 : 0));
+    static constexpr int kStages = (int)sizeof...(K);
     template <int KIND, int S, bool kStack, bool kLean>
     __device__ static uint32_t step(const mgpu_chain& chain, PhotonL& ph, int i, bool valid) {
         return (uint32_t)run_stage_l<KIND, kStack, true, true, kLean>(chain.stages[S], ph, i, valid,
@@ -1225,7 +1242,8 @@ struct FixedChain {
 };
 
 // the configuration the plain fixed chains are compiled for (kLean): lenses
-// without a reflectivity table;
+// without a reflectivity table; scatter surfaces with both widths nonzero;
+// facet arrays with an id column;
 // grating arrays whose facets all use one efficiency table with increasing
 // energy rows, row midpoints and a guide table, with no column evaluated on
 // the host
@@ -1248,6 +1266,9 @@ bool lean_ok(const mgpu_chain& chain) {
     for (int s = 0; s < chain.n_stages; ++s) {
         const mgpu_stage& st = chain.stages[s];
         if (st.kind == MGPU_STAGE_LENS && st.spline.n_surf > 0) return false;
+        if (st.kind == MGPU_STAGE_SCATTER && (st.p[0] == 0.0 || st.p[1] == 0.0)) return false;
+        if ((st.kind == MGPU_STAGE_GRATINGS || st.kind == MGPU_STAGE_DETARRAY) && !st.id_out)
+            return false;
         if (st.kind == MGPU_STAGE_GRATINGS) {
             const mgpu_selector& q = st.sel0;
             if (!st.facet_sel0 || st.stack || st.grating_d.ptr || st.blaze_add.ptr ||
@@ -1320,7 +1341,8 @@ chain_fp32local_kernel(const __grid_constant__ mgpu_chain chain, const __grid_co
             store3i(io.pol_out, i, d3{(double)ph.pol.x, (double)ph.pol.y, (double)ph.pol.z});
             *at(io.prob_out.ptr, i, io.prob_out.stride) = kLeanChain ? ph.prob_d : (double)ph.prob;
         }
-        count_hits(hits, s_hits, chain.n_stages, lane);
+        if constexpr (Chain::kFixed) count_hits_fixed<Chain::kStages>(hits, s_hits, lane);
+        else count_hits(hits, s_hits, chain.n_stages, lane);
     }
     __syncthreads();
     if (threadIdx.x < chain.n_stages && s_hits[threadIdx.x])
