@@ -108,9 +108,18 @@ __device__ __forceinline__ T* at(T* p, int i, int64_t s) {
     return (T*)((uintptr_t)p + (uintptr_t)((int64_t)i * (int64_t)(int)(s * (int64_t)sizeof(T))));
 }
 
+// photon columns are written once and not read again by the kernel: stored
+// evict-first (st.global.cs) so they do not displace the facet records,
+// candidate lists and order tables in L1/L2 (measured 0.6 % faster than
+// plain stores on the CAT chain; streaming loads of the inputs gained less)
+template <class T>
+__device__ __forceinline__ void put(T* p, T v) {
+    __stcs(p, v);
+}
+
 template <bool kAll = false>
 __device__ __forceinline__ void storef(const mgpu_col& c, int i, float v) {
-    if (kAll || c.ptr) *at(c.ptr, i, c.stride) = f2d_bits(v);
+    if (kAll || c.ptr) put(at(c.ptr, i, c.stride), f2d_bits(v));
 }
 // the same for values that are finite by construction (hit coordinates,
 // pixels, angles): no infinity / NaN cases in the conversion
@@ -119,16 +128,16 @@ __device__ __forceinline__ void storef(const mgpu_col& c, int i, float v) {
 // the CAT chain: they split the stages' straight-line code)
 template <bool kAll = false>
 __device__ __forceinline__ void store_hit(const mgpu_col& c, int i, float v) {
-    if (kAll || c.ptr) *at(c.ptr, i, c.stride) = f2d_fin_bits(v);
+    if (kAll || c.ptr) put(at(c.ptr, i, c.stride), f2d_fin_bits(v));
 }
 template <bool kAll = false>
 __device__ __forceinline__ void stored(const mgpu_col& c, int i, double v) {
-    if (kAll || c.ptr) *at(c.ptr, i, c.stride) = v;
+    if (kAll || c.ptr) put(at(c.ptr, i, c.stride), v);
 }
 
 __device__ __forceinline__ void store_id(const mgpu_stage& st, int i, int64_t v) {
-    if ((st.first_writer >> 17) & 1) *at((int64_t*)st.id_out, i, st.id_stride) = v;
-    else *at((int32_t*)st.id_out, i, st.id_stride) = (int32_t)v;
+    if ((st.first_writer >> 17) & 1) put(at((long long*)st.id_out, i, st.id_stride), (long long)v);
+    else put(at((int*)st.id_out, i, st.id_stride), (int)v);
 }
 
 // 3-vector columns: component c of photon i at ptr + c * cstride, stride s
@@ -137,9 +146,9 @@ __device__ __forceinline__ d3 load3i(const mgpu_vec& v, int i) {
               *at(v.ptr + 2 * v.cstride, i, v.stride)};
 }
 __device__ __forceinline__ void store3i(const mgpu_vec& v, int i, d3 a) {
-    *at(v.ptr, i, v.stride) = a.x;
-    *at(v.ptr + v.cstride, i, v.stride) = a.y;
-    *at(v.ptr + 2 * v.cstride, i, v.stride) = a.z;
+    put(at(v.ptr, i, v.stride), a.x);
+    put(at(v.ptr + v.cstride, i, v.stride), a.y);
+    put(at(v.ptr + 2 * v.cstride, i, v.stride), a.z);
 }
 
 __device__ __forceinline__ void write_miss_defaults(const mgpu_stage& st, int i, int nout) {
@@ -1339,7 +1348,7 @@ chain_fp32local_kernel(const __grid_constant__ mgpu_chain chain, const __grid_co
             // all on the integer pipe, which the columns keep)
             store3i(io.dir_out, i, d3{(double)ph.dir.x, (double)ph.dir.y, (double)ph.dir.z});
             store3i(io.pol_out, i, d3{(double)ph.pol.x, (double)ph.pol.y, (double)ph.pol.z});
-            *at(io.prob_out.ptr, i, io.prob_out.stride) = kLeanChain ? ph.prob_d : (double)ph.prob;
+            put(at(io.prob_out.ptr, i, io.prob_out.stride), kLeanChain ? ph.prob_d : (double)ph.prob);
         }
         if constexpr (Chain::kFixed) count_hits_fixed<Chain::kStages>(hits, s_hits, lane);
         else count_hits(hits, s_hits, chain.n_stages, lane);
