@@ -44,7 +44,7 @@ WORKLOAD = 'cat_rowland_1000facets_circular_detector'
 # capture (dram__bytes_read.sum + dram__bytes_write.sum) of a 4e6-photon
 # launch, scaled to the launch by photon count
 NCU_TRAFFIC_BYTES_PER_PHOTON = {'fp64': (358.2e6 + 735.3e6) / 4e6,
-                                'fp32local': (356.4e6 + 725.9e6) / 4e6}
+                                'fp32local': (355.7e6 + 724.0e6) / 4e6}
 
 
 def parse():
