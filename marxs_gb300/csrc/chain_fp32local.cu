@@ -1179,7 +1179,6 @@ __device__ __forceinline__ void count_hits(uint32_t mask, unsigned* s_hits, int 
 // generic chain: stage loop over the descriptors
 struct GenericChain {
     static constexpr bool kFixed = false;
-    static constexpr int kStages = 0;
     static constexpr int kSearches = 2;
     template <bool kStack, bool kLean>
     __device__ static uint32_t run(const mgpu_chain& chain, PhotonL& ph, int i, bool valid) {
